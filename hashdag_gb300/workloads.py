@@ -1,0 +1,124 @@
+"""Seeded workloads of the benchmark configurations (seeds: scene 1,
+colours 2, edits 3, cameras 4, serving trace 5).
+
+Cameras are built as the reference's get_trace_params (dag_tracer.cu:71-113)
+builds Tracer::TracePathsParams, with the scene's bounding box equal to the
+voxel cube [0, 2^depth]^3 so that world and voxel space coincide.
+"""
+import math
+
+import numpy as np
+
+from . import scene
+
+SEED_SCENE, SEED_COLORS, SEED_EDITS, SEED_CAMERAS, SEED_SERVING = 1, 2, 3, 4, 5
+
+SPHERE_REMOVE, SPHERE_ADD, BOX_REMOVE, BOX_ADD = 0, 1, 2, 3
+
+
+def color_tree_levels(depth):
+    """C_colorTreeLevels per depth: the reference's 10, lowered on shallow
+    scenes where 10 would reach the leaf level."""
+    return min(10, depth - 5)
+
+
+def top_bucket_bits(depth):
+    """BUCKETS_BITS_FOR_TOP_LEVELS: the reference's 10, raised to 12 on scenes
+    of depth 11 and more whose level 8 holds over 10^5 nodes."""
+    return 10 if depth <= 10 else 12
+
+
+# ---------------------------------------------------------------- cameras --
+
+def _norm(v):
+    v = np.asarray(v, np.float64)
+    return v / math.sqrt(float(v @ v))
+
+
+def trace_params(position, target, width, height, fov_deg=90.0, up=(0.0, 1.0, 0.0)):
+    """get_trace_params (dag_tracer.cu:71-113) for a camera at `position`
+    looking at `target`; returns dict(position, ray_min, ray_ddx, ray_ddy)."""
+    position = np.asarray(position, np.float64)
+    forward = _norm(np.asarray(target, np.float64) - position)
+    right = _norm(np.cross(forward, np.asarray(up, np.float64)))
+    upv = np.cross(right, forward)
+    fov = fov_deg / 2.0 * (math.pi / 180.0)
+    aspect = float(width) / float(height)
+    X = right * math.sin(fov) * aspect
+    Y = upv * math.sin(fov)
+    Z = forward * math.cos(fov)
+    bottom_left = position + Z - Y - X
+    bottom_right = position + Z - Y + X
+    top_left = position + Z + Y - X
+    dx = (bottom_right - bottom_left) * (1.0 / width)
+    dy = (top_left - bottom_left) * (1.0 / height)
+    return dict(position=position.tolist(), ray_min=bottom_left.tolist(), ray_ddx=dx.tolist(),
+                ray_ddy=dy.tolist())
+
+
+def orbit_camera(depth, width, height, seed=SEED_CAMERAS):
+    """One seeded pose at distance 1.5 E from the centre, outside the box,
+    looking at the centre (90 degree FOV)."""
+    rng = np.random.default_rng(seed)
+    e = float(1 << depth)
+    centre = np.array([e / 2, e / 2, e / 2])
+    theta = rng.uniform(0, 2 * math.pi)
+    elev = rng.uniform(0.15, 0.6)
+    d = np.array([math.cos(theta) * math.cos(elev), math.sin(elev), math.sin(theta) * math.cos(elev)])
+    return trace_params(centre + 1.5 * e * d, centre, width, height)
+
+
+def catmull_rom_path(depth, n_poses, width, height, seed=SEED_CAMERAS):
+    """n_poses cameras on a closed Catmull-Rom spline through 8 seeded
+    control points outside the bounding box, looking at points near the
+    centre."""
+    rng = np.random.default_rng(seed)
+    e = float(1 << depth)
+    centre = np.array([e / 2, e / 2, e / 2])
+    ctrl = []
+    for k in range(8):
+        theta = 2 * math.pi * k / 8 + rng.uniform(-0.3, 0.3)
+        elev = rng.uniform(0.1, 0.7)
+        dist = rng.uniform(0.9, 1.4) * e
+        ctrl.append(centre + dist * np.array([math.cos(theta) * math.cos(elev), math.sin(elev),
+                                              math.sin(theta) * math.cos(elev)]))
+    ctrl = np.array(ctrl)
+    looks = centre + rng.uniform(-0.15, 0.15, (8, 3)) * e
+    poses = []
+    for i in range(n_poses):
+        u = 8.0 * i / n_poses
+        k = int(u)
+        t = u - k
+        p0, p1, p2, p3 = (ctrl[(k + j) % 8] for j in (-1, 0, 1, 2))
+        pos = 0.5 * ((2 * p1) + (-p0 + p2) * t + (2 * p0 - 5 * p1 + 4 * p2 - p3) * t * t +
+                     (-p0 + 3 * p1 - 3 * p2 + p3) * t ** 3)
+        look = looks[k] * (1 - t) + looks[(k + 1) % 8] * t
+        poses.append(trace_params(pos, look, width, height))
+    return poses
+
+
+# ------------------------------------------------------------------ edits --
+
+def _centres(depth, n, rng):
+    pts = scene.surface_points(SEED_SCENE, depth, n, rng).astype(np.float64)
+    return pts + 0.5
+
+
+def carve_edits(depth, n=16, r_range=(16.0, 48.0), seed=SEED_EDITS):
+    """Sphere carves with uniform radius centred on seeded surface voxels."""
+    rng = np.random.default_rng(seed)
+    c = _centres(depth, n, rng)
+    r = rng.uniform(r_range[0], r_range[1], n)
+    return [(SPHERE_REMOVE, tuple(float(np.float32(v)) for v in c[i]), float(np.float32(r[i]))) for i in range(n)]
+
+
+def mixed_edits(depth, n, r_range=(4.0, 512.0), seed=SEED_EDITS, mix=(0.5, 0.3, 0.2)):
+    """Batch mix: 50% sphere carve, 30% sphere fill, 20% box fill, radius
+    log-uniform in r_range, centres on seeded surface voxels."""
+    rng = np.random.default_rng(seed)
+    c = _centres(depth, n, rng)
+    lr = rng.uniform(math.log(r_range[0]), math.log(r_range[1]), n)
+    u = rng.uniform(0, 1, n)
+    tools = np.where(u < mix[0], SPHERE_REMOVE, np.where(u < mix[0] + mix[1], SPHERE_ADD, BOX_ADD))
+    return [(int(tools[i]), tuple(float(np.float32(v)) for v in c[i]), float(np.float32(math.exp(lr[i]))))
+            for i in range(n)]

@@ -1,0 +1,220 @@
+/*
+ * hashdag_gb300 — C ABI of the GB300-native hashed sparse voxel DAG hot path.
+ *
+ * One opaque context (hd_ctx) owns a device-resident HashDAG: the paged
+ * per-level hash table (physical page pool, virtual page table, bucket sizes,
+ * full-node indices) plus the root index.  Every call runs sm_103a kernels on
+ * the context's CUDA stream; there is no CPU fallback.  All entry points
+ * return an hd_status and never abort; hd_last_error() gives the message.
+ *
+ * Each entry point names the reference interface it replaces
+ * (Phyronnaz/HashDAG, file:line).  The table format is the reference's
+ * (typedefs.h:201-239, hash_dag_globals.h:7-30, hash_table.h:19-77): 512-word
+ * pages, virtual address = (level, bucket, position), interior nodes
+ * [header, child pointers...] with header = mask | count << 8, leaves = two
+ * words {low, high} holding a 4x4x4 voxel block.
+ *
+ * Pointers named d_* are device pointers owned by the caller and borrowed for
+ * the duration of the call; h_* are host pointers.
+ */
+#ifndef HASHDAG_GB300_H
+#define HASHDAG_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HD_ABI_VERSION 1u
+#define HD_PAGE_SIZE 512u
+#define HD_MAX_DEPTH 20u
+/* Sentinel of the edit recursion (hash_dag_edits.h:17). */
+#define HD_INVALID_NODE 0xDFFFFFFu
+
+typedef struct hd_ctx hd_ctx;
+
+typedef enum hd_status {
+    HD_OK = 0,
+    HD_ERR_INVALID = 1,     /* bad argument or configuration            */
+    HD_ERR_CUDA = 2,        /* CUDA runtime error                       */
+    HD_ERR_POOL_FULL = 3,   /* physical page pool exhausted             */
+    HD_ERR_BUCKET_FULL = 4, /* a bucket ran past its virtual range      */
+    HD_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up       */
+    HD_ERR_OOM = 6,         /* device allocation failed                 */
+    HD_ERR_STATE = 7        /* call not valid in the context's state    */
+} hd_status;
+
+/* Table geometry.  The defaults are the reference's compile-time macros
+ * (typedefs.h:152-239): 9 top levels with 2^10 buckets of 1024 words, low
+ * levels with 2^16 buckets of 4096 words.  color_tree_levels is
+ * C_colorTreeLevels (hash_dag_globals.h:7): levels below it keep mask-only
+ * headers when edited, levels at or above it carry voxel counts. */
+typedef struct hd_config {
+    uint32_t depth;             /* SCENE_DEPTH: leaves sit at depth - 2     */
+    uint32_t color_tree_levels; /* C_colorTreeLevels                        */
+    uint32_t top_levels;        /* BUCKETS_NUM_TOP_LEVELS                   */
+    uint32_t top_bucket_bits;   /* BUCKETS_BITS_FOR_TOP_LEVELS              */
+    uint32_t low_bucket_bits;   /* BUCKETS_BITS_FOR_LOW_LEVELS              */
+    uint32_t top_bucket_size;   /* BUCKETS_SIZE_FOR_TOP_LEVELS (words)      */
+    uint32_t low_bucket_size;   /* BUCKETS_SIZE_FOR_LOW_LEVELS (words)      */
+    uint32_t pool_pages;        /* physical pages (HashTable::create arg)   */
+} hd_config;
+
+/* Camera in voxel space: Tracer::TracePathsParams (tracer.h:81-91) as built
+ * by get_trace_params (dag_tracer.cu:71-113).  Pixel (x, y) looks along
+ * normalize(ray_min + x * ray_ddx + y * ray_ddy - position). */
+typedef struct hd_camera {
+    double position[3];
+    double ray_min[3];
+    double ray_ddx[3];
+    double ray_ddy[3];
+} hd_camera;
+
+/* Edit tools (hash_dag_editors.h): sphere carve/fill (SphereEditor<bool>,
+ * :272-313), box carve/fill (BoxEditor<bool>, :223-270). */
+typedef enum hd_tool {
+    HD_TOOL_SPHERE_REMOVE = 0,
+    HD_TOOL_SPHERE_ADD = 1,
+    HD_TOOL_BOX_REMOVE = 2,
+    HD_TOOL_BOX_ADD = 3
+} hd_tool;
+
+typedef struct hd_edit {
+    uint32_t tool;      /* hd_tool */
+    float center[3];
+    float radius;       /* sphere radius, or box half extent */
+} hd_edit;
+
+/* Counters of one edit call (or a batch): the reference's EditStats
+ * (hash_dag_edits.h:39-49) plus find-or-add work. */
+typedef struct hd_edit_stats {
+    uint64_t num_voxels;        /* "num voxels" (hash_dag.h:374-378)        */
+    uint64_t num_nodes;         /* visited edit nodes ("num nodes")         */
+    uint64_t find_or_add_calls; /* leaf + interior find_or_add calls        */
+    uint64_t nodes_added;       /* appended nodes                           */
+    uint64_t words_scanned;     /* bucket words compared by the probes      */
+    float device_ms;            /* device time of the call                  */
+    float host_ms;              /* wall time of the call                    */
+} hd_edit_stats;
+
+/* Per-level occupancy of the table (HashTable::get_level_size,
+ * hash_table.cpp:277-285; get_virtual_used_size, :246-275;
+ * get_allocated_pages, hash_table.h:729-744). */
+typedef struct hd_level_stats {
+    uint64_t words[HD_MAX_DEPTH];   /* sum of bucket sizes (incl. padding)  */
+    uint64_t nodes[HD_MAX_DEPTH];   /* stored nodes (walk of every bucket)  */
+    uint64_t pages_used;            /* allocated physical pages             */
+    uint32_t root;                  /* firstNodeIndex                       */
+    uint32_t levels;                /* depth                                */
+} hd_level_stats;
+
+/* ---- lifetime (HashTable::create/destroy, hash_table.cpp:5-104) -------- */
+
+void hd_default_config(uint32_t depth, hd_config* out);
+/* HashTable::create(poolSizeInPages) on the device; every page of the pool
+ * and the page table start at zero. */
+hd_status hd_create(const hd_config* cfg, hd_ctx** out);
+hd_status hd_destroy(hd_ctx* ctx);
+const char* hd_last_error(const hd_ctx* ctx);
+uint32_t hd_abi_version(void);
+/* Binds the context to a cudaStream_t (NULL = legacy default stream). */
+hd_status hd_set_stream(hd_ctx* ctx, void* stream);
+hd_status hd_sync(hd_ctx* ctx);
+
+/* ---- scene ingest ------------------------------------------------------ */
+
+/* HashDAGFactory::load_from_DAG (hash_dag_factory.cpp:152-184): full nodes
+ * for levels leaf..1 first, then every BasicDAG node appended in depth-first
+ * first-visit order (create_hash_dag, :5-99).  h_words is a BasicDAG word
+ * array (basic_dag.h:11-40): root at word 0, interior nodes
+ * [header, absolute child word indices...], leaves two words. */
+hd_status hd_load_basic_dag(hd_ctx* ctx, const uint32_t* h_words, uint64_t n_words);
+/* Seeded procedural scene (fractal value-noise height field unioned with
+ * 64 spheres) voxelised on the device straight into a BasicDAG, then
+ * imported as hd_load_basic_dag does.  The words of the BasicDAG can be read
+ * back with hd_export_basic_dag. */
+hd_status hd_generate_scene(hd_ctx* ctx, uint64_t seed);
+hd_status hd_export_basic_dag(hd_ctx* ctx, uint32_t* h_words, uint64_t capacity, uint64_t* n_words);
+
+/* ---- traversal (DAGTracer, dag_tracer.cu:116-219) ---------------------- */
+
+/* Tracer::trace_paths (tracer.cu:145-252): one primary ray per pixel,
+ * nearest hit voxel path written as uint4 (x, y, z, 0) at row
+ * (height - 1 - y), or (0, 0, 0, 0) on a miss.  d_paths holds
+ * width * height * 4 uint32. */
+hd_status hd_trace_primary(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint32_t height,
+                           uint32_t* d_paths, float* ms);
+/* Tracer::trace_shadows (tracer.cu:589-697) reduced to its hit test: from
+ * the exact hit point of each pixel's primary ray (ray_box_intersection,
+ * :574-587) plus bias * light, an any-hit ray toward light
+ * (intersect_ray_node_out_of_order, :453-543).  d_mask[i] = 1 if shadowed,
+ * 0 if lit, 2 if the pixel has no primary hit.  light is normalised on the
+ * device as the reference's sun_direction (:546-549). */
+hd_status hd_trace_shadow(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint32_t height,
+                          const uint32_t* d_paths, const float light[3], float bias,
+                          uint8_t* d_mask, float* ms);
+/* Primary + shadow in one call: the per-frame traversal step. */
+hd_status hd_trace_frame(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint32_t height,
+                         const float light[3], float bias, uint32_t* d_paths, uint8_t* d_mask,
+                         float* ms_primary, float* ms_shadow);
+/* Selects the arithmetic of the ray set-up: 0 = every float/double op
+ * rounded on its own, 1 = the fused multiply-adds nvcc contracts in the
+ * reference's default build.  Default 1. */
+hd_status hd_set_fp_mode(hd_ctx* ctx, uint32_t mode);
+
+/* ---- point queries (DAGUtils::get_value, dag_utils.h:138-172) ---------- */
+
+/* d_xyz: n x 3 uint32 voxel coordinates; d_out: n uint8 occupancy. */
+hd_status hd_get_values(hd_ctx* ctx, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out);
+
+/* ---- edits (HashDAG::edit_threads, hash_dag.h:255-405) ----------------- */
+
+/* One edit: the editor's top-down descent with the reference's early exits
+ * (should_edit / is_empty / is_full, hash_dag_edits.h:356-444), the 64-voxel
+ * leaf rebuild (:451-546), then bottom-up find_or_add of every changed node
+ * (hash_table.h:470-560), level by level, in depth-first order. */
+hd_status hd_edit_apply(hd_ctx* ctx, const hd_edit* edit, hd_edit_stats* stats);
+/* A sequence of edits applied in order with the same result as calling
+ * hd_edit_apply for each; runs as one device-driven pipeline with no host round
+ * trip between edits. */
+hd_status hd_edit_batch(hd_ctx* ctx, const hd_edit* edits, uint32_t n, hd_edit_stats* stats);
+
+/* ---- garbage collection (HashDAG::remove_stale_nodes, hash_dag.h:407-547) */
+
+/* Marks the nodes reachable from the root and from the n extra roots, then
+ * rebuilds every level bottom-up: buckets emptied, full node re-added first,
+ * live nodes re-appended in increasing old-address order with children
+ * remapped.  Pages stay mapped (the reference never unmaps them). */
+hd_status hd_gc(hd_ctx* ctx, const uint32_t* h_extra_roots, uint32_t n_extra);
+
+/* ---- state and statistics ---------------------------------------------- */
+
+hd_status hd_get_root(hd_ctx* ctx, uint32_t* root);
+hd_status hd_set_root(hd_ctx* ctx, uint32_t root);
+hd_status hd_get_config(hd_ctx* ctx, hd_config* cfg);
+hd_status hd_get_level_stats(hd_ctx* ctx, hd_level_stats* out);
+/* Copies the table to the host.  Arrays sized by hd_table_sizes: bucket
+ * sizes (total buckets), page table (virtual pages), pool (pages_used + 1
+ * pages of 512 words; page 0 is the reserved null page), full-node indices
+ * (depth). Any pointer may be NULL to skip that array. */
+hd_status hd_table_sizes(hd_ctx* ctx, uint64_t* n_buckets, uint64_t* n_virtual_pages,
+                         uint64_t* n_pool_pages_used);
+hd_status hd_export_table(hd_ctx* ctx, uint32_t* h_bucket_sizes, uint32_t* h_page_table,
+                          uint32_t* h_pool, uint64_t pool_words_capacity,
+                          uint32_t* h_full_nodes);
+/* Replaces the table with host copies (pool_words = pages * 512). */
+hd_status hd_import_table(hd_ctx* ctx, const uint32_t* h_bucket_sizes, const uint32_t* h_page_table,
+                          const uint32_t* h_pool, uint64_t pool_words,
+                          const uint32_t* h_full_nodes, uint32_t root);
+/* Device pointers of the table (for zero-copy consumers): pool, page
+ * table, bucket sizes. */
+hd_status hd_device_table(hd_ctx* ctx, uint32_t** d_pool, uint32_t** d_page_table,
+                          uint32_t** d_bucket_sizes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HASHDAG_GB300_H */

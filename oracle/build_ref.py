@@ -1,0 +1,56 @@
+"""ORACLE — builds the reference's own code from its sources (test
+infrastructure only).
+
+    python oracle/build_ref.py [depth] [color_tree_levels] [top_bucket_bits]
+
+Compiles oracle/refharness/ref_host.cpp, which #includes the reference's
+unmodified host sources (hash_table.cpp, stats.cpp, hash_dag_factory.cpp and
+the headers of the edit path) from /root/reference/src, into
+oracle/_ref/libhdref_d<D>_t<T>_b<B>.so.  No reference file is copied; the
+output directory is git-ignored.  Build flags follow the reference's
+parity build: -O2 -ffp-contract=off, no fast-math.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = "/root/reference"
+OUT = os.path.join(HERE, "_ref")
+
+
+def lib_path(depth, ctl, top_bits):
+    return os.path.join(OUT, f"libhdref_d{depth}_t{ctl}_b{top_bits}.so")
+
+
+def available():
+    return os.path.isdir(os.path.join(REF, "src"))
+
+
+def build(depth, ctl, top_bits, force=False):
+    out = lib_path(depth, ctl, top_bits)
+    if os.path.exists(out) and not force:
+        return out
+    if not available():
+        raise FileNotFoundError("reference sources are not present on this machine")
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(REF, "src")
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-w",
+           "-DBENCHMARK=1", "-DUSE_BLOOM_FILTER=0", "-DEDITS_ENABLE_COLORS=0", "-DEDITS_COUNTERS=1",
+           "-DENABLE_CHECKS=0", "-DTRACK_GLOBAL_NEWDELETE=0",
+           f"-DHARNESS_DEPTH={depth}", f"-DBUCKETS_BITS_FOR_TOP_LEVELS={top_bits}",
+           f"-DC_colorTreeLevels=CTL_VALUE = {ctl}, CTL_IGNORED",
+           "-I", os.path.join(HERE, "refharness", "shim"),
+           "-I", src, "-I", os.path.join(src, "dags"), "-I", os.path.join(src, "dags", "hash_dag"),
+           "-I", os.path.join(src, "gmath"), "-I", "/usr/local/cuda/include",
+           os.path.join(HERE, "refharness", "ref_host.cpp"), "-o", out + ".tmp"]
+    subprocess.check_call(cmd)
+    os.replace(out + ".tmp", out)
+    return out
+
+
+if __name__ == "__main__":
+    d = int(sys.argv[1]) if len(sys.argv) > 1 else 10
+    t = int(sys.argv[2]) if len(sys.argv) > 2 else min(10, d - 5)
+    b = int(sys.argv[3]) if len(sys.argv) > 3 else (10 if d <= 10 else 12)
+    print(build(d, t, b, force=True))

@@ -1,0 +1,1770 @@
+/*
+ * ORACLE — test infrastructure only (see hd_oracle.h).  Plain-C restatement
+ * of the reference's hashed-DAG hot path; every function cites the
+ * reference file:line it follows.  Build: oracle/build_oracle.py
+ * (gcc -O2 -ffp-contract=off -fno-fast-math).
+ */
+#include "hd_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define PAGE HD_PAGE_SIZE
+#define NOT_FOUND 0xFFFFFFFFu
+#define INVALID HD_INVALID_NODE
+
+/* ======================================================================
+ * Geometry (hash_table.h:19-77, hash_dag_globals.h:10-30)
+ * ====================================================================== */
+
+static uint32_t bucket_count(const hd_config* c, uint32_t level)
+{
+    return level < c->top_levels ? (1u << c->top_bucket_bits) : (1u << c->low_bucket_bits);
+}
+static uint32_t bucket_capacity(const hd_config* c, uint32_t level)
+{
+    return level < c->top_levels ? c->top_bucket_size : c->low_bucket_size;
+}
+static uint32_t n_top(const hd_config* c)
+{
+    return c->top_levels < c->depth ? c->top_levels : c->depth;
+}
+/* get_bucket_global_index (hash_table.h:19-36) */
+static uint32_t bucket_global(const hd_config* c, uint32_t level, uint32_t bucket)
+{
+    if (level < c->top_levels)
+        return level * (1u << c->top_bucket_bits) + bucket;
+    return n_top(c) * (1u << c->top_bucket_bits) + (level - c->top_levels) * (1u << c->low_bucket_bits) + bucket;
+}
+/* make_ptr (hash_table.h:45-63) */
+uint32_t or_make_ptr(const hd_config* c, uint32_t level, uint32_t bucket, uint32_t pos)
+{
+    uint64_t index;
+    if (level < c->top_levels)
+        index = ((uint64_t)level * (1u << c->top_bucket_bits) + bucket) * c->top_bucket_size;
+    else
+        index = (uint64_t)n_top(c) * (1u << c->top_bucket_bits) * c->top_bucket_size +
+                ((uint64_t)(level - c->top_levels) * (1u << c->low_bucket_bits) + bucket) * c->low_bucket_size;
+    return (uint32_t)(index + pos);
+}
+uint64_t or_total_buckets(const hd_config* c)
+{
+    uint64_t low = c->depth > c->top_levels ? c->depth - c->top_levels : 0;
+    return (uint64_t)n_top(c) * (1u << c->top_bucket_bits) + low * (1u << c->low_bucket_bits);
+}
+uint64_t or_total_virtual_pages(const hd_config* c)
+{
+    uint64_t low = c->depth > c->top_levels ? c->depth - c->top_levels : 0;
+    return ((uint64_t)n_top(c) * (1u << c->top_bucket_bits) * c->top_bucket_size +
+            low * (1u << c->low_bucket_bits) * c->low_bucket_size) / PAGE;
+}
+
+/* ======================================================================
+ * Hashes (utils.h:355-396, hash_table.h:80-89)
+ * ====================================================================== */
+
+uint32_t or_murmurhash32(uint32_t h)
+{
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+uint64_t or_murmurhash64(uint64_t h)
+{
+    h ^= h >> 33;
+    h *= 0xff51afd7ed558ccdull;
+    h ^= h >> 33;
+    h *= 0xc4ceb9fe1a85ec53ull;
+    h ^= h >> 33;
+    return h;
+}
+/* murmurhash32xN with seed 0 (utils.h:375-396, USE_ALTERNATE_HASH) */
+static uint32_t murmurhash32xN(const uint32_t* ph, uint32_t n)
+{
+    uint32_t h = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t k = ph[i];
+        k *= 0xcc9e2d51u;
+        k = (k << 15) | (k >> 17);
+        k *= 0x1b873593u;
+        h ^= k;
+        h = (h << 13) | (h >> 19);
+        h = h * 5u + 0xe6546b64u;
+    }
+    h ^= n;
+    return or_murmurhash32(h);
+}
+uint32_t or_hash_leaf(uint64_t leaf) { return (uint32_t)or_murmurhash64(leaf); }
+uint32_t or_hash_interior(uint32_t n, const uint32_t* node) { return murmurhash32xN(node, n); }
+
+static uint32_t popc32(uint32_t v) { return (uint32_t)__builtin_popcount(v); }
+static uint32_t popc64(uint64_t v) { return (uint32_t)__builtin_popcountll(v); }
+/* Utils::total_size / child_offset (utils.h:343-354) */
+static uint32_t total_size(uint32_t header) { return popc32(header & 0xffu) + 1; }
+static uint32_t child_offset(uint32_t mask, uint32_t child) { return popc32(mask & ((1u << child) - 1u)) + 1; }
+
+/* ======================================================================
+ * Paged hash table (hash_table.h:137-898, hash_table.cpp)
+ * ====================================================================== */
+
+struct or_table {
+    hd_config cfg;
+    uint32_t leaf_level;
+    uint32_t* pool;        /* pool_pages * PAGE words (physical)            */
+    uint32_t* page_table;  /* virtual page -> physical page (0 = unmapped)  */
+    uint32_t* bucket_sizes;
+    uint64_t n_buckets, n_vpages;
+    uint32_t pool_top;     /* poolTop (hash_table.h:818): starts at 1       */
+    uint32_t full[HD_MAX_DEPTH];
+    uint64_t level_nodes[HD_MAX_DEPTH];
+    uint32_t root;
+    int error;
+    /* find-or-add counters of the current edit */
+    uint64_t foa_calls, nodes_added, words_scanned;
+};
+
+static uint64_t unique_sorted(uint32_t* v, uint64_t n);
+
+static void set_error(or_table* t, int e)
+{
+    if (!t->error)
+        t->error = e;
+}
+
+or_table* or_table_create(const hd_config* cfg)
+{
+    if (!cfg || cfg->depth < 4 || cfg->depth > HD_MAX_DEPTH || cfg->color_tree_levels > cfg->depth - 2)
+        return NULL;
+    or_table* t = (or_table*)calloc(1, sizeof(or_table));
+    t->cfg = *cfg;
+    t->leaf_level = cfg->depth - 2;
+    t->n_buckets = or_total_buckets(cfg);
+    t->n_vpages = or_total_virtual_pages(cfg);
+    t->pool = (uint32_t*)calloc((size_t)cfg->pool_pages * PAGE, sizeof(uint32_t));
+    t->page_table = (uint32_t*)calloc(t->n_vpages, sizeof(uint32_t));
+    t->bucket_sizes = (uint32_t*)calloc(t->n_buckets, sizeof(uint32_t));
+    t->pool_top = 1;
+    if (!t->pool || !t->page_table || !t->bucket_sizes) {
+        or_table_destroy(t);
+        return NULL;
+    }
+    return t;
+}
+void or_table_destroy(or_table* t)
+{
+    if (!t)
+        return;
+    free(t->pool);
+    free(t->page_table);
+    free(t->bucket_sizes);
+    free(t);
+}
+int or_table_error(const or_table* t) { return t->error; }
+uint32_t or_table_root(const or_table* t) { return t->root; }
+void or_table_set_root(or_table* t, uint32_t root) { t->root = root; }
+const uint32_t* or_table_full_nodes(const or_table* t) { return t->full; }
+uint32_t or_table_pool_top(const or_table* t) { return t->pool_top; }
+
+/* get_sys_ptr (hash_table.h:155-173) */
+static uint32_t* sys_ptr(const or_table* t, uint32_t vptr)
+{
+    uint32_t phys = t->page_table[vptr / PAGE];
+    return t->pool + (uint64_t)phys * PAGE + (vptr % PAGE);
+}
+uint32_t or_read_word(const or_table* t, uint32_t vptr) { return *sys_ptr(t, vptr); }
+
+/* allocate_page (hash_table.h:794-809) */
+static void allocate_page(or_table* t, uint32_t page)
+{
+    if (t->pool_top >= t->cfg.pool_pages) {
+        set_error(t, HD_ERR_POOL_FULL);
+        return;
+    }
+    t->page_table[page] = t->pool_top++;
+}
+
+/* find_leaf_node_in_bucket (hash_table.h:196-274), Bloom filter off */
+static uint32_t find_leaf(or_table* t, uint32_t bucket_size, uint32_t bucket, uint64_t leaf)
+{
+    const uint32_t level = t->leaf_level;
+    const uint32_t base = or_make_ptr(&t->cfg, level, bucket, 0);
+    for (uint32_t pindex = 0; pindex < bucket_size; pindex += PAGE) {
+        const uint32_t* p = sys_ptr(t, base + pindex);
+        uint32_t end = bucket_size < pindex + PAGE ? bucket_size : pindex + PAGE;
+        for (uint32_t index = pindex; index < end; index += 2, p += 2) {
+            uint64_t bits = (uint64_t)p[0] | ((uint64_t)p[1] << 32);
+            if (bits == leaf) {
+                t->words_scanned += index + 2;
+                return base + index;
+            }
+        }
+    }
+    t->words_scanned += bucket_size;
+    return NOT_FOUND;
+}
+
+/* find_interior_node_in_bucket (hash_table.h:276-357).  Note the two
+ * boundary rules kept as written: the scan returns "not found" as soon as a
+ * page holds no more than n used words, and a node is only compared while
+ * index < pageEnd - n, so a node flush with the bucket tail or the page end
+ * is never found by a query of its own size. */
+static uint32_t find_interior(or_table* t, uint32_t bucket_size, uint32_t level, uint32_t bucket,
+                              uint32_t n, const uint32_t* node)
+{
+    const uint32_t base = or_make_ptr(&t->cfg, level, bucket, 0);
+    for (uint32_t pindex = 0; pindex < bucket_size; pindex += PAGE) {
+        const uint32_t* page = sys_ptr(t, base + pindex);
+        uint32_t page_end = bucket_size < pindex + PAGE ? bucket_size : pindex + PAGE;
+        if (pindex + n >= page_end) {
+            t->words_scanned += bucket_size;
+            return NOT_FOUND;
+        }
+        page_end -= n;
+        for (uint32_t index = pindex; index < page_end;) {
+            const uint32_t* p = page + (index - pindex);
+            if (memcmp(node, p, n * sizeof(uint32_t)) == 0) {
+                t->words_scanned += index + n;
+                return base + index;
+            }
+            index += total_size(*p);
+        }
+    }
+    t->words_scanned += bucket_size;
+    return NOT_FOUND;
+}
+
+/* add_leaf_node (hash_table.h:359-400) */
+static uint32_t add_leaf(or_table* t, uint64_t leaf, uint32_t hash)
+{
+    const uint32_t level = t->leaf_level;
+    const uint32_t bucket = hash & (bucket_count(&t->cfg, level) - 1);
+    uint32_t* size_ptr = &t->bucket_sizes[bucket_global(&t->cfg, level, bucket)];
+    const uint32_t size = *size_ptr;
+    if (size + 2 > bucket_capacity(&t->cfg, level)) {
+        set_error(t, HD_ERR_BUCKET_FULL);
+        return INVALID;
+    }
+    const uint32_t ptr = or_make_ptr(&t->cfg, level, bucket, size);
+    const uint32_t page = ptr / PAGE;
+    if (size % PAGE == 0 && t->page_table[page] == 0)
+        allocate_page(t, page);
+    if (t->error)
+        return INVALID;
+    uint32_t* p = sys_ptr(t, ptr);
+    p[0] = (uint32_t)leaf;
+    p[1] = (uint32_t)(leaf >> 32);
+    *size_ptr = size + 2;
+    t->level_nodes[level]++;
+    t->nodes_added++;
+    return ptr;
+}
+
+/* add_interior_node (hash_table.h:401-468): a node never straddles a page;
+ * the rest of the page is skipped as padding. */
+static uint32_t add_interior(or_table* t, uint32_t level, uint32_t n, const uint32_t* node, uint32_t hash)
+{
+    const uint32_t bucket = hash & (bucket_count(&t->cfg, level) - 1);
+    uint32_t* size_ptr = &t->bucket_sizes[bucket_global(&t->cfg, level, bucket)];
+    uint32_t size = *size_ptr;
+    const uint32_t left = PAGE - (size % PAGE);
+    uint32_t ptr;
+    if (left == PAGE || left < n) {
+        if (left != PAGE)
+            size += left;
+        if (size + n > bucket_capacity(&t->cfg, level)) {
+            set_error(t, HD_ERR_BUCKET_FULL);
+            return INVALID;
+        }
+        ptr = or_make_ptr(&t->cfg, level, bucket, size);
+        if (t->page_table[ptr / PAGE] == 0)
+            allocate_page(t, ptr / PAGE);
+    } else {
+        if (size + n > bucket_capacity(&t->cfg, level)) {
+            set_error(t, HD_ERR_BUCKET_FULL);
+            return INVALID;
+        }
+        ptr = or_make_ptr(&t->cfg, level, bucket, size);
+    }
+    if (t->error)
+        return INVALID;
+    uint32_t* p = sys_ptr(t, ptr);
+    for (uint32_t i = 0; i < n; i++)
+        p[i] = node[i];
+    *size_ptr = size + n;
+    t->level_nodes[level]++;
+    t->nodes_added++;
+    return ptr;
+}
+
+/* find_or_add_leaf_node (hash_table.h:470-514), single writer */
+uint32_t or_find_or_add_leaf(or_table* t, uint64_t leaf)
+{
+    const uint32_t level = t->leaf_level;
+    const uint32_t hash = or_hash_leaf(leaf);
+    const uint32_t bucket = hash & (bucket_count(&t->cfg, level) - 1);
+    const uint32_t size = t->bucket_sizes[bucket_global(&t->cfg, level, bucket)];
+    t->foa_calls++;
+    uint32_t r = find_leaf(t, size, bucket, leaf);
+    if (r == NOT_FOUND)
+        r = add_leaf(t, leaf, hash);
+    return r;
+}
+/* find_or_add_interior_node (hash_table.h:515-560), single writer */
+uint32_t or_find_or_add_interior(or_table* t, uint32_t level, uint32_t n, const uint32_t* node)
+{
+    const uint32_t hash = or_hash_interior(n, node);
+    const uint32_t bucket = hash & (bucket_count(&t->cfg, level) - 1);
+    const uint32_t size = t->bucket_sizes[bucket_global(&t->cfg, level, bucket)];
+    t->foa_calls++;
+    uint32_t r = find_interior(t, size, level, bucket, n, node);
+    if (r == NOT_FOUND)
+        r = add_interior(t, level, n, node, hash);
+    return r;
+}
+
+/* add_full_node (hash_table.h:749-789) */
+static void add_full_node(or_table* t, uint32_t level)
+{
+    if (level == t->leaf_level) {
+        const uint64_t leaf = ~0ull;
+        t->full[level] = add_leaf(t, leaf, or_hash_leaf(leaf));
+    } else {
+        const uint32_t depth = t->cfg.depth - level;
+        const uint32_t voxels = level < t->cfg.color_tree_levels ? 0u : (1u << (3 * depth));
+        uint32_t node[9];
+        node[0] = (voxels << 8) | 0xffu;
+        for (uint32_t c = 0; c < 8; c++)
+            node[1 + c] = t->full[level + 1];
+        t->full[level] = add_interior(t, level, 9, node, or_hash_interior(9, node));
+    }
+}
+
+void or_table_export(const or_table* t, uint32_t* bucket_sizes, uint32_t* page_table, uint32_t* pool,
+                     uint64_t pool_words_capacity, uint32_t* full_nodes)
+{
+    if (bucket_sizes)
+        memcpy(bucket_sizes, t->bucket_sizes, t->n_buckets * sizeof(uint32_t));
+    if (page_table)
+        memcpy(page_table, t->page_table, t->n_vpages * sizeof(uint32_t));
+    if (pool) {
+        uint64_t words = (uint64_t)t->pool_top * PAGE;
+        if (words > pool_words_capacity)
+            words = pool_words_capacity;
+        memcpy(pool, t->pool, words * sizeof(uint32_t));
+    }
+    if (full_nodes)
+        memcpy(full_nodes, t->full, t->cfg.depth * sizeof(uint32_t));
+}
+
+int or_table_import(or_table* t, const uint32_t* bucket_sizes, const uint32_t* page_table, const uint32_t* pool,
+                    uint64_t pool_words, const uint32_t* full_nodes, uint32_t root)
+{
+    if (pool_words > (uint64_t)t->cfg.pool_pages * PAGE || pool_words % PAGE)
+        return HD_ERR_INVALID;
+    memcpy(t->bucket_sizes, bucket_sizes, t->n_buckets * sizeof(uint32_t));
+    memcpy(t->page_table, page_table, t->n_vpages * sizeof(uint32_t));
+    memset(t->pool, 0, (size_t)t->cfg.pool_pages * PAGE * sizeof(uint32_t));
+    memcpy(t->pool, pool, pool_words * sizeof(uint32_t));
+    memcpy(t->full, full_nodes, t->cfg.depth * sizeof(uint32_t));
+    t->pool_top = (uint32_t)(pool_words / PAGE);
+    t->root = root;
+    /* node counts are not part of the reference's table: recount by walks */
+    for (uint32_t level = 0; level < t->cfg.depth - 1; level++) {
+        uint64_t count = 0;
+        for (uint32_t b = 0; b < bucket_count(&t->cfg, level); b++) {
+            uint32_t size = t->bucket_sizes[bucket_global(&t->cfg, level, b)];
+            if (level == t->leaf_level) {
+                count += size / 2;
+                continue;
+            }
+            uint32_t base = or_make_ptr(&t->cfg, level, b, 0);
+            for (uint32_t pindex = 0; pindex < size; pindex += PAGE) {
+                uint32_t end = size < pindex + PAGE ? size : pindex + PAGE;
+                uint32_t i = pindex;
+                while (i < end) {
+                    uint32_t h = *sys_ptr(t, base + i);
+                    if ((h & 0xffu) == 0)
+                        break; /* zero padding to the page end */
+                    i += total_size(h);
+                    count++;
+                }
+            }
+        }
+        t->level_nodes[level] = count;
+    }
+    return HD_OK;
+}
+
+void or_level_stats(const or_table* t, hd_level_stats* out)
+{
+    memset(out, 0, sizeof(*out));
+    for (uint32_t level = 0; level < t->cfg.depth - 1; level++) {
+        uint64_t words = 0;
+        for (uint32_t b = 0; b < bucket_count(&t->cfg, level); b++)
+            words += t->bucket_sizes[bucket_global(&t->cfg, level, b)];
+        out->words[level] = words;
+        out->nodes[level] = t->level_nodes[level];
+    }
+    out->pages_used = t->pool_top - 1;
+    out->root = t->root;
+    out->levels = t->cfg.depth;
+}
+
+/* ======================================================================
+ * Seeded scene generator (own format; identical integer arithmetic on the
+ * device in hashdag_gb300/csrc/hd_scene.cu).
+ *   height(x, z) = E/2 + floor(E/4 * fbm(x, z) / 1.9375), fbm = 5 octaves of
+ *   value noise (lattice period E/4 >> o, amplitude 2^-o, smoothstep
+ *   interpolation), all in Q16 fixed point;  solid = {y <= height} united
+ *   with 64 spheres (centres uniform in [0, E)^3, radius uniform in [8, 64]).
+ * ====================================================================== */
+
+static uint64_t mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static int64_t lattice(uint64_t seed, uint32_t octave, uint32_t i, uint32_t j)
+{
+    uint64_t k = mix64(seed ^ mix64(((uint64_t)octave << 58) ^ ((uint64_t)i << 29) ^ (uint64_t)j));
+    return (int64_t)(k >> 47) - 65536;
+}
+static int64_t smooth_q16(int64_t t) { return (t * t * (3 * 65536 - 2 * t)) >> 32; }
+static int64_t floor_div(int64_t a, int64_t b)
+{
+    int64_t q = a / b;
+    if ((a % b) != 0 && a < 0)
+        q -= 1;
+    return q;
+}
+int32_t or_scene_height(uint64_t seed, uint32_t depth, uint32_t x, uint32_t z)
+{
+    int64_t total = 0;
+    for (uint32_t o = 0; o < 5; o++) {
+        const uint32_t lp = depth - 2 - o; /* log2 of the lattice period */
+        const uint32_t i = x >> lp, j = z >> lp;
+        const uint32_t fx = x & ((1u << lp) - 1), fz = z & ((1u << lp) - 1);
+        const int64_t sx = smooth_q16((int64_t)(((uint64_t)fx << 16) >> lp));
+        const int64_t sz = smooth_q16((int64_t)(((uint64_t)fz << 16) >> lp));
+        const int64_t v00 = lattice(seed, o, i, j), v10 = lattice(seed, o, i + 1, j);
+        const int64_t v01 = lattice(seed, o, i, j + 1), v11 = lattice(seed, o, i + 1, j + 1);
+        const int64_t a = v00 + (((v10 - v00) * sx) >> 16);
+        const int64_t b = v01 + (((v11 - v01) * sx) >> 16);
+        const int64_t n = a + (((b - a) * sz) >> 16);
+        total += n >> o;
+    }
+    const int64_t e = (int64_t)1 << depth;
+    return (int32_t)((e >> 1) + floor_div(total * e, 31 * 16384));
+}
+void or_scene_spheres(uint64_t seed, uint32_t depth, int64_t* out)
+{
+    uint64_t state = seed ^ 0x5EED5EED12345678ull;
+    const uint64_t mask = ((uint64_t)1 << depth) - 1;
+    for (int s = 0; s < 64; s++) {
+        state += 0x9E3779B97F4A7C15ull;
+        out[4 * s + 0] = (int64_t)(mix64(state) & mask);
+        state += 0x9E3779B97F4A7C15ull;
+        out[4 * s + 1] = (int64_t)(mix64(state) & mask);
+        state += 0x9E3779B97F4A7C15ull;
+        out[4 * s + 2] = (int64_t)(mix64(state) & mask);
+        state += 0x9E3779B97F4A7C15ull;
+        out[4 * s + 3] = 8 + (int64_t)(mix64(state) % 57);
+    }
+}
+static int in_sphere(const int64_t* s, int64_t x, int64_t y, int64_t z)
+{
+    int64_t dx = x - s[0], dy = y - s[1], dz = z - s[2];
+    return dx * dx + dy * dy + dz * dz <= s[3] * s[3];
+}
+int or_scene_solid(uint64_t seed, uint32_t depth, uint32_t x, uint32_t y, uint32_t z)
+{
+    if ((int64_t)y <= or_scene_height(seed, depth, x, z))
+        return 1;
+    int64_t sp[256];
+    or_scene_spheres(seed, depth, sp);
+    for (int s = 0; s < 64; s++)
+        if (in_sphere(sp + 4 * s, x, y, z))
+            return 1;
+    return 0;
+}
+
+/* --- BasicDAG construction: top-down classification, bottom-up dedup --- */
+
+typedef struct {
+    uint64_t* keys;   /* per entry: content hash                      */
+    uint32_t* ids;    /* entry -> node id + 1 (0 = empty slot)        */
+    uint64_t cap;
+} dedup_map;
+
+typedef struct {
+    /* per node: mask, count, first child slot in `kids` (interior) or the
+     * 64-bit leaf mask */
+    uint64_t n, cap;
+    uint8_t* mask;
+    uint64_t* count;
+    uint64_t* leaf;
+    uint32_t* kid0;
+    uint32_t* kids;
+    uint64_t nkids, capkids;
+    dedup_map map;
+} gen_level;
+
+typedef struct {
+    uint64_t seed;
+    uint32_t depth, leaf_level, T;
+    int32_t* hmin[HD_MAX_DEPTH]; /* min/max of the height over each node footprint, per level */
+    int32_t* hmax[HD_MAX_DEPTH];
+    int64_t spheres[256];
+    gen_level lv[HD_MAX_DEPTH];
+    uint32_t full_id[HD_MAX_DEPTH];
+} gen_ctx;
+
+#define GEN_EMPTY 0xFFFFFFFFu
+
+static void map_grow(dedup_map* m, gen_level* L, int is_leaf);
+
+static uint64_t node_key(const gen_level* L, uint32_t id, int is_leaf)
+{
+    if (is_leaf)
+        return mix64(L->leaf[id] ^ 0x1EAF1EAF1EAF1EAFull);
+    uint64_t h = mix64(L->mask[id]);
+    uint32_t nk = popc32(L->mask[id]);
+    for (uint32_t k = 0; k < nk; k++)
+        h = mix64(h ^ L->kids[L->kid0[id] + k]);
+    return h;
+}
+
+static uint32_t level_insert(gen_level* L, int is_leaf, uint8_t mask, uint64_t count, uint64_t leaf,
+                             const uint32_t* kids)
+{
+    /* tentatively append, then dedup */
+    if (L->n == L->cap) {
+        L->cap = L->cap ? 2 * L->cap : 1024;
+        L->mask = (uint8_t*)realloc(L->mask, L->cap);
+        L->count = (uint64_t*)realloc(L->count, L->cap * 8);
+        L->leaf = (uint64_t*)realloc(L->leaf, L->cap * 8);
+        L->kid0 = (uint32_t*)realloc(L->kid0, L->cap * 4);
+    }
+    uint32_t nk = is_leaf ? 0 : popc32(mask);
+    if (L->nkids + nk > L->capkids) {
+        L->capkids = L->capkids ? 2 * L->capkids + nk : 4096;
+        L->kids = (uint32_t*)realloc(L->kids, L->capkids * 4);
+    }
+    uint32_t id = (uint32_t)L->n;
+    L->mask[id] = mask;
+    L->count[id] = count;
+    L->leaf[id] = leaf;
+    L->kid0[id] = (uint32_t)L->nkids;
+    for (uint32_t k = 0; k < nk; k++)
+        L->kids[L->nkids + k] = kids[k];
+    if (2 * (L->n + 1) > L->map.cap)
+        map_grow(&L->map, L, is_leaf);
+    uint64_t key = node_key(L, id, is_leaf);
+    uint64_t slot = key & (L->map.cap - 1);
+    for (;;) {
+        uint32_t e = L->map.ids[slot];
+        if (e == 0)
+            break;
+        uint32_t other = e - 1;
+        if (L->map.keys[slot] == key) {
+            int same;
+            if (is_leaf)
+                same = L->leaf[other] == leaf;
+            else
+                same = L->mask[other] == mask &&
+                       memcmp(L->kids + L->kid0[other], kids, nk * sizeof(uint32_t)) == 0;
+            if (same)
+                return other;
+        }
+        slot = (slot + 1) & (L->map.cap - 1);
+    }
+    L->map.ids[slot] = id + 1;
+    L->map.keys[slot] = key;
+    L->n++;
+    L->nkids += nk;
+    return id;
+}
+
+static void map_grow(dedup_map* m, gen_level* L, int is_leaf)
+{
+    uint64_t ncap = m->cap ? 2 * m->cap : 4096;
+    uint64_t* keys = (uint64_t*)calloc(ncap, 8);
+    uint32_t* ids = (uint32_t*)calloc(ncap, 4);
+    for (uint64_t id = 0; id < L->n; id++) {
+        uint64_t key = node_key(L, (uint32_t)id, is_leaf);
+        uint64_t slot = key & (ncap - 1);
+        while (ids[slot])
+            slot = (slot + 1) & (ncap - 1);
+        ids[slot] = (uint32_t)id + 1;
+        keys[slot] = key;
+    }
+    free(m->keys);
+    free(m->ids);
+    m->keys = keys;
+    m->ids = ids;
+    m->cap = ncap;
+}
+
+static uint32_t gen_full(gen_ctx* g, uint32_t level)
+{
+    if (g->full_id[level] != GEN_EMPTY)
+        return g->full_id[level];
+    uint32_t id;
+    if (level == g->leaf_level) {
+        id = level_insert(&g->lv[level], 1, 0xff, 64, ~0ull, NULL);
+    } else {
+        uint32_t child = gen_full(g, level + 1);
+        uint32_t kids[8];
+        for (int c = 0; c < 8; c++)
+            kids[c] = child;
+        uint64_t count = (uint64_t)1 << (3 * (g->depth - level));
+        id = level_insert(&g->lv[level], 0, 0xff, count, 0, kids);
+    }
+    g->full_id[level] = id;
+    return id;
+}
+
+/* 0 = empty, 1 = full, 2 = maybe mixed */
+static int classify(const gen_ctx* g, uint32_t level, uint32_t x0, uint32_t y0, uint32_t z0,
+                    const uint8_t* live, uint8_t* live_out)
+{
+    const uint32_t shift = g->depth - level;
+    const int64_t s = (int64_t)1 << shift;
+    const uint64_t cell = ((uint64_t)(x0 >> shift) << level) | (z0 >> shift);
+    const int64_t hmin = g->hmin[level][cell], hmax = g->hmax[level][cell];
+    int full = (int64_t)y0 + s - 1 <= hmin;
+    int touched = (int64_t)y0 <= hmax;
+    for (int k = 0; k < 64; k++) {
+        live_out[k] = 0;
+        if (!live[k])
+            continue;
+        const int64_t* sp = g->spheres + 4 * k;
+        int64_t lo[3] = {x0, y0, z0};
+        int64_t d2near = 0, d2far = 0;
+        for (int a = 0; a < 3; a++) {
+            int64_t c = sp[a], l = lo[a], h = lo[a] + s - 1;
+            int64_t dn = c < l ? l - c : (c > h ? c - h : 0);
+            int64_t df = (c - l) > (h - c) ? (c - l) : (h - c);
+            d2near += dn * dn;
+            d2far += df * df;
+        }
+        if (d2near <= sp[3] * sp[3]) {
+            live_out[k] = 1;
+            touched = 1;
+            if (d2far <= sp[3] * sp[3])
+                full = 1;
+        }
+    }
+    if (full)
+        return 1;
+    if (!touched)
+        return 0;
+    return 2;
+}
+
+/* returns node id at `level` or GEN_EMPTY; *count = voxels */
+static uint32_t gen_build(gen_ctx* g, uint32_t level, uint32_t x0, uint32_t y0, uint32_t z0,
+                          const uint8_t* live, uint64_t* count)
+{
+    uint8_t live2[64];
+    int cls = classify(g, level, x0, y0, z0, live, live2);
+    if (cls == 0) {
+        *count = 0;
+        return GEN_EMPTY;
+    }
+    if (cls == 1) {
+        *count = (uint64_t)1 << (3 * (g->depth - level));
+        return gen_full(g, level);
+    }
+    if (level == g->leaf_level) {
+        uint64_t leaf = 0;
+        for (uint32_t lx = 0; lx < 4; lx++)
+            for (uint32_t lz = 0; lz < 4; lz++) {
+                const uint32_t x = x0 + lx, z = z0 + lz;
+                const int64_t h = or_scene_height(g->seed, g->depth, x, z);
+                for (uint32_t ly = 0; ly < 4; ly++) {
+                    const uint32_t y = y0 + ly;
+                    int solid = (int64_t)y <= h;
+                    for (int k = 0; k < 64 && !solid; k++)
+                        if (live2[k] && in_sphere(g->spheres + 4 * k, x, y, z))
+                            solid = 1;
+                    if (solid) {
+                        uint32_t c1 = ((lx >> 1) << 2) | ((ly >> 1) << 1) | (lz >> 1);
+                        uint32_t c2 = ((lx & 1) << 2) | ((ly & 1) << 1) | (lz & 1);
+                        leaf |= 1ull << (c1 * 8 + c2);
+                    }
+                }
+            }
+        *count = popc64(leaf);
+        if (!leaf)
+            return GEN_EMPTY;
+        return level_insert(&g->lv[level], 1, 0, *count, leaf, NULL);
+    }
+    const uint32_t half = 1u << (g->depth - level - 1);
+    uint32_t kids[8];
+    uint8_t mask = 0;
+    uint32_t nk = 0;
+    uint64_t total = 0;
+    for (uint32_t c = 0; c < 8; c++) {
+        uint64_t cc;
+        uint32_t id = gen_build(g, level + 1, x0 + ((c >> 2) & 1) * half, y0 + ((c >> 1) & 1) * half,
+                                z0 + (c & 1) * half, live2, &cc);
+        if (id != GEN_EMPTY) {
+            mask |= (uint8_t)(1u << c);
+            kids[nk++] = id;
+            total += cc;
+        }
+    }
+    *count = total;
+    if (!mask)
+        return GEN_EMPTY;
+    return level_insert(&g->lv[level], 0, mask, total, 0, kids);
+}
+
+uint32_t* or_generate_basic_dag(uint64_t seed, uint32_t depth, uint32_t T, uint64_t* n_words)
+{
+    if (depth < 6 || depth > 16 || T > depth - 2)
+        return NULL;
+    gen_ctx* g = (gen_ctx*)calloc(1, sizeof(gen_ctx));
+    g->seed = seed;
+    g->depth = depth;
+    g->leaf_level = depth - 2;
+    g->T = T;
+    for (uint32_t l = 0; l < HD_MAX_DEPTH; l++)
+        g->full_id[l] = GEN_EMPTY;
+    or_scene_spheres(seed, depth, g->spheres);
+    /* height min/max pyramid over node footprints, levels leaf..0 */
+    {
+        const uint32_t E = 1u << depth;
+        int32_t* h = (int32_t*)malloc((size_t)E * E * 4);
+        for (uint32_t x = 0; x < E; x++)
+            for (uint32_t z = 0; z < E; z++)
+                h[(size_t)x * E + z] = or_scene_height(seed, depth, x, z);
+        const uint32_t n = 1u << g->leaf_level; /* 4x4 footprints */
+        g->hmin[g->leaf_level] = (int32_t*)malloc((size_t)n * n * 4);
+        g->hmax[g->leaf_level] = (int32_t*)malloc((size_t)n * n * 4);
+        for (uint32_t cx = 0; cx < n; cx++)
+            for (uint32_t cz = 0; cz < n; cz++) {
+                int32_t lo = 0x7fffffff, hi = -0x7fffffff;
+                for (uint32_t a = 0; a < 4; a++)
+                    for (uint32_t b = 0; b < 4; b++) {
+                        int32_t v = h[(size_t)(4 * cx + a) * E + 4 * cz + b];
+                        lo = v < lo ? v : lo;
+                        hi = v > hi ? v : hi;
+                    }
+                g->hmin[g->leaf_level][(size_t)cx * n + cz] = lo;
+                g->hmax[g->leaf_level][(size_t)cx * n + cz] = hi;
+            }
+        free(h);
+        for (int32_t l = (int32_t)g->leaf_level - 1; l >= 0; l--) {
+            const uint32_t m = 1u << l, m2 = 2 * m;
+            g->hmin[l] = (int32_t*)malloc((size_t)m * m * 4);
+            g->hmax[l] = (int32_t*)malloc((size_t)m * m * 4);
+            for (uint32_t cx = 0; cx < m; cx++)
+                for (uint32_t cz = 0; cz < m; cz++) {
+                    int32_t lo = 0x7fffffff, hi = -0x7fffffff;
+                    for (uint32_t a = 0; a < 2; a++)
+                        for (uint32_t b = 0; b < 2; b++) {
+                            size_t i = (size_t)(2 * cx + a) * m2 + 2 * cz + b;
+                            lo = g->hmin[l + 1][i] < lo ? g->hmin[l + 1][i] : lo;
+                            hi = g->hmax[l + 1][i] > hi ? g->hmax[l + 1][i] : hi;
+                        }
+                    g->hmin[l][(size_t)cx * m + cz] = lo;
+                    g->hmax[l][(size_t)cx * m + cz] = hi;
+                }
+        }
+    }
+    uint8_t live[64];
+    memset(live, 1, 64);
+    uint64_t total;
+    uint32_t root = gen_build(g, 0, 0, 0, 0, live, &total);
+    uint32_t* words = NULL;
+    if (root != GEN_EMPTY) {
+        /* depth-first first-visit rank per level (create_hash_dag order) */
+        uint32_t* rank[HD_MAX_DEPTH];
+        uint64_t nrank[HD_MAX_DEPTH] = {0};
+        for (uint32_t l = 0; l <= g->leaf_level; l++) {
+            rank[l] = (uint32_t*)malloc((g->lv[l].n + 1) * 4);
+            memset(rank[l], 0xff, (g->lv[l].n + 1) * 4);
+        }
+        struct frame { uint32_t level, id, next; } stack[HD_MAX_DEPTH + 1];
+        int sp = 0;
+        rank[0][root] = (uint32_t)nrank[0]++;
+        stack[sp++] = (struct frame){0, root, 0};
+        while (sp) {
+            struct frame* f = &stack[sp - 1];
+            if (f->level == g->leaf_level || f->next == popc32(g->lv[f->level].mask[f->id])) {
+                sp--;
+                continue;
+            }
+            uint32_t child = g->lv[f->level].kids[g->lv[f->level].kid0[f->id] + f->next++];
+            uint32_t cl = f->level + 1;
+            if (rank[cl][child] == 0xFFFFFFFFu) {
+                rank[cl][child] = (uint32_t)nrank[cl]++;
+                stack[sp++] = (struct frame){cl, child, 0};
+            }
+        }
+        /* word offsets per level in rank order */
+        uint64_t level_base[HD_MAX_DEPTH + 1];
+        uint32_t* order[HD_MAX_DEPTH];
+        uint64_t off = 0;
+        for (uint32_t l = 0; l <= g->leaf_level; l++) {
+            level_base[l] = off;
+            order[l] = (uint32_t*)malloc((nrank[l] + 1) * 4);
+            for (uint64_t id = 0; id < g->lv[l].n; id++)
+                if (rank[l][id] != 0xFFFFFFFFu)
+                    order[l][rank[l][id]] = (uint32_t)id;
+            for (uint64_t r = 0; r < nrank[l]; r++)
+                off += l == g->leaf_level ? 2 : 1 + popc32(g->lv[l].mask[order[l][r]]);
+        }
+        /* word index of each node */
+        uint64_t* where[HD_MAX_DEPTH];
+        for (uint32_t l = 0; l <= g->leaf_level; l++) {
+            where[l] = (uint64_t*)malloc((g->lv[l].n + 1) * 8);
+            uint64_t o = level_base[l];
+            for (uint64_t r = 0; r < nrank[l]; r++) {
+                uint32_t id = order[l][r];
+                where[l][id] = o;
+                o += l == g->leaf_level ? 2 : 1 + popc32(g->lv[l].mask[id]);
+            }
+        }
+        words = (uint32_t*)malloc(off * 4);
+        uint64_t enclosed = 0;
+        int bad = 0;
+        for (uint32_t l = 0; l <= g->leaf_level; l++) {
+            for (uint64_t r = 0; r < nrank[l]; r++) {
+                uint32_t id = order[l][r];
+                uint64_t w = where[l][id];
+                if (l == g->leaf_level) {
+                    words[w] = (uint32_t)g->lv[l].leaf[id];
+                    words[w + 1] = (uint32_t)(g->lv[l].leaf[id] >> 32);
+                    continue;
+                }
+                uint32_t upper;
+                if (l < T)
+                    upper = (uint32_t)(enclosed + r);
+                else
+                    upper = (uint32_t)g->lv[l].count[id];
+                if ((l < T ? enclosed + r : g->lv[l].count[id]) >= (1u << 24))
+                    bad = 1;
+                words[w] = (upper << 8) | g->lv[l].mask[id];
+                uint32_t nk = popc32(g->lv[l].mask[id]);
+                for (uint32_t k = 0; k < nk; k++)
+                    words[w + 1 + k] = (uint32_t)where[l + 1][g->lv[l].kids[g->lv[l].kid0[id] + k]];
+            }
+            if (l < T)
+                enclosed += nrank[l];
+        }
+        *n_words = off;
+        for (uint32_t l = 0; l <= g->leaf_level; l++) {
+            free(rank[l]);
+            free(order[l]);
+            free(where[l]);
+        }
+        if (bad) {
+            free(words);
+            words = NULL;
+        }
+    }
+    for (uint32_t l = 0; l <= g->leaf_level; l++) {
+        gen_level* L = &g->lv[l];
+        free(L->mask); free(L->count); free(L->leaf); free(L->kid0); free(L->kids);
+        free(L->map.keys); free(L->map.ids);
+        free(g->hmin[l]); free(g->hmax[l]);
+    }
+    free(g);
+    return words;
+}
+void or_free(void* p) { free(p); }
+
+/* ======================================================================
+ * Ingest: HashDAGFactory::load_from_DAG (hash_dag_factory.cpp:152-184) and
+ * create_hash_dag (:5-99)
+ * ====================================================================== */
+
+static uint32_t create_hash_dag(or_table* t, const uint32_t* words, uint32_t* map, uint32_t level, uint32_t index)
+{
+    if (level == t->leaf_level) {
+        uint64_t leaf = (uint64_t)words[index] | ((uint64_t)words[index + 1] << 32);
+        return add_leaf(t, leaf, or_hash_leaf(leaf));
+    }
+    const uint32_t node = words[index];
+    const uint32_t mask = node & 0xffu;
+    uint32_t buf[9];
+    uint32_t n = 0;
+    buf[n++] = node;
+    for (uint32_t c = 0; c < 8; c++) {
+        if (!(mask & (1u << c)))
+            continue;
+        const uint32_t child = words[index + child_offset(mask, c)];
+        uint32_t id = map[child];
+        if (id == 0) {
+            id = create_hash_dag(t, words, map, level + 1, child);
+            map[child] = id + 1;
+        } else {
+            id--;
+        }
+        buf[n++] = id;
+        if (t->error)
+            return INVALID;
+    }
+    return add_interior(t, level, n, buf, or_hash_interior(n, buf));
+}
+
+int or_load_basic_dag(or_table* t, const uint32_t* words, uint64_t n_words)
+{
+    for (uint32_t level = t->leaf_level; level > 0; level--)
+        add_full_node(t, level);
+    uint32_t* map = (uint32_t*)calloc(n_words + 1, 4);
+    t->root = create_hash_dag(t, words, map, 0, 0);
+    free(map);
+    return t->error;
+}
+
+/* ======================================================================
+ * Queries (dag_utils.h:138-172)
+ * ====================================================================== */
+
+static uint32_t leaf_bit(uint32_t x, uint32_t y, uint32_t z)
+{
+    return ((x & 1) ? 4 : 0) | ((y & 1) ? 2 : 0) | ((z & 1) ? 1 : 0) | ((x & 2) ? 32 : 0) |
+           ((y & 2) ? 16 : 0) | ((z & 2) ? 8 : 0);
+}
+
+int or_get_value(const or_table* t, uint32_t x, uint32_t y, uint32_t z)
+{
+    const uint32_t D = t->cfg.depth;
+    uint32_t index = t->root;
+    for (uint32_t level = 0; level < D; level++) {
+        if (level < t->leaf_level) {
+            const uint32_t mask = *sys_ptr(t, index) & 0xffu;
+            const uint32_t s = D - (level + 1);
+            const uint32_t child = (((x >> s) & 1) << 2) | (((y >> s) & 1) << 1) | ((z >> s) & 1);
+            if (!(mask & (1u << child)))
+                return 0;
+            index = *sys_ptr(t, index + child_offset(mask, child));
+        } else {
+            const uint32_t* p = sys_ptr(t, index);
+            uint64_t leaf = (uint64_t)p[0] | ((uint64_t)p[1] << 32);
+            return (int)((leaf >> leaf_bit(x, y, z)) & 1);
+        }
+    }
+    return 1;
+}
+
+typedef struct {
+    uint32_t* keys;
+    uint64_t* vals;
+    uint64_t cap, n;
+} fp_map;
+
+static uint64_t fp_node(const or_table* t, fp_map* maps, uint32_t level, uint32_t index)
+{
+    fp_map* m = &maps[level];
+    if (2 * (m->n + 1) > m->cap) {
+        uint64_t ncap = m->cap ? 2 * m->cap : 1024;
+        uint32_t* k = (uint32_t*)malloc(ncap * 4);
+        uint64_t* v = (uint64_t*)malloc(ncap * 8);
+        memset(k, 0xff, ncap * 4);
+        for (uint64_t i = 0; i < m->cap; i++)
+            if (m->keys[i] != 0xFFFFFFFFu) {
+                uint64_t s = or_murmurhash64(m->keys[i]) & (ncap - 1);
+                while (k[s] != 0xFFFFFFFFu)
+                    s = (s + 1) & (ncap - 1);
+                k[s] = m->keys[i];
+                v[s] = m->vals[i];
+            }
+        free(m->keys);
+        free(m->vals);
+        m->keys = k;
+        m->vals = v;
+        m->cap = ncap;
+    }
+    uint64_t s = or_murmurhash64(index) & (m->cap - 1);
+    while (m->keys[s] != 0xFFFFFFFFu) {
+        if (m->keys[s] == index)
+            return m->vals[s];
+        s = (s + 1) & (m->cap - 1);
+    }
+    uint64_t h;
+    const uint32_t* p = sys_ptr(t, index);
+    if (level == t->leaf_level) {
+        h = mix64(((uint64_t)p[0] | ((uint64_t)p[1] << 32)) ^ 0x1EAF1EAF1EAF1EAFull);
+    } else {
+        const uint32_t mask = p[0] & 0xffu;
+        uint32_t kids[8];
+        for (uint32_t k = 0; k < popc32(mask); k++)
+            kids[k] = p[1 + k];
+        h = mix64(mask);
+        for (uint32_t k = 0; k < popc32(mask); k++)
+            h = mix64(h ^ fp_node(t, maps, level + 1, kids[k]));
+    }
+    /* re-probe: the recursion may have grown the map */
+    s = or_murmurhash64(index) & (m->cap - 1);
+    while (m->keys[s] != 0xFFFFFFFFu)
+        s = (s + 1) & (m->cap - 1);
+    m->keys[s] = index;
+    m->vals[s] = h;
+    m->n++;
+    return h;
+}
+
+void or_reachable_counts(const or_table* t, uint32_t root, uint64_t* out)
+{
+    uint32_t* cur = (uint32_t*)malloc(4);
+    uint64_t n = 1;
+    cur[0] = root;
+    for (uint32_t level = 0; level <= t->leaf_level; level++) {
+        out[level] = n;
+        if (level == t->leaf_level)
+            break;
+        uint64_t cap = 0;
+        for (uint64_t i = 0; i < n; i++)
+            cap += total_size(*sys_ptr(t, cur[i])) - 1;
+        uint32_t* nxt = (uint32_t*)malloc((cap + 1) * 4);
+        uint64_t k = 0;
+        for (uint64_t i = 0; i < n; i++) {
+            const uint32_t* p = sys_ptr(t, cur[i]);
+            for (uint32_t o = 1; o < total_size(p[0]); o++)
+                nxt[k++] = p[o];
+        }
+        free(cur);
+        cur = nxt;
+        n = unique_sorted(cur, k);
+    }
+    free(cur);
+}
+
+uint64_t or_occupancy_fingerprint(const or_table* t, uint32_t root)
+{
+    fp_map maps[HD_MAX_DEPTH];
+    memset(maps, 0, sizeof(maps));
+    uint64_t h = fp_node(t, maps, 0, root);
+    for (uint32_t l = 0; l < HD_MAX_DEPTH; l++) {
+        free(maps[l].keys);
+        free(maps[l].vals);
+    }
+    return h;
+}
+
+/* ======================================================================
+ * Traversal (tracer.cu).  fp_mode 1 places fused multiply-adds where the
+ * reference's default nvcc build contracts a product into a following add.
+ * ====================================================================== */
+
+typedef struct { float x, y, z; } f3;
+typedef struct { double x, y, z; } d3;
+
+static float fmaxr(float a, float b) { return a > b ? a : b; } /* constexpr_max (cuda_math.h:13) */
+static float fminr(float a, float b) { return a < b ? a : b; }
+
+/* normalize(rayMin + x * ddx + y * ddy - position) in double
+ * (tracer.cu:157, cuda_math.h:55-56) */
+static d3 camera_dir(const hd_camera* cam, double px, double py, uint32_t mode)
+{
+    double v[3];
+    for (int a = 0; a < 3; a++) {
+        double t;
+        if (mode) {
+            t = fma(px, cam->ray_ddx[a], cam->ray_min[a]);
+            t = fma(py, cam->ray_ddy[a], t);
+        } else {
+            t = cam->ray_min[a] + px * cam->ray_ddx[a];
+            t = t + py * cam->ray_ddy[a];
+        }
+        v[a] = t - cam->position[a];
+    }
+    double dot = mode ? fma(v[2], v[2], fma(v[1], v[1], v[0] * v[0])) : (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+    double inv = 1.0 / sqrt(dot);
+    d3 r = {inv * v[0], inv * v[1], inv * v[2]};
+    return r;
+}
+
+/* compute_intersection_mask (tracer.cu:19-136) */
+static uint32_t intersection_mask(uint32_t D, int is_root, uint32_t level, const uint32_t path[3], f3 o, f3 d,
+                                  f3 inv, uint32_t mode)
+{
+    const uint32_t shift = D - level;
+    const float radius = (float)(1u << (shift - 1));
+    const float cx = radius + (float)(path[0] << shift);
+    const float cy = radius + (float)(path[1] << shift);
+    const float cz = radius + (float)(path[2] << shift);
+    const f3 crr = {cx - o.x, cy - o.y, cz - o.z};
+    const f3 tmid = {crr.x * inv.x, crr.y * inv.y, crr.z * inv.z};
+    const f3 slab = {radius * fabsf(inv.x), radius * fabsf(inv.y), radius * fabsf(inv.z)};
+    f3 pmin, pmax;
+    if (mode) {
+        pmin = (f3){fmaf(crr.x, inv.x, -slab.x), fmaf(crr.y, inv.y, -slab.y), fmaf(crr.z, inv.z, -slab.z)};
+        pmax = (f3){fmaf(crr.x, inv.x, slab.x), fmaf(crr.y, inv.y, slab.y), fmaf(crr.z, inv.z, slab.z)};
+    } else {
+        pmin = (f3){tmid.x - slab.x, tmid.y - slab.y, tmid.z - slab.z};
+        pmax = (f3){tmid.x + slab.x, tmid.y + slab.y, tmid.z + slab.z};
+    }
+    const float tmin = fmaxr(fmaxr(pmin.x, fmaxr(pmin.y, pmin.z)), 0.0f);
+    const float tmax = fminr(pmax.x, fminr(pmax.y, pmax.z));
+    if (is_root && tmin >= tmax)
+        return 0;
+    uint32_t result = 0;
+    {
+        const float s = 0.5f * (tmin + tmax);
+        const f3 p = {s * d.x, s * d.y, s * d.z};
+        const uint32_t first = (p.x >= crr.x ? 4u : 0u) + (p.y >= crr.y ? 2u : 0u) + (p.z >= crr.z ? 1u : 0u);
+        result |= 1u << first;
+    }
+    const float eps = 1e-4f;
+    if (tmin <= tmid.x && tmid.x <= tmax) {
+        const f3 p = {tmid.x * d.x, tmid.x * d.y, tmid.x * d.z};
+        uint32_t A = 0, B = 0;
+        if (p.y >= crr.y - eps) A |= 0xCC;
+        if (p.y <= crr.y + eps) A |= 0x33;
+        if (p.z >= crr.z - eps) B |= 0xAA;
+        if (p.z <= crr.z + eps) B |= 0x55;
+        result |= A & B;
+    }
+    if (tmin <= tmid.y && tmid.y <= tmax) {
+        const f3 p = {tmid.y * d.x, tmid.y * d.y, tmid.y * d.z};
+        uint32_t C = 0, Dm = 0;
+        if (p.x >= crr.x - eps) C |= 0xF0;
+        if (p.x <= crr.x + eps) C |= 0x0F;
+        if (p.z >= crr.z - eps) Dm |= 0xAA;
+        if (p.z <= crr.z + eps) Dm |= 0x55;
+        result |= C & Dm;
+    }
+    if (tmin <= tmid.z && tmid.z <= tmax) {
+        const f3 p = {tmid.z * d.x, tmid.z * d.y, tmid.z * d.z};
+        uint32_t E = 0, F = 0;
+        if (p.x >= crr.x - eps) E |= 0xF0;
+        if (p.x <= crr.x + eps) E |= 0x0F;
+        if (p.y >= crr.y - eps) F |= 0xCC;
+        if (p.y <= crr.y + eps) F |= 0x33;
+        result |= E & F;
+    }
+    return result & 0xffu;
+}
+
+/* next_child (tracer.cu:7-17) */
+static uint32_t next_child(uint32_t order, uint32_t mask)
+{
+    for (uint32_t c = 0; c < 8; c++) {
+        uint32_t ci = c ^ order;
+        if (mask & (1u << ci))
+            return ci;
+    }
+    return 0;
+}
+static uint32_t first_child_mask(uint64_t leaf) /* Leaf::get_first_child_mask (base_dag.h:16-52) */
+{
+    uint32_t m = 0;
+    for (uint32_t b = 0; b < 8; b++)
+        if ((leaf >> (8 * b)) & 0xffu)
+            m |= 1u << b;
+    return m;
+}
+static uint32_t second_child_mask(uint64_t leaf, uint32_t c) /* base_dag.h:53-59 */
+{
+    return (uint32_t)(leaf >> (8 * c)) & 0xffu;
+}
+
+typedef struct {
+    uint32_t index, child_mask, visit_mask;
+} stack_entry;
+
+/* The shared stack walk of trace_paths (tracer.cu:168-249) and
+ * intersect_ray_node_out_of_order (:453-543).  any_hit selects the shadow
+ * variant (children highest bit first, return on the first voxel). */
+static int walk(const or_table* t, f3 o, f3 d, f3 inv, uint32_t order, int any_hit, uint32_t mode,
+                uint32_t out_path[3], uint64_t* visits)
+{
+    const uint32_t D = t->cfg.depth, leafl = t->leaf_level;
+    uint32_t level = 0;
+    uint32_t path[3] = {0, 0, 0};
+    stack_entry stack[HD_MAX_DEPTH];
+    stack_entry cache;
+    uint64_t cached_leaf = 0;
+    cache.index = t->root;
+    cache.child_mask = *sys_ptr(t, cache.index) & 0xffu;
+    cache.visit_mask = cache.child_mask & intersection_mask(D, 1, 0, path, o, d, inv, mode);
+    uint64_t v = 1;
+    for (;;) {
+        uint32_t nl = level;
+        while (nl > 0 && !cache.visit_mask) {
+            nl--;
+            cache = stack[nl];
+        }
+        if (nl == 0 && !cache.visit_mask) {
+            path[0] = path[1] = path[2] = 0;
+            if (visits)
+                *visits += v;
+            if (out_path)
+                out_path[0] = out_path[1] = out_path[2] = 0;
+            return 0;
+        }
+        for (int a = 0; a < 3; a++)
+            path[a] >>= (level - nl);
+        level = nl;
+        const uint32_t nc = any_hit ? 31u - (uint32_t)__builtin_clz(cache.visit_mask) : next_child(order, cache.visit_mask);
+        cache.visit_mask &= ~(1u << nc);
+        path[0] = (path[0] << 1) | ((nc >> 2) & 1);
+        path[1] = (path[1] << 1) | ((nc >> 1) & 1);
+        path[2] = (path[2] << 1) | (nc & 1);
+        stack[level] = cache;
+        level++;
+        if (level == D) {
+            if (visits)
+                *visits += v;
+            if (out_path) {
+                out_path[0] = path[0];
+                out_path[1] = path[1];
+                out_path[2] = path[2];
+            }
+            return 1;
+        }
+        if (level < leafl) {
+            cache.index = *sys_ptr(t, cache.index + child_offset(cache.child_mask, nc));
+            cache.child_mask = *sys_ptr(t, cache.index) & 0xffu;
+            cache.visit_mask = cache.child_mask & intersection_mask(D, 0, level, path, o, d, inv, mode);
+            v++;
+        } else {
+            uint32_t cm;
+            if (level == leafl) {
+                const uint32_t addr = *sys_ptr(t, cache.index + child_offset(cache.child_mask, nc));
+                const uint32_t* p = sys_ptr(t, addr);
+                cached_leaf = (uint64_t)p[0] | ((uint64_t)p[1] << 32);
+                cm = first_child_mask(cached_leaf);
+                v++;
+            } else {
+                cm = second_child_mask(cached_leaf, nc);
+            }
+            cache.child_mask = cm;
+            cache.visit_mask = cm & intersection_mask(D, 0, level, path, o, d, inv, mode);
+        }
+    }
+}
+
+static f3 to_f3(d3 v)
+{
+    f3 r = {(float)v.x, (float)v.y, (float)v.z};
+    return r;
+}
+static f3 inverse_dir(f3 d) /* make_float3(make_double3(1. / d.x, ...)) (tracer.cu:160) */
+{
+    f3 r = {(float)(1.0 / (double)d.x), (float)(1.0 / (double)d.y), (float)(1.0 / (double)d.z)};
+    return r;
+}
+
+void or_trace_primary(const or_table* t, const hd_camera* cam, uint32_t W, uint32_t H, uint32_t mode,
+                      uint32_t* paths, uint32_t row0, uint32_t row1, uint64_t* visits)
+{
+    const f3 o = {(float)cam->position[0], (float)cam->position[1], (float)cam->position[2]};
+    for (uint32_t y = row0; y < row1 && y < H; y++)
+        for (uint32_t x = 0; x < W; x++) {
+            const f3 d = to_f3(camera_dir(cam, (double)x, (double)y, mode));
+            const f3 inv = inverse_dir(d);
+            const uint32_t order = (d.x < 0.f ? 4u : 0u) + (d.y < 0.f ? 2u : 0u) + (d.z < 0.f ? 1u : 0u);
+            uint32_t p[3];
+            walk(t, o, d, inv, order, 0, mode, p, visits);
+            uint32_t* out = paths + 4 * ((uint64_t)(H - 1 - y) * W + x);
+            out[0] = p[0];
+            out[1] = p[1];
+            out[2] = p[2];
+            out[3] = 0;
+        }
+}
+
+/* trace_shadows (tracer.cu:589-697) reduced to its hit test; rows are
+ * output rows (the layout of the paths image). */
+void or_trace_shadow(const or_table* t, const hd_camera* cam, uint32_t W, uint32_t H, uint32_t mode,
+                     const uint32_t* paths, const float light[3], float bias, uint8_t* mask,
+                     uint32_t row0, uint32_t row1, uint64_t* visits)
+{
+    /* sun_direction(): normalize(float3) in float (tracer.cu:546-549) */
+    const f3 L = {light[0], light[1], light[2]};
+    const float dot = mode ? fmaf(L.z, L.z, fmaf(L.y, L.y, L.x * L.x)) : (L.x * L.x + L.y * L.y) + L.z * L.z;
+    const float il = 1.0f / sqrtf(dot);
+    const f3 dir = {il * L.x, il * L.y, il * L.z};
+    const f3 inv = inverse_dir(dir);
+    for (uint32_t r = row0; r < row1 && r < H; r++)
+        for (uint32_t x = 0; x < W; x++) {
+            const uint32_t* p = paths + 4 * ((uint64_t)r * W + x);
+            uint8_t* out = mask + (uint64_t)r * W + x;
+            if (p[0] == 0 && p[1] == 0 && p[2] == 0) {
+                *out = 2;
+                continue;
+            }
+            const d3 cd = camera_dir(cam, (double)x, (double)(H - 1 - r), mode);
+            /* ray_box_intersection (tracer.cu:574-587) */
+            const double bmin[3] = {(double)(float)p[0], (double)(float)p[1], (double)(float)p[2]};
+            const double dd[3] = {cd.x, cd.y, cd.z};
+            double real_min[3];
+            for (int a = 0; a < 3; a++) {
+                const double t0 = (bmin[a] - cam->position[a]) / dd[a];
+                const double t1 = ((bmin[a] + 1.0) - cam->position[a]) / dd[a];
+                real_min[a] = t0 < t1 ? t0 : t1;
+            }
+            const double maxmin = fmax(fmax(real_min[0], real_min[1]), real_min[2]);
+            f3 start;
+            if (mode)
+                start = (f3){(float)fma(dd[0], maxmin, cam->position[0]), (float)fma(dd[1], maxmin, cam->position[1]),
+                             (float)fma(dd[2], maxmin, cam->position[2])};
+            else
+                start = (f3){(float)(cam->position[0] + dd[0] * maxmin), (float)(cam->position[1] + dd[1] * maxmin),
+                             (float)(cam->position[2] + dd[2] * maxmin)};
+            f3 o;
+            if (mode)
+                o = (f3){fmaf(bias, dir.x, start.x), fmaf(bias, dir.y, start.y), fmaf(bias, dir.z, start.z)};
+            else
+                o = (f3){start.x + bias * dir.x, start.y + bias * dir.y, start.z + bias * dir.z};
+            *out = (uint8_t)walk(t, o, dir, inv, 0, 1, mode, NULL, visits);
+        }
+}
+
+typedef struct {
+    const or_table* t;
+    const hd_camera* cam;
+    uint32_t W, H, mode;
+    const float* light;
+    float bias;
+    uint32_t* paths;
+    uint8_t* mask;
+    uint32_t r0, r1;
+} frame_job;
+
+static void* frame_worker(void* arg)
+{
+    frame_job* j = (frame_job*)arg;
+    /* primary rows [r0, r1) of pixel space land in output rows H-1-y */
+    or_trace_primary(j->t, j->cam, j->W, j->H, j->mode, j->paths, j->r0, j->r1, NULL);
+    return NULL;
+}
+static void* shadow_worker(void* arg)
+{
+    frame_job* j = (frame_job*)arg;
+    or_trace_shadow(j->t, j->cam, j->W, j->H, j->mode, j->paths, j->light, j->bias, j->mask, j->r0, j->r1, NULL);
+    return NULL;
+}
+
+void or_trace_frame_mt(const or_table* t, const hd_camera* cam, uint32_t W, uint32_t H, uint32_t mode,
+                       const float light[3], float bias, uint32_t* paths, uint8_t* mask, uint32_t n_threads,
+                       uint32_t row0, uint32_t row1)
+{
+    if (n_threads < 1)
+        n_threads = 1;
+    if (n_threads > 256)
+        n_threads = 256;
+    if (row1 > H)
+        row1 = H;
+    pthread_t th[256];
+    frame_job jobs[256];
+    const uint32_t rows = row1 > row0 ? row1 - row0 : 0;
+    for (int pass = 0; pass < 2; pass++) {
+        for (uint32_t i = 0; i < n_threads; i++) {
+            jobs[i] = (frame_job){t, cam, W, H, mode, light, bias, paths, mask,
+                                  row0 + (uint32_t)((uint64_t)rows * i / n_threads),
+                                  row0 + (uint32_t)((uint64_t)rows * (i + 1) / n_threads)};
+            if (pass == 1) {
+                /* the shadow pass reads output rows; primary pixel row y was
+                 * written to output row H-1-y */
+                uint32_t a = H - jobs[i].r1, b = H - jobs[i].r0;
+                jobs[i].r0 = a;
+                jobs[i].r1 = b;
+            }
+            pthread_create(&th[i], NULL, pass == 0 ? frame_worker : shadow_worker, &jobs[i]);
+        }
+        for (uint32_t i = 0; i < n_threads; i++)
+            pthread_join(th[i], NULL);
+    }
+}
+
+/* ======================================================================
+ * Editors (hash_dag_editors.h) and the edit recursion (hash_dag_edits.h)
+ * ====================================================================== */
+
+typedef struct {
+    uint32_t tool;
+    f3 c;        /* sphere centre */
+    float r, r2; /* radius, radius * radius (SphereEditorBase, :99-110) */
+    f3 bmin, bmax; /* box bounds (BoxEditorBase, :57-75) */
+} editor;
+
+static editor make_editor(const hd_edit* e)
+{
+    editor ed;
+    memset(&ed, 0, sizeof(ed));
+    ed.tool = e->tool;
+    ed.c = (f3){e->center[0], e->center[1], e->center[2]};
+    ed.r = e->radius;
+    ed.r2 = e->radius * e->radius;
+    ed.bmin = (f3){e->center[0] - e->radius, e->center[1] - e->radius, e->center[2] - e->radius};
+    ed.bmax = (f3){e->center[0] + e->radius, e->center[1] + e->radius, e->center[2] + e->radius};
+    return ed;
+}
+static int is_sphere(const editor* e) { return e->tool == HD_TOOL_SPHERE_ADD || e->tool == HD_TOOL_SPHERE_REMOVE; }
+static int is_adding(const editor* e) { return e->tool == HD_TOOL_SPHERE_ADD || e->tool == HD_TOOL_BOX_ADD; }
+
+static float sq(float f) { return f * f; }
+
+/* SphereEditorBase::should_edit_impl (:112-126), BoxEditorBase (:76-91) */
+static int should_edit_impl(const editor* e, f3 mn, f3 mx)
+{
+    if (is_sphere(e)) {
+        float dist = e->r2;
+        if (e->c.x < mn.x) dist -= sq(e->c.x - mn.x);
+        else if (e->c.x > mx.x) dist -= sq(e->c.x - mx.x);
+        if (e->c.y < mn.y) dist -= sq(e->c.y - mn.y);
+        else if (e->c.y > mx.y) dist -= sq(e->c.y - mx.y);
+        if (e->c.z < mn.z) dist -= sq(e->c.z - mn.z);
+        else if (e->c.z > mx.z) dist -= sq(e->c.z - mx.z);
+        return dist > 0;
+    }
+    return !(e->bmin.x >= mx.x || e->bmin.y >= mx.y || e->bmin.z >= mx.z || e->bmax.x <= mn.x ||
+             e->bmax.y <= mn.y || e->bmax.z <= mn.z || mn.x >= e->bmax.x || mn.y >= e->bmax.y ||
+             mn.z >= e->bmax.z || mx.x <= e->bmin.x || mx.y <= e->bmin.y || mx.z <= e->bmin.z);
+}
+/* SphereEditor::is_full_impl/is_empty_impl (:280-295), BoxEditor (:233-252):
+ * the region is inside the tool */
+static int inside_tool(const editor* e, f3 mn, f3 mx)
+{
+    if (is_sphere(e)) {
+        const float a = fmaxr(sq(mn.x - e->c.x), sq(mx.x - e->c.x));
+        const float b = fmaxr(sq(mn.y - e->c.y), sq(mx.y - e->c.y));
+        const float c = fmaxr(sq(mn.z - e->c.z), sq(mx.z - e->c.z));
+        return (a + b) + c < e->r2;
+    }
+    return e->bmin.x <= mn.x && e->bmin.y <= mn.y && e->bmin.z <= mn.z && e->bmax.x >= mx.x &&
+           e->bmax.y >= mx.y && e->bmax.z >= mx.z;
+}
+
+/* Editor::should_edit/is_full/is_empty on the node AABB (:12-27) */
+static void node_box(const uint32_t path[3], uint32_t depth, f3* mn, f3* mx)
+{
+    *mn = (f3){(float)(path[0] << depth), (float)(path[1] << depth), (float)(path[2] << depth)};
+    const float s = (float)(1u << depth);
+    *mx = (f3){mn->x + s, mn->y + s, mn->z + s};
+}
+
+typedef struct {
+    or_table* t;
+    editor ed;
+    uint64_t num_voxels, num_nodes;
+} edit_job;
+
+static void descend(const uint32_t in[3], uint32_t c, uint32_t out[3])
+{
+    out[0] = (in[0] << 1) | ((c >> 2) & 1);
+    out[1] = (in[1] << 1) | ((c >> 1) & 1);
+    out[2] = (in[2] << 1) | (c & 1);
+}
+
+/* HashDagEdits::edit_leaf (hash_dag_edits.h:335-643), colours off */
+static uint32_t edit_leaf(edit_job* j, uint32_t level, uint32_t index, const uint32_t path[3], uint32_t* count_out)
+{
+    or_table* t = j->t;
+    const uint32_t D = t->cfg.depth, leafl = t->leaf_level;
+    j->num_nodes++;
+    f3 mn, mx;
+    node_box(path, D - level, &mn, &mx);
+    const uint32_t full_count = 1u << (3 * (D - level));
+    if (!should_edit_impl(&j->ed, mn, mx)) {
+        uint32_t count = 0;
+        if (index != INVALID) {
+            const uint32_t* p = sys_ptr(t, index);
+            count = level < leafl ? p[0] >> 8 : popc32(p[0]) + popc32(p[1]);
+        }
+        *count_out = count;
+        return index;
+    }
+    const int inside = inside_tool(&j->ed, mn, mx);
+    if (!is_adding(&j->ed) && inside) { /* is_empty */
+        j->num_voxels += full_count;
+        *count_out = 0;
+        return INVALID;
+    }
+    if (is_adding(&j->ed) && inside) { /* is_full */
+        j->num_voxels += full_count;
+        *count_out = full_count;
+        return t->full[level];
+    }
+    if (level == leafl) {
+        uint64_t leaf = 0;
+        if (index != INVALID) {
+            const uint32_t* p = sys_ptr(t, index);
+            leaf = (uint64_t)p[0] | ((uint64_t)p[1] << 32);
+        }
+        const uint64_t initial = leaf;
+        for (uint32_t c1 = 0; c1 < 8; c1++) {
+            uint32_t p1[3];
+            descend(path, c1, p1);
+            for (uint32_t c2 = 0; c2 < 8; c2++) {
+                uint32_t p2[3];
+                descend(p1, c2, p2);
+                const f3 pos = {(float)p2[0], (float)p2[1], (float)p2[2]};
+                const f3 pos1 = {pos.x + 1.0f, pos.y + 1.0f, pos.z + 1.0f};
+                const uint64_t bit = 1ull << (c1 * 8 + c2);
+                const int se = should_edit_impl(&j->ed, pos, pos1);
+                const int prev = (leaf & bit) != 0;
+                const int nv = se ? is_adding(&j->ed) : prev;
+                j->num_voxels += (uint64_t)se;
+                if (prev != nv) {
+                    if (nv)
+                        leaf |= bit;
+                    else
+                        leaf &= ~bit;
+                }
+            }
+        }
+        if (leaf == initial) {
+            *count_out = popc64(leaf);
+            return index;
+        }
+        if (leaf == 0) {
+            *count_out = 0;
+            return INVALID;
+        }
+        *count_out = popc64(leaf);
+        return or_find_or_add_leaf(t, leaf);
+    }
+    uint32_t mask = 0;
+    const uint32_t* p = NULL;
+    if (index != INVALID) {
+        p = sys_ptr(t, index);
+        mask = p[0] & 0xffu;
+    }
+    uint32_t off = 1, kids[8], total = 0;
+    int changed = 0;
+    for (uint32_t c = 0; c < 8; c++) {
+        uint32_t np[3];
+        descend(path, c, np);
+        const uint32_t old = (mask & (1u << c)) ? p[off++] : INVALID;
+        uint32_t cc;
+        const uint32_t nk = edit_leaf(j, level + 1, old, np, &cc);
+        if (t->error)
+            return INVALID;
+        if (nk != INVALID)
+            total += cc;
+        changed |= old != nk;
+        kids[c] = nk;
+        if (index != INVALID)
+            p = sys_ptr(t, index); /* unchanged by appends; kept explicit */
+    }
+    *count_out = total;
+    if (!changed)
+        return index;
+    uint32_t node[9], n = 0;
+    node[n++] = total << 8;
+    for (uint32_t c = 0; c < 8; c++)
+        if (kids[c] != INVALID) {
+            node[n++] = kids[c];
+            node[0] |= 1u << c;
+        }
+    if ((node[0] & 0xffu) == 0) {
+        *count_out = 0;
+        return INVALID;
+    }
+    return or_find_or_add_interior(t, level, n, node);
+}
+
+/* HashDagEdits::edit_threaded (hash_dag_edits.h:106-333) with both passes
+ * folded into one depth-first recursion (tasks run in depth-first order). */
+static uint32_t edit_top(edit_job* j, uint32_t level, uint32_t index, const uint32_t path[3])
+{
+    or_table* t = j->t;
+    const uint32_t D = t->cfg.depth, T = t->cfg.color_tree_levels;
+    /* the reference runs this recursion twice (queue pass, build pass) and
+     * counts the node in both (hash_dag_edits.h:120, hash_dag.h:287, :358) */
+    j->num_nodes += 2;
+    f3 mn, mx;
+    node_box(path, D - level, &mn, &mx);
+    if (!should_edit_impl(&j->ed, mn, mx))
+        return index;
+    uint32_t mask = 0;
+    const uint32_t* p = NULL;
+    if (index != INVALID) {
+        p = sys_ptr(t, index);
+        mask = p[0] & 0xffu;
+    }
+    uint32_t off = 1, kids[8];
+    int changed = 0;
+    for (uint32_t c = 0; c < 8; c++) {
+        uint32_t np[3];
+        descend(path, c, np);
+        const uint32_t old = (mask & (1u << c)) ? p[off++] : INVALID;
+        uint32_t nk;
+        if (level == T - 1) {
+            f3 cmn, cmx;
+            node_box(np, D - level - 1, &cmn, &cmx);
+            if (should_edit_impl(&j->ed, cmn, cmx)) {
+                uint32_t cc;
+                nk = edit_leaf(j, T, old, np, &cc);
+            } else {
+                nk = old;
+            }
+        } else {
+            nk = edit_top(j, level + 1, old, np);
+        }
+        if (t->error)
+            return INVALID;
+        changed |= old != nk;
+        kids[c] = nk;
+    }
+    if (!changed)
+        return index;
+    uint32_t node[9], n = 0;
+    node[n++] = 0;
+    for (uint32_t c = 0; c < 8; c++)
+        if (kids[c] != INVALID) {
+            node[n++] = kids[c];
+            node[0] |= 1u << c;
+        }
+    if ((node[0] & 0xffu) == 0)
+        return INVALID;
+    return or_find_or_add_interior(t, level, n, node);
+}
+
+int or_edit(or_table* t, const hd_edit* e, hd_edit_stats* stats)
+{
+    edit_job j;
+    memset(&j, 0, sizeof(j));
+    j.t = t;
+    j.ed = make_editor(e);
+    t->foa_calls = t->nodes_added = t->words_scanned = 0;
+    const uint32_t path[3] = {0, 0, 0};
+    uint32_t root;
+    if (t->cfg.color_tree_levels == 0) {
+        uint32_t cc;
+        root = edit_leaf(&j, 0, t->root, path, &cc);
+    } else {
+        root = edit_top(&j, 0, t->root, path);
+    }
+    if (!t->error)
+        t->root = root;
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->num_voxels = j.num_voxels;
+        stats->num_nodes = j.num_nodes;
+        stats->find_or_add_calls = t->foa_calls;
+        stats->nodes_added = t->nodes_added;
+        stats->words_scanned = t->words_scanned;
+    }
+    return t->error;
+}
+
+/* ======================================================================
+ * GC: HashDAG::remove_stale_nodes (hash_dag.h:407-547) with a canonical
+ * re-insertion order (increasing old address per level).
+ * ====================================================================== */
+
+static int cmp_u32(const void* a, const void* b)
+{
+    uint32_t x = *(const uint32_t*)a, y = *(const uint32_t*)b;
+    return x < y ? -1 : x > y;
+}
+static uint64_t unique_sorted(uint32_t* v, uint64_t n)
+{
+    if (!n)
+        return 0;
+    qsort(v, n, 4, cmp_u32);
+    uint64_t m = 1;
+    for (uint64_t i = 1; i < n; i++)
+        if (v[i] != v[m - 1])
+            v[m++] = v[i];
+    return m;
+}
+static uint64_t find_sorted(const uint32_t* v, uint64_t n, uint32_t x)
+{
+    uint64_t lo = 0, hi = n;
+    while (lo < hi) {
+        uint64_t mid = (lo + hi) / 2;
+        if (v[mid] < x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+int or_gc(or_table* t, uint32_t* extra, uint32_t n_extra)
+{
+    const uint32_t maxl = t->leaf_level;
+    uint32_t* live[HD_MAX_DEPTH];
+    uint64_t nlive[HD_MAX_DEPTH];
+    /* mark (hash_dag.h:424-438) */
+    live[0] = (uint32_t*)malloc((1 + n_extra) * 4);
+    live[0][0] = t->root;
+    for (uint32_t i = 0; i < n_extra; i++)
+        live[0][1 + i] = extra[i];
+    nlive[0] = unique_sorted(live[0], 1 + n_extra);
+    for (uint32_t level = 0; level < maxl; level++) {
+        uint64_t cap = 0;
+        for (uint64_t i = 0; i < nlive[level]; i++)
+            cap += total_size(*sys_ptr(t, live[level][i])) - 1;
+        live[level + 1] = (uint32_t*)malloc((cap + 1) * 4);
+        uint64_t k = 0;
+        for (uint64_t i = 0; i < nlive[level]; i++) {
+            const uint32_t* p = sys_ptr(t, live[level][i]);
+            for (uint32_t o = 1; o < total_size(p[0]); o++)
+                live[level + 1][k++] = p[o];
+        }
+        nlive[level + 1] = unique_sorted(live[level + 1], k);
+    }
+    /* rebuild bottom-up (:443-538) */
+    uint32_t* newidx[HD_MAX_DEPTH] = {0};
+    for (int32_t level = (int32_t)maxl; level >= 0; level--) {
+        const int leaf = (uint32_t)level == t->leaf_level;
+        uint64_t words = 0;
+        for (uint64_t i = 0; i < nlive[level]; i++)
+            words += leaf ? 2 : total_size(*sys_ptr(t, live[level][i]));
+        uint32_t* temp = (uint32_t*)malloc((words + 1) * 4);
+        uint64_t* at = (uint64_t*)malloc((nlive[level] + 1) * 8);
+        uint64_t w = 0;
+        for (uint64_t i = 0; i < nlive[level]; i++) {
+            const uint32_t* p = sys_ptr(t, live[level][i]);
+            const uint32_t n = leaf ? 2 : total_size(p[0]);
+            at[i] = w;
+            temp[w] = p[0];
+            for (uint32_t o = 1; o < n; o++) {
+                if (!leaf && (uint32_t)level != maxl) {
+                    uint64_t pos = find_sorted(live[level + 1], nlive[level + 1], p[o]);
+                    temp[w + o] = newidx[level + 1][pos];
+                } else {
+                    temp[w + o] = p[o];
+                }
+            }
+            w += n;
+        }
+        for (uint32_t b = 0; b < bucket_count(&t->cfg, (uint32_t)level); b++)
+            t->bucket_sizes[bucket_global(&t->cfg, (uint32_t)level, b)] = 0;
+        t->level_nodes[level] = 0;
+        add_full_node(t, (uint32_t)level);
+        newidx[level] = (uint32_t*)malloc((nlive[level] + 1) * 4);
+        for (uint64_t i = 0; i < nlive[level]; i++) {
+            const uint32_t* node = temp + at[i];
+            if (leaf) {
+                const uint64_t lf = (uint64_t)node[0] | ((uint64_t)node[1] << 32);
+                newidx[level][i] = add_leaf(t, lf, or_hash_leaf(lf));
+            } else {
+                const uint32_t n = total_size(node[0]);
+                newidx[level][i] = add_interior(t, (uint32_t)level, n, node, or_hash_interior(n, node));
+            }
+        }
+        free(temp);
+        free(at);
+        if (level + 1 <= (int32_t)maxl) {
+            free(newidx[level + 1]);
+            newidx[level + 1] = NULL;
+        }
+    }
+    t->root = newidx[0][find_sorted(live[0], nlive[0], t->root)];
+    for (uint32_t i = 0; i < n_extra; i++)
+        extra[i] = newidx[0][find_sorted(live[0], nlive[0], extra[i])];
+    free(newidx[0]);
+    for (uint32_t l = 0; l <= maxl; l++)
+        free(live[l]);
+    return t->error;
+}

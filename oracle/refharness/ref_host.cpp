@@ -1,0 +1,242 @@
+// ORACLE — test infrastructure only.
+//
+// Builds the reference's own host-side hot path (HashTable, HashDAGFactory,
+// HashDagEdits, editors, remove_stale_nodes) from its unmodified sources and
+// exposes a small C API used to generate the golden fixtures that pin the
+// C restatement (oracle/hd_oracle.c).  Compiled by oracle/build_ref.py into
+// oracle/_ref/libhdref_d<depth>.so; never shipped, never linked by the
+// product.
+//
+// Compile-time configuration (command line): BENCHMARK=1 (single-threaded,
+// no undo), USE_BLOOM_FILTER=0, EDITS_ENABLE_COLORS=0, EDITS_COUNTERS=1,
+// HARNESS_DEPTH, BUCKETS_BITS_FOR_TOP_LEVELS, and
+// C_colorTreeLevels="CTL_VALUE = <T>, CTL_IGNORED" which turns the
+// reference's `constexpr uint32 C_colorTreeLevels = 10;`
+// (hash_dag_globals.h:7) into `constexpr uint32 CTL_VALUE = <T>, CTL_IGNORED
+// = 10;` so that the colour-tree depth can follow the scene depth.
+
+// Standard headers first: the harness opens the reference's classes for
+// reading (private -> public) and the library headers must not see that.
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <chrono>
+#include <cinttypes>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <functional>
+#include <iomanip>
+#include <iostream>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <random>
+#include <set>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <type_traits>
+#include <unordered_map>
+#include <unordered_set>
+#include <utility>
+#include <vector>
+#include <cuda_runtime.h>
+#define private public
+#define protected public
+
+#include "typedefs.h"
+// script_definitions.h forces USE_VIDEO=1 and with it SCENE_DEPTH=17; every
+// use of the depth goes through MAX_LEVELS -> SCENE_DEPTH later on.
+#undef SCENE_DEPTH
+#define SCENE_DEPTH HARNESS_DEPTH
+#include "dags/hash_dag/hash_dag_globals.h"
+#undef C_colorTreeLevels
+#define C_colorTreeLevels CTL_VALUE
+
+#include "camera_view.h"
+#include "dags/hash_dag/hash_dag.h"
+#include "dags/hash_dag/hash_dag_editors.h"
+#include "dags/hash_dag/hash_dag_factory.h"
+
+// The reference's translation units, compiled here as one unit so the
+// overrides above apply everywhere.
+#include "hash_table.cpp"
+#include "stats.cpp"
+#include "hash_dag_factory.cpp"
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+
+// ---------------------------------------------------------------------------
+// Host-memory stand-ins for Memory (memory.h:15-117) and the few CUDA runtime
+// calls the host path makes: device allocations become host allocations and
+// host<->device copies become memcpy, so the table the reference "uploads"
+// is simply left in host memory.
+// ---------------------------------------------------------------------------
+Memory Memory::singleton;
+Memory::~Memory() {}
+void* Memory::malloc_impl(size_t size, const char*, EMemoryType)
+{
+    void* p = std::calloc(1, size ? size : 1);
+    Element e;
+    e.size = size;
+    allocations[p] = e;
+    return p;
+}
+void Memory::free_impl(void* ptr)
+{
+    allocations.erase(ptr);
+    std::free(ptr);
+}
+void Memory::realloc_impl(void*& ptr, size_t newSize)
+{
+    size_t old = allocations.count(ptr) ? allocations[ptr].size : 0;
+    void* p = std::calloc(1, newSize ? newSize : 1);
+    if (ptr)
+        std::memcpy(p, ptr, std::min(old, newSize));
+    allocations.erase(ptr);
+    std::free(ptr);
+    Element e;
+    e.size = newSize;
+    allocations[p] = e;
+    ptr = p;
+}
+void Memory::cuda_memcpy_impl(uint8* dst, const uint8* src, uint64 size, cudaMemcpyKind)
+{
+    std::memmove(dst, src, size);
+}
+const char* Memory::get_alloc_name_impl(void*) const { return "harness"; }
+std::string Memory::get_stats_string_impl() const { return {}; }
+
+extern "C" {
+cudaError_t cudaMemcpyAsync(void* dst, const void* src, size_t count, cudaMemcpyKind, cudaStream_t)
+{
+    std::memmove(dst, src, count);
+    return cudaSuccess;
+}
+cudaError_t cudaMemcpy(void* dst, const void* src, size_t count, cudaMemcpyKind)
+{
+    std::memmove(dst, src, count);
+    return cudaSuccess;
+}
+cudaError_t cudaDeviceSynchronize(void) { return cudaSuccess; }
+cudaError_t cudaGetLastError(void) { return cudaSuccess; }
+const char* cudaGetErrorString(cudaError_t) { return "harness"; }
+}
+
+// ---------------------------------------------------------------------------
+// Harness state: one scene per process (the reference's HashTable keeps its
+// host data in a static singleton, hash_table.h:862).
+// ---------------------------------------------------------------------------
+static HashDAG g_dag;
+static HashDAGColors g_colors;
+static StatsRecorder* g_recorder = nullptr;
+static bool g_loaded = false;
+
+extern "C" uint32 ref_depth() { return MAX_LEVELS; }
+extern "C" uint32 ref_color_tree_levels() { return C_colorTreeLevels; }
+extern "C" uint32 ref_total_buckets() { return C_totalNumberOfBuckets; }
+extern "C" uint32 ref_total_pages() { return C_totalPages; }
+
+// HashDAGFactory::load_from_DAG on a BasicDAG word array.
+extern "C" int ref_load(const uint32* words, uint64 nWords, uint32 poolPages)
+{
+    if (g_loaded)
+        return 1;
+    BasicDAG basic;
+    basic.data = StaticArray<uint32>::allocate("basic dag", nWords, EMemoryType::CPU);
+    std::memcpy(basic.data.data(), words, nWords * sizeof(uint32));
+    HashDAGFactory::load_from_DAG(g_dag, basic, poolPages);
+    // A colour tree whose root has no children: the edit recursion reads it
+    // (hash_dag_edits.h:168-173) but, with colours off, never fills it.
+    HashColorsBuilder builder;
+    builder.nodes.assign(8, 0);
+    builder.build(g_colors, CompressedColorLeaf{});
+    g_recorder = new StatsRecorder();
+    g_loaded = true;
+    return 0;
+}
+
+extern "C" uint32 ref_root() { return g_dag.firstNodeIndex; }
+extern "C" uint32 ref_pool_top() { return uint32(g_dag.data.get_allocated_pages() + 1); }
+
+// Copies the reference's own table: bucket sizes, page table, pool
+// (poolTop pages), full-node indices.
+extern "C" void ref_export(uint32* bucketSizes, uint32* pageTable, uint32* pool, uint64 poolWords, uint32* fullNodes)
+{
+    auto& cpu = HashTable::cpuData;
+    std::memcpy(bucketSizes, cpu.bucketsSizes, C_totalNumberOfBuckets * sizeof(uint32));
+    std::memcpy(pageTable, cpu.cpuPageTable, C_totalPages * sizeof(uint32));
+    const uint64 words = std::min<uint64>(poolWords, uint64(g_dag.data.poolTop) * C_pageSize);
+    std::memcpy(pool, cpu.cpuPool, words * sizeof(uint32));
+    for (uint32 level = 0; level < C_maxNumberOfLevels; level++)
+        fullNodes[level] = level <= C_leafLevel ? cpu.fullNodeIndices[level] : 0;
+}
+
+extern "C" uint32 ref_read_word(uint32 level, uint32 vptr) { return *g_dag.data.get_sys_ptr(level, vptr); }
+
+static uint64 morton(uint3 p, uint32 bits)
+{
+    uint64 key = 0;
+    for (int32 b = int32(bits) - 1; b >= 0; b--)
+        key = (key << 3) | (uint64((p.x >> b) & 1) << 2) | (uint64((p.y >> b) & 1) << 1) | uint64((p.z >> b) & 1);
+    return key;
+}
+
+// HashDAG::edit_threads (hash_dag.h:255-405) with its task list run in
+// depth-first order of the tasks' level-C_colorTreeLevels paths instead of
+// unordered_map iteration order; colours and undo off (BENCHMARK).
+template<typename TEditor>
+static void run_edit(const TEditor& editor, uint64* stats)
+{
+    HashDagEdits::ThreadedEditParameters parameters{ g_dag.data, g_colors, *g_recorder };
+    HashDagEdits::edit_threaded<true>(0, g_dag.firstNodeIndex, 0, Path(0, 0, 0), editor, parameters);
+    std::vector<std::pair<uint64, HashDagEdits::Thread*>> tasks;
+    for (auto& it : parameters.threads)
+        tasks.emplace_back(morton(it.first, C_colorTreeLevels), it.second.get());
+    std::sort(tasks.begin(), tasks.end(),
+              [](const std::pair<uint64, HashDagEdits::Thread*>& a, const std::pair<uint64, HashDagEdits::Thread*>& b) {
+                  return a.first < b.first;
+              });
+    for (auto& task : tasks)
+        task.second->lambda();
+    for (auto& it : parameters.threads)
+        parameters.stats += it.second->stats;
+    g_dag.firstNodeIndex =
+        HashDagEdits::edit_threaded<false>(0, g_dag.firstNodeIndex, 0, Path(0, 0, 0), editor, parameters).nodeIndex;
+    stats[0] = parameters.stats.numVoxels;
+    stats[1] = parameters.stats.numNodes;
+}
+
+// tool: 0 sphere remove, 1 sphere add, 2 box remove, 3 box add
+extern "C" int ref_edit(uint32 tool, float cx, float cy, float cz, float radius, uint64* stats)
+{
+    const float3 c = make_float3(cx, cy, cz);
+    switch (tool) {
+    case 0: run_edit(SphereEditor<false>(c, radius), stats); break;
+    case 1: run_edit(SphereEditor<true>(c, radius), stats); break;
+    case 2: run_edit(BoxEditor<false>(c, radius), stats); break;
+    case 3: run_edit(BoxEditor<true>(c, radius), stats); break;
+    default: return 1;
+    }
+    return 0;
+}
+
+// HashDAG::remove_stale_nodes(levels - 2) (hash_dag.h:407-547), which also
+// re-uploads the whole table (a host copy here).
+extern "C" void ref_gc() { g_dag.remove_stale_nodes(C_leafLevel); }
+
+// DAGUtils::get_value (dag_utils.h:138-172)
+extern "C" int ref_get_value(uint32 x, uint32 y, uint32 z) { return DAGUtils::get_value(g_dag, Path(x, y, z)) ? 1 : 0; }
+
+// HashTable::get_level_size (hash_table.cpp:277-285)
+extern "C" uint32 ref_level_size(uint32 level) { return g_dag.data.get_level_size(level); }
+
+// Hash known-answer vectors (hash_table.h:80-89).
+extern "C" uint32 ref_hash_leaf(uint64 leaf) { return HashDagUtils::hash_leaf(leaf); }
+extern "C" uint32 ref_hash_interior(uint32 n, const uint32* node) { return HashDagUtils::hash_interior(n, node); }
