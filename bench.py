@@ -1,0 +1,385 @@
+#!/usr/bin/env python
+"""Traversal benchmark of the seeded 2^15 scene (primary + shadow rays).
+
+Workload (Catmull-Rom traversal of the 2^15 scene): the seeded procedural
+scene at depth 15 generated and ingested on the device before timing; 64
+camera poses on a seeded Catmull-Rom path at 1920x1080 (90 degree FOV); one
+step = one pose: a primary ray per pixel and, on a hit, one shadow ray toward
+normalize(0.3, 1, 0.2) with bias 1.  Metric: Mrays/s (primary + shadow).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+value  = device throughput (CUDA events around the two launches of each
+         step; L2 flushed with a 512 MB write before every timed step).
+e2e    = the same metric through the C ABI with host buffers: camera from
+         host memory, paths + shadow mask copied back to pinned host memory
+         every step.
+--impl reference times the oracle's CPU restatement of the reference tracer
+(the reference has no CPU tracer) on all host cores, a bounded band of rows
+per step.  Under torchrun every rank renders its own poses on its own GPU
+(replicas, no collective on the data path).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s primary+shadow"
+LIGHT = (0.3, 1.0, 0.2)
+BIAS = 1.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=64)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    p.add_argument("--depth", type=int, default=15)
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--poses", type=int, default=64)
+    p.add_argument("--ref-rows", type=int, default=192, help="rows per step of the CPU reference arm")
+    p.add_argument("--cpu-sample-rows", type=int, default=256, help="rows of the cpu_baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl" if os.environ.get("HD_BENCH_GLOO") is None else "gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], device="cuda")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], device="cuda")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def traffic_from_profiles(workload):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
+    summary, when it covers this workload."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(workload)
+    except (OSError, ValueError):
+        return None
+
+
+def algorithmic_bytes(counts):
+    """Bytes a ray touches by the traversal's own accounting: 8 B for the
+    root (page-table entry + header), 16 B per interior descent (child
+    pointer, header, two page-table entries), 20 B per leaf fetch (pointer,
+    8 B leaf, two page-table entries), plus the output (16 B path for a
+    primary ray; 16 B path read + 1 B mask for a shadow ray)."""
+    prim = 8 * counts[0] + 16 * counts[1] + 20 * counts[2] + 16 * counts[0]
+    shad = 8 * counts[3] + 16 * counts[4] + 20 * counts[5] + 17 * counts[3]
+    return prim, shad
+
+
+def load_scene(depth):
+    import hashdag_gb300 as hd
+    dag = hd.HashDAG(depth)
+    t0 = time.perf_counter()
+    dag.generate_scene(1)
+    return dag, time.perf_counter() - t0
+
+
+def oracle_from(dag, depth):
+    from oracle import pyoracle as po
+    t = dag.export_table()
+    ot = po.Table(po.default_config(depth, pool_pages=int(t["pool"].size // 512) + 16))
+    ot.import_(t)
+    return ot
+
+
+def cpu_baseline(ot, cams_params, W, H, rows):
+    threads = os.cpu_count() or 1
+    r0 = max(0, H // 2 - rows // 2)
+    t0 = time.perf_counter()
+    paths, mask = ot.trace_frame(cams_params[0], W, H, LIGHT, BIAS, fp_mode=1, threads=threads, rows=(r0, r0 + rows))
+    dt = time.perf_counter() - t0
+    out_rows = slice(H - (r0 + rows), H - r0)
+    hits = int((mask[out_rows] != 2).sum())
+    rays = rows * W + hits
+    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{rows} rows x {W} px of pose 0 (primary + {hits} shadow rays), oracle C restatement, "
+                      f"{threads} threads, {dt:.1f} s"}
+
+
+def run_reference(args, dist):
+    """The CPU arm: the oracle's restatement of the reference tracer."""
+    if dist.rank != 0:
+        return
+    import torch
+    torch.cuda.set_device(dist.local)
+    from hashdag_gb300 import workloads
+    W, H, depth = args.width, args.height, args.depth
+    dag, _ = load_scene(depth)
+    ot = oracle_from(dag, depth)
+    dag.free()
+    poses = workloads.catmull_rom_path(depth, args.poses, W, H)
+    threads = os.cpu_count() or 1
+    rows = args.ref_rows
+
+    def step(k):
+        cam = poses[k % len(poses)]
+        r0 = (k * 37) % max(1, H - rows)
+        paths, mask = ot.trace_frame(cam, W, H, LIGHT, BIAS, fp_mode=1, threads=threads, rows=(r0, r0 + rows))
+        out_rows = slice(H - (r0 + rows), H - r0)
+        return rows * W + int((mask[out_rows] != 2).sum())
+
+    for k in range(args.warmup):
+        step(k)
+    t0 = time.perf_counter()
+    rays = 0
+    for k in range(args.steps):
+        rays += step(args.warmup + k)
+    dt = time.perf_counter() - t0
+    value = rays / dt / 1e6
+    line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"catmull_rom_d{depth}_{W}x{H}", "depth": depth, "poses": args.poses,
+                       "rows_per_step": rows, "l2": "host CPU run"},
+            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": f"{rows} rows x {W} px per step, oracle C restatement of the reference "
+                                       f"tracer (the reference has no CPU tracer)"},
+            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, dist):
+    import torch
+    torch.cuda.set_device(dist.local)
+    import hashdag_gb300 as hd
+    from hashdag_gb300 import _capi, build, workloads
+    build.build()
+    L = _capi.lib()
+    W, H, depth, K = args.width, args.height, args.depth, args.steps
+    dag, gen_s = load_scene(depth)
+    poses = workloads.catmull_rom_path(depth, args.poses, W, H)
+    cams = [_capi.Camera.from_params(p) for p in poses]
+    paths = torch.zeros(W * H * 4, dtype=torch.int32, device="cuda")
+    mask = torch.zeros(W * H, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    light = (C.c_float * 3)(*LIGHT)
+    h = dag.handle
+
+    def pose(k):
+        return cams[(k + dist.rank * 7) % len(cams)]
+
+    # traversal counters of every pose the timed steps render (outside timing)
+    counts = [0] * 6
+    per_pose = {}
+    for k in range(K):
+        i = (k + dist.rank * 7) % len(cams)
+        if i not in per_pose:
+            out = (C.c_uint64 * 6)()
+            dag._check(L.hd_trace_counters(h, C.byref(cams[i]), W, H, light, BIAS, paths.data_ptr(),
+                                           mask.data_ptr(), out))
+            per_pose[i] = list(out)
+        counts = [a + b for a, b in zip(counts, per_pose[i])]
+    rays_total = counts[0] + counts[3]
+    prim_bytes, shad_bytes = algorithmic_bytes(counts)
+
+    def launch(k):
+        cam = pose(k)
+        dag._check(L.hd_trace_primary(h, C.byref(cam), W, H, paths.data_ptr(), None))
+        dag._check(L.hd_trace_shadow(h, C.byref(cam), W, H, paths.data_ptr(), light, BIAS, mask.data_ptr(), None))
+
+    for k in range(args.warmup):
+        launch(k)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+            torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    clocks = ClockSampler(torch.cuda.current_device())
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    wall0 = time.perf_counter()
+    for k in range(K):
+        flush.fill_(k & 0xff)  # writes 512 MB: evicts the 129 MB L2
+        e0, e1, e2 = evs[k]
+        e0.record()
+        cam = pose(k)
+        dag._check(L.hd_trace_primary(h, C.byref(cam), W, H, paths.data_ptr(), None))
+        e1.record()
+        dag._check(L.hd_trace_shadow(h, C.byref(cam), W, H, paths.data_ptr(), light, BIAS, mask.data_ptr(), None))
+        e2.record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    dist.barrier()
+    clk = clocks.stop()
+    ms_p = sum(e0.elapsed_time(e1) for e0, e1, _ in evs)
+    ms_s = sum(e1.elapsed_time(e2) for _, e1, e2 in evs)
+    total_ms = dist.max(ms_p + ms_s)
+    rays_all = dist.sum(rays_total)
+    value = rays_all / (total_ms * 1e-3) / 1e6
+
+    # end to end through the C ABI with host buffers
+    h_paths = torch.empty(W * H * 4, dtype=torch.int32, pin_memory=True)
+    h_mask = torch.empty(W * H, dtype=torch.uint8, pin_memory=True)
+    host_cam = [_capi.Camera.from_params(poses[(k + dist.rank * 7) % len(cams)]) for k in range(K)]
+    torch.cuda.synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for k in range(K):
+        flush.fill_(k & 0xff)
+        dag._check(L.hd_trace_frame(h, C.byref(host_cam[k]), W, H, light, BIAS, paths.data_ptr(), mask.data_ptr(),
+                                    None, None))
+        h_paths.copy_(paths, non_blocking=True)
+        h_mask.copy_(mask, non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    # the L2 flush is not part of the traversal: time it alone and take it out
+    torch.cuda.synchronize()
+    f0 = time.perf_counter()
+    for k in range(K):
+        flush.fill_(k & 0xff)
+    torch.cuda.synchronize()
+    flush_s = time.perf_counter() - f0
+    e2e_value = rays_all / max(1e-9, e2e_s - flush_s) / 1e6
+
+    peaks, peak_kind = measured_peaks()
+    dominant = "trace_primary" if ms_p >= ms_s else "trace_shadow"
+    dom_ms = (ms_p if ms_p >= ms_s else ms_s) / K
+    dom_bytes = (prim_bytes if ms_p >= ms_s else shad_bytes) / K
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    workload = f"catmull_rom_d{depth}_{W}x{H}"
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": dom_bytes, "traffic": traffic_from_profiles(workload),
+                "primary_ms_per_launch": ms_p / K, "shadow_ms_per_launch": ms_s / K,
+                "primary_bytes_per_launch": prim_bytes / K, "shadow_bytes_per_launch": shad_bytes / K}
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        try:
+            ot = oracle_from(dag, depth)
+            cpu = cpu_baseline(ot, poses, W, H, args.cpu_sample_rows)
+            del ot
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {e}"}
+    line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": dist.world, "steps": K,
+            "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload, "depth": depth, "width": W, "height": H, "poses": args.poses,
+                       "light": list(LIGHT), "shadow_bias": BIAS, "l2": "flushed (512 MB write) before every step",
+                       "scene_gen_s": round(gen_s, 2), "rays_per_step": rays_total / K,
+                       "parallelism": f"replicas x{dist.world}"},
+            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(_capi.Camera),
+                    "d2h_bytes_per_step": W * H * 16 + W * H},
+            "gpu_launches": 2 * K, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "wall_s": wall}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dag.free()
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+    else:
+        run_gpu(args, dist)
+    if dist.pg:
+        dist.pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

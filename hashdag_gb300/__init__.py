@@ -1,0 +1,245 @@
+"""hashdag_gb300 — GB300-native hashed sparse voxel DAG hot path.
+
+Host-side mirror of the reference's interfaces (Phyronnaz/HashDAG) over the
+C ABI of libhashdag_gb300.so:
+
+* HashDAG        — HashDAG (hash_dag.h:214-636) with the device-resident
+                   HashTable; load_from_DAG (hash_dag_factory.cpp:152-184),
+                   edit_threads (hash_dag.h:255-405), remove_stale_nodes
+                   (hash_dag.h:407-547).
+* DAGTracer      — DAGTracer (dag_tracer.h:9-42), headless: resolve_paths /
+                   resolve_shadows return kernel milliseconds and keep their
+                   results in device buffers.
+* SphereEditor / BoxEditor — the editors (hash_dag_editors.h:223-313).
+
+Every call runs sm_103a kernels; there is no CPU path.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import Camera, Config, Edit, EditStats, HashDagError, LevelStats, lib
+
+__all__ = ["HashDAG", "DAGTracer", "SphereEditor", "BoxEditor", "Camera", "Config", "EditStats", "LevelStats",
+           "HashDagError", "default_config"]
+
+TOOL_SPHERE_REMOVE, TOOL_SPHERE_ADD, TOOL_BOX_REMOVE, TOOL_BOX_ADD = 0, 1, 2, 3
+
+
+def default_config(depth, **overrides):
+    cfg = Config()
+    lib().hd_default_config(depth, C.byref(cfg))
+    for k, v in overrides.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise HashDagError(_capi.HD_ERR_STATE, "no CUDA device")
+    return torch
+
+
+class _Editor:
+    tool = None
+
+    def __init__(self, center, radius):
+        self.center = tuple(float(np.float32(v)) for v in center)
+        self.radius = float(np.float32(radius))
+
+    def to_edit(self):
+        return Edit(self.tool, (C.c_float * 3)(*self.center), self.radius)
+
+
+class SphereEditor(_Editor):
+    """SphereEditor<isAdding> (hash_dag_editors.h:272-313)."""
+
+    def __init__(self, center, radius, adding):
+        super().__init__(center, radius)
+        self.tool = TOOL_SPHERE_ADD if adding else TOOL_SPHERE_REMOVE
+
+
+class BoxEditor(_Editor):
+    """BoxEditor<isAdding> (hash_dag_editors.h:223-270); radius is the half
+    extent."""
+
+    def __init__(self, center, radius, adding):
+        super().__init__(center, radius)
+        self.tool = TOOL_BOX_ADD if adding else TOOL_BOX_REMOVE
+
+
+def editor_from_tuple(t):
+    tool, center, radius = t
+    if tool in (TOOL_SPHERE_REMOVE, TOOL_SPHERE_ADD):
+        return SphereEditor(center, radius, tool == TOOL_SPHERE_ADD)
+    return BoxEditor(center, radius, tool == TOOL_BOX_ADD)
+
+
+class HashDAG:
+    """A device-resident hash DAG (one hd_ctx)."""
+
+    def __init__(self, depth=None, config=None):
+        if config is None:
+            config = default_config(depth)
+        self.config = config
+        self._h = C.c_void_p()
+        st = lib().hd_create(C.byref(config), C.byref(self._h))
+        if st != _capi.HD_OK:
+            raise HashDagError(st, "hd_create failed")
+
+    # -- lifetime ----------------------------------------------------------
+    def free(self):
+        if self._h:
+            lib().hd_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        _capi.check(self._h, st)
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def levels(self):
+        return self.config.depth
+
+    def leaf_level(self):
+        return self.config.depth - 2
+
+    # -- ingest ------------------------------------------------------------
+    def load_from_DAG(self, words):
+        """HashDAGFactory::load_from_DAG on BasicDAG words (host array)."""
+        words = np.ascontiguousarray(words, np.uint32)
+        self._check(lib().hd_load_basic_dag(self._h, words.ctypes.data, words.size))
+
+    def generate_scene(self, seed):
+        self._check(lib().hd_generate_scene(self._h, seed))
+
+    def export_basic_dag(self):
+        n = C.c_uint64()
+        self._check(lib().hd_export_basic_dag(self._h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.uint32)
+        self._check(lib().hd_export_basic_dag(self._h, out.ctypes.data, out.size, C.byref(n)))
+        return out
+
+    # -- state -------------------------------------------------------------
+    @property
+    def firstNodeIndex(self):
+        v = C.c_uint32()
+        self._check(lib().hd_get_root(self._h, C.byref(v)))
+        return v.value
+
+    @firstNodeIndex.setter
+    def firstNodeIndex(self, v):
+        self._check(lib().hd_set_root(self._h, int(v)))
+
+    def level_stats(self):
+        s = LevelStats()
+        self._check(lib().hd_get_level_stats(self._h, C.byref(s)))
+        return s
+
+    def export_table(self):
+        nb, nv, npu = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self._check(lib().hd_table_sizes(self._h, C.byref(nb), C.byref(nv), C.byref(npu)))
+        bs = np.zeros(nb.value, np.uint32)
+        pt = np.zeros(nv.value, np.uint32)
+        pool = np.zeros((npu.value + 1) * 512, np.uint32)
+        full = np.zeros(self.config.depth, np.uint32)
+        self._check(lib().hd_export_table(self._h, bs.ctypes.data, pt.ctypes.data, pool.ctypes.data, pool.size,
+                                          full.ctypes.data))
+        return dict(bucket_sizes=bs, page_table=pt, pool=pool, full_nodes=full, root=self.firstNodeIndex)
+
+    def import_table(self, t):
+        self._check(lib().hd_import_table(self._h, t["bucket_sizes"].ctypes.data, t["page_table"].ctypes.data,
+                                          t["pool"].ctypes.data, t["pool"].size, t["full_nodes"].ctypes.data,
+                                          int(t["root"])))
+
+    def device_table(self):
+        pool, pt, bs = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        self._check(lib().hd_device_table(self._h, C.byref(pool), C.byref(pt), C.byref(bs)))
+        return pool.value, pt.value, bs.value
+
+    def sync(self):
+        self._check(lib().hd_sync(self._h))
+
+    # -- queries -----------------------------------------------------------
+    def get_values(self, xyz):
+        """DAGUtils::get_value for n x 3 voxel coordinates (host array)."""
+        torch = _torch()
+        xyz = np.ascontiguousarray(xyz, np.uint32).reshape(-1, 3)
+        d_in = torch.from_numpy(xyz.view(np.int32)).cuda()
+        d_out = torch.empty(len(xyz), dtype=torch.uint8, device="cuda")
+        self._check(lib().hd_get_values(self._h, d_in.data_ptr(), len(xyz), d_out.data_ptr()))
+        self.sync()
+        return d_out.cpu().numpy()
+
+    # -- edits and GC --------------------------------------------------------
+    def edit_threads(self, editor):
+        """HashDAG::edit_threads(editor, ...): one edit; returns EditStats."""
+        s = EditStats()
+        e = editor.to_edit()
+        self._check(lib().hd_edit_apply(self._h, C.byref(e), C.byref(s)))
+        return s
+
+    def edit_batch(self, editors):
+        arr = (Edit * len(editors))(*[e.to_edit() for e in editors])
+        s = EditStats()
+        self._check(lib().hd_edit_batch(self._h, arr, len(editors), C.byref(s)))
+        return s
+
+    def remove_stale_nodes(self, extra_roots=()):
+        """HashDAG::remove_stale_nodes(levels - 2), marking from the root and
+        from extra_roots (kept undo states); returns the remapped extra
+        roots."""
+        arr = np.array(list(extra_roots) + [0], np.uint32)
+        self._check(lib().hd_gc(self._h, arr.ctypes.data, len(extra_roots)))
+        return [int(v) for v in arr[:len(extra_roots)]]
+
+    def set_fp_mode(self, mode):
+        self._check(lib().hd_set_fp_mode(self._h, int(mode)))
+
+
+class DAGTracer:
+    """Headless DAGTracer: results in device buffers (torch tensors)."""
+
+    def __init__(self, width, height):
+        torch = _torch()
+        self.width, self.height = int(width), int(height)
+        self.paths = torch.zeros((self.height, self.width, 4), dtype=torch.int32, device="cuda")
+        self.shadows = torch.zeros((self.height, self.width), dtype=torch.uint8, device="cuda")
+
+    def resolve_paths(self, camera, dag):
+        """Tracer::trace_paths; returns kernel ms."""
+        cam = camera if isinstance(camera, Camera) else Camera.from_params(camera)
+        ms = C.c_float()
+        dag._check(lib().hd_trace_primary(dag.handle, C.byref(cam), self.width, self.height,
+                                          self.paths.data_ptr(), C.byref(ms)))
+        return ms.value
+
+    def resolve_shadows(self, camera, dag, shadow_bias=1.0, light=(0.3, 1.0, 0.2)):
+        """trace_shadows' hit test from the paths of resolve_paths; returns ms."""
+        cam = camera if isinstance(camera, Camera) else Camera.from_params(camera)
+        ms = C.c_float()
+        lt = (C.c_float * 3)(*light)
+        dag._check(lib().hd_trace_shadow(dag.handle, C.byref(cam), self.width, self.height,
+                                         self.paths.data_ptr(), lt, float(shadow_bias),
+                                         self.shadows.data_ptr(), C.byref(ms)))
+        return ms.value
+
+    def get_paths(self):
+        return self.paths.cpu().numpy().view(np.uint32)
+
+    def get_shadows(self):
+        return self.shadows.cpu().numpy()
+
+    def get_path(self, x, y):
+        return tuple(int(v) for v in self.paths[y, x, :3].cpu().numpy().view(np.uint32))

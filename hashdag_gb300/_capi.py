@@ -1,0 +1,115 @@
+"""ctypes bindings of the C ABI (include/hashdag_gb300.h) over the in-tree
+libhashdag_gb300.so.  There is no fallback: importing the bindings without
+the built library raises."""
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libhashdag_gb300.so")
+
+HD_OK, HD_ERR_INVALID, HD_ERR_CUDA, HD_ERR_POOL_FULL, HD_ERR_BUCKET_FULL, HD_ERR_TIMEOUT, HD_ERR_OOM, \
+    HD_ERR_STATE = range(8)
+STATUS_NAMES = {0: "HD_OK", 1: "HD_ERR_INVALID", 2: "HD_ERR_CUDA", 3: "HD_ERR_POOL_FULL", 4: "HD_ERR_BUCKET_FULL",
+                5: "HD_ERR_TIMEOUT", 6: "HD_ERR_OOM", 7: "HD_ERR_STATE"}
+MAX_DEPTH = 20
+INVALID_NODE = 0xDFFFFFF
+
+
+class Config(C.Structure):
+    _fields_ = [("depth", C.c_uint32), ("color_tree_levels", C.c_uint32), ("top_levels", C.c_uint32),
+                ("top_bucket_bits", C.c_uint32), ("low_bucket_bits", C.c_uint32),
+                ("top_bucket_size", C.c_uint32), ("low_bucket_size", C.c_uint32),
+                ("pool_pages", C.c_uint32)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", C.c_double * 3), ("ray_min", C.c_double * 3), ("ray_ddx", C.c_double * 3),
+                ("ray_ddy", C.c_double * 3)]
+
+    @classmethod
+    def from_params(cls, p):
+        c = cls()
+        for f in ("position", "ray_min", "ray_ddx", "ray_ddy"):
+            getattr(c, f)[:] = [float(v) for v in (p[f] if isinstance(p, dict) else getattr(p, f))]
+        return c
+
+
+class Edit(C.Structure):
+    _fields_ = [("tool", C.c_uint32), ("center", C.c_float * 3), ("radius", C.c_float)]
+
+
+class EditStats(C.Structure):
+    _fields_ = [("num_voxels", C.c_uint64), ("num_nodes", C.c_uint64), ("find_or_add_calls", C.c_uint64),
+                ("nodes_added", C.c_uint64), ("words_scanned", C.c_uint64), ("device_ms", C.c_float),
+                ("host_ms", C.c_float)]
+
+
+class LevelStats(C.Structure):
+    _fields_ = [("words", C.c_uint64 * MAX_DEPTH), ("nodes", C.c_uint64 * MAX_DEPTH), ("pages_used", C.c_uint64),
+                ("root", C.c_uint32), ("levels", C.c_uint32)]
+
+
+class HashDagError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+# (name, restype, argtypes) of every exported entry point
+_P = C.c_void_p
+_u32, _u64, _f32 = C.c_uint32, C.c_uint64, C.c_float
+SIGNATURES = [
+    ("hd_abi_version", _u32, []),
+    ("hd_default_config", None, [_u32, C.POINTER(Config)]),
+    ("hd_create", C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
+    ("hd_destroy", C.c_int, [_P]),
+    ("hd_last_error", C.c_char_p, [_P]),
+    ("hd_set_stream", C.c_int, [_P, _P]),
+    ("hd_sync", C.c_int, [_P]),
+    ("hd_load_basic_dag", C.c_int, [_P, _P, _u64]),
+    ("hd_generate_scene", C.c_int, [_P, _u64]),
+    ("hd_export_basic_dag", C.c_int, [_P, _P, _u64, C.POINTER(_u64)]),
+    ("hd_trace_primary", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _P, C.POINTER(_f32)]),
+    ("hd_trace_shadow", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _P, C.POINTER(_f32), _f32, _P,
+                                  C.POINTER(_f32)]),
+    ("hd_trace_frame", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, C.POINTER(_f32), _f32, _P, _P,
+                                 C.POINTER(_f32), C.POINTER(_f32)]),
+    ("hd_trace_counters", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, C.POINTER(_f32), _f32, _P, _P,
+                                    C.POINTER(_u64)]),
+    ("hd_set_fp_mode", C.c_int, [_P, _u32]),
+    ("hd_get_values", C.c_int, [_P, _P, _u64, _P]),
+    ("hd_edit_apply", C.c_int, [_P, C.POINTER(Edit), C.POINTER(EditStats)]),
+    ("hd_edit_batch", C.c_int, [_P, C.POINTER(Edit), _u32, C.POINTER(EditStats)]),
+    ("hd_gc", C.c_int, [_P, _P, _u32]),
+    ("hd_get_root", C.c_int, [_P, C.POINTER(_u32)]),
+    ("hd_set_root", C.c_int, [_P, _u32]),
+    ("hd_get_config", C.c_int, [_P, C.POINTER(Config)]),
+    ("hd_get_level_stats", C.c_int, [_P, C.POINTER(LevelStats)]),
+    ("hd_table_sizes", C.c_int, [_P, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_u64)]),
+    ("hd_export_table", C.c_int, [_P, _P, _P, _P, _u64, _P]),
+    ("hd_import_table", C.c_int, [_P, _P, _P, _P, _u64, _P, _u32]),
+    ("hd_device_table", C.c_int, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+]
+
+_lib = None
+
+
+def lib():
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -m hashdag_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(ctx, status):
+    if status != HD_OK:
+        msg = lib().hd_last_error(ctx)
+        raise HashDagError(status, msg.decode() if msg else "")

@@ -1,0 +1,422 @@
+// The C ABI (include/hashdag_gb300.h): status codes instead of aborts, one
+// context per table, all work on the context's stream.
+#include <chrono>
+#include <functional>
+#include <cstring>
+#include <new>
+
+#include "hd_ctx.h"
+
+using namespace hd;
+
+namespace {
+
+template <typename F>
+hd_status guarded(hd_ctx* c, F&& f)
+{
+    try {
+        f();
+        return HD_OK;
+    } catch (const StatusError& e) {
+        if (c)
+            c->err = e.msg;
+        return e.status;
+    } catch (const CudaError& e) {
+        if (c)
+            c->err = std::string("CUDA error ") + cudaGetErrorString(e.code) + " in " + e.where;
+        return e.code == cudaErrorMemoryAllocation ? HD_ERR_OOM : HD_ERR_CUDA;
+    } catch (const std::bad_alloc&) {
+        if (c)
+            c->err = "host allocation failed";
+        return HD_ERR_OOM;
+    }
+}
+
+bool valid_config(const hd_config& c, std::string& why)
+{
+    if (c.depth < 4 || c.depth > HD_MAX_DEPTH)
+        return why = "depth must be in [4, 20]", false;
+    if (c.color_tree_levels > c.depth - 2)
+        return why = "color_tree_levels must not exceed the leaf level", false;
+    if (c.top_bucket_bits > 20 || c.low_bucket_bits > 24)
+        return why = "bucket bits too large", false;
+    if (c.top_bucket_size % HD_PAGE_SIZE || c.low_bucket_size % HD_PAGE_SIZE || !c.top_bucket_size ||
+        !c.low_bucket_size)
+        return why = "bucket sizes must be multiples of the 512-word page", false;
+    if (c.color_tree_levels + 7 < c.depth)
+        return why = "a full node at color_tree_levels would need more than 24 count bits", false;
+    const Geom g = make_geom(c);
+    if (g.total_vpages * HD_PAGE_SIZE > 0xFFFFFFFFull)
+        return why = "virtual address space exceeds 32 bits", false;
+    if (c.pool_pages < 2)
+        return why = "pool_pages too small", false;
+    return true;
+}
+
+void refresh_root(hd_ctx* c) { c->root = read_scalar(c->d_root, c->stream); }
+
+void check_device_error(hd_ctx* c, const char* what)
+{
+    const uint32_t e = check_error(c);
+    if (e)
+        throw StatusError{e == kErrCapacity ? HD_ERR_INVALID : hd_status(e), std::string(what) + " failed on the device"};
+}
+
+} // namespace
+
+extern "C" {
+
+uint32_t hd_abi_version(void) { return HD_ABI_VERSION; }
+
+void hd_default_config(uint32_t depth, hd_config* out)
+{
+    out->depth = depth;
+    out->color_tree_levels = depth >= 15 ? 10 : (depth > 5 ? depth - 5 : 0);
+    out->top_levels = 9;
+    out->top_bucket_bits = depth <= 10 ? 10 : 12;
+    out->low_bucket_bits = 16;
+    out->top_bucket_size = 1024;
+    out->low_bucket_size = 4096;
+    // enough pages for every bucket of the table
+    const Geom g = make_geom(*out);
+    uint64_t pages = g.total_vpages + 1;
+    if (pages > (1ull << 23))
+        pages = 1ull << 23; // 16 GB of pool
+    out->pool_pages = uint32_t(pages);
+}
+
+hd_status hd_create(const hd_config* cfg, hd_ctx** out)
+{
+    if (!out)
+        return HD_ERR_INVALID;
+    *out = nullptr;
+    hd_config conf;
+    if (cfg)
+        conf = *cfg;
+    else
+        hd_default_config(16, &conf);
+    std::string why;
+    if (!valid_config(conf, why))
+        return HD_ERR_INVALID;
+    hd_ctx* c = new (std::nothrow) hd_ctx();
+    if (!c)
+        return HD_ERR_OOM;
+    c->cfg = conf;
+    c->g = make_geom(conf);
+    hd_status st = guarded(c, [&] {
+        Table& t = c->t;
+        t.g = c->g;
+        HD_CUDA(cudaMalloc(&t.pool, size_t(conf.pool_pages) * HD_PAGE_SIZE * 4));
+        HD_CUDA(cudaMalloc(&t.page_table, c->g.total_vpages * 4));
+        HD_CUDA(cudaMalloc(&t.bucket_sizes, c->g.total_buckets * 4));
+        HD_CUDA(cudaMalloc(&t.full_nodes, HD_MAX_DEPTH * 4));
+        HD_CUDA(cudaMalloc(&t.pool_top, 4));
+        HD_CUDA(cudaMalloc(&t.error, 4));
+        HD_CUDA(cudaMalloc(&t.level_nodes, HD_MAX_DEPTH * 8));
+        HD_CUDA(cudaMalloc(&c->d_root, 4));
+        HD_CUDA(cudaEventCreate(&c->ev0));
+        HD_CUDA(cudaEventCreate(&c->ev1));
+        table_reset(c);
+        HD_CUDA(cudaStreamSynchronize(c->stream));
+    });
+    if (st != HD_OK) {
+        hd_destroy(c);
+        return st;
+    }
+    *out = c;
+    return HD_OK;
+}
+
+hd_status hd_destroy(hd_ctx* c)
+{
+    if (!c)
+        return HD_ERR_INVALID;
+    cudaStreamSynchronize(c->stream);
+    cudaFree(c->t.pool);
+    cudaFree(c->t.page_table);
+    cudaFree(c->t.bucket_sizes);
+    cudaFree(c->t.full_nodes);
+    cudaFree(c->t.pool_top);
+    cudaFree(c->t.error);
+    cudaFree(c->t.level_nodes);
+    cudaFree(c->d_root);
+    cudaFree(c->d_basic);
+    if (c->ev0)
+        cudaEventDestroy(c->ev0);
+    if (c->ev1)
+        cudaEventDestroy(c->ev1);
+    c->scratch.release();
+    delete c;
+    return HD_OK;
+}
+
+const char* hd_last_error(const hd_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+hd_status hd_set_stream(hd_ctx* c, void* stream)
+{
+    if (!c)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        HD_CUDA(cudaStreamSynchronize(c->stream));
+        c->stream = static_cast<cudaStream_t>(stream);
+    });
+}
+
+hd_status hd_sync(hd_ctx* c)
+{
+    if (!c)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] { HD_CUDA(cudaStreamSynchronize(c->stream)); });
+}
+
+hd_status hd_load_basic_dag(hd_ctx* c, const uint32_t* h_words, uint64_t n_words)
+{
+    if (!c || !h_words || n_words < 2)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        uint32_t* d = c->scratch.get<uint32_t>("basic_in", n_words);
+        HD_CUDA(cudaMemcpyAsync(d, h_words, n_words * 4, cudaMemcpyHostToDevice, c->stream));
+        table_reset(c);
+        import_basic_dag(c, d, n_words);
+    });
+}
+
+hd_status hd_generate_scene(hd_ctx* c, uint64_t seed)
+{
+    if (!c)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        uint32_t* words;
+        uint64_t n;
+        generate_scene(c, seed, &words, &n);
+        c->scratch.release(); // the generator's buffers are large; start the ingest clean
+        table_reset(c);
+        import_basic_dag(c, words, n);
+        c->scratch.release();
+    });
+}
+
+hd_status hd_export_basic_dag(hd_ctx* c, uint32_t* h_words, uint64_t capacity, uint64_t* n_words)
+{
+    if (!c || !n_words)
+        return HD_ERR_INVALID;
+    if (!c->d_basic)
+        return HD_ERR_STATE;
+    *n_words = c->n_basic;
+    if (!h_words)
+        return HD_OK;
+    if (capacity < c->n_basic)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        HD_CUDA(cudaMemcpyAsync(h_words, c->d_basic, c->n_basic * 4, cudaMemcpyDeviceToHost, c->stream));
+        HD_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
+hd_status hd_set_fp_mode(hd_ctx* c, uint32_t mode)
+{
+    if (!c || mode > 1)
+        return HD_ERR_INVALID;
+    c->fp_mode = mode;
+    return HD_OK;
+}
+
+static hd_status timed(hd_ctx* c, float* ms, const std::function<void()>& f)
+{
+    return guarded(c, [&] {
+        HD_CUDA(cudaEventRecord(c->ev0, c->stream));
+        f();
+        HD_CUDA(cudaEventRecord(c->ev1, c->stream));
+        if (ms) {
+            HD_CUDA(cudaEventSynchronize(c->ev1));
+            HD_CUDA(cudaEventElapsedTime(ms, c->ev0, c->ev1));
+        }
+    });
+}
+
+hd_status hd_trace_primary(hd_ctx* c, const hd_camera* cam, uint32_t w, uint32_t h, uint32_t* d_paths, float* ms)
+{
+    if (!c || !cam || !d_paths || !w || !h)
+        return HD_ERR_INVALID;
+    return timed(c, ms, [&] { trace_primary(c, *cam, w, h, d_paths); });
+}
+
+hd_status hd_trace_shadow(hd_ctx* c, const hd_camera* cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
+                          const float light[3], float bias, uint8_t* d_mask, float* ms)
+{
+    if (!c || !cam || !d_paths || !d_mask || !light || !w || !h)
+        return HD_ERR_INVALID;
+    return timed(c, ms, [&] { trace_shadow(c, *cam, w, h, d_paths, light, bias, d_mask); });
+}
+
+hd_status hd_trace_frame(hd_ctx* c, const hd_camera* cam, uint32_t w, uint32_t h, const float light[3], float bias,
+                         uint32_t* d_paths, uint8_t* d_mask, float* ms_primary, float* ms_shadow)
+{
+    hd_status s = hd_trace_primary(c, cam, w, h, d_paths, ms_primary);
+    if (s != HD_OK)
+        return s;
+    return hd_trace_shadow(c, cam, w, h, d_paths, light, bias, d_mask, ms_shadow);
+}
+
+hd_status hd_trace_counters(hd_ctx* c, const hd_camera* cam, uint32_t w, uint32_t h, const float light[3],
+                            float bias, uint32_t* d_paths, uint8_t* d_mask, uint64_t out[6])
+{
+    if (!c || !cam || !d_paths || !d_mask || !light || !out || !w || !h)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        unsigned long long* d = c->scratch.get<unsigned long long>("trace_counters", 6);
+        HD_CUDA(cudaMemsetAsync(d, 0, 6 * 8, c->stream));
+        trace_primary(c, *cam, w, h, d_paths, d);
+        trace_shadow(c, *cam, w, h, d_paths, light, bias, d_mask, d + 3);
+        HD_CUDA(cudaMemcpyAsync(out, d, 6 * 8, cudaMemcpyDeviceToHost, c->stream));
+        HD_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
+hd_status hd_get_values(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out)
+{
+    if (!c || (n && (!d_xyz || !d_out)))
+        return HD_ERR_INVALID;
+    return guarded(c, [&] { get_values(c, d_xyz, n, d_out); });
+}
+
+hd_status hd_get_root(hd_ctx* c, uint32_t* root)
+{
+    if (!c || !root)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        refresh_root(c);
+        *root = c->root;
+    });
+}
+
+hd_status hd_set_root(hd_ctx* c, uint32_t root)
+{
+    if (!c)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        HD_CUDA(cudaMemcpyAsync(c->d_root, &root, 4, cudaMemcpyHostToDevice, c->stream));
+        HD_CUDA(cudaStreamSynchronize(c->stream));
+        c->root = root;
+    });
+}
+
+hd_status hd_get_config(hd_ctx* c, hd_config* cfg)
+{
+    if (!c || !cfg)
+        return HD_ERR_INVALID;
+    *cfg = c->cfg;
+    return HD_OK;
+}
+
+__global__ void k_level_words(Table t, uint64_t* out)
+{
+    // one block per level
+    const uint32_t level = blockIdx.x;
+    if (level >= t.g.depth)
+        return;
+    const uint32_t nb = t.g.buckets(level), first = t.g.level_first_bucket(level);
+    unsigned long long sum = 0;
+    for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x)
+        sum += t.bucket_sizes[first + b];
+    for (int o = 16; o; o >>= 1)
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0)
+        atomicAdd(reinterpret_cast<unsigned long long*>(out + level), sum);
+}
+
+hd_status hd_get_level_stats(hd_ctx* c, hd_level_stats* out)
+{
+    if (!c || !out)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        std::memset(out, 0, sizeof(*out));
+        uint64_t* d = c->scratch.get<uint64_t>("stats_words", HD_MAX_DEPTH);
+        HD_CUDA(cudaMemsetAsync(d, 0, HD_MAX_DEPTH * 8, c->stream));
+        const uint32_t levels = c->g.leaf_level + 1;
+        k_level_words<<<levels, 256, 0, c->stream>>>(c->t, d);
+        HD_LAUNCH_CHECK();
+        HD_CUDA(cudaMemcpyAsync(out->words, d, levels * 8, cudaMemcpyDeviceToHost, c->stream));
+        HD_CUDA(cudaMemcpyAsync(out->nodes, c->t.level_nodes, levels * 8, cudaMemcpyDeviceToHost, c->stream));
+        uint32_t top = 0;
+        HD_CUDA(cudaMemcpyAsync(&top, c->t.pool_top, 4, cudaMemcpyDeviceToHost, c->stream));
+        HD_CUDA(cudaMemcpyAsync(&c->root, c->d_root, 4, cudaMemcpyDeviceToHost, c->stream));
+        HD_CUDA(cudaStreamSynchronize(c->stream));
+        out->pages_used = top - 1;
+        out->root = c->root;
+        out->levels = c->cfg.depth;
+    });
+}
+
+hd_status hd_table_sizes(hd_ctx* c, uint64_t* n_buckets, uint64_t* n_vpages, uint64_t* n_pool_pages_used)
+{
+    if (!c)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        if (n_buckets)
+            *n_buckets = c->g.total_buckets;
+        if (n_vpages)
+            *n_vpages = c->g.total_vpages;
+        if (n_pool_pages_used)
+            *n_pool_pages_used = read_scalar(c->t.pool_top, c->stream) - 1;
+    });
+}
+
+hd_status hd_export_table(hd_ctx* c, uint32_t* bs, uint32_t* pt, uint32_t* pool, uint64_t pool_cap, uint32_t* full)
+{
+    if (!c)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        cudaStream_t st = c->stream;
+        if (bs)
+            HD_CUDA(cudaMemcpyAsync(bs, c->t.bucket_sizes, c->g.total_buckets * 4, cudaMemcpyDeviceToHost, st));
+        if (pt)
+            HD_CUDA(cudaMemcpyAsync(pt, c->t.page_table, c->g.total_vpages * 4, cudaMemcpyDeviceToHost, st));
+        if (pool) {
+            const uint64_t top = read_scalar(c->t.pool_top, st);
+            uint64_t words = top * HD_PAGE_SIZE;
+            if (words > pool_cap)
+                words = pool_cap;
+            HD_CUDA(cudaMemcpyAsync(pool, c->t.pool, words * 4, cudaMemcpyDeviceToHost, st));
+        }
+        if (full)
+            HD_CUDA(cudaMemcpyAsync(full, c->t.full_nodes, c->cfg.depth * 4, cudaMemcpyDeviceToHost, st));
+        HD_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+hd_status hd_import_table(hd_ctx* c, const uint32_t* bs, const uint32_t* pt, const uint32_t* pool, uint64_t pool_words,
+                          const uint32_t* full, uint32_t root)
+{
+    if (!c || !bs || !pt || !pool || !full || pool_words % HD_PAGE_SIZE ||
+        pool_words > uint64_t(c->cfg.pool_pages) * HD_PAGE_SIZE)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        cudaStream_t st = c->stream;
+        table_reset(c);
+        HD_CUDA(cudaMemcpyAsync(c->t.bucket_sizes, bs, c->g.total_buckets * 4, cudaMemcpyHostToDevice, st));
+        HD_CUDA(cudaMemcpyAsync(c->t.page_table, pt, c->g.total_vpages * 4, cudaMemcpyHostToDevice, st));
+        HD_CUDA(cudaMemcpyAsync(c->t.pool, pool, pool_words * 4, cudaMemcpyHostToDevice, st));
+        HD_CUDA(cudaMemcpyAsync(c->t.full_nodes, full, c->cfg.depth * 4, cudaMemcpyHostToDevice, st));
+        const uint32_t top = uint32_t(pool_words / HD_PAGE_SIZE);
+        HD_CUDA(cudaMemcpyAsync(c->t.pool_top, &top, 4, cudaMemcpyHostToDevice, st));
+        HD_CUDA(cudaMemcpyAsync(c->d_root, &root, 4, cudaMemcpyHostToDevice, st));
+        HD_CUDA(cudaStreamSynchronize(st));
+        c->root = root;
+    });
+}
+
+hd_status hd_device_table(hd_ctx* c, uint32_t** pool, uint32_t** pt, uint32_t** bs)
+{
+    if (!c)
+        return HD_ERR_INVALID;
+    if (pool)
+        *pool = c->t.pool;
+    if (pt)
+        *pt = c->t.page_table;
+    if (bs)
+        *bs = c->t.bucket_sizes;
+    return HD_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,184 @@
+// Shared device/host definitions of the hashed-DAG table format.
+//
+// Format (Phyronnaz/HashDAG): 512-word pages (typedefs.h:201-203); virtual
+// address of (level, bucket, position) as make_ptr (hash_table.h:45-63);
+// translation pool[pageTable[v / 512] * 512 + v % 512] (get_sys_ptr,
+// hash_table.h:155-173); interior nodes [mask | count << 8, children...],
+// leaves two words (base_dag.h:6-59); hashes murmurhash64 / murmurhash32xN
+// (utils.h:355-396, hash_table.h:80-89).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/hashdag_gb300.h"
+
+#define HD_HD __host__ __device__ __forceinline__
+#define HD_D __device__ __forceinline__
+
+namespace hd {
+
+constexpr uint32_t kPage = HD_PAGE_SIZE;
+constexpr uint32_t kPageShift = 9;
+constexpr uint32_t kInvalid = HD_INVALID_NODE;
+constexpr uint32_t kNotFound = 0xFFFFFFFFu;
+constexpr uint32_t kEmptyId = 0xFFFFFFFFu; // "no node" in scratch id arrays
+
+// Device-side error word values (first error wins).
+enum : uint32_t {
+    kErrNone = 0,
+    kErrPoolFull = HD_ERR_POOL_FULL,
+    kErrBucketFull = HD_ERR_BUCKET_FULL,
+    kErrTimeout = HD_ERR_TIMEOUT,
+    kErrCapacity = 8, // a scratch array ran out of room
+};
+
+// Geometry of one table, passed by value to kernels.
+struct Geom {
+    uint32_t depth;       // levels; leaves at depth - 2
+    uint32_t leaf_level;
+    uint32_t T;           // color tree levels
+    uint32_t top_levels;
+    uint32_t top_bits, low_bits;
+    uint32_t top_size, low_size;
+    uint32_t ntop;        // min(top_levels, depth)
+    uint32_t pool_pages;
+    uint64_t total_buckets;
+    uint64_t total_vpages;
+
+    HD_HD uint32_t buckets(uint32_t level) const { return level < top_levels ? (1u << top_bits) : (1u << low_bits); }
+    HD_HD uint32_t capacity(uint32_t level) const { return level < top_levels ? top_size : low_size; }
+    HD_HD uint32_t bucket_global(uint32_t level, uint32_t bucket) const
+    {
+        return level < top_levels ? level * (1u << top_bits) + bucket
+                                  : ntop * (1u << top_bits) + (level - top_levels) * (1u << low_bits) + bucket;
+    }
+    HD_HD uint32_t level_first_bucket(uint32_t level) const { return bucket_global(level, 0); }
+    HD_HD uint32_t make_ptr(uint32_t level, uint32_t bucket, uint32_t pos) const
+    {
+        uint64_t index;
+        if (level < top_levels)
+            index = (uint64_t(level) * (1u << top_bits) + bucket) * top_size;
+        else
+            index = uint64_t(ntop) * (1u << top_bits) * top_size +
+                    (uint64_t(level - top_levels) * (1u << low_bits) + bucket) * low_size;
+        return uint32_t(index + pos);
+    }
+};
+
+inline Geom make_geom(const hd_config& c)
+{
+    Geom g{};
+    g.depth = c.depth;
+    g.leaf_level = c.depth - 2;
+    g.T = c.color_tree_levels;
+    g.top_levels = c.top_levels;
+    g.top_bits = c.top_bucket_bits;
+    g.low_bits = c.low_bucket_bits;
+    g.top_size = c.top_bucket_size;
+    g.low_size = c.low_bucket_size;
+    g.ntop = c.top_levels < c.depth ? c.top_levels : c.depth;
+    g.pool_pages = c.pool_pages;
+    const uint64_t low = c.depth > c.top_levels ? c.depth - c.top_levels : 0;
+    g.total_buckets = uint64_t(g.ntop) * (1u << g.top_bits) + low * (1u << g.low_bits);
+    g.total_vpages = (uint64_t(g.ntop) * (1u << g.top_bits) * g.top_size + low * (1u << g.low_bits) * g.low_size) / kPage;
+    return g;
+}
+
+// Device view of a table (HashDAG passed by value to kernels, as the
+// reference's tracer does, tracer.cu:146).
+struct Table {
+    uint32_t* pool;
+    uint32_t* page_table;
+    uint32_t* bucket_sizes;
+    uint32_t* full_nodes;   // [depth]
+    uint32_t* pool_top;     // device counter (poolTop)
+    uint32_t* error;        // device error word
+    uint64_t* level_nodes;  // stored node count per level
+    Geom g;
+
+    HD_D const uint32_t* sys(uint32_t v) const
+    {
+        return pool + (uint64_t(__ldg(page_table + (v >> kPageShift))) << kPageShift) + (v & (kPage - 1));
+    }
+    HD_D uint32_t* sys_rw(uint32_t v) const
+    {
+        return pool + (uint64_t(page_table[v >> kPageShift]) << kPageShift) + (v & (kPage - 1));
+    }
+};
+
+HD_D void set_error(uint32_t* err, uint32_t code) { atomicCAS(err, 0u, code); }
+
+// ---- hashes (utils.h:355-396) --------------------------------------------
+HD_HD uint32_t murmur32(uint32_t h)
+{
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h;
+}
+HD_HD uint64_t murmur64(uint64_t h)
+{
+    h ^= h >> 33;
+    h *= 0xff51afd7ed558ccdull;
+    h ^= h >> 33;
+    h *= 0xc4ceb9fe1a85ec53ull;
+    h ^= h >> 33;
+    return h;
+}
+HD_HD uint32_t hash_leaf(uint64_t leaf) { return uint32_t(murmur64(leaf)); }
+HD_HD uint32_t hash_interior(uint32_t n, const uint32_t* node)
+{
+    uint32_t h = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t k = node[i];
+        k *= 0xcc9e2d51u;
+        k = (k << 15) | (k >> 17);
+        k *= 0x1b873593u;
+        h ^= k;
+        h = (h << 13) | (h >> 19);
+        h = h * 5u + 0xe6546b64u;
+    }
+    h ^= n;
+    return murmur32(h);
+}
+
+HD_HD uint32_t popc32(uint32_t v)
+{
+#ifdef __CUDA_ARCH__
+    return __popc(v);
+#else
+    return uint32_t(__builtin_popcount(v));
+#endif
+}
+HD_HD uint32_t popc64(uint64_t v)
+{
+#ifdef __CUDA_ARCH__
+    return __popcll(v);
+#else
+    return uint32_t(__builtin_popcountll(v));
+#endif
+}
+HD_HD uint32_t total_size(uint32_t header) { return popc32(header & 0xffu) + 1; }
+HD_HD uint32_t child_offset(uint32_t mask, uint32_t child) { return popc32(mask & ((1u << child) - 1u)) + 1; }
+
+HD_HD uint64_t mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Leaf bit of voxel (x, y, z) inside its 4x4x4 block (dag_utils.h:160-167).
+HD_HD uint32_t leaf_bit(uint32_t x, uint32_t y, uint32_t z)
+{
+    return ((x & 1) ? 4 : 0) | ((y & 1) ? 2 : 0) | ((z & 1) ? 1 : 0) | ((x & 2) ? 32 : 0) | ((y & 2) ? 16 : 0) |
+           ((z & 2) ? 8 : 0);
+}
+
+inline uint32_t ceil_div(uint64_t a, uint64_t b) { return uint32_t((a + b - 1) / b); }
+
+} // namespace hd

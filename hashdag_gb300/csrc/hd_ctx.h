@@ -1,0 +1,50 @@
+// The context behind the opaque hd_ctx handle, shared by the .cu files.
+#pragma once
+
+#include <string>
+
+#include "hd_common.cuh"
+#include "hd_util.cuh"
+
+struct hd_ctx {
+    hd_config cfg{};
+    hd::Geom g{};
+    hd::Table t{};           // device pointers of the table
+    cudaStream_t stream = nullptr;
+    uint32_t* d_root = nullptr;        // firstNodeIndex on the device
+    uint32_t root = 0;                 // host copy, refreshed after each call
+    uint32_t fp_mode = 1;
+    std::string err;
+    hd::Scratch scratch;               // grow-only working buffers
+    // BasicDAG of the last generated scene (device), kept for export
+    uint32_t* d_basic = nullptr;
+    uint64_t n_basic = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // bucket list heads of the edit path stay all-empty between calls
+    bool edit_head_ready = false;
+    uint32_t* edit_head_ptr = nullptr;
+};
+
+namespace hd {
+
+// hd_table.cu
+void table_reset(hd_ctx* c);
+void add_full_nodes(hd_ctx* c, uint32_t first_level, uint32_t last_level);
+void import_basic_dag(hd_ctx* c, const uint32_t* d_words, uint64_t n_words);
+uint32_t check_error(hd_ctx* c); // reads and clears the device error word
+// Appends items (9-word contents) bucket by bucket in item order; the bucket
+// lists must have been linked (link_item) for `level`.
+void append_items(hd_ctx* c, uint32_t level, const uint32_t* content, uint64_t n_items, uint32_t* head,
+                  const uint32_t* next, const uint32_t* touched, const uint32_t* n_touched, uint32_t* out_addr);
+
+// hd_scene.cu
+void generate_scene(hd_ctx* c, uint64_t seed, uint32_t** d_words, uint64_t* n_words);
+
+// hd_trace.cu
+void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint32_t* d_paths,
+                   unsigned long long* d_counters = nullptr);
+void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
+                  const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters = nullptr);
+void get_values(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out);
+
+} // namespace hd

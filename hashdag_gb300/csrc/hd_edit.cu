@@ -1,0 +1,615 @@
+// Edit pipeline: sphere / box carve and fill, per-level hashing and bucket
+// find-or-add, on the device.
+//
+// Reference: HashDAG::edit_threads (hash_dag.h:255-405), which runs
+// HashDagEdits::edit_threaded over the levels above C_colorTreeLevels
+// (hash_dag_edits.h:106-333) and edit_leaf below (:335-643); editors
+// (hash_dag_editors.h:57-127, :223-313); find_or_add_leaf_node /
+// find_or_add_interior_node with their bucket scans (hash_table.h:196-357,
+// :470-560).
+//
+// The recursion becomes two level-synchronous sweeps:
+//  * top-down, every level's edit entries (a node path and its old index) are
+//    classified as in the reference (untouched, carved away, filled, a leaf
+//    to rebuild, or an interior node to descend into); descended entries
+//    spawn their 8 children, in child order, so each level's entries stay in
+//    depth-first (Morton) order;
+//  * bottom-up, every rebuilt node is compared with its old self and, when
+//    changed, hashed and resolved by find-or-add.  Candidates of a level are
+//    grouped by bucket and each bucket is resolved by one warp, candidates in
+//    depth-first order one after the other: the same sequence of bucket scans
+//    and appends as the reference's single-threaded depth-first recursion,
+//    including its scan rules (a node flush with the bucket tail or the page
+//    end is invisible to an equal-size query).
+#include <chrono>
+#include <vector>
+
+#include "hd_ctx.h"
+#include "hd_table.cuh"
+
+namespace hd {
+
+// ---- editors ----------------------------------------------------------------
+struct Editor {
+    uint32_t tool;
+    float cx, cy, cz, r, r2;
+    float bminx, bminy, bminz, bmaxx, bmaxy, bmaxz;
+    HD_HD bool sphere() const { return tool == HD_TOOL_SPHERE_ADD || tool == HD_TOOL_SPHERE_REMOVE; }
+    HD_HD bool adding() const { return tool == HD_TOOL_SPHERE_ADD || tool == HD_TOOL_BOX_ADD; }
+};
+
+inline Editor make_editor(const hd_edit& e)
+{
+    Editor ed{};
+    ed.tool = e.tool;
+    ed.cx = e.center[0];
+    ed.cy = e.center[1];
+    ed.cz = e.center[2];
+    ed.r = e.radius;
+    ed.r2 = e.radius * e.radius;
+    ed.bminx = e.center[0] - e.radius;
+    ed.bminy = e.center[1] - e.radius;
+    ed.bminz = e.center[2] - e.radius;
+    ed.bmaxx = e.center[0] + e.radius;
+    ed.bmaxy = e.center[1] + e.radius;
+    ed.bmaxz = e.center[2] + e.radius;
+    return ed;
+}
+
+HD_D float sqr(float f) { return f * f; }
+HD_D float fmax_r(float a, float b) { return a > b ? a : b; }
+
+// SphereEditorBase::should_edit_impl (:112-126) / BoxEditorBase (:76-91)
+HD_D bool should_edit_impl(const Editor& e, float mnx, float mny, float mnz, float mxx, float mxy, float mxz)
+{
+    if (e.sphere()) {
+        float dist = e.r2;
+        if (e.cx < mnx)
+            dist -= sqr(e.cx - mnx);
+        else if (e.cx > mxx)
+            dist -= sqr(e.cx - mxx);
+        if (e.cy < mny)
+            dist -= sqr(e.cy - mny);
+        else if (e.cy > mxy)
+            dist -= sqr(e.cy - mxy);
+        if (e.cz < mnz)
+            dist -= sqr(e.cz - mnz);
+        else if (e.cz > mxz)
+            dist -= sqr(e.cz - mxz);
+        return dist > 0;
+    }
+    return !(e.bminx >= mxx || e.bminy >= mxy || e.bminz >= mxz || e.bmaxx <= mnx || e.bmaxy <= mny ||
+             e.bmaxz <= mnz || mnx >= e.bmaxx || mny >= e.bmaxy || mnz >= e.bmaxz || mxx <= e.bminx ||
+             mxy <= e.bminy || mxz <= e.bminz);
+}
+
+// is_full_impl / is_empty_impl (:280-295, :233-252): the region lies inside
+// the tool.
+HD_D bool inside_tool(const Editor& e, float mnx, float mny, float mnz, float mxx, float mxy, float mxz)
+{
+    if (e.sphere()) {
+        const float a = fmax_r(sqr(mnx - e.cx), sqr(mxx - e.cx));
+        const float b = fmax_r(sqr(mny - e.cy), sqr(mxy - e.cy));
+        const float c = fmax_r(sqr(mnz - e.cz), sqr(mxz - e.cz));
+        return (a + b) + c < e.r2;
+    }
+    return e.bminx <= mnx && e.bminy <= mny && e.bminz <= mnz && e.bmaxx >= mxx && e.bmaxy >= mxy && e.bmaxz >= mxz;
+}
+
+// ---- per-level entry state ---------------------------------------------------
+enum : uint8_t {
+    kSkip = 0,      // level-C_colorTreeLevels child the parent never hands to edit_leaf
+    kKeep = 1,      // untouched: result = old
+    kEmptied = 2,   // carved away (is_empty)
+    kFilled = 3,    // filled (is_full): the level's full node
+    kLeafEval = 4,  // leaf rebuilt voxel by voxel
+    kDescend = 5,   // interior node rebuilt from its children
+};
+
+struct Level {
+    uint32_t* x;
+    uint32_t* y;
+    uint32_t* z;
+    uint32_t* old;
+    uint8_t* state;
+    uint32_t* res;   // new index (kInvalid = empty)
+    uint32_t* cnt;   // voxel count of the new node (levels >= T)
+    uint32_t* flag;  // 1 = descends
+    uint32_t* exp;   // exclusive scan of flag
+    uint64_t* leaf;  // new leaf masks (leaf level only)
+    uint32_t* cand;  // candidate content, 9 words per entry
+};
+
+struct EditCounters {
+    unsigned long long num_voxels, num_nodes, foa, added, scanned;
+};
+
+HD_D void warp_add(unsigned long long* p, unsigned long long v)
+{
+    // warp-aggregated atomic
+    const uint32_t mask = __activemask();
+    for (int o = 16; o; o >>= 1)
+        v += __shfl_down_sync(mask, v, o);
+    if ((threadIdx.x & 31) == __ffs(mask) - 1)
+        atomicAdd(p, v);
+}
+
+// Top-down classification of level L's entries.
+__global__ void k_edit_classify(Table t, Editor ed, uint32_t level, uint32_t n, Level lv, EditCounters* ctr)
+{
+    const uint32_t D = t.g.depth, T = t.g.T, leafl = t.g.leaf_level;
+    HD_GRID_STRIDE(i, n)
+    {
+        const uint32_t depth = D - level;
+        const float s = float(1u << depth);
+        const float mnx = float(lv.x[i] << depth), mny = float(lv.y[i] << depth), mnz = float(lv.z[i] << depth);
+        const float mxx = mnx + s, mxy = mny + s, mxz = mnz + s;
+        const uint32_t old = lv.old[i];
+        const bool se = should_edit_impl(ed, mnx, mny, mnz, mxx, mxy, mxz);
+        uint8_t state;
+        uint32_t res = old, cnt = 0;
+        unsigned long long nodes = 0, voxels = 0;
+        if (level < T) {
+            // edit_threaded: visited in both passes; no early full/empty exits
+            nodes = 2;
+            state = se ? kDescend : kKeep;
+        } else {
+            if (level == T && !se) {
+                state = kSkip; // the parent keeps the old child without a visit
+            } else {
+                nodes = 1;
+                if (!se) {
+                    state = kKeep;
+                    if (old != kInvalid) {
+                        const uint32_t* p = t.sys(old);
+                        cnt = level < leafl ? (p[0] >> 8) : popc32(p[0]) + popc32(p[1]);
+                    }
+                } else if (inside_tool(ed, mnx, mny, mnz, mxx, mxy, mxz)) {
+                    const uint32_t full_count = 1u << (3 * depth);
+                    voxels = full_count;
+                    if (ed.adding()) {
+                        state = kFilled;
+                        res = t.full_nodes[level];
+                        cnt = full_count;
+                    } else {
+                        state = kEmptied;
+                        res = kInvalid;
+                    }
+                } else if (level == leafl) {
+                    state = kLeafEval;
+                    uint64_t leaf = 0;
+                    if (old != kInvalid) {
+                        const uint32_t* p = t.sys(old);
+                        leaf = uint64_t(p[0]) | (uint64_t(p[1]) << 32);
+                    }
+                    const uint32_t x0 = lv.x[i] << 2, y0 = lv.y[i] << 2, z0 = lv.z[i] << 2;
+                    uint32_t edited = 0;
+                    for (uint32_t c1 = 0; c1 < 8; c1++)
+                        for (uint32_t c2 = 0; c2 < 8; c2++) {
+                            const float px = float(x0 + ((c1 >> 2) & 1) * 2 + ((c2 >> 2) & 1));
+                            const float py = float(y0 + ((c1 >> 1) & 1) * 2 + ((c2 >> 1) & 1));
+                            const float pz = float(z0 + (c1 & 1) * 2 + (c2 & 1));
+                            if (should_edit_impl(ed, px, py, pz, px + 1.0f, py + 1.0f, pz + 1.0f)) {
+                                edited++;
+                                const uint64_t bit = 1ull << (c1 * 8 + c2);
+                                leaf = ed.adding() ? (leaf | bit) : (leaf & ~bit);
+                            }
+                        }
+                    voxels = edited;
+                    lv.leaf[i] = leaf;
+                } else {
+                    state = kDescend;
+                }
+            }
+        }
+        lv.state[i] = state;
+        lv.res[i] = res;
+        lv.cnt[i] = cnt;
+        lv.flag[i] = state == kDescend;
+        warp_add(&ctr->num_nodes, nodes);
+        warp_add(&ctr->num_voxels, voxels);
+    }
+}
+
+// Descended entries spawn their 8 children (child order) on the next level.
+__global__ void k_edit_spawn(Table t, uint32_t n, Level lv, Level next)
+{
+    HD_GRID_STRIDE(i, n)
+    {
+        if (!lv.flag[i])
+            continue;
+        const uint32_t base = 8 * lv.exp[i];
+        const uint32_t old = lv.old[i];
+        uint32_t mask = 0;
+        const uint32_t* p = nullptr;
+        if (old != kInvalid) {
+            p = t.sys(old);
+            mask = p[0] & 0xffu;
+        }
+        uint32_t k = 1;
+        for (uint32_t c = 0; c < 8; c++) {
+            next.x[base + c] = (lv.x[i] << 1) | ((c >> 2) & 1);
+            next.y[base + c] = (lv.y[i] << 1) | ((c >> 1) & 1);
+            next.z[base + c] = (lv.z[i] << 1) | (c & 1);
+            next.old[base + c] = (mask & (1u << c)) ? p[k++] : kInvalid;
+        }
+    }
+}
+
+// Bottom-up: rebuilt content of every kLeafEval / kDescend entry; unchanged
+// and emptied nodes resolve at once, the rest become find-or-add candidates.
+__global__ void k_edit_candidates(Table t, uint32_t level, uint32_t n, Level lv, Level child, uint32_t* head,
+                                  uint32_t* next_item, uint32_t* touched, uint32_t* n_touched)
+{
+    const uint32_t T = t.g.T, leafl = t.g.leaf_level;
+    HD_GRID_STRIDE(i, n)
+    {
+        const uint8_t state = lv.state[i];
+        uint32_t* c = lv.cand + 9 * i;
+        uint32_t hash, nw;
+        if (state == kLeafEval) {
+            const uint64_t leaf = lv.leaf[i];
+            const uint32_t old = lv.old[i];
+            uint64_t initial = 0;
+            if (old != kInvalid) {
+                const uint32_t* p = t.sys(old);
+                initial = uint64_t(p[0]) | (uint64_t(p[1]) << 32);
+            }
+            lv.cnt[i] = popc64(leaf);
+            if (leaf == initial) {
+                lv.res[i] = old;
+                continue;
+            }
+            if (!leaf) {
+                lv.res[i] = kInvalid;
+                lv.cnt[i] = 0;
+                continue;
+            }
+            c[0] = uint32_t(leaf);
+            c[1] = uint32_t(leaf >> 32);
+            hash = hash_leaf(leaf);
+            nw = 2;
+        } else if (state == kDescend) {
+            const uint32_t base = 8 * lv.exp[i];
+            const uint32_t old = lv.old[i];
+            uint32_t mask = 0, k = 1, total = 0;
+            bool changed = false;
+            uint32_t omask = 0;
+            const uint32_t* p = nullptr;
+            if (old != kInvalid) {
+                p = t.sys(old);
+                omask = p[0] & 0xffu;
+            }
+            uint32_t ok = 1;
+            for (uint32_t s = 0; s < 8; s++) {
+                const uint32_t oc = (omask & (1u << s)) ? p[ok++] : kInvalid;
+                const uint8_t cs = child.state[base + s];
+                const uint32_t nc = cs == kSkip ? oc : child.res[base + s];
+                changed |= nc != oc;
+                if (nc != kInvalid) {
+                    mask |= 1u << s;
+                    c[k++] = nc;
+                    if (level >= T)
+                        total += child.cnt[base + s];
+                }
+            }
+            lv.cnt[i] = total;
+            if (!changed) {
+                lv.res[i] = old;
+                continue;
+            }
+            if (!mask) {
+                lv.res[i] = kInvalid;
+                lv.cnt[i] = 0;
+                continue;
+            }
+            c[0] = (level >= T ? (total << 8) : 0u) | mask;
+            nw = k;
+            hash = hash_interior(nw, c);
+        } else {
+            continue;
+        }
+        (void)leafl;
+        (void)nw;
+        const uint32_t bucket = hash & (t.g.buckets(level) - 1);
+        lv.res[i] = kNotFound; // resolved by find-or-add
+        link_item(t.g.bucket_global(level, bucket), uint32_t(i), head, next_item, touched, n_touched);
+    }
+}
+
+// One warp per touched bucket: the bucket's candidates, in depth-first
+// order, each scanned against the bucket as it stands (earlier candidates'
+// appends included) and appended when not found.
+constexpr uint32_t kFoaWarps = 4;
+
+__global__ void __launch_bounds__(32 * kFoaWarps)
+    k_edit_find_or_add(Table t, uint32_t level, Level lv, uint32_t* head, const uint32_t* next_item,
+                       const uint32_t* touched, const uint32_t* n_touched, EditCounters* ctr)
+{
+    __shared__ uint32_t items_s[kFoaWarps][kMaxBucketItems];
+    __shared__ uint32_t page_s[kFoaWarps][kPage];
+    __shared__ uint32_t q_s[kFoaWarps][9];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t* items = items_s[warp];
+    uint32_t* page = page_s[warp];
+    uint32_t* q = q_s[warp];
+    const bool leaf = level == t.g.leaf_level;
+    const uint32_t nt = *n_touched;
+    unsigned long long foa = 0, added = 0, scanned = 0;
+    for (uint32_t ti = blockIdx.x * kFoaWarps + warp; ti < nt; ti += gridDim.x * kFoaWarps) {
+        const uint32_t gb = touched[ti];
+        const uint32_t cnt = collect_sorted(gb, head, next_item, items, t.error);
+        const uint32_t bucket = gb - t.g.level_first_bucket(level);
+        const uint32_t vbase = t.g.make_ptr(level, bucket, 0);
+        uint32_t S = t.bucket_sizes[gb];
+        bool failed = false;
+        for (uint32_t j = 0; j < cnt && !failed; j++) {
+            const uint32_t ci = items[j];
+            if (lane < 9)
+                q[lane] = lv.cand[9 * ci + lane];
+            __syncwarp();
+            const uint32_t n = leaf ? 2 : total_size(q[0]);
+            uint32_t found = kNotFound;
+            for (uint32_t pindex = 0; pindex < S && found == kNotFound; pindex += kPage) {
+                uint32_t page_end = S < pindex + kPage ? S : pindex + kPage;
+                if (!leaf && pindex + n >= page_end)
+                    break; // find_interior_node_in_bucket: "return 0xFFFFFFFF"
+                const uint32_t used = page_end - pindex;
+                const uint32_t* src = t.sys(vbase + pindex);
+                for (uint32_t w = lane * 4; w < used; w += 128) {
+                    const uint4 v = *reinterpret_cast<const uint4*>(src + w);
+                    page[w] = v.x;
+                    page[w + 1] = v.y;
+                    page[w + 2] = v.z;
+                    page[w + 3] = v.w;
+                }
+                __syncwarp();
+                if (leaf) {
+                    for (uint32_t w0 = 0; w0 < used && found == kNotFound; w0 += 64) {
+                        const uint32_t w = w0 + 2 * lane;
+                        const bool m = w < used && page[w] == q[0] && page[w + 1] == q[1];
+                        const uint32_t b = __ballot_sync(0xffffffffu, m);
+                        if (b)
+                            found = vbase + pindex + w0 + 2 * (__ffs(b) - 1);
+                    }
+                } else {
+                    // positions compared by the reference: walk starts below
+                    // page_end - n; content matches first, the walk to confirm
+                    const uint32_t lim = used - n;
+                    for (uint32_t w0 = 0; w0 < lim && found == kNotFound; w0 += 32) {
+                        const uint32_t w = w0 + lane;
+                        bool m = w < lim && page[w] == q[0];
+                        if (m)
+                            for (uint32_t k = 1; k < n; k++)
+                                m &= page[w + k] == q[k];
+                        uint32_t b = __ballot_sync(0xffffffffu, m);
+                        while (b && found == kNotFound) {
+                            const uint32_t cand = w0 + __ffs(b) - 1;
+                            b &= b - 1;
+                            uint32_t on_walk = 0;
+                            if (lane == 0) {
+                                uint32_t p = 0;
+                                while (p < cand)
+                                    p += total_size(page[p]);
+                                on_walk = p == cand;
+                            }
+                            on_walk = __shfl_sync(0xffffffffu, on_walk, 0);
+                            if (on_walk)
+                                found = vbase + pindex + cand;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+            foa++;
+            if (found != kNotFound) {
+                scanned += found - vbase + n;
+            } else {
+                scanned += S;
+                // append (add_leaf_node / add_interior_node)
+                uint32_t ok = 1;
+                if (lane == 0) {
+                    uint32_t size = S;
+                    const uint32_t pos = append_position(size, n, leaf);
+                    if (size > t.g.capacity(level)) {
+                        set_error(t.error, kErrBucketFull);
+                        ok = 0;
+                    } else if (!map_pages(t, level, bucket, pos, size)) {
+                        ok = 0;
+                    } else {
+                        uint32_t* dst = t.sys_rw(vbase + pos);
+                        for (uint32_t k = 0; k < n; k++)
+                            dst[k] = q[k];
+                        found = vbase + pos;
+                        S = size;
+                    }
+                }
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                found = __shfl_sync(0xffffffffu, found, 0);
+                S = __shfl_sync(0xffffffffu, S, 0);
+                if (!ok) {
+                    failed = true;
+                    break;
+                }
+                added++;
+            }
+            if (lane == 0)
+                lv.res[ci] = found;
+            __syncwarp();
+        }
+        if (lane == 0) {
+            t.bucket_sizes[gb] = S;
+        }
+    }
+    if (lane == 0) {
+        atomicAdd(&ctr->foa, foa);
+        atomicAdd(&ctr->added, added);
+        atomicAdd(&ctr->scanned, scanned);
+        atomicAdd(reinterpret_cast<unsigned long long*>(t.level_nodes + level), added);
+    }
+}
+
+__global__ void k_edit_finish(const Level lv0, uint32_t* d_root, uint32_t* err)
+{
+    const uint32_t r = lv0.res[0];
+    if (r == kInvalid || r == kNotFound)
+        set_error(err, kErrCapacity);
+    else
+        *d_root = r;
+}
+
+// ---- host orchestration -------------------------------------------------------
+struct EditBuffers {
+    std::vector<Level> lv;
+    std::vector<uint32_t> cap;
+};
+
+static Level alloc_level(Scratch& s, uint32_t L, uint64_t n, bool leaf)
+{
+    char nm[48];
+    auto buf = [&](const char* what, size_t bytes) {
+        snprintf(nm, sizeof(nm), "ed_%s_%u", what, L);
+        return s.get(nm, bytes);
+    };
+    Level l{};
+    l.x = static_cast<uint32_t*>(buf("x", n * 4));
+    l.y = static_cast<uint32_t*>(buf("y", n * 4));
+    l.z = static_cast<uint32_t*>(buf("z", n * 4));
+    l.old = static_cast<uint32_t*>(buf("old", n * 4));
+    l.state = static_cast<uint8_t*>(buf("state", n));
+    l.res = static_cast<uint32_t*>(buf("res", n * 4));
+    l.cnt = static_cast<uint32_t*>(buf("cnt", n * 4));
+    l.flag = static_cast<uint32_t*>(buf("flag", n * 4));
+    l.exp = static_cast<uint32_t*>(buf("exp", n * 4));
+    l.leaf = leaf ? static_cast<uint64_t*>(buf("leaf", n * 8)) : nullptr;
+    l.cand = static_cast<uint32_t*>(buf("cand", n * 36));
+    return l;
+}
+
+void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats)
+{
+    cudaStream_t st = c->stream;
+    Scratch& s = c->scratch;
+    const Geom& g = c->g;
+    const uint32_t levels = g.leaf_level + 1;
+    const Editor ed = make_editor(e);
+    const auto t0 = std::chrono::steady_clock::now();
+    HD_CUDA(cudaEventRecord(c->ev0, st));
+    EditCounters* ctr = s.get<EditCounters>("ed_ctr", 1);
+    HD_CUDA(cudaMemsetAsync(ctr, 0, sizeof(EditCounters), st));
+    uint32_t* d_n = s.get<uint32_t>("ed_n", 4);
+    std::vector<Level> lv(levels);
+    std::vector<uint32_t> count(levels, 0);
+    lv[0] = alloc_level(s, 0, 1, levels == 1);
+    HD_CUDA(cudaMemsetAsync(lv[0].x, 0, 4, st));
+    HD_CUDA(cudaMemsetAsync(lv[0].y, 0, 4, st));
+    HD_CUDA(cudaMemsetAsync(lv[0].z, 0, 4, st));
+    HD_CUDA(cudaMemcpyAsync(lv[0].old, c->d_root, 4, cudaMemcpyDeviceToDevice, st));
+    count[0] = 1;
+    // top-down
+    uint32_t deepest = 0;
+    for (uint32_t L = 0; L < levels; L++) {
+        const uint32_t n = count[L];
+        deepest = L;
+        k_edit_classify<<<grid_for(n, 128), 128, 0, st>>>(c->t, ed, L, n, lv[L], ctr);
+        HD_LAUNCH_CHECK();
+        if (L + 1 == levels)
+            break;
+        exclusive_scan<uint32_t, uint32_t>(s, lv[L].flag, lv[L].exp, n, d_n, st);
+        const uint32_t ne = read_scalar(d_n, st);
+        if (ne == 0)
+            break;
+        count[L + 1] = 8 * ne;
+        lv[L + 1] = alloc_level(s, L + 1, count[L + 1], L + 1 == g.leaf_level);
+        k_edit_spawn<<<grid_for(n, 128), 128, 0, st>>>(c->t, n, lv[L], lv[L + 1]);
+        HD_LAUNCH_CHECK();
+    }
+    // bottom-up
+    uint32_t maxn = 1;
+    for (uint32_t L = 0; L <= deepest; L++)
+        maxn = count[L] > maxn ? count[L] : maxn;
+    uint32_t* head = s.get<uint32_t>("ed_head", g.total_buckets);
+    uint32_t* next_item = s.get<uint32_t>("ed_next", maxn);
+    uint32_t* touched = s.get<uint32_t>("ed_touched", g.total_buckets);
+    if (!c->edit_head_ready || c->edit_head_ptr != head) {
+        fill<uint32_t>(head, kEmpty, g.total_buckets, st);
+        c->edit_head_ready = true;
+        c->edit_head_ptr = head;
+    }
+    for (int32_t L = int32_t(deepest); L >= 0; L--) {
+        const uint32_t n = count[L];
+        HD_CUDA(cudaMemsetAsync(d_n, 0, 4, st));
+        const Level child = uint32_t(L) < deepest ? lv[L + 1] : Level{};
+        k_edit_candidates<<<grid_for(n, 128), 128, 0, st>>>(c->t, uint32_t(L), n, lv[L], child, head, next_item,
+                                                            touched, d_n);
+        HD_LAUNCH_CHECK();
+        k_edit_find_or_add<<<grid_for(uint64_t(n) * 32, 32 * kFoaWarps, 152 * 8), 32 * kFoaWarps, 0, st>>>(
+            c->t, uint32_t(L), lv[L], head, next_item, touched, d_n, ctr);
+        HD_LAUNCH_CHECK();
+    }
+    k_edit_finish<<<1, 1, 0, st>>>(lv[0], c->d_root, c->t.error);
+    HD_LAUNCH_CHECK();
+    HD_CUDA(cudaEventRecord(c->ev1, st));
+    EditCounters h{};
+    HD_CUDA(cudaMemcpyAsync(&h, ctr, sizeof(h), cudaMemcpyDeviceToHost, st));
+    HD_CUDA(cudaStreamSynchronize(st));
+    const uint32_t err = check_error(c);
+    if (err)
+        throw StatusError{err == kErrCapacity ? HD_ERR_STATE : hd_status(err),
+                          err == kErrCapacity ? "edit would empty the whole scene" : "edit failed on the device"};
+    c->root = read_scalar(c->d_root, st);
+    if (stats) {
+        stats->num_voxels = h.num_voxels;
+        stats->num_nodes = h.num_nodes;
+        stats->find_or_add_calls = h.foa;
+        stats->nodes_added = h.added;
+        stats->words_scanned = h.scanned;
+        HD_CUDA(cudaEventElapsedTime(&stats->device_ms, c->ev0, c->ev1));
+        stats->host_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+}
+
+} // namespace hd
+
+extern "C" {
+
+hd_status hd_edit_apply(hd_ctx* c, const hd_edit* edit, hd_edit_stats* stats)
+{
+    if (!c || !edit || edit->tool > HD_TOOL_BOX_ADD || !(edit->radius >= 0.0f))
+        return HD_ERR_INVALID;
+    try {
+        hd::edit_one(c, *edit, stats);
+        return HD_OK;
+    } catch (const hd::StatusError& e) {
+        c->err = e.msg;
+        return e.status;
+    } catch (const hd::CudaError& e) {
+        c->err = std::string("CUDA error ") + cudaGetErrorString(e.code) + " in " + e.where;
+        return HD_ERR_CUDA;
+    }
+}
+
+hd_status hd_edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* stats)
+{
+    if (!c || (n && !edits))
+        return HD_ERR_INVALID;
+    hd_edit_stats total{};
+    for (uint32_t i = 0; i < n; i++) {
+        hd_edit_stats s{};
+        const hd_status r = hd_edit_apply(c, edits + i, &s);
+        if (r != HD_OK)
+            return r;
+        total.num_voxels += s.num_voxels;
+        total.num_nodes += s.num_nodes;
+        total.find_or_add_calls += s.find_or_add_calls;
+        total.nodes_added += s.nodes_added;
+        total.words_scanned += s.words_scanned;
+        total.device_ms += s.device_ms;
+        total.host_ms += s.host_ms;
+    }
+    if (stats)
+        *stats = total;
+    return HD_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,206 @@
+// Garbage collection on the device: mark-and-compact of the hash table.
+//
+// Reference: HashDAG::remove_stale_nodes (hash_dag.h:407-547).  Mark: the
+// nodes reachable from the root level by level (here as a bitmap over each
+// level's virtual range, so the live list comes out sorted by address).
+// Rebuild bottom-up: every live node's content is gathered with its children
+// remapped, the level's buckets are emptied, the full node is added first
+// (add_full_node) and the live nodes are re-appended without a find, in
+// increasing old-address order (the reference uses its hash-set order), so a
+// reachable full node is kept twice as in the reference.  Pages stay mapped;
+// the words past a bucket's new size keep their old contents.
+#include <algorithm>
+#include <vector>
+
+#include "hd_ctx.h"
+#include "hd_table.cuh"
+
+namespace hd {
+
+__global__ void k_gc_mark(Table t, const uint32_t* __restrict__ live, uint32_t n, uint32_t child_base,
+                          uint32_t* __restrict__ bitmap)
+{
+    HD_GRID_STRIDE(i, n)
+    {
+        const uint32_t* p = t.sys(live[i]);
+        const uint32_t cnt = popc32(p[0] & 0xffu);
+        for (uint32_t k = 0; k < cnt; k++) {
+            const uint32_t off = p[1 + k] - child_base;
+            atomicOr(bitmap + (off >> 5), 1u << (off & 31));
+        }
+    }
+}
+
+__global__ void k_popc_words(const uint32_t* __restrict__ bitmap, uint64_t n, uint32_t* __restrict__ counts)
+{
+    HD_GRID_STRIDE(i, n) counts[i] = popc32(bitmap[i]);
+}
+
+__global__ void k_bitmap_to_list(const uint32_t* __restrict__ bitmap, const uint32_t* __restrict__ pos, uint64_t n,
+                                 uint32_t base, uint32_t* __restrict__ list)
+{
+    HD_GRID_STRIDE(i, n)
+    {
+        uint32_t b = bitmap[i];
+        uint32_t o = pos[i];
+        while (b) {
+            const uint32_t bit = __ffs(b) - 1;
+            b &= b - 1;
+            list[o++] = base + uint32_t(i) * 32 + bit;
+        }
+    }
+}
+
+HD_D uint32_t lower_bound(const uint32_t* v, uint32_t n, uint32_t x)
+{
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (v[mid] < x)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Gathers the live nodes of a level (children remapped) before the level is
+// emptied; hashes and links them into the bucket lists.
+__global__ void k_gc_gather(Table t, uint32_t level, const uint32_t* __restrict__ live, uint32_t n,
+                            const uint32_t* __restrict__ child_live, uint32_t n_child,
+                            const uint32_t* __restrict__ child_new, uint32_t* __restrict__ content,
+                            uint32_t* __restrict__ head, uint32_t* __restrict__ next, uint32_t* __restrict__ touched,
+                            uint32_t* __restrict__ n_touched)
+{
+    const bool leaf = level == t.g.leaf_level;
+    HD_GRID_STRIDE(i, n)
+    {
+        const uint32_t* p = t.sys(live[i]);
+        uint32_t* c = content + 9 * i;
+        uint32_t hash;
+        if (leaf) {
+            c[0] = p[0];
+            c[1] = p[1];
+            hash = hash_leaf(uint64_t(c[0]) | (uint64_t(c[1]) << 32));
+        } else {
+            const uint32_t cnt = popc32(p[0] & 0xffu);
+            c[0] = p[0];
+            for (uint32_t k = 0; k < cnt; k++)
+                c[1 + k] = child_new[lower_bound(child_live, n_child, p[1 + k])];
+            hash = hash_interior(cnt + 1, c);
+        }
+        const uint32_t bucket = hash & (t.g.buckets(level) - 1);
+        link_item(t.g.bucket_global(level, bucket), uint32_t(i), head, next, touched, n_touched);
+    }
+}
+
+__global__ void k_gc_remap_roots(const uint32_t* __restrict__ live, uint32_t n, const uint32_t* __restrict__ newaddr,
+                                 uint32_t* roots, uint32_t n_roots, uint32_t* d_root)
+{
+    for (uint32_t i = 0; i < n_roots; i++)
+        roots[i] = newaddr[lower_bound(live, n, roots[i])];
+    *d_root = roots[0];
+}
+
+void gc(hd_ctx* c, std::vector<uint32_t>& roots)
+{
+    cudaStream_t st = c->stream;
+    Scratch& s = c->scratch;
+    const Geom& g = c->g;
+    const uint32_t leafl = g.leaf_level;
+    uint32_t* d_n = s.get<uint32_t>("gc_n", 4);
+    // level 0: the roots, sorted unique
+    std::vector<uint32_t> r0(roots.begin(), roots.end());
+    std::sort(r0.begin(), r0.end());
+    r0.erase(std::unique(r0.begin(), r0.end()), r0.end());
+    std::vector<uint32_t*> live(leafl + 1), newaddr(leafl + 1);
+    std::vector<uint32_t> nlive(leafl + 1);
+    live[0] = s.get<uint32_t>("gc_live_0", r0.size());
+    HD_CUDA(cudaMemcpyAsync(live[0], r0.data(), r0.size() * 4, cudaMemcpyHostToDevice, st));
+    nlive[0] = uint32_t(r0.size());
+    // mark
+    for (uint32_t L = 0; L < leafl; L++) {
+        const uint32_t base = g.make_ptr(L + 1, 0, 0);
+        const uint64_t range = uint64_t(g.buckets(L + 1)) * g.capacity(L + 1);
+        const uint64_t nwords = (range + 31) / 32;
+        uint32_t* bitmap = s.get<uint32_t>("gc_bitmap", nwords);
+        HD_CUDA(cudaMemsetAsync(bitmap, 0, nwords * 4, st));
+        k_gc_mark<<<grid_for(nlive[L], 256), 256, 0, st>>>(c->t, live[L], nlive[L], base, bitmap);
+        HD_LAUNCH_CHECK();
+        uint32_t* counts = s.get<uint32_t>("gc_counts", nwords);
+        uint32_t* pos = s.get<uint32_t>("gc_pos", nwords);
+        k_popc_words<<<grid_for(nwords, 256), 256, 0, st>>>(bitmap, nwords, counts);
+        HD_LAUNCH_CHECK();
+        exclusive_scan<uint32_t, uint32_t>(s, counts, pos, nwords, d_n, st);
+        nlive[L + 1] = read_scalar(d_n, st);
+        char nm[32];
+        snprintf(nm, sizeof(nm), "gc_live_%u", L + 1);
+        live[L + 1] = s.get<uint32_t>(nm, uint64_t(nlive[L + 1]) + 1);
+        k_bitmap_to_list<<<grid_for(nwords, 256), 256, 0, st>>>(bitmap, pos, nwords, base, live[L + 1]);
+        HD_LAUNCH_CHECK();
+    }
+    // rebuild bottom-up
+    uint32_t maxn = 1;
+    for (uint32_t L = 0; L <= leafl; L++)
+        maxn = std::max(maxn, nlive[L]);
+    uint32_t* content = s.get<uint32_t>("gc_content", uint64_t(maxn) * 9);
+    uint32_t* next = s.get<uint32_t>("gc_next", maxn);
+    uint32_t* head = s.get<uint32_t>("gc_head", g.total_buckets);
+    uint32_t* touched = s.get<uint32_t>("gc_touched", g.total_buckets);
+    fill<uint32_t>(head, kEmpty, g.total_buckets, st);
+    for (int32_t L = int32_t(leafl); L >= 0; L--) {
+        const uint32_t n = nlive[L];
+        char nm[32];
+        snprintf(nm, sizeof(nm), "gc_new_%d", L);
+        newaddr[L] = s.get<uint32_t>(nm, uint64_t(n) + 1);
+        HD_CUDA(cudaMemsetAsync(d_n, 0, 4, st));
+        k_gc_gather<<<grid_for(n, 256), 256, 0, st>>>(c->t, uint32_t(L), live[L], n,
+                                                      L < int32_t(leafl) ? live[L + 1] : nullptr,
+                                                      L < int32_t(leafl) ? nlive[L + 1] : 0,
+                                                      L < int32_t(leafl) ? newaddr[L + 1] : nullptr, content, head,
+                                                      next, touched, d_n);
+        HD_LAUNCH_CHECK();
+        // empty the level's buckets, then the full node first
+        HD_CUDA(cudaMemsetAsync(c->t.bucket_sizes + g.level_first_bucket(uint32_t(L)), 0,
+                                uint64_t(g.buckets(uint32_t(L))) * 4, st));
+        HD_CUDA(cudaMemsetAsync(c->t.level_nodes + L, 0, 8, st));
+        add_full_nodes(c, uint32_t(L), uint32_t(L));
+        append_items(c, uint32_t(L), content, n, head, next, touched, d_n, newaddr[L]);
+    }
+    uint32_t* d_roots = s.get<uint32_t>("gc_roots", roots.size());
+    HD_CUDA(cudaMemcpyAsync(d_roots, roots.data(), roots.size() * 4, cudaMemcpyHostToDevice, st));
+    k_gc_remap_roots<<<1, 1, 0, st>>>(live[0], nlive[0], newaddr[0], d_roots, uint32_t(roots.size()), c->d_root);
+    HD_LAUNCH_CHECK();
+    HD_CUDA(cudaMemcpyAsync(roots.data(), d_roots, roots.size() * 4, cudaMemcpyDeviceToHost, st));
+    HD_CUDA(cudaStreamSynchronize(st));
+    const uint32_t e = check_error(c);
+    if (e)
+        throw StatusError{hd_status(e), "garbage collection failed on the device"};
+    c->root = roots[0];
+    c->edit_head_ready = false;
+}
+
+} // namespace hd
+
+extern "C" hd_status hd_gc(hd_ctx* c, uint32_t* extra, uint32_t n)
+{
+    if (!c || (n && !extra))
+        return HD_ERR_INVALID;
+    try {
+        std::vector<uint32_t> roots(1 + n);
+        roots[0] = hd::read_scalar(c->d_root, c->stream);
+        for (uint32_t i = 0; i < n; i++)
+            roots[1 + i] = extra[i];
+        hd::gc(c, roots);
+        // the remapped extra roots go back to the caller
+        for (uint32_t i = 0; i < n; i++)
+            extra[i] = roots[1 + i];
+        return HD_OK;
+    } catch (const hd::StatusError& e) {
+        c->err = e.msg;
+        return e.status;
+    } catch (const hd::CudaError& e) {
+        c->err = std::string("CUDA error ") + cudaGetErrorString(e.code) + " in " + e.where;
+        return HD_ERR_CUDA;
+    }
+}

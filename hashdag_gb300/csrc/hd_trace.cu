@@ -1,0 +1,363 @@
+// Primary and shadow ray traversal over the device-resident hash DAG, and
+// point queries.
+//
+// Reference: Tracer::trace_paths (tracer.cu:145-252) with
+// compute_intersection_mask (:19-136) and next_child (:7-17);
+// intersect_ray_node_out_of_order (:453-543) and trace_shadows (:589-697)
+// with ray_box_intersection (:574-587); DAGUtils::get_value
+// (dag_utils.h:138-172).  Camera rays as get_trace_params builds them
+// (dag_tracer.cu:71-113).
+//
+// Arithmetic: this file is compiled with -fmad=false, so every float/double
+// expression is rounded operation by operation in source order; FMA = 1
+// places explicit fused multiply-adds where the reference's default nvcc
+// build contracts a product into the following add.
+#include "hd_ctx.h"
+
+namespace hd {
+
+struct F3 {
+    float x, y, z;
+};
+
+HD_D float fmax_r(float a, float b) { return a > b ? a : b; } // constexpr_max (cuda_math.h:13)
+HD_D float fmin_r(float a, float b) { return a < b ? a : b; }
+
+// normalize(ray_min + px * ddx + py * ddy - position), double
+template <int FMA>
+HD_D void camera_dir(const hd_camera& cam, double px, double py, double out[3])
+{
+    double v[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        double t;
+        if (FMA) {
+            t = __fma_rn(px, cam.ray_ddx[a], cam.ray_min[a]);
+            t = __fma_rn(py, cam.ray_ddy[a], t);
+        } else {
+            t = cam.ray_min[a] + px * cam.ray_ddx[a];
+            t = t + py * cam.ray_ddy[a];
+        }
+        v[a] = t - cam.position[a];
+    }
+    const double dot = FMA ? __fma_rn(v[2], v[2], __fma_rn(v[1], v[1], v[0] * v[0]))
+                           : (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+    const double inv = 1.0 / sqrt(dot);
+    out[0] = inv * v[0];
+    out[1] = inv * v[1];
+    out[2] = inv * v[2];
+}
+
+// compute_intersection_mask: children of node `path` at `level` crossed by
+// the ray, as an 8-bit mask.
+template <int FMA>
+HD_D uint32_t intersection_mask(uint32_t D, bool is_root, uint32_t level, uint32_t px, uint32_t py, uint32_t pz,
+                                const F3& o, const F3& d, const F3& inv)
+{
+    const uint32_t shift = D - level;
+    const float radius = float(1u << (shift - 1));
+    const F3 crr = {(radius + float(px << shift)) - o.x, (radius + float(py << shift)) - o.y,
+                    (radius + float(pz << shift)) - o.z};
+    const F3 tmid = {crr.x * inv.x, crr.y * inv.y, crr.z * inv.z};
+    const F3 slab = {radius * fabsf(inv.x), radius * fabsf(inv.y), radius * fabsf(inv.z)};
+    F3 pmin, pmax;
+    if (FMA) {
+        pmin = {__fmaf_rn(crr.x, inv.x, -slab.x), __fmaf_rn(crr.y, inv.y, -slab.y), __fmaf_rn(crr.z, inv.z, -slab.z)};
+        pmax = {__fmaf_rn(crr.x, inv.x, slab.x), __fmaf_rn(crr.y, inv.y, slab.y), __fmaf_rn(crr.z, inv.z, slab.z)};
+    } else {
+        pmin = {tmid.x - slab.x, tmid.y - slab.y, tmid.z - slab.z};
+        pmax = {tmid.x + slab.x, tmid.y + slab.y, tmid.z + slab.z};
+    }
+    const float tmin = fmax_r(fmax_r(pmin.x, fmax_r(pmin.y, pmin.z)), 0.0f);
+    const float tmax = fmin_r(pmax.x, fmin_r(pmax.y, pmax.z));
+    if (is_root && tmin >= tmax)
+        return 0;
+    uint32_t result;
+    {
+        const float s = 0.5f * (tmin + tmax);
+        const uint32_t first = ((s * d.x) >= crr.x ? 4u : 0u) + ((s * d.y) >= crr.y ? 2u : 0u) +
+                               ((s * d.z) >= crr.z ? 1u : 0u);
+        result = 1u << first;
+    }
+    const float eps = 1e-4f;
+    if (tmin <= tmid.x && tmid.x <= tmax) {
+        const float py_ = tmid.x * d.y, pz_ = tmid.x * d.z;
+        uint32_t A = 0, B = 0;
+        if (py_ >= crr.y - eps) A |= 0xCC;
+        if (py_ <= crr.y + eps) A |= 0x33;
+        if (pz_ >= crr.z - eps) B |= 0xAA;
+        if (pz_ <= crr.z + eps) B |= 0x55;
+        result |= A & B;
+    }
+    if (tmin <= tmid.y && tmid.y <= tmax) {
+        const float px_ = tmid.y * d.x, pz_ = tmid.y * d.z;
+        uint32_t C = 0, E = 0;
+        if (px_ >= crr.x - eps) C |= 0xF0;
+        if (px_ <= crr.x + eps) C |= 0x0F;
+        if (pz_ >= crr.z - eps) E |= 0xAA;
+        if (pz_ <= crr.z + eps) E |= 0x55;
+        result |= C & E;
+    }
+    if (tmin <= tmid.z && tmid.z <= tmax) {
+        const float px_ = tmid.z * d.x, py_ = tmid.z * d.y;
+        uint32_t G = 0, H = 0;
+        if (px_ >= crr.x - eps) G |= 0xF0;
+        if (px_ <= crr.x + eps) G |= 0x0F;
+        if (py_ >= crr.y - eps) H |= 0xCC;
+        if (py_ <= crr.y + eps) H |= 0x33;
+        result |= G & H;
+    }
+    return result & 0xffu;
+}
+
+HD_D uint32_t first_child_mask(uint32_t low, uint32_t high) // Leaf::get_first_child_mask (base_dag.h:16-52)
+{
+    const uint32_t a = __vcmpne4(low, 0u) & 0x08040201u;
+    const uint32_t b = __vcmpne4(high, 0u) & 0x08040201u;
+    return ((a * 0x01010101u) >> 24) | (((b * 0x01010101u) >> 24) << 4);
+}
+
+HD_D uint32_t next_child(uint32_t order, uint32_t mask) // next_child (tracer.cu:7-17)
+{
+    // first set bit of mask in the order child ^ order, child = 0..7
+    uint32_t permuted = 0;
+#pragma unroll
+    for (uint32_t c = 0; c < 8; c++)
+        permuted |= ((mask >> (c ^ order)) & 1u) << c;
+    return (__ffs(permuted) - 1) ^ order;
+}
+
+struct Entry {
+    uint32_t index;
+    uint32_t masks; // child mask | visit mask << 8
+};
+
+// The stack walk shared by the primary ray (nearest hit, children in the
+// ray's octant order) and the shadow ray (any hit, children highest first).
+template <int FMA, bool ANY_HIT>
+HD_D bool walk(const Table& t, uint32_t root, const F3& o, const F3& d, const F3& inv, uint32_t order, uint32_t* hit,
+               uint32_t& descents, uint32_t& leaves)
+{
+    const uint32_t D = t.g.depth, leafl = t.g.leaf_level;
+    Entry stack[HD_MAX_DEPTH];
+    uint32_t level = 0, px = 0, py = 0, pz = 0;
+    uint32_t index = root;
+    uint32_t child_mask = __ldg(t.sys(root)) & 0xffu;
+    uint32_t visit = child_mask & intersection_mask<FMA>(D, true, 0, 0, 0, 0, o, d, inv);
+    uint32_t leaf_lo = 0, leaf_hi = 0;
+    for (;;) {
+        uint32_t nl = level;
+        while (nl > 0 && !visit) {
+            nl--;
+            index = stack[nl].index;
+            child_mask = stack[nl].masks & 0xffu;
+            visit = stack[nl].masks >> 8;
+        }
+        if (nl == 0 && !visit) {
+            hit[0] = hit[1] = hit[2] = 0;
+            return false;
+        }
+        const uint32_t up = level - nl;
+        px >>= up;
+        py >>= up;
+        pz >>= up;
+        level = nl;
+        const uint32_t nc = ANY_HIT ? 31u - __clz(visit) : next_child(order, visit);
+        visit &= ~(1u << nc);
+        px = (px << 1) | ((nc >> 2) & 1);
+        py = (py << 1) | ((nc >> 1) & 1);
+        pz = (pz << 1) | (nc & 1);
+        stack[level] = {index, child_mask | (visit << 8)};
+        level++;
+        if (level == D) {
+            hit[0] = px;
+            hit[1] = py;
+            hit[2] = pz;
+            return true;
+        }
+        if (level < leafl) {
+            index = __ldg(t.sys(index + child_offset(child_mask, nc)));
+            child_mask = __ldg(t.sys(index)) & 0xffu;
+            descents++;
+        } else if (level == leafl) {
+            const uint32_t addr = __ldg(t.sys(index + child_offset(child_mask, nc)));
+            const uint2 lf = __ldg(reinterpret_cast<const uint2*>(t.sys(addr)));
+            leaf_lo = lf.x;
+            leaf_hi = lf.y;
+            child_mask = first_child_mask(leaf_lo, leaf_hi);
+            leaves++;
+        } else {
+            child_mask = ((nc & 4) ? leaf_hi : leaf_lo) >> ((nc & 3) * 8) & 0xffu;
+        }
+        visit = child_mask & intersection_mask<FMA>(D, false, level, px, py, pz, o, d, inv);
+    }
+}
+
+HD_D F3 inverse_dir(const F3& d)
+{
+    return {float(1.0 / double(d.x)), float(1.0 / double(d.y)), float(1.0 / double(d.z))};
+}
+
+// 8x8 pixel tiles per 64-thread block; a warp covers 8x4 pixels.
+// Traversal work counters (COUNT instances only): rays, interior descents,
+// leaf fetches.
+HD_D void add_counts(unsigned long long* counters, uint32_t rays, uint32_t descents, uint32_t leaves)
+{
+    atomicAdd(counters + 0, rays);
+    atomicAdd(counters + 1, descents);
+    atomicAdd(counters + 2, leaves);
+}
+
+template <int FMA, bool COUNT>
+__global__ void __launch_bounds__(64) k_trace_primary(Table t, const uint32_t* __restrict__ d_root, hd_camera cam,
+                                                      uint32_t W, uint32_t H, uint4* __restrict__ out,
+                                                      unsigned long long* counters)
+{
+    const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7);
+    const uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 3);
+    if (x >= W || y >= H)
+        return;
+    double dd[3];
+    camera_dir<FMA>(cam, double(x), double(y), dd);
+    const F3 d = {float(dd[0]), float(dd[1]), float(dd[2])};
+    const F3 inv = inverse_dir(d);
+    const F3 o = {float(cam.position[0]), float(cam.position[1]), float(cam.position[2])};
+    const uint32_t order = (d.x < 0.f ? 4u : 0u) + (d.y < 0.f ? 2u : 0u) + (d.z < 0.f ? 1u : 0u);
+    uint32_t hit[3], descents = 0, leaves = 0;
+    walk<FMA, false>(t, *d_root, o, d, inv, order, hit, descents, leaves);
+    out[uint64_t(H - 1 - y) * W + x] = make_uint4(hit[0], hit[1], hit[2], 0);
+    if (COUNT)
+        add_counts(counters, 1, descents, leaves);
+}
+
+// Rows are output rows (the layout of the paths image).
+template <int FMA, bool COUNT>
+__global__ void __launch_bounds__(64) k_trace_shadow(Table t, const uint32_t* __restrict__ d_root, hd_camera cam,
+                                                     uint32_t W, uint32_t H, const uint4* __restrict__ paths,
+                                                     F3 light, float bias, uint8_t* __restrict__ mask,
+                                                     unsigned long long* counters)
+{
+    const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7);
+    const uint32_t r = blockIdx.y * 8 + (threadIdx.x >> 3);
+    if (x >= W || r >= H)
+        return;
+    const uint64_t i = uint64_t(r) * W + x;
+    const uint4 p = paths[i];
+    if (p.x == 0 && p.y == 0 && p.z == 0) {
+        mask[i] = 2;
+        return;
+    }
+    // sun_direction(): normalize in float (tracer.cu:546-549)
+    const float dot = FMA ? __fmaf_rn(light.z, light.z, __fmaf_rn(light.y, light.y, light.x * light.x))
+                          : (light.x * light.x + light.y * light.y) + light.z * light.z;
+    const float il = 1.0f / sqrtf(dot);
+    const F3 dir = {il * light.x, il * light.y, il * light.z};
+    double cd[3];
+    camera_dir<FMA>(cam, double(x), double(H - 1 - r), cd);
+    // ray_box_intersection with the hit voxel's box
+    const double bmin[3] = {double(float(p.x)), double(float(p.y)), double(float(p.z))};
+    double real_min[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const double t0 = (bmin[a] - cam.position[a]) / cd[a];
+        const double t1 = ((bmin[a] + 1.0) - cam.position[a]) / cd[a];
+        real_min[a] = t0 < t1 ? t0 : t1;
+    }
+    const double maxmin = fmax(fmax(real_min[0], real_min[1]), real_min[2]);
+    F3 start, o;
+    if (FMA) {
+        start = {float(__fma_rn(cd[0], maxmin, cam.position[0])), float(__fma_rn(cd[1], maxmin, cam.position[1])),
+                 float(__fma_rn(cd[2], maxmin, cam.position[2]))};
+        o = {__fmaf_rn(bias, dir.x, start.x), __fmaf_rn(bias, dir.y, start.y), __fmaf_rn(bias, dir.z, start.z)};
+    } else {
+        start = {float(cam.position[0] + cd[0] * maxmin), float(cam.position[1] + cd[1] * maxmin),
+                 float(cam.position[2] + cd[2] * maxmin)};
+        o = {start.x + bias * dir.x, start.y + bias * dir.y, start.z + bias * dir.z};
+    }
+    uint32_t hit[3], descents = 0, leaves = 0;
+    mask[i] = walk<FMA, true>(t, *d_root, o, dir, inverse_dir(dir), 0, hit, descents, leaves) ? 1 : 0;
+    if (COUNT)
+        add_counts(counters, 1, descents, leaves);
+}
+
+void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint32_t* d_paths,
+                   unsigned long long* d_counters)
+{
+    dim3 grid((w + 7) / 8, (h + 7) / 8);
+    uint4* out = reinterpret_cast<uint4*>(d_paths);
+    if (d_counters) {
+        if (c->fp_mode)
+            k_trace_primary<1, true><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, out, d_counters);
+        else
+            k_trace_primary<0, true><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, out, d_counters);
+    } else {
+        if (c->fp_mode)
+            k_trace_primary<1, false><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, out, nullptr);
+        else
+            k_trace_primary<0, false><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, out, nullptr);
+    }
+    HD_LAUNCH_CHECK();
+}
+
+void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
+                  const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters)
+{
+    dim3 grid((w + 7) / 8, (h + 7) / 8);
+    const F3 l = {light[0], light[1], light[2]};
+    const uint4* p = reinterpret_cast<const uint4*>(d_paths);
+    if (d_counters) {
+        if (c->fp_mode)
+            k_trace_shadow<1, true><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, p, l, bias, d_mask,
+                                                                d_counters);
+        else
+            k_trace_shadow<0, true><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, p, l, bias, d_mask,
+                                                                d_counters);
+    } else {
+        if (c->fp_mode)
+            k_trace_shadow<1, false><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, p, l, bias, d_mask,
+                                                                 nullptr);
+        else
+            k_trace_shadow<0, false><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, p, l, bias, d_mask,
+                                                                 nullptr);
+    }
+    HD_LAUNCH_CHECK();
+}
+
+// DAGUtils::get_value
+__global__ void k_get_values(Table t, const uint32_t* __restrict__ d_root, const uint32_t* __restrict__ xyz,
+                             uint64_t n, uint8_t* __restrict__ out)
+{
+    const uint32_t root = *d_root;
+    HD_GRID_STRIDE(i, n)
+    {
+        const uint32_t x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        uint32_t index = root;
+        uint8_t v = 0;
+        for (uint32_t level = 0; level < t.g.depth; level++) {
+            if (level < t.g.leaf_level) {
+                const uint32_t mask = __ldg(t.sys(index)) & 0xffu;
+                const uint32_t s = t.g.depth - (level + 1);
+                const uint32_t child = (((x >> s) & 1) << 2) | (((y >> s) & 1) << 1) | ((z >> s) & 1);
+                if (!(mask & (1u << child)))
+                    break;
+                index = __ldg(t.sys(index + child_offset(mask, child)));
+            } else {
+                const uint32_t* p = t.sys(index);
+                const uint64_t leaf = uint64_t(__ldg(p)) | (uint64_t(__ldg(p + 1)) << 32);
+                v = uint8_t((leaf >> leaf_bit(x, y, z)) & 1);
+                break;
+            }
+        }
+        out[i] = v;
+    }
+}
+
+void get_values(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out)
+{
+    if (!n)
+        return;
+    k_get_values<<<grid_for(n, 256), 256, 0, c->stream>>>(c->t, c->d_root, d_xyz, n, d_out);
+    HD_LAUNCH_CHECK();
+}
+
+} // namespace hd

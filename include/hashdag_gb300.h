@@ -159,6 +159,13 @@ hd_status hd_trace_shadow(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uin
 hd_status hd_trace_frame(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint32_t height,
                          const float light[3], float bias, uint32_t* d_paths, uint8_t* d_mask,
                          float* ms_primary, float* ms_shadow);
+/* hd_trace_frame with work counters, for the roofline's algorithmic bytes:
+ * out = {primary rays, primary interior descents, primary leaf fetches,
+ * shadow rays, shadow interior descents, shadow leaf fetches}; shadow rays
+ * are the pixels with a primary hit. */
+hd_status hd_trace_counters(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint32_t height,
+                            const float light[3], float bias, uint32_t* d_paths, uint8_t* d_mask,
+                            uint64_t out[6]);
 /* Selects the arithmetic of the ray set-up: 0 = every float/double op
  * rounded on its own, 1 = the fused multiply-adds nvcc contracts in the
  * reference's default build.  Default 1. */
@@ -186,8 +193,9 @@ hd_status hd_edit_batch(hd_ctx* ctx, const hd_edit* edits, uint32_t n, hd_edit_s
 /* Marks the nodes reachable from the root and from the n extra roots, then
  * rebuilds every level bottom-up: buckets emptied, full node re-added first,
  * live nodes re-appended in increasing old-address order with children
- * remapped.  Pages stay mapped (the reference never unmaps them). */
-hd_status hd_gc(hd_ctx* ctx, const uint32_t* h_extra_roots, uint32_t n_extra);
+ * remapped.  Pages stay mapped (the reference never unmaps them).  The root
+ * and h_extra_roots (in/out) are rewritten to their new addresses. */
+hd_status hd_gc(hd_ctx* ctx, uint32_t* h_extra_roots, uint32_t n_extra);
 
 /* ---- state and statistics ---------------------------------------------- */
 
