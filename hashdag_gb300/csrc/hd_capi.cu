@@ -111,7 +111,7 @@ hd_status hd_create(const hd_config* cfg, hd_ctx** out)
         HD_CUDA(cudaMalloc(&t.bucket_sizes, c->g.total_buckets * 4));
         HD_CUDA(cudaMalloc(&t.full_nodes, HD_MAX_DEPTH * 4));
         HD_CUDA(cudaMalloc(&t.pool_top, 4));
-        HD_CUDA(cudaMalloc(&t.error, 4));
+        HD_CUDA(cudaMalloc(&t.error, 16));
         HD_CUDA(cudaMalloc(&t.level_nodes, HD_MAX_DEPTH * 8));
         HD_CUDA(cudaMalloc(&c->d_root, 4));
         HD_CUDA(cudaEventCreate(&c->ev0));

@@ -97,9 +97,18 @@ struct Table {
     uint64_t* level_nodes;  // stored node count per level
     Geom g;
 
+    // Translation through the read-only data path: for kernels during which
+    // neither the page table nor the pool changes (traversal, the edit
+    // descent, GC gathers).
     HD_D const uint32_t* sys(uint32_t v) const
     {
         return pool + (uint64_t(__ldg(page_table + (v >> kPageShift))) << kPageShift) + (v & (kPage - 1));
+    }
+    // Translation with an L2-coherent read of the page table, for kernels
+    // that map pages while they scan.
+    HD_D const uint32_t* sys_cg(uint32_t v) const
+    {
+        return pool + (uint64_t(__ldcg(page_table + (v >> kPageShift))) << kPageShift) + (v & (kPage - 1));
     }
     HD_D uint32_t* sys_rw(uint32_t v) const
     {
@@ -107,7 +116,15 @@ struct Table {
     }
 };
 
-HD_D void set_error(uint32_t* err, uint32_t code) { atomicCAS(err, 0u, code); }
+// err[0] = first error code; err[1..3] = its detail words.
+HD_D void set_error(uint32_t* err, uint32_t code, uint32_t a = 0, uint32_t b = 0, uint32_t c = 0)
+{
+    if (atomicCAS(err, 0u, code) == 0u) {
+        err[1] = a;
+        err[2] = b;
+        err[3] = c;
+    }
+}
 
 // ---- hashes (utils.h:355-396) --------------------------------------------
 HD_HD uint32_t murmur32(uint32_t h)

@@ -15,6 +15,7 @@ struct hd_ctx {
     uint32_t root = 0;                 // host copy, refreshed after each call
     uint32_t fp_mode = 1;
     std::string err;
+    std::string err_detail;           // detail words of the last device error
     hd::Scratch scratch;               // grow-only working buffers
     // BasicDAG of the last generated scene (device), kept for export
     uint32_t* d_basic = nullptr;

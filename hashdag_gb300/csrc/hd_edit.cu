@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "hd_ctx.h"
+#include "hd_sort.cuh"
 #include "hd_table.cuh"
 
 namespace hd {
@@ -238,14 +239,16 @@ __global__ void k_edit_spawn(Table t, uint32_t n, Level lv, Level next)
 
 // Bottom-up: rebuilt content of every kLeafEval / kDescend entry; unchanged
 // and emptied nodes resolve at once, the rest become find-or-add candidates.
-__global__ void k_edit_candidates(Table t, uint32_t level, uint32_t n, Level lv, Level child, uint32_t* head,
-                                  uint32_t* next_item, uint32_t* touched, uint32_t* n_touched)
+__global__ void k_edit_candidates(Table t, uint32_t level, uint32_t n, Level lv, Level child, uint32_t* keys,
+                                  uint32_t* vals, uint32_t* n_cand)
 {
     const uint32_t T = t.g.T, leafl = t.g.leaf_level;
     HD_GRID_STRIDE(i, n)
     {
         const uint8_t state = lv.state[i];
         uint32_t* c = lv.cand + 9 * i;
+        keys[i] = kEmpty;
+        vals[i] = uint32_t(i);
         uint32_t hash, nw;
         if (state == kLeafEval) {
             const uint64_t leaf = lv.leaf[i];
@@ -313,133 +316,274 @@ __global__ void k_edit_candidates(Table t, uint32_t level, uint32_t n, Level lv,
         (void)nw;
         const uint32_t bucket = hash & (t.g.buckets(level) - 1);
         lv.res[i] = kNotFound; // resolved by find-or-add
-        link_item(t.g.bucket_global(level, bucket), uint32_t(i), head, next_item, touched, n_touched);
+        keys[i] = t.g.bucket_global(level, bucket);
+        atomicAdd(n_cand, 1u);
     }
 }
 
-// One warp per touched bucket: the bucket's candidates, in depth-first
-// order, each scanned against the bucket as it stands (earlier candidates'
-// appends included) and appended when not found.
+// After the stable sort by bucket: the first position of every bucket's run.
+__global__ void k_segment_flags(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ flag)
+{
+    HD_GRID_STRIDE(j, n) flag[j] = keys[j] != kEmpty && (j == 0 || keys[j] != keys[j - 1]);
+}
+
+__global__ void k_segment_starts(const uint32_t* __restrict__ flag, const uint32_t* __restrict__ pos, uint32_t n,
+                                 uint32_t* __restrict__ starts)
+{
+    HD_GRID_STRIDE(j, n)
+    {
+        if (flag[j])
+            starts[pos[j]] = uint32_t(j);
+    }
+}
+
+// One warp per bucket: the bucket's candidates, in depth-first order, each
+// resolved against the bucket as it stands (earlier candidates' appends
+// included) and appended when not found.  A per-warp cache remembers, for
+// every content already resolved in this bucket, the positions where a copy
+// lies (the first match a scan sees, the bucket's last node when it holds
+// the content, and the copies appended since): a repeated content then needs
+// no new scan, only the visibility rule on those positions.  Runs of
+// identical candidates after a found result take that result at once.
 constexpr uint32_t kFoaWarps = 4;
+constexpr uint32_t kCache = 32;
+constexpr uint32_t kCachePos = 3;
+
+struct FoaCache {
+    uint32_t words[kCache][9];
+    uint32_t n[kCache];
+    uint32_t npos[kCache];
+    uint32_t pos[kCache][kCachePos];
+};
+
+// A node at bucket position p (a walk position) of size n is compared by the
+// reference's interior scan iff p + n < min(S, page end) (leaves: always).
+HD_D bool visible(uint32_t p, uint32_t n, uint32_t S, bool leaf)
+{
+    if (leaf)
+        return p + 2 <= S;
+    const uint32_t pe = (p & ~(kPage - 1)) + kPage;
+    return p + n < (S < pe ? S : pe);
+}
+
+// Warp-wide scan of the bucket for the first compared position holding q
+// (find_leaf_node_in_bucket / find_interior_node_in_bucket); returns the
+// bucket position or kNotFound.  *last_match: for interiors, the bucket's
+// last node when it holds q (compared by no scan until something follows).
+HD_D uint32_t scan_bucket(const Table& t, uint32_t vbase, uint32_t S, const uint32_t* q, uint32_t n, bool leaf,
+                          uint32_t* page, uint32_t* last_match, unsigned long long& scanned)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t found = kNotFound;
+    *last_match = kNotFound;
+    for (uint32_t pindex = 0; pindex < S && found == kNotFound; pindex += kPage) {
+        const uint32_t page_end = S < pindex + kPage ? S : pindex + kPage;
+        if (!leaf && pindex + n >= page_end)
+            break; // "return 0xFFFFFFFF" of the reference scan
+        const uint32_t used = page_end - pindex;
+        // L2-coherent loads: this kernel appends nodes and maps pages
+        const uint32_t* src = t.sys_cg(vbase + pindex);
+        for (uint32_t w = lane * 4; w < used; w += 128) {
+            const uint4 v = __ldcg(reinterpret_cast<const uint4*>(src + w));
+            page[w] = v.x;
+            page[w + 1] = v.y;
+            page[w + 2] = v.z;
+            page[w + 3] = v.w;
+        }
+        __syncwarp();
+        if (leaf) {
+            for (uint32_t w0 = 0; w0 < used && found == kNotFound; w0 += 64) {
+                const uint32_t w = w0 + 2 * lane;
+                const bool m = w < used && page[w] == q[0] && page[w + 1] == q[1];
+                const uint32_t b = __ballot_sync(0xffffffffu, m);
+                if (b)
+                    found = pindex + w0 + 2 * (__ffs(b) - 1);
+            }
+        } else {
+            const uint32_t lim = used - n;
+            for (uint32_t w0 = 0; w0 < lim && found == kNotFound; w0 += 32) {
+                const uint32_t w = w0 + lane;
+                bool m = w < lim && page[w] == q[0];
+                if (m)
+                    for (uint32_t k = 1; k < n; k++)
+                        m &= page[w + k] == q[k];
+                uint32_t b = __ballot_sync(0xffffffffu, m);
+                while (b && found == kNotFound) {
+                    const uint32_t cand = w0 + __ffs(b) - 1;
+                    b &= b - 1;
+                    uint32_t on_walk = 0;
+                    if (lane == 0) {
+                        uint32_t p = 0;
+                        while (p < cand)
+                            p += total_size(page[p]);
+                        on_walk = p == cand;
+                    }
+                    on_walk = __shfl_sync(0xffffffffu, on_walk, 0);
+                    if (on_walk)
+                        found = pindex + cand;
+                }
+            }
+        }
+        scanned += found == kNotFound ? used : (found - pindex + n);
+        __syncwarp();
+    }
+    if (!leaf && found == kNotFound && S >= n) {
+        // the bucket's last node ends at S; it holds q iff it starts at S - n
+        const uint32_t p = S - n;
+        const uint32_t pindex = p & ~(kPage - 1);
+        const uint32_t used = S - pindex;
+        const uint32_t* src = t.sys_cg(vbase + pindex);
+        for (uint32_t w = lane * 4; w < used; w += 128) {
+            const uint4 v = __ldcg(reinterpret_cast<const uint4*>(src + w));
+            page[w] = v.x;
+            page[w + 1] = v.y;
+            page[w + 2] = v.z;
+            page[w + 3] = v.w;
+        }
+        __syncwarp();
+        uint32_t ok = 0;
+        if (lane == 0 && S - n >= pindex) {
+            bool m = true;
+            for (uint32_t k = 0; k < n; k++)
+                m &= page[p - pindex + k] == q[k];
+            if (m) {
+                uint32_t w = 0;
+                while (w < p - pindex)
+                    w += total_size(page[w]);
+                ok = w == p - pindex;
+            }
+        }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (ok)
+            *last_match = p;
+        __syncwarp();
+    }
+    return found;
+}
 
 __global__ void __launch_bounds__(32 * kFoaWarps)
-    k_edit_find_or_add(Table t, uint32_t level, Level lv, uint32_t* head, const uint32_t* next_item,
-                       const uint32_t* touched, const uint32_t* n_touched, EditCounters* ctr)
+    k_edit_find_or_add(Table t, uint32_t level, Level lv, const uint32_t* __restrict__ keys,
+                       const uint32_t* __restrict__ vals, const uint32_t* __restrict__ starts,
+                       const uint32_t* __restrict__ n_seg, const uint32_t* __restrict__ n_cand, EditCounters* ctr)
 {
-    __shared__ uint32_t items_s[kFoaWarps][kMaxBucketItems];
     __shared__ uint32_t page_s[kFoaWarps][kPage];
     __shared__ uint32_t q_s[kFoaWarps][9];
+    __shared__ FoaCache cache_s[kFoaWarps];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t* items = items_s[warp];
     uint32_t* page = page_s[warp];
     uint32_t* q = q_s[warp];
+    FoaCache& cache = cache_s[warp];
     const bool leaf = level == t.g.leaf_level;
-    const uint32_t nt = *n_touched;
+    const uint32_t nseg = *n_seg, ncand = *n_cand;
     unsigned long long foa = 0, added = 0, scanned = 0;
-    for (uint32_t ti = blockIdx.x * kFoaWarps + warp; ti < nt; ti += gridDim.x * kFoaWarps) {
-        const uint32_t gb = touched[ti];
-        const uint32_t cnt = collect_sorted(gb, head, next_item, items, t.error);
+    for (uint32_t si = blockIdx.x * kFoaWarps + warp; si < nseg; si += gridDim.x * kFoaWarps) {
+        const uint32_t j0 = starts[si], j1 = si + 1 < nseg ? starts[si + 1] : ncand;
+        const uint32_t gb = keys[j0];
         const uint32_t bucket = gb - t.g.level_first_bucket(level);
         const uint32_t vbase = t.g.make_ptr(level, bucket, 0);
-        uint32_t S = t.bucket_sizes[gb];
+        uint32_t S = __ldcg(t.bucket_sizes + gb);
+        uint32_t used_entries = 0, next_slot = 0;
         bool failed = false;
-        for (uint32_t j = 0; j < cnt && !failed; j++) {
-            const uint32_t ci = items[j];
+        uint32_t j = j0;
+        while (j < j1 && !failed) {
+            const uint32_t ci = vals[j];
             if (lane < 9)
-                q[lane] = lv.cand[9 * ci + lane];
+                q[lane] = lv.cand[9 * uint64_t(ci) + lane];
             __syncwarp();
             const uint32_t n = leaf ? 2 : total_size(q[0]);
-            uint32_t found = kNotFound;
-            for (uint32_t pindex = 0; pindex < S && found == kNotFound; pindex += kPage) {
-                uint32_t page_end = S < pindex + kPage ? S : pindex + kPage;
-                if (!leaf && pindex + n >= page_end)
-                    break; // find_interior_node_in_bucket: "return 0xFFFFFFFF"
-                const uint32_t used = page_end - pindex;
-                const uint32_t* src = t.sys(vbase + pindex);
-                for (uint32_t w = lane * 4; w < used; w += 128) {
-                    const uint4 v = *reinterpret_cast<const uint4*>(src + w);
-                    page[w] = v.x;
-                    page[w + 1] = v.y;
-                    page[w + 2] = v.z;
-                    page[w + 3] = v.w;
-                }
-                __syncwarp();
-                if (leaf) {
-                    for (uint32_t w0 = 0; w0 < used && found == kNotFound; w0 += 64) {
-                        const uint32_t w = w0 + 2 * lane;
-                        const bool m = w < used && page[w] == q[0] && page[w + 1] == q[1];
-                        const uint32_t b = __ballot_sync(0xffffffffu, m);
-                        if (b)
-                            found = vbase + pindex + w0 + 2 * (__ffs(b) - 1);
-                    }
-                } else {
-                    // positions compared by the reference: walk starts below
-                    // page_end - n; content matches first, the walk to confirm
-                    const uint32_t lim = used - n;
-                    for (uint32_t w0 = 0; w0 < lim && found == kNotFound; w0 += 32) {
-                        const uint32_t w = w0 + lane;
-                        bool m = w < lim && page[w] == q[0];
-                        if (m)
-                            for (uint32_t k = 1; k < n; k++)
-                                m &= page[w + k] == q[k];
-                        uint32_t b = __ballot_sync(0xffffffffu, m);
-                        while (b && found == kNotFound) {
-                            const uint32_t cand = w0 + __ffs(b) - 1;
-                            b &= b - 1;
-                            uint32_t on_walk = 0;
-                            if (lane == 0) {
-                                uint32_t p = 0;
-                                while (p < cand)
-                                    p += total_size(page[p]);
-                                on_walk = p == cand;
-                            }
-                            on_walk = __shfl_sync(0xffffffffu, on_walk, 0);
-                            if (on_walk)
-                                found = vbase + pindex + cand;
-                        }
-                    }
+            // cache lookup: lane e checks entry e
+            bool hit = lane < used_entries && cache.n[lane] == n;
+            if (hit)
+                for (uint32_t k = 0; k < n; k++)
+                    hit &= cache.words[lane][k] == q[k];
+            const uint32_t hb = __ballot_sync(0xffffffffu, hit);
+            uint32_t e;
+            if (hb) {
+                e = __ffs(hb) - 1;
+            } else {
+                uint32_t last_match;
+                const uint32_t f = scan_bucket(t, vbase, S, q, n, leaf, page, &last_match, scanned);
+                e = next_slot;
+                next_slot = (next_slot + 1) % kCache;
+                used_entries = used_entries < kCache ? used_entries + 1 : kCache;
+                if (lane < 9)
+                    cache.words[e][lane] = q[lane];
+                if (lane == 0) {
+                    cache.n[e] = n;
+                    cache.npos[e] = 0;
+                    if (f != kNotFound)
+                        cache.pos[e][cache.npos[e]++] = f;
+                    else if (last_match != kNotFound)
+                        cache.pos[e][cache.npos[e]++] = last_match;
                 }
                 __syncwarp();
             }
-            foa++;
-            if (found != kNotFound) {
-                scanned += found - vbase + n;
-            } else {
-                scanned += S;
-                // append (add_leaf_node / add_interior_node)
-                uint32_t ok = 1;
-                if (lane == 0) {
+            // the first visible copy, else append (lane 0)
+            uint32_t result = kNotFound, appended = 0, ok = 1;
+            if (lane == 0) {
+                for (uint32_t k = 0; k < cache.npos[e] && result == kNotFound; k++)
+                    if (visible(cache.pos[e][k], n, S, leaf))
+                        result = cache.pos[e][k];
+                if (result == kNotFound) {
                     uint32_t size = S;
                     const uint32_t pos = append_position(size, n, leaf);
                     if (size > t.g.capacity(level)) {
-                        set_error(t.error, kErrBucketFull);
+                        set_error(t.error, kErrBucketFull, level, bucket, size);
                         ok = 0;
                     } else if (!map_pages(t, level, bucket, pos, size)) {
                         ok = 0;
                     } else {
                         uint32_t* dst = t.sys_rw(vbase + pos);
                         for (uint32_t k = 0; k < n; k++)
-                            dst[k] = q[k];
-                        found = vbase + pos;
+                            __stcg(dst + k, q[k]);
+                        result = pos;
                         S = size;
+                        appended = 1;
+                        if (cache.npos[e] == kCachePos) { // keep the newest copies
+                            for (uint32_t k = 1; k < kCachePos; k++)
+                                cache.pos[e][k - 1] = cache.pos[e][k];
+                            cache.npos[e]--;
+                        }
+                        cache.pos[e][cache.npos[e]++] = pos;
                     }
                 }
-                ok = __shfl_sync(0xffffffffu, ok, 0);
-                found = __shfl_sync(0xffffffffu, found, 0);
-                S = __shfl_sync(0xffffffffu, S, 0);
-                if (!ok) {
-                    failed = true;
-                    break;
-                }
-                added++;
+                lv.res[ci] = vbase + result;
             }
-            if (lane == 0)
-                lv.res[ci] = found;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            result = __shfl_sync(0xffffffffu, result, 0);
+            appended = __shfl_sync(0xffffffffu, appended, 0);
+            S = __shfl_sync(0xffffffffu, S, 0);
+            foa++;
+            added += appended;
+            if (!ok) {
+                failed = true;
+                break;
+            }
+            j++;
+            // a found result holds for the identical candidates that follow
+            if (!appended) {
+                for (;;) {
+                    const uint32_t jj = j + lane;
+                    bool same = jj < j1;
+                    if (same) {
+                        const uint32_t* c = lv.cand + 9 * uint64_t(vals[jj]);
+                        for (uint32_t k = 0; k < n; k++)
+                            same &= c[k] == q[k];
+                    }
+                    const uint32_t b = __ballot_sync(0xffffffffu, same);
+                    const uint32_t run = b == 0xffffffffu ? 32u : __ffs(~b) - 1;
+                    if (lane < run)
+                        lv.res[vals[jj]] = vbase + result;
+                    foa += run;
+                    j += run;
+                    if (run < 32)
+                        break;
+                }
+            }
             __syncwarp();
         }
-        if (lane == 0) {
-            t.bucket_sizes[gb] = S;
-        }
+        if (lane == 0)
+            __stcg(t.bucket_sizes + gb, S);
     }
     if (lane == 0) {
         atomicAdd(&ctr->foa, foa);
@@ -528,23 +672,30 @@ void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats)
     uint32_t maxn = 1;
     for (uint32_t L = 0; L <= deepest; L++)
         maxn = count[L] > maxn ? count[L] : maxn;
-    uint32_t* head = s.get<uint32_t>("ed_head", g.total_buckets);
-    uint32_t* next_item = s.get<uint32_t>("ed_next", maxn);
-    uint32_t* touched = s.get<uint32_t>("ed_touched", g.total_buckets);
-    if (!c->edit_head_ready || c->edit_head_ptr != head) {
-        fill<uint32_t>(head, kEmpty, g.total_buckets, st);
-        c->edit_head_ready = true;
-        c->edit_head_ptr = head;
-    }
+    uint32_t* keys = s.get<uint32_t>("ed_keys", maxn);
+    uint32_t* vals = s.get<uint32_t>("ed_vals", maxn);
+    uint32_t* flag = s.get<uint32_t>("ed_segflag", maxn);
+    uint32_t* pos = s.get<uint32_t>("ed_segpos", maxn);
+    uint32_t* starts = s.get<uint32_t>("ed_segstart", maxn);
+    uint32_t* d_cnt = s.get<uint32_t>("ed_cnt", 4); // [0] candidates, [1] segments
+    uint32_t key_bits = 1;
+    while ((uint64_t(1) << key_bits) <= g.total_buckets)
+        key_bits++;
     for (int32_t L = int32_t(deepest); L >= 0; L--) {
         const uint32_t n = count[L];
-        HD_CUDA(cudaMemsetAsync(d_n, 0, 4, st));
+        HD_CUDA(cudaMemsetAsync(d_cnt, 0, 8, st));
         const Level child = uint32_t(L) < deepest ? lv[L + 1] : Level{};
-        k_edit_candidates<<<grid_for(n, 128), 128, 0, st>>>(c->t, uint32_t(L), n, lv[L], child, head, next_item,
-                                                            touched, d_n);
+        k_edit_candidates<<<grid_for(n, 128), 128, 0, st>>>(c->t, uint32_t(L), n, lv[L], child, keys, vals, d_cnt);
+        HD_LAUNCH_CHECK();
+        // candidates grouped by bucket, depth-first order kept inside a bucket
+        radix_sort_pairs(s, keys, vals, n, key_bits, st);
+        k_segment_flags<<<grid_for(n, 256), 256, 0, st>>>(keys, n, flag);
+        HD_LAUNCH_CHECK();
+        exclusive_scan<uint32_t, uint32_t>(s, flag, pos, n, d_cnt + 1, st);
+        k_segment_starts<<<grid_for(n, 256), 256, 0, st>>>(flag, pos, n, starts);
         HD_LAUNCH_CHECK();
         k_edit_find_or_add<<<grid_for(uint64_t(n) * 32, 32 * kFoaWarps, 152 * 8), 32 * kFoaWarps, 0, st>>>(
-            c->t, uint32_t(L), lv[L], head, next_item, touched, d_n, ctr);
+            c->t, uint32_t(L), lv[L], keys, vals, starts, d_cnt + 1, d_cnt, ctr);
         HD_LAUNCH_CHECK();
     }
     k_edit_finish<<<1, 1, 0, st>>>(lv[0], c->d_root, c->t.error);
@@ -556,7 +707,8 @@ void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats)
     const uint32_t err = check_error(c);
     if (err)
         throw StatusError{err == kErrCapacity ? HD_ERR_STATE : hd_status(err),
-                          err == kErrCapacity ? "edit would empty the whole scene" : "edit failed on the device"};
+                          err == kErrCapacity ? "edit would empty the whole scene"
+                                              : "edit failed on the device (" + c->err_detail + ")"};
     c->root = read_scalar(c->d_root, st);
     if (stats) {
         stats->num_voxels = h.num_voxels;

@@ -63,10 +63,15 @@ void add_full_nodes(hd_ctx* c, uint32_t first_level, uint32_t last_level)
 
 uint32_t check_error(hd_ctx* c)
 {
-    uint32_t e = read_scalar(c->t.error, c->stream);
-    if (e)
-        HD_CUDA(cudaMemsetAsync(c->t.error, 0, 4, c->stream));
-    return e;
+    uint32_t e[4];
+    HD_CUDA(cudaMemcpyAsync(e, c->t.error, 16, cudaMemcpyDeviceToHost, c->stream));
+    HD_CUDA(cudaStreamSynchronize(c->stream));
+    if (e[0]) {
+        HD_CUDA(cudaMemsetAsync(c->t.error, 0, 16, c->stream));
+        c->err_detail = "level " + std::to_string(int32_t(e[1])) + ", bucket " + std::to_string(e[2]) + ", value " +
+                        std::to_string(e[3]);
+    }
+    return e[0];
 }
 
 void table_reset(hd_ctx* c)
@@ -77,7 +82,7 @@ void table_reset(hd_ctx* c)
     HD_CUDA(cudaMemsetAsync(c->t.bucket_sizes, 0, g.total_buckets * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.full_nodes, 0, HD_MAX_DEPTH * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.level_nodes, 0, HD_MAX_DEPTH * 8, c->stream));
-    HD_CUDA(cudaMemsetAsync(c->t.error, 0, 4, c->stream));
+    HD_CUDA(cudaMemsetAsync(c->t.error, 0, 16, c->stream));
     const uint32_t one = 1;
     HD_CUDA(cudaMemcpyAsync(c->t.pool_top, &one, 4, cudaMemcpyHostToDevice, c->stream));
     HD_CUDA(cudaMemsetAsync(c->d_root, 0, 4, c->stream));

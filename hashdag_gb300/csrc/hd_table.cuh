@@ -37,13 +37,13 @@ HD_D bool map_pages(const Table& t, uint32_t level, uint32_t bucket, uint32_t fr
     const uint32_t v0 = t.g.make_ptr(level, bucket, from) >> kPageShift;
     const uint32_t v1 = t.g.make_ptr(level, bucket, to - 1) >> kPageShift;
     for (uint32_t vp = v0; vp <= v1; vp++) {
-        if (t.page_table[vp] == 0) {
+        if (__ldcg(t.page_table + vp) == 0) {
             const uint32_t p = atomicAdd(t.pool_top, 1u);
             if (p >= t.g.pool_pages) {
-                set_error(t.error, kErrPoolFull);
+                set_error(t.error, kErrPoolFull, level, bucket, p);
                 return false;
             }
-            t.page_table[vp] = p;
+            __stcg(t.page_table + vp, p);
         }
     }
     return true;
@@ -73,7 +73,7 @@ HD_D uint32_t collect_sorted(uint32_t gb, uint32_t* head, const uint32_t* next, 
             it = next[it];
         }
         if (it != kEmpty) {
-            set_error(err, kErrBucketFull);
+            set_error(err, kErrBucketFull, 0xFFFFFFFFu, gb, cnt);
             cnt = 0;
         }
         head[gb] = kEmpty;

@@ -20,8 +20,8 @@ def _fixture(name):
         return json.load(f)
 
 
-def _oracle_of(t, depth):
-    ot = po.Table(po.default_config(depth, pool_pages=int(t["pool"].size // 512) + 64))
+def _oracle_of(t, depth, spare_pages=64):
+    ot = po.Table(po.default_config(depth, pool_pages=int(t["pool"].size // 512) + spare_pages))
     ot.import_(t)
     return ot
 
@@ -120,7 +120,7 @@ def test_edit_depth15_matches_oracle_sample(gpu):
     depth = 15
     d = hd.HashDAG(depth)
     d.generate_scene(1)
-    ot = _oracle_of(d.export_table(), depth)
+    ot = _oracle_of(d.export_table(), depth, spare_pages=1 << 18)
     edits = workloads.mixed_edits(depth, 3, (128.0, 384.0), seed=41)
     for e in edits:
         s = d.edit_threads(hd.editor_from_tuple(e))
