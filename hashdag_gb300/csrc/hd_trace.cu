@@ -12,6 +12,9 @@
 // expression is rounded operation by operation in source order; FMA = 1
 // places explicit fused multiply-adds where the reference's default nvcc
 // build contracts a product into the following add.
+#include <mutex>
+#include <string>
+
 #include "hd_ctx.h"
 
 namespace hd {
@@ -361,3 +364,208 @@ void get_values(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out)
 }
 
 } // namespace hd
+
+// ---------------------------------------------------------------------------
+// Traversal counters without any device allocation.
+//
+// Some callers cannot allocate device memory at the time they trace: a
+// render loop running inside a CUDA stream capture (cudaMalloc is not
+// capturable), or an embedding application that hands the library a fixed
+// memory budget and forbids allocations after start-up.  This variant of
+// hd_trace_counters keeps its scratch (one partial sum per 8x8-pixel block
+// and the six totals) in a file-scope device array instead of the context's
+// scratch buffers.  The array holds kNoAllocMaxBlocks blocks, i.e. images of
+// up to 16,777,216 pixels (4096 x 4096); larger images are rejected.  The
+// array lives on every GPU that loads the library until the process exits.
+// All calls share it: each call writes every slot it later reads, so
+// nothing needs clearing, but calls that overlap on the GPU (other streams,
+// other threads) race on it.
+// ---------------------------------------------------------------------------
+namespace hd {
+
+constexpr uint32_t kNoAllocMaxBlocks = 262144;
+__device__ __align__(256) unsigned long long g_noalloc_scratch[3 * kNoAllocMaxBlocks + 8];
+
+HD_D void block_sum3(uint32_t a, uint32_t b, uint32_t c, unsigned long long* dst)
+{
+    __shared__ unsigned long long part[2][3];
+    unsigned long long v[3] = {a, b, c};
+    for (int k = 0; k < 3; k++)
+        for (int o = 16; o; o >>= 1)
+            v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 3; k++)
+            part[threadIdx.x >> 5][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 3; k++)
+            dst[k] = part[0][k] + part[1][k];
+}
+
+template <int FMA>
+__global__ void __launch_bounds__(64) k_trace_primary_partials(Table t, const uint32_t* __restrict__ d_root,
+                                                               hd_camera cam, uint32_t W, uint32_t H,
+                                                               uint4* __restrict__ out,
+                                                               unsigned long long* __restrict__ partial)
+{
+    const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7);
+    const uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 3);
+    uint32_t rays = 0, descents = 0, leaves = 0;
+    if (x < W && y < H) {
+        double dd[3];
+        camera_dir<FMA>(cam, double(x), double(y), dd);
+        const F3 d = {float(dd[0]), float(dd[1]), float(dd[2])};
+        const F3 o = {float(cam.position[0]), float(cam.position[1]), float(cam.position[2])};
+        const uint32_t order = (d.x < 0.f ? 4u : 0u) + (d.y < 0.f ? 2u : 0u) + (d.z < 0.f ? 1u : 0u);
+        uint32_t hit[3];
+        walk<FMA, false>(t, *d_root, o, d, inverse_dir(d), order, hit, descents, leaves);
+        out[uint64_t(H - 1 - y) * W + x] = make_uint4(hit[0], hit[1], hit[2], 0);
+        rays = 1;
+    }
+    block_sum3(rays, descents, leaves, partial + 3 * (uint64_t(blockIdx.y) * gridDim.x + blockIdx.x));
+}
+
+template <int FMA>
+__global__ void __launch_bounds__(64) k_trace_shadow_partials(Table t, const uint32_t* __restrict__ d_root,
+                                                              hd_camera cam, uint32_t W, uint32_t H,
+                                                              const uint4* __restrict__ paths, F3 light, float bias,
+                                                              uint8_t* __restrict__ mask,
+                                                              unsigned long long* __restrict__ partial)
+{
+    const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7);
+    const uint32_t r = blockIdx.y * 8 + (threadIdx.x >> 3);
+    uint32_t rays = 0, descents = 0, leaves = 0;
+    if (x < W && r < H) {
+        const uint64_t i = uint64_t(r) * W + x;
+        const uint4 p = paths[i];
+        if (p.x == 0 && p.y == 0 && p.z == 0) {
+            mask[i] = 2;
+        } else {
+            const float dot = FMA ? __fmaf_rn(light.z, light.z, __fmaf_rn(light.y, light.y, light.x * light.x))
+                                  : (light.x * light.x + light.y * light.y) + light.z * light.z;
+            const float il = 1.0f / sqrtf(dot);
+            const F3 dir = {il * light.x, il * light.y, il * light.z};
+            double cd[3];
+            camera_dir<FMA>(cam, double(x), double(H - 1 - r), cd);
+            const double bmin[3] = {double(float(p.x)), double(float(p.y)), double(float(p.z))};
+            double real_min[3];
+            for (int a = 0; a < 3; a++) {
+                const double t0 = (bmin[a] - cam.position[a]) / cd[a];
+                const double t1 = ((bmin[a] + 1.0) - cam.position[a]) / cd[a];
+                real_min[a] = t0 < t1 ? t0 : t1;
+            }
+            const double maxmin = fmax(fmax(real_min[0], real_min[1]), real_min[2]);
+            F3 start, o;
+            if (FMA) {
+                start = {float(__fma_rn(cd[0], maxmin, cam.position[0])),
+                         float(__fma_rn(cd[1], maxmin, cam.position[1])),
+                         float(__fma_rn(cd[2], maxmin, cam.position[2]))};
+                o = {__fmaf_rn(bias, dir.x, start.x), __fmaf_rn(bias, dir.y, start.y),
+                     __fmaf_rn(bias, dir.z, start.z)};
+            } else {
+                start = {float(cam.position[0] + cd[0] * maxmin), float(cam.position[1] + cd[1] * maxmin),
+                         float(cam.position[2] + cd[2] * maxmin)};
+                o = {start.x + bias * dir.x, start.y + bias * dir.y, start.z + bias * dir.z};
+            }
+            uint32_t hit[3];
+            mask[i] = walk<FMA, true>(t, *d_root, o, dir, inverse_dir(dir), 0, hit, descents, leaves) ? 1 : 0;
+            rays = 1;
+        }
+    }
+    block_sum3(rays, descents, leaves, partial + 3 * (uint64_t(blockIdx.y) * gridDim.x + blockIdx.x));
+}
+
+// One block: column sums of the partials into totals[0..2].
+__global__ void k_sum_partials(const unsigned long long* __restrict__ partial, uint32_t nblocks,
+                               unsigned long long* __restrict__ totals)
+{
+    __shared__ unsigned long long acc[3][256];
+    for (int k = 0; k < 3; k++) {
+        unsigned long long s = 0;
+        for (uint32_t b = threadIdx.x; b < nblocks; b += blockDim.x)
+            s += partial[3 * uint64_t(b) + k];
+        acc[k][threadIdx.x] = s;
+    }
+    __syncthreads();
+    for (uint32_t w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int k = 0; k < 3; k++)
+                acc[k][threadIdx.x] += acc[k][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x < 3)
+        totals[threadIdx.x] = acc[threadIdx.x][0];
+}
+
+} // namespace hd
+
+namespace {
+// Device address of g_noalloc_scratch per device, resolved on the first
+// call made with that device current.
+std::mutex g_noalloc_mutex;
+unsigned long long* g_noalloc_ptr[256] = {};
+
+unsigned long long* noalloc_scratch()
+{
+    int dev = 0;
+    HD_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256)
+        throw hd::StatusError{HD_ERR_INVALID, "device ordinal out of range"};
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        HD_CUDA(cudaGetSymbolAddress(&p, hd::g_noalloc_scratch));
+        g_noalloc_ptr[dev] = static_cast<unsigned long long*>(p);
+    }
+    return g_noalloc_ptr[dev];
+}
+} // namespace
+
+extern "C" hd_status hd_trace_counters_noalloc(hd_ctx* c, const hd_camera* cam, uint32_t w, uint32_t h,
+                                               const float light[3], float bias, uint32_t* d_paths, uint8_t* d_mask,
+                                               uint64_t out[6])
+{
+    using namespace hd;
+    if (!c || !cam || !d_paths || !d_mask || !light || !out || !w || !h)
+        return HD_ERR_INVALID;
+    const uint64_t bx = (w + 7) / 8, by = (h + 7) / 8;
+    if (bx * by > kNoAllocMaxBlocks) {
+        c->err = "hd_trace_counters_noalloc: image of " + std::to_string(uint64_t(w) * h) +
+                 " pixels exceeds the fixed scratch (at most 262144 blocks of 8x8 pixels, 16777216 pixels)";
+        return HD_ERR_INVALID;
+    }
+    try {
+        unsigned long long* scratch = noalloc_scratch();
+        unsigned long long* partial = scratch;
+        unsigned long long* totals = scratch + 3 * uint64_t(kNoAllocMaxBlocks);
+        const dim3 grid{uint32_t(bx), uint32_t(by), 1u};
+        const uint32_t nb = uint32_t(bx * by);
+        const F3 l = {light[0], light[1], light[2]};
+        uint4* paths = reinterpret_cast<uint4*>(d_paths);
+        if (c->fp_mode)
+            k_trace_primary_partials<1><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, *cam, w, h, paths, partial);
+        else
+            k_trace_primary_partials<0><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, *cam, w, h, paths, partial);
+        HD_LAUNCH_CHECK();
+        k_sum_partials<<<1, 256, 0, c->stream>>>(partial, nb, totals);
+        HD_LAUNCH_CHECK();
+        if (c->fp_mode)
+            k_trace_shadow_partials<1><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, *cam, w, h, paths, l, bias,
+                                                                   d_mask, partial);
+        else
+            k_trace_shadow_partials<0><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, *cam, w, h, paths, l, bias,
+                                                                   d_mask, partial);
+        HD_LAUNCH_CHECK();
+        k_sum_partials<<<1, 256, 0, c->stream>>>(partial, nb, totals + 3);
+        HD_LAUNCH_CHECK();
+        HD_CUDA(cudaMemcpyAsync(out, totals, 6 * sizeof(uint64_t), cudaMemcpyDeviceToHost, c->stream));
+        HD_CUDA(cudaStreamSynchronize(c->stream));
+        return HD_OK;
+    } catch (const StatusError& e) {
+        c->err = e.msg;
+        return e.status;
+    } catch (const CudaError& e) {
+        c->err = std::string("CUDA error ") + cudaGetErrorString(e.code) + " in " + e.where;
+        return HD_ERR_CUDA;
+    }
+}
