@@ -50,6 +50,7 @@ def parse():
     p.add_argument("--ref-rows", type=int, default=192, help="rows per step of the CPU reference arm")
     p.add_argument("--cpu-sample-rows", type=int, default=256, help="rows of the cpu_baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--pool-pages", type=int, default=0, help="physical pool pages (0 = library default)")
     return p.parse_args()
 
 
@@ -167,9 +168,12 @@ def algorithmic_bytes(counts):
     return prim, shad
 
 
-def load_scene(depth):
+def load_scene(depth, pool_pages=0):
     import hashdag_gb300 as hd
-    dag = hd.HashDAG(depth)
+    cfg = hd.default_config(depth)
+    if pool_pages:
+        cfg.pool_pages = pool_pages
+    dag = hd.HashDAG(config=cfg)
     t0 = time.perf_counter()
     dag.generate_scene(1)
     return dag, time.perf_counter() - t0
@@ -205,7 +209,7 @@ def run_reference(args, dist):
     torch.cuda.set_device(dist.local)
     from hashdag_gb300 import workloads
     W, H, depth = args.width, args.height, args.depth
-    dag, _ = load_scene(depth)
+    dag, _ = load_scene(depth, args.pool_pages)
     ot = oracle_from(dag, depth)
     dag.free()
     poses = workloads.catmull_rom_path(depth, args.poses, W, H)
@@ -248,7 +252,8 @@ def run_gpu(args, dist):
     build.build()
     L = _capi.lib()
     W, H, depth, K = args.width, args.height, args.depth, args.steps
-    dag, gen_s = load_scene(depth)
+    dag, gen_s = load_scene(depth, args.pool_pages)
+    lstats = dag.level_stats()
     poses = workloads.catmull_rom_path(depth, args.poses, W, H)
     cams = [_capi.Camera.from_params(p) for p in poses]
     paths = torch.zeros(W * H * 4, dtype=torch.int32, device="cuda")
@@ -360,6 +365,8 @@ def run_gpu(args, dist):
             "config": {"workload": workload, "depth": depth, "width": W, "height": H, "poses": args.poses,
                        "light": list(LIGHT), "shadow_bias": BIAS, "l2": "flushed (512 MB write) before every step",
                        "scene_gen_s": round(gen_s, 2), "rays_per_step": rays_total / K,
+                       "scene_pages_used": int(lstats.pages_used),
+                       "scene_nodes": int(sum(lstats.nodes[:depth - 1])),
                        "parallelism": f"replicas x{dist.world}"},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(_capi.Camera),
                     "d2h_bytes_per_step": W * H * 16 + W * H},

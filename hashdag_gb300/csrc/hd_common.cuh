@@ -110,9 +110,12 @@ struct Table {
     {
         return pool + (uint64_t(__ldcg(page_table + (v >> kPageShift))) << kPageShift) + (v & (kPage - 1));
     }
+    // Translation for writers: the page-table entry is read from L2, never
+    // from a possibly stale L1 line (pages are mapped inside the same
+    // kernels that write through this translation).
     HD_D uint32_t* sys_rw(uint32_t v) const
     {
-        return pool + (uint64_t(page_table[v >> kPageShift]) << kPageShift) + (v & (kPage - 1));
+        return pool + (uint64_t(__ldcg(page_table + (v >> kPageShift))) << kPageShift) + (v & (kPage - 1));
     }
 };
 

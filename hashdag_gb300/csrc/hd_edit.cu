@@ -427,11 +427,12 @@ HD_D uint32_t scan_bucket(const Table& t, uint32_t vbase, uint32_t S, const uint
         scanned += found == kNotFound ? used : (found - pindex + n);
         __syncwarp();
     }
-    if (!leaf && found == kNotFound && S >= n) {
+    if (!leaf && found == kNotFound && S >= n && ((S - n) & ~(kPage - 1)) == ((S - 1) & ~(kPage - 1))) {
         // the bucket's last node ends at S; it holds q iff it starts at S - n
+        // (nodes never straddle a page, so S - n lies in the tail's page)
         const uint32_t p = S - n;
         const uint32_t pindex = p & ~(kPage - 1);
-        const uint32_t used = S - pindex;
+        const uint32_t used = S - pindex; // <= kPage
         const uint32_t* src = t.sys_cg(vbase + pindex);
         for (uint32_t w = lane * 4; w < used; w += 128) {
             const uint4 v = __ldcg(reinterpret_cast<const uint4*>(src + w));

@@ -7,6 +7,7 @@
 #include "hd_oracle.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -301,6 +302,26 @@ static uint32_t add_interior(or_table* t, uint32_t level, uint32_t n, const uint
     return ptr;
 }
 
+/* Optional call log of find_or_add (level, 9 content words, result), for
+ * debugging comparisons. */
+static FILE* g_foa_log = NULL;
+void or_set_foa_log(const char* path)
+{
+    if (g_foa_log)
+        fclose(g_foa_log);
+    g_foa_log = path ? fopen(path, "wb") : NULL;
+}
+static void log_foa(uint32_t level, uint32_t n, const uint32_t* node, uint32_t result)
+{
+    if (!g_foa_log)
+        return;
+    uint32_t rec[11] = {level};
+    for (uint32_t i = 0; i < n && i < 9; i++)
+        rec[1 + i] = node[i];
+    rec[10] = result;
+    fwrite(rec, 4, 11, g_foa_log);
+}
+
 /* find_or_add_leaf_node (hash_table.h:470-514), single writer */
 uint32_t or_find_or_add_leaf(or_table* t, uint64_t leaf)
 {
@@ -312,6 +333,8 @@ uint32_t or_find_or_add_leaf(or_table* t, uint64_t leaf)
     uint32_t r = find_leaf(t, size, bucket, leaf);
     if (r == NOT_FOUND)
         r = add_leaf(t, leaf, hash);
+    const uint32_t words[2] = {(uint32_t)leaf, (uint32_t)(leaf >> 32)};
+    log_foa(level, 2, words, r);
     return r;
 }
 /* find_or_add_interior_node (hash_table.h:515-560), single writer */
@@ -324,6 +347,7 @@ uint32_t or_find_or_add_interior(or_table* t, uint32_t level, uint32_t n, const 
     uint32_t r = find_interior(t, size, level, bucket, n, node);
     if (r == NOT_FOUND)
         r = add_interior(t, level, n, node, hash);
+    log_foa(level, n, node, r);
     return r;
 }
 

@@ -86,6 +86,8 @@ void or_trace_frame_mt(const or_table* t, const hd_camera* cam, uint32_t width, 
 /* ---- edits (hash_dag_edits.h) and GC (hash_dag.h:407-547) ------------- */
 int or_edit(or_table* t, const hd_edit* edit, hd_edit_stats* stats);
 int or_gc(or_table* t, uint32_t* extra_roots, uint32_t n_extra);
+/* Debugging aid: log every find_or_add call (level, content, result). */
+void or_set_foa_log(const char* path);
 
 #ifdef __cplusplus
 }

@@ -108,6 +108,7 @@ def lib():
         L.or_reachable_counts.argtypes = [P, u32, np.ctypeslib.ndpointer(np.uint64, flags="C")]
         L.or_edit.argtypes = [P, C.POINTER(HdEdit), C.POINTER(HdEditStats)]
         L.or_gc.argtypes = [P, P, u32]
+        L.or_set_foa_log.argtypes = [C.c_char_p]
         _lib = L
     return _lib
 
