@@ -152,8 +152,8 @@ def traffic_from_profiles(workload):
     try:
         with open(path) as f:
             d = json.load(f)
-        return d.get(workload)
-    except (OSError, ValueError):
+        return d.get(workload, {}).get("bytes_per_launch")
+    except (OSError, ValueError, AttributeError):
         return None
 
 
