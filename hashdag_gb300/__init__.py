@@ -19,9 +19,9 @@ import ctypes as C
 import numpy as np
 
 from . import _capi
-from ._capi import Camera, Config, Edit, EditStats, HashDagError, LevelStats, lib
+from ._capi import BatchTuning, Camera, Config, Edit, EditStats, HashDagError, LevelStats, lib
 
-__all__ = ["HashDAG", "DAGTracer", "SphereEditor", "BoxEditor", "Camera", "Config", "EditStats", "LevelStats",
+__all__ = ["HashDAG", "DAGTracer", "SphereEditor", "BoxEditor", "BatchTuning", "Camera", "Config", "EditStats", "LevelStats",
            "HashDagError", "default_config"]
 
 TOOL_SPHERE_REMOVE, TOOL_SPHERE_ADD, TOOL_BOX_REMOVE, TOOL_BOX_ADD = 0, 1, 2, 3
@@ -190,11 +190,43 @@ class HashDAG:
         self._check(lib().hd_edit_apply(self._h, C.byref(e), C.byref(s)))
         return s
 
-    def edit_batch(self, editors):
+    def edit_batch(self, editors, per_edit=False):
+        """The batched form: the edits in order, one captured CUDA graph per
+        edit launched back to back.  Returns the total EditStats, and with
+        per_edit=True also the list of per-edit EditStats (device_ms = the
+        edit's device time, host_ms = its completion time since the batch
+        started)."""
         arr = (Edit * len(editors))(*[e.to_edit() for e in editors])
         s = EditStats()
-        self._check(lib().hd_edit_batch(self._h, arr, len(editors), C.byref(s)))
-        return s
+        per = (EditStats * max(1, len(editors)))()
+        self._check(lib().hd_edit_batch_ex(self._h, arr, len(editors), per if per_edit else None, C.byref(s)))
+        return (s, list(per)[:len(editors)]) if per_edit else s
+
+    @property
+    def batch_tuning(self):
+        t = BatchTuning()
+        self._check(lib().hd_get_batch_tuning(self._h, C.byref(t)))
+        return t
+
+    @batch_tuning.setter
+    def batch_tuning(self, t):
+        if not isinstance(t, BatchTuning):
+            t = BatchTuning(*t)
+        self._check(lib().hd_set_batch_tuning(self._h, C.byref(t)))
+
+    def autotune_batch(self, editors):
+        """Times every launch shape of the batched path on a device copy of
+        the table with these sample edits; keeps and returns the fastest
+        (BatchTuning, device ms of the sample)."""
+        arr = (Edit * len(editors))(*[e.to_edit() for e in editors])
+        t, ms = BatchTuning(), C.c_float()
+        self._check(lib().hd_autotune_batch(self._h, arr, len(editors), C.byref(t), C.byref(ms)))
+        return t, ms.value
+
+    def batch_fallbacks(self):
+        v = C.c_uint64()
+        self._check(lib().hd_batch_fallbacks(self._h, C.byref(v)))
+        return v.value
 
     def remove_stale_nodes(self, extra_roots=()):
         """HashDAG::remove_stale_nodes(levels - 2), marking from the root and

@@ -44,6 +44,13 @@ class EditStats(C.Structure):
                 ("host_ms", C.c_float)]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [("foa_warps", C.c_uint32), ("probe_words", C.c_uint32), ("grid_blocks", C.c_uint32)]
+
+    def __repr__(self):
+        return f"BatchTuning(foa_warps={self.foa_warps}, probe_words={self.probe_words}, grid_blocks={self.grid_blocks})"
+
+
 class LevelStats(C.Structure):
     _fields_ = [("words", C.c_uint64 * MAX_DEPTH), ("nodes", C.c_uint64 * MAX_DEPTH), ("pages_used", C.c_uint64),
                 ("root", C.c_uint32), ("levels", C.c_uint32)]
@@ -82,6 +89,11 @@ SIGNATURES = [
     ("hd_get_values", C.c_int, [_P, _P, _u64, _P]),
     ("hd_edit_apply", C.c_int, [_P, C.POINTER(Edit), C.POINTER(EditStats)]),
     ("hd_edit_batch", C.c_int, [_P, C.POINTER(Edit), _u32, C.POINTER(EditStats)]),
+    ("hd_edit_batch_ex", C.c_int, [_P, C.POINTER(Edit), _u32, C.POINTER(EditStats), C.POINTER(EditStats)]),
+    ("hd_set_batch_tuning", C.c_int, [_P, C.POINTER(BatchTuning)]),
+    ("hd_get_batch_tuning", C.c_int, [_P, C.POINTER(BatchTuning)]),
+    ("hd_autotune_batch", C.c_int, [_P, C.POINTER(Edit), _u32, C.POINTER(BatchTuning), C.POINTER(_f32)]),
+    ("hd_batch_fallbacks", C.c_int, [_P, C.POINTER(_u64)]),
     ("hd_gc", C.c_int, [_P, _P, _u32]),
     ("hd_get_root", C.c_int, [_P, C.POINTER(_u32)]),
     ("hd_set_root", C.c_int, [_P, _u32]),

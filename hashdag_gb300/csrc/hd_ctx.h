@@ -6,6 +6,10 @@
 #include "hd_common.cuh"
 #include "hd_util.cuh"
 
+namespace hd {
+struct BatchGraph; // hd_edit_batch.cu
+}
+
 struct hd_ctx {
     hd_config cfg{};
     hd::Geom g{};
@@ -24,6 +28,11 @@ struct hd_ctx {
     // bucket list heads of the edit path stay all-empty between calls
     bool edit_head_ready = false;
     uint32_t* edit_head_ptr = nullptr;
+    // batched edits: tuning, the captured graph, edits that took the
+    // one-edit path because a level outgrew its bound
+    hd_batch_tuning tuning{4, 4, 304};
+    hd::BatchGraph* batch = nullptr;
+    uint64_t batch_fallbacks = 0;
 };
 
 namespace hd {
@@ -40,6 +49,11 @@ void append_items(hd_ctx* c, uint32_t level, const uint32_t* content, uint64_t n
 
 // hd_scene.cu
 void generate_scene(hd_ctx* c, uint64_t seed, uint32_t** d_words, uint64_t* n_words);
+
+// hd_edit.cu / hd_edit_batch.cu
+void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats);
+void edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* per_edit, hd_edit_stats* total);
+void batch_release(hd_ctx* c);
 
 // hd_trace.cu
 void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint32_t* d_paths,

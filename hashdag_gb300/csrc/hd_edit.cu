@@ -1,323 +1,48 @@
-// Edit pipeline: sphere / box carve and fill, per-level hashing and bucket
-// find-or-add, on the device.
-//
-// Reference: HashDAG::edit_threads (hash_dag.h:255-405), which runs
-// HashDagEdits::edit_threaded over the levels above C_colorTreeLevels
-// (hash_dag_edits.h:106-333) and edit_leaf below (:335-643); editors
-// (hash_dag_editors.h:57-127, :223-313); find_or_add_leaf_node /
-// find_or_add_interior_node with their bucket scans (hash_table.h:196-357,
-// :470-560).
-//
-// The recursion becomes two level-synchronous sweeps:
-//  * top-down, every level's edit entries (a node path and its old index) are
-//    classified as in the reference (untouched, carved away, filled, a leaf
-//    to rebuild, or an interior node to descend into); descended entries
-//    spawn their 8 children, in child order, so each level's entries stay in
-//    depth-first (Morton) order;
-//  * bottom-up, every rebuilt node is compared with its old self and, when
-//    changed, hashed and resolved by find-or-add.  Candidates of a level are
-//    grouped by bucket and each bucket is resolved by one warp, candidates in
-//    depth-first order one after the other: the same sequence of bucket scans
-//    and appends as the reference's single-threaded depth-first recursion,
-//    including its scan rules (a node flush with the bucket tail or the page
-//    end is invisible to an equal-size query).
+// Edit pipeline, one edit per call: the host sizes every level from the
+// previous one and launches the level kernels (see hd_edit.cuh for the
+// design and the reference lines).  The batched, graph-captured form is in
+// hd_edit_batch.cu.
 #include <chrono>
 #include <vector>
 
-#include "hd_ctx.h"
+#include "hd_edit.cuh"
 #include "hd_sort.cuh"
-#include "hd_table.cuh"
 
 namespace hd {
 
-// ---- editors ----------------------------------------------------------------
-struct Editor {
-    uint32_t tool;
-    float cx, cy, cz, r, r2;
-    float bminx, bminy, bminz, bmaxx, bmaxy, bmaxz;
-    HD_HD bool sphere() const { return tool == HD_TOOL_SPHERE_ADD || tool == HD_TOOL_SPHERE_REMOVE; }
-    HD_HD bool adding() const { return tool == HD_TOOL_SPHERE_ADD || tool == HD_TOOL_BOX_ADD; }
-};
+constexpr uint32_t kFoaWarps = 4;
+constexpr int kFoaProbe = 4;
 
-inline Editor make_editor(const hd_edit& e)
-{
-    Editor ed{};
-    ed.tool = e.tool;
-    ed.cx = e.center[0];
-    ed.cy = e.center[1];
-    ed.cz = e.center[2];
-    ed.r = e.radius;
-    ed.r2 = e.radius * e.radius;
-    ed.bminx = e.center[0] - e.radius;
-    ed.bminy = e.center[1] - e.radius;
-    ed.bminz = e.center[2] - e.radius;
-    ed.bmaxx = e.center[0] + e.radius;
-    ed.bmaxy = e.center[1] + e.radius;
-    ed.bmaxz = e.center[2] + e.radius;
-    return ed;
-}
-
-HD_D float sqr(float f) { return f * f; }
-HD_D float fmax_r(float a, float b) { return a > b ? a : b; }
-
-// SphereEditorBase::should_edit_impl (:112-126) / BoxEditorBase (:76-91)
-HD_D bool should_edit_impl(const Editor& e, float mnx, float mny, float mnz, float mxx, float mxy, float mxz)
-{
-    if (e.sphere()) {
-        float dist = e.r2;
-        if (e.cx < mnx)
-            dist -= sqr(e.cx - mnx);
-        else if (e.cx > mxx)
-            dist -= sqr(e.cx - mxx);
-        if (e.cy < mny)
-            dist -= sqr(e.cy - mny);
-        else if (e.cy > mxy)
-            dist -= sqr(e.cy - mxy);
-        if (e.cz < mnz)
-            dist -= sqr(e.cz - mnz);
-        else if (e.cz > mxz)
-            dist -= sqr(e.cz - mxz);
-        return dist > 0;
-    }
-    return !(e.bminx >= mxx || e.bminy >= mxy || e.bminz >= mxz || e.bmaxx <= mnx || e.bmaxy <= mny ||
-             e.bmaxz <= mnz || mnx >= e.bmaxx || mny >= e.bmaxy || mnz >= e.bmaxz || mxx <= e.bminx ||
-             mxy <= e.bminy || mxz <= e.bminz);
-}
-
-// is_full_impl / is_empty_impl (:280-295, :233-252): the region lies inside
-// the tool.
-HD_D bool inside_tool(const Editor& e, float mnx, float mny, float mnz, float mxx, float mxy, float mxz)
-{
-    if (e.sphere()) {
-        const float a = fmax_r(sqr(mnx - e.cx), sqr(mxx - e.cx));
-        const float b = fmax_r(sqr(mny - e.cy), sqr(mxy - e.cy));
-        const float c = fmax_r(sqr(mnz - e.cz), sqr(mxz - e.cz));
-        return (a + b) + c < e.r2;
-    }
-    return e.bminx <= mnx && e.bminy <= mny && e.bminz <= mnz && e.bmaxx >= mxx && e.bmaxy >= mxy && e.bmaxz >= mxz;
-}
-
-// ---- per-level entry state ---------------------------------------------------
-enum : uint8_t {
-    kSkip = 0,      // level-C_colorTreeLevels child the parent never hands to edit_leaf
-    kKeep = 1,      // untouched: result = old
-    kEmptied = 2,   // carved away (is_empty)
-    kFilled = 3,    // filled (is_full): the level's full node
-    kLeafEval = 4,  // leaf rebuilt voxel by voxel
-    kDescend = 5,   // interior node rebuilt from its children
-};
-
-struct Level {
-    uint32_t* x;
-    uint32_t* y;
-    uint32_t* z;
-    uint32_t* old;
-    uint8_t* state;
-    uint32_t* res;   // new index (kInvalid = empty)
-    uint32_t* cnt;   // voxel count of the new node (levels >= T)
-    uint32_t* flag;  // 1 = descends
-    uint32_t* exp;   // exclusive scan of flag
-    uint64_t* leaf;  // new leaf masks (leaf level only)
-    uint32_t* cand;  // candidate content, 9 words per entry
-};
-
-struct EditCounters {
-    unsigned long long num_voxels, num_nodes, foa, added, scanned;
-};
-
-HD_D void warp_add(unsigned long long* p, unsigned long long v)
-{
-    // warp-aggregated atomic
-    const uint32_t mask = __activemask();
-    for (int o = 16; o; o >>= 1)
-        v += __shfl_down_sync(mask, v, o);
-    if ((threadIdx.x & 31) == __ffs(mask) - 1)
-        atomicAdd(p, v);
-}
-
-// Top-down classification of level L's entries.
 __global__ void k_edit_classify(Table t, Editor ed, uint32_t level, uint32_t n, Level lv, EditCounters* ctr)
 {
-    const uint32_t D = t.g.depth, T = t.g.T, leafl = t.g.leaf_level;
     HD_GRID_STRIDE(i, n)
     {
-        const uint32_t depth = D - level;
-        const float s = float(1u << depth);
-        const float mnx = float(lv.x[i] << depth), mny = float(lv.y[i] << depth), mnz = float(lv.z[i] << depth);
-        const float mxx = mnx + s, mxy = mny + s, mxz = mnz + s;
-        const uint32_t old = lv.old[i];
-        const bool se = should_edit_impl(ed, mnx, mny, mnz, mxx, mxy, mxz);
-        uint8_t state;
-        uint32_t res = old, cnt = 0;
-        unsigned long long nodes = 0, voxels = 0;
-        if (level < T) {
-            // edit_threaded: visited in both passes; no early full/empty exits
-            nodes = 2;
-            state = se ? kDescend : kKeep;
-        } else {
-            if (level == T && !se) {
-                state = kSkip; // the parent keeps the old child without a visit
-            } else {
-                nodes = 1;
-                if (!se) {
-                    state = kKeep;
-                    if (old != kInvalid) {
-                        const uint32_t* p = t.sys(old);
-                        cnt = level < leafl ? (p[0] >> 8) : popc32(p[0]) + popc32(p[1]);
-                    }
-                } else if (inside_tool(ed, mnx, mny, mnz, mxx, mxy, mxz)) {
-                    const uint32_t full_count = 1u << (3 * depth);
-                    voxels = full_count;
-                    if (ed.adding()) {
-                        state = kFilled;
-                        res = t.full_nodes[level];
-                        cnt = full_count;
-                    } else {
-                        state = kEmptied;
-                        res = kInvalid;
-                    }
-                } else if (level == leafl) {
-                    state = kLeafEval;
-                    uint64_t leaf = 0;
-                    if (old != kInvalid) {
-                        const uint32_t* p = t.sys(old);
-                        leaf = uint64_t(p[0]) | (uint64_t(p[1]) << 32);
-                    }
-                    const uint32_t x0 = lv.x[i] << 2, y0 = lv.y[i] << 2, z0 = lv.z[i] << 2;
-                    uint32_t edited = 0;
-                    for (uint32_t c1 = 0; c1 < 8; c1++)
-                        for (uint32_t c2 = 0; c2 < 8; c2++) {
-                            const float px = float(x0 + ((c1 >> 2) & 1) * 2 + ((c2 >> 2) & 1));
-                            const float py = float(y0 + ((c1 >> 1) & 1) * 2 + ((c2 >> 1) & 1));
-                            const float pz = float(z0 + (c1 & 1) * 2 + (c2 & 1));
-                            if (should_edit_impl(ed, px, py, pz, px + 1.0f, py + 1.0f, pz + 1.0f)) {
-                                edited++;
-                                const uint64_t bit = 1ull << (c1 * 8 + c2);
-                                leaf = ed.adding() ? (leaf | bit) : (leaf & ~bit);
-                            }
-                        }
-                    voxels = edited;
-                    lv.leaf[i] = leaf;
-                } else {
-                    state = kDescend;
-                }
-            }
-        }
-        lv.state[i] = state;
-        lv.res[i] = res;
-        lv.cnt[i] = cnt;
-        lv.flag[i] = state == kDescend;
+        unsigned long long nodes, voxels;
+        classify_entry(t, ed, level, lv, uint32_t(i), nodes, voxels);
         warp_add(&ctr->num_nodes, nodes);
         warp_add(&ctr->num_voxels, voxels);
     }
 }
 
-// Descended entries spawn their 8 children (child order) on the next level.
 __global__ void k_edit_spawn(Table t, uint32_t n, Level lv, Level next)
 {
-    HD_GRID_STRIDE(i, n)
-    {
-        if (!lv.flag[i])
-            continue;
-        const uint32_t base = 8 * lv.exp[i];
-        const uint32_t old = lv.old[i];
-        uint32_t mask = 0;
-        const uint32_t* p = nullptr;
-        if (old != kInvalid) {
-            p = t.sys(old);
-            mask = p[0] & 0xffu;
-        }
-        uint32_t k = 1;
-        for (uint32_t c = 0; c < 8; c++) {
-            next.x[base + c] = (lv.x[i] << 1) | ((c >> 2) & 1);
-            next.y[base + c] = (lv.y[i] << 1) | ((c >> 1) & 1);
-            next.z[base + c] = (lv.z[i] << 1) | (c & 1);
-            next.old[base + c] = (mask & (1u << c)) ? p[k++] : kInvalid;
-        }
-    }
+    HD_GRID_STRIDE(i, n) spawn_entry(t, lv, next, uint32_t(i));
 }
 
-// Bottom-up: rebuilt content of every kLeafEval / kDescend entry; unchanged
-// and emptied nodes resolve at once, the rest become find-or-add candidates.
+// Candidates keyed by global bucket index; kEmpty for resolved entries.
 __global__ void k_edit_candidates(Table t, uint32_t level, uint32_t n, Level lv, Level child, uint32_t* keys,
                                   uint32_t* vals, uint32_t* n_cand)
 {
-    const uint32_t T = t.g.T, leafl = t.g.leaf_level;
     HD_GRID_STRIDE(i, n)
     {
-        const uint8_t state = lv.state[i];
-        uint32_t* c = lv.cand + 9 * i;
-        keys[i] = kEmpty;
+        const uint32_t b = candidate_entry(t, level, lv, child, uint32_t(i));
         vals[i] = uint32_t(i);
-        uint32_t hash, nw;
-        if (state == kLeafEval) {
-            const uint64_t leaf = lv.leaf[i];
-            const uint32_t old = lv.old[i];
-            uint64_t initial = 0;
-            if (old != kInvalid) {
-                const uint32_t* p = t.sys(old);
-                initial = uint64_t(p[0]) | (uint64_t(p[1]) << 32);
-            }
-            lv.cnt[i] = popc64(leaf);
-            if (leaf == initial) {
-                lv.res[i] = old;
-                continue;
-            }
-            if (!leaf) {
-                lv.res[i] = kInvalid;
-                lv.cnt[i] = 0;
-                continue;
-            }
-            c[0] = uint32_t(leaf);
-            c[1] = uint32_t(leaf >> 32);
-            hash = hash_leaf(leaf);
-            nw = 2;
-        } else if (state == kDescend) {
-            const uint32_t base = 8 * lv.exp[i];
-            const uint32_t old = lv.old[i];
-            uint32_t mask = 0, k = 1, total = 0;
-            bool changed = false;
-            uint32_t omask = 0;
-            const uint32_t* p = nullptr;
-            if (old != kInvalid) {
-                p = t.sys(old);
-                omask = p[0] & 0xffu;
-            }
-            uint32_t ok = 1;
-            for (uint32_t s = 0; s < 8; s++) {
-                const uint32_t oc = (omask & (1u << s)) ? p[ok++] : kInvalid;
-                const uint8_t cs = child.state[base + s];
-                const uint32_t nc = cs == kSkip ? oc : child.res[base + s];
-                changed |= nc != oc;
-                if (nc != kInvalid) {
-                    mask |= 1u << s;
-                    c[k++] = nc;
-                    if (level >= T)
-                        total += child.cnt[base + s];
-                }
-            }
-            lv.cnt[i] = total;
-            if (!changed) {
-                lv.res[i] = old;
-                continue;
-            }
-            if (!mask) {
-                lv.res[i] = kInvalid;
-                lv.cnt[i] = 0;
-                continue;
-            }
-            c[0] = (level >= T ? (total << 8) : 0u) | mask;
-            nw = k;
-            hash = hash_interior(nw, c);
+        if (b == kNoBucket) {
+            keys[i] = kEmpty;
         } else {
-            continue;
+            keys[i] = t.g.bucket_global(level, b);
+            atomicAdd(n_cand, 1u);
         }
-        (void)leafl;
-        (void)nw;
-        const uint32_t bucket = hash & (t.g.buckets(level) - 1);
-        lv.res[i] = kNotFound; // resolved by find-or-add
-        keys[i] = t.g.bucket_global(level, bucket);
-        atomicAdd(n_cand, 1u);
     }
 }
 
@@ -337,131 +62,6 @@ __global__ void k_segment_starts(const uint32_t* __restrict__ flag, const uint32
     }
 }
 
-// One warp per bucket: the bucket's candidates, in depth-first order, each
-// resolved against the bucket as it stands (earlier candidates' appends
-// included) and appended when not found.  A per-warp cache remembers, for
-// every content already resolved in this bucket, the positions where a copy
-// lies (the first match a scan sees, the bucket's last node when it holds
-// the content, and the copies appended since): a repeated content then needs
-// no new scan, only the visibility rule on those positions.  Runs of
-// identical candidates after a found result take that result at once.
-constexpr uint32_t kFoaWarps = 4;
-constexpr uint32_t kCache = 32;
-constexpr uint32_t kCachePos = 3;
-
-struct FoaCache {
-    uint32_t words[kCache][9];
-    uint32_t n[kCache];
-    uint32_t npos[kCache];
-    uint32_t pos[kCache][kCachePos];
-};
-
-// A node at bucket position p (a walk position) of size n is compared by the
-// reference's interior scan iff p + n < min(S, page end) (leaves: always).
-HD_D bool visible(uint32_t p, uint32_t n, uint32_t S, bool leaf)
-{
-    if (leaf)
-        return p + 2 <= S;
-    const uint32_t pe = (p & ~(kPage - 1)) + kPage;
-    return p + n < (S < pe ? S : pe);
-}
-
-// Warp-wide scan of the bucket for the first compared position holding q
-// (find_leaf_node_in_bucket / find_interior_node_in_bucket); returns the
-// bucket position or kNotFound.  *last_match: for interiors, the bucket's
-// last node when it holds q (compared by no scan until something follows).
-HD_D uint32_t scan_bucket(const Table& t, uint32_t vbase, uint32_t S, const uint32_t* q, uint32_t n, bool leaf,
-                          uint32_t* page, uint32_t* last_match, unsigned long long& scanned)
-{
-    const uint32_t lane = threadIdx.x & 31;
-    uint32_t found = kNotFound;
-    *last_match = kNotFound;
-    for (uint32_t pindex = 0; pindex < S && found == kNotFound; pindex += kPage) {
-        const uint32_t page_end = S < pindex + kPage ? S : pindex + kPage;
-        if (!leaf && pindex + n >= page_end)
-            break; // "return 0xFFFFFFFF" of the reference scan
-        const uint32_t used = page_end - pindex;
-        // L2-coherent loads: this kernel appends nodes and maps pages
-        const uint32_t* src = t.sys_cg(vbase + pindex);
-        for (uint32_t w = lane * 4; w < used; w += 128) {
-            const uint4 v = __ldcg(reinterpret_cast<const uint4*>(src + w));
-            page[w] = v.x;
-            page[w + 1] = v.y;
-            page[w + 2] = v.z;
-            page[w + 3] = v.w;
-        }
-        __syncwarp();
-        if (leaf) {
-            for (uint32_t w0 = 0; w0 < used && found == kNotFound; w0 += 64) {
-                const uint32_t w = w0 + 2 * lane;
-                const bool m = w < used && page[w] == q[0] && page[w + 1] == q[1];
-                const uint32_t b = __ballot_sync(0xffffffffu, m);
-                if (b)
-                    found = pindex + w0 + 2 * (__ffs(b) - 1);
-            }
-        } else {
-            const uint32_t lim = used - n;
-            for (uint32_t w0 = 0; w0 < lim && found == kNotFound; w0 += 32) {
-                const uint32_t w = w0 + lane;
-                bool m = w < lim && page[w] == q[0];
-                if (m)
-                    for (uint32_t k = 1; k < n; k++)
-                        m &= page[w + k] == q[k];
-                uint32_t b = __ballot_sync(0xffffffffu, m);
-                while (b && found == kNotFound) {
-                    const uint32_t cand = w0 + __ffs(b) - 1;
-                    b &= b - 1;
-                    uint32_t on_walk = 0;
-                    if (lane == 0) {
-                        uint32_t p = 0;
-                        while (p < cand)
-                            p += total_size(page[p]);
-                        on_walk = p == cand;
-                    }
-                    on_walk = __shfl_sync(0xffffffffu, on_walk, 0);
-                    if (on_walk)
-                        found = pindex + cand;
-                }
-            }
-        }
-        scanned += found == kNotFound ? used : (found - pindex + n);
-        __syncwarp();
-    }
-    if (!leaf && found == kNotFound && S >= n && ((S - n) & ~(kPage - 1)) == ((S - 1) & ~(kPage - 1))) {
-        // the bucket's last node ends at S; it holds q iff it starts at S - n
-        // (nodes never straddle a page, so S - n lies in the tail's page)
-        const uint32_t p = S - n;
-        const uint32_t pindex = p & ~(kPage - 1);
-        const uint32_t used = S - pindex; // <= kPage
-        const uint32_t* src = t.sys_cg(vbase + pindex);
-        for (uint32_t w = lane * 4; w < used; w += 128) {
-            const uint4 v = __ldcg(reinterpret_cast<const uint4*>(src + w));
-            page[w] = v.x;
-            page[w + 1] = v.y;
-            page[w + 2] = v.z;
-            page[w + 3] = v.w;
-        }
-        __syncwarp();
-        uint32_t ok = 0;
-        if (lane == 0 && S - n >= pindex) {
-            bool m = true;
-            for (uint32_t k = 0; k < n; k++)
-                m &= page[p - pindex + k] == q[k];
-            if (m) {
-                uint32_t w = 0;
-                while (w < p - pindex)
-                    w += total_size(page[w]);
-                ok = w == p - pindex;
-            }
-        }
-        ok = __shfl_sync(0xffffffffu, ok, 0);
-        if (ok)
-            *last_match = p;
-        __syncwarp();
-    }
-    return found;
-}
-
 __global__ void __launch_bounds__(32 * kFoaWarps)
     k_edit_find_or_add(Table t, uint32_t level, Level lv, const uint32_t* __restrict__ keys,
                        const uint32_t* __restrict__ vals, const uint32_t* __restrict__ starts,
@@ -471,120 +71,13 @@ __global__ void __launch_bounds__(32 * kFoaWarps)
     __shared__ uint32_t q_s[kFoaWarps][9];
     __shared__ FoaCache cache_s[kFoaWarps];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint32_t* page = page_s[warp];
-    uint32_t* q = q_s[warp];
-    FoaCache& cache = cache_s[warp];
-    const bool leaf = level == t.g.leaf_level;
     const uint32_t nseg = *n_seg, ncand = *n_cand;
+    const uint32_t first = t.g.level_first_bucket(level);
     unsigned long long foa = 0, added = 0, scanned = 0;
     for (uint32_t si = blockIdx.x * kFoaWarps + warp; si < nseg; si += gridDim.x * kFoaWarps) {
         const uint32_t j0 = starts[si], j1 = si + 1 < nseg ? starts[si + 1] : ncand;
-        const uint32_t gb = keys[j0];
-        const uint32_t bucket = gb - t.g.level_first_bucket(level);
-        const uint32_t vbase = t.g.make_ptr(level, bucket, 0);
-        uint32_t S = __ldcg(t.bucket_sizes + gb);
-        uint32_t used_entries = 0, next_slot = 0;
-        bool failed = false;
-        uint32_t j = j0;
-        while (j < j1 && !failed) {
-            const uint32_t ci = vals[j];
-            if (lane < 9)
-                q[lane] = lv.cand[9 * uint64_t(ci) + lane];
-            __syncwarp();
-            const uint32_t n = leaf ? 2 : total_size(q[0]);
-            // cache lookup: lane e checks entry e
-            bool hit = lane < used_entries && cache.n[lane] == n;
-            if (hit)
-                for (uint32_t k = 0; k < n; k++)
-                    hit &= cache.words[lane][k] == q[k];
-            const uint32_t hb = __ballot_sync(0xffffffffu, hit);
-            uint32_t e;
-            if (hb) {
-                e = __ffs(hb) - 1;
-            } else {
-                uint32_t last_match;
-                const uint32_t f = scan_bucket(t, vbase, S, q, n, leaf, page, &last_match, scanned);
-                e = next_slot;
-                next_slot = (next_slot + 1) % kCache;
-                used_entries = used_entries < kCache ? used_entries + 1 : kCache;
-                if (lane < 9)
-                    cache.words[e][lane] = q[lane];
-                if (lane == 0) {
-                    cache.n[e] = n;
-                    cache.npos[e] = 0;
-                    if (f != kNotFound)
-                        cache.pos[e][cache.npos[e]++] = f;
-                    else if (last_match != kNotFound)
-                        cache.pos[e][cache.npos[e]++] = last_match;
-                }
-                __syncwarp();
-            }
-            // the first visible copy, else append (lane 0)
-            uint32_t result = kNotFound, appended = 0, ok = 1;
-            if (lane == 0) {
-                for (uint32_t k = 0; k < cache.npos[e] && result == kNotFound; k++)
-                    if (visible(cache.pos[e][k], n, S, leaf))
-                        result = cache.pos[e][k];
-                if (result == kNotFound) {
-                    uint32_t size = S;
-                    const uint32_t pos = append_position(size, n, leaf);
-                    if (size > t.g.capacity(level)) {
-                        set_error(t.error, kErrBucketFull, level, bucket, size);
-                        ok = 0;
-                    } else if (!map_pages(t, level, bucket, pos, size)) {
-                        ok = 0;
-                    } else {
-                        uint32_t* dst = t.sys_rw(vbase + pos);
-                        for (uint32_t k = 0; k < n; k++)
-                            __stcg(dst + k, q[k]);
-                        result = pos;
-                        S = size;
-                        appended = 1;
-                        if (cache.npos[e] == kCachePos) { // keep the newest copies
-                            for (uint32_t k = 1; k < kCachePos; k++)
-                                cache.pos[e][k - 1] = cache.pos[e][k];
-                            cache.npos[e]--;
-                        }
-                        cache.pos[e][cache.npos[e]++] = pos;
-                    }
-                }
-                lv.res[ci] = vbase + result;
-            }
-            ok = __shfl_sync(0xffffffffu, ok, 0);
-            result = __shfl_sync(0xffffffffu, result, 0);
-            appended = __shfl_sync(0xffffffffu, appended, 0);
-            S = __shfl_sync(0xffffffffu, S, 0);
-            foa++;
-            added += appended;
-            if (!ok) {
-                failed = true;
-                break;
-            }
-            j++;
-            // a found result holds for the identical candidates that follow
-            if (!appended) {
-                for (;;) {
-                    const uint32_t jj = j + lane;
-                    bool same = jj < j1;
-                    if (same) {
-                        const uint32_t* c = lv.cand + 9 * uint64_t(vals[jj]);
-                        for (uint32_t k = 0; k < n; k++)
-                            same &= c[k] == q[k];
-                    }
-                    const uint32_t b = __ballot_sync(0xffffffffu, same);
-                    const uint32_t run = b == 0xffffffffu ? 32u : __ffs(~b) - 1;
-                    if (lane < run)
-                        lv.res[vals[jj]] = vbase + result;
-                    foa += run;
-                    j += run;
-                    if (run < 32)
-                        break;
-                }
-            }
-            __syncwarp();
-        }
-        if (lane == 0)
-            __stcg(t.bucket_sizes + gb, S);
+        foa_segment<kFoaProbe>(t, level, lv, vals, j0, j1, keys[j0] - first, page_s[warp], q_s[warp], cache_s[warp],
+                               foa, added, scanned);
     }
     if (lane == 0) {
         atomicAdd(&ctr->foa, foa);
@@ -740,29 +233,6 @@ hd_status hd_edit_apply(hd_ctx* c, const hd_edit* edit, hd_edit_stats* stats)
         c->err = std::string("CUDA error ") + cudaGetErrorString(e.code) + " in " + e.where;
         return HD_ERR_CUDA;
     }
-}
-
-hd_status hd_edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* stats)
-{
-    if (!c || (n && !edits))
-        return HD_ERR_INVALID;
-    hd_edit_stats total{};
-    for (uint32_t i = 0; i < n; i++) {
-        hd_edit_stats s{};
-        const hd_status r = hd_edit_apply(c, edits + i, &s);
-        if (r != HD_OK)
-            return r;
-        total.num_voxels += s.num_voxels;
-        total.num_nodes += s.num_nodes;
-        total.find_or_add_calls += s.find_or_add_calls;
-        total.nodes_added += s.nodes_added;
-        total.words_scanned += s.words_scanned;
-        total.device_ms += s.device_ms;
-        total.host_ms += s.host_ms;
-    }
-    if (stats)
-        *stats = total;
-    return HD_OK;
 }
 
 } // extern "C"

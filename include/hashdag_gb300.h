@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define HD_ABI_VERSION 1u
+#define HD_ABI_VERSION 2u
 #define HD_PAGE_SIZE 512u
 #define HD_MAX_DEPTH 20u
 /* Sentinel of the edit recursion (hash_dag_edits.h:17). */
@@ -195,10 +195,32 @@ hd_status hd_get_values(hd_ctx* ctx, const uint32_t* d_xyz, uint64_t n, uint8_t*
  * leaf rebuild (:451-546), then bottom-up find_or_add of every changed node
  * (hash_table.h:470-560), level by level, in depth-first order. */
 hd_status hd_edit_apply(hd_ctx* ctx, const hd_edit* edit, hd_edit_stats* stats);
-/* A sequence of edits applied in order with the same result as calling
- * hd_edit_apply for each; runs as one device-driven pipeline with no host round
- * trip between edits. */
+/* Batched form of HashDAG::edit_threads over a list of edits: the same
+ * result as calling hd_edit_apply for each in order (same table, same
+ * addresses), run as one CUDA graph per edit launched back to back, with no
+ * host round trip between levels or edits.  stats: the sums over the batch
+ * (device_ms = device time of the whole batch). */
 hd_status hd_edit_batch(hd_ctx* ctx, const hd_edit* edits, uint32_t n, hd_edit_stats* stats);
+/* hd_edit_batch with per-edit results: per_edit[i] (n entries, may be NULL)
+ * holds edit i's counters, its device time (device_ms) and its completion
+ * time since the batch started on the device (host_ms). */
+hd_status hd_edit_batch_ex(hd_ctx* ctx, const hd_edit* edits, uint32_t n, hd_edit_stats* per_edit,
+                           hd_edit_stats* total);
+
+/* Launch shape of the batched edit kernels (results never depend on it). */
+typedef struct hd_batch_tuning {
+    uint32_t foa_warps;   /* warps per find-or-add block: 2, 4 or 8            */
+    uint32_t probe_words; /* words per lane per bucket-page load: 1, 2 or 4    */
+    uint32_t grid_blocks; /* blocks of the level kernels: 64 .. 2048           */
+} hd_batch_tuning;
+hd_status hd_set_batch_tuning(hd_ctx* ctx, const hd_batch_tuning* tuning);
+hd_status hd_get_batch_tuning(hd_ctx* ctx, hd_batch_tuning* tuning);
+/* Times every launch shape on a device copy of the table with the n sample
+ * edits and keeps the fastest for ctx; the table itself is not changed. */
+hd_status hd_autotune_batch(hd_ctx* ctx, const hd_edit* sample, uint32_t n, hd_batch_tuning* best, float* best_ms);
+/* Edits that the batched path handed to the one-edit path (a level outgrew
+ * its bound), since the context was created. */
+hd_status hd_batch_fallbacks(hd_ctx* ctx, uint64_t* count);
 
 /* ---- garbage collection (HashDAG::remove_stale_nodes, hash_dag.h:407-547) */
 

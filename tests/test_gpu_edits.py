@@ -135,3 +135,72 @@ def test_edit_depth15_matches_oracle_sample(gpu):
     want = np.array([ot.get_value(*map(int, p)) for p in q], np.uint8)
     assert np.array_equal(got, want)
     d.free()
+
+
+def _stats_tuple(s):
+    return (s.num_voxels, s.num_nodes, s.find_or_add_calls, s.nodes_added, s.words_scanned)
+
+
+@pytest.mark.parametrize("tuning", [(4, 4, 304), (2, 1, 1216), (8, 2, 608)])
+def test_batch_launch_shapes_agree(gpu, tuning):
+    """Every launch shape of the batched path gives the plain path's table
+    and per-edit counters (depth 12, uneven radii)."""
+    depth = 12
+    edits = workloads.mixed_edits(depth, 24, (2.0, 200.0), seed=37)
+    a = hd.HashDAG(depth)
+    a.generate_scene(1)
+    plain = [a.edit_threads(hd.editor_from_tuple(e)) for e in edits]
+    b = hd.HashDAG(depth)
+    b.generate_scene(1)
+    b.batch_tuning = tuning
+    total, per = b.edit_batch([hd.editor_from_tuple(e) for e in edits], per_edit=True)
+    assert [_stats_tuple(s) for s in per] == [_stats_tuple(s) for s in plain]
+    assert a.firstNodeIndex == b.firstNodeIndex
+    assert table_digest(a.export_table(), depth) == table_digest(b.export_table(), depth)
+    assert b.batch_fallbacks() == 0
+    ends = [s.host_ms for s in per]
+    assert all(x <= y for x, y in zip(ends, ends[1:]))
+    a.free()
+    b.free()
+
+
+def test_batch_depth15_matches_plain(gpu):
+    """A batch of 64 edits of radius 4..512 on the 2^15 scene: same roots,
+    per-level words and nodes, counters and sampled occupancy as the
+    one-edit path."""
+    depth = 15
+    edits = workloads.mixed_edits(depth, 64, (4.0, 512.0), seed=3)
+    a = hd.HashDAG(depth)
+    a.generate_scene(1)
+    plain = [a.edit_threads(hd.editor_from_tuple(e)) for e in edits]
+    b = hd.HashDAG(depth)
+    b.generate_scene(1)
+    total, per = b.edit_batch([hd.editor_from_tuple(e) for e in edits], per_edit=True)
+    assert [_stats_tuple(s) for s in per] == [_stats_tuple(s) for s in plain]
+    assert a.firstNodeIndex == b.firstNodeIndex
+    sa, sb = a.level_stats(), b.level_stats()
+    assert list(sa.words[:depth]) == list(sb.words[:depth])
+    assert list(sa.nodes[:depth]) == list(sb.nodes[:depth])
+    assert sa.pages_used == sb.pages_used
+    assert b.batch_fallbacks() == 0
+    rng = np.random.default_rng(5)
+    q = rng.integers(0, 1 << depth, (50000, 3)).astype(np.uint32)
+    assert np.array_equal(a.get_values(q), b.get_values(q))
+    a.free()
+    b.free()
+
+
+def test_autotune_leaves_table_unchanged(gpu):
+    depth = 12
+    d = hd.HashDAG(depth)
+    d.generate_scene(1)
+    before = table_digest(d.export_table(), depth)
+    r0 = d.firstNodeIndex
+    edits = [hd.editor_from_tuple(e) for e in workloads.mixed_edits(depth, 8, (2.0, 100.0), seed=41)]
+    t, ms = d.autotune_batch(edits)
+    assert t.foa_warps in (2, 4, 8) and t.probe_words in (1, 2, 4) and ms > 0
+    assert d.firstNodeIndex == r0
+    assert table_digest(d.export_table(), depth) == before
+    cur = d.batch_tuning
+    assert (cur.foa_warps, cur.probe_words, cur.grid_blocks) == (t.foa_warps, t.probe_words, t.grid_blocks)
+    d.free()
