@@ -18,6 +18,13 @@ e2e    = the same metric through the C ABI with host buffers: camera from
 (the reference has no CPU tracer) on all host cores, a bounded band of rows
 per step.  Under torchrun every rank renders its own poses on its own GPU
 (replicas, no collective on the data path).
+
+"edits" (the same JSON line): the batched-edit workload on the 2^15 scene,
+--edits edits (default 256; 50% sphere carve, 30% sphere fill, 20% box fill,
+radius log-uniform in [4, 512]) applied plainly (hd_edit_apply per edit) and
+batched (hd_edit_batch, autotuned): edited voxels/s, find-or-add/s, p50/p99
+per-edit device latency of both forms, and the oracle's single-thread CPU
+editor on a bounded sample of the same edits.
 """
 import argparse
 import ctypes as C
@@ -48,9 +55,11 @@ def parse():
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--poses", type=int, default=64)
     p.add_argument("--ref-rows", type=int, default=192, help="rows per step of the CPU reference arm")
-    p.add_argument("--cpu-sample-rows", type=int, default=256, help="rows of the cpu_baseline sample")
+    p.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the traversal cpu_baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pool-pages", type=int, default=0, help="physical pool pages (0 = library default)")
+    p.add_argument("--edits", type=int, default=256, help="edits of the edit benchmark (0 = skip it)")
+    p.add_argument("--edit-cpu-seconds", type=float, default=12.0, help="budget of the CPU edit sample")
     return p.parse_args()
 
 
@@ -179,26 +188,126 @@ def load_scene(depth, pool_pages=0):
     return dag, time.perf_counter() - t0
 
 
-def oracle_from(dag, depth):
+def oracle_from(dag, depth, spare_pages=16):
     from oracle import pyoracle as po
     t = dag.export_table()
-    ot = po.Table(po.default_config(depth, pool_pages=int(t["pool"].size // 512) + 16))
+    ot = po.Table(po.default_config(depth, pool_pages=int(t["pool"].size // 512) + spare_pages))
     ot.import_(t)
     return ot
 
 
-def cpu_baseline(ot, cams_params, W, H, rows):
+def cpu_baseline(ot, cams_params, W, H, seconds):
+    """The oracle tracer on all host cores: whole frames of the path's poses,
+    in order, until the time budget is spent."""
     threads = os.cpu_count() or 1
-    r0 = max(0, H // 2 - rows // 2)
     t0 = time.perf_counter()
-    paths, mask = ot.trace_frame(cams_params[0], W, H, LIGHT, BIAS, fp_mode=1, threads=threads, rows=(r0, r0 + rows))
+    rays = frames = 0
+    while frames < len(cams_params) and time.perf_counter() - t0 < seconds:
+        paths, mask = ot.trace_frame(cams_params[frames], W, H, LIGHT, BIAS, fp_mode=1, threads=threads)
+        rays += W * H + int((mask != 2).sum())
+        frames += 1
     dt = time.perf_counter() - t0
-    out_rows = slice(H - (r0 + rows), H - r0)
-    hits = int((mask[out_rows] != 2).sum())
-    rays = rows * W + hits
     return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"{rows} rows x {W} px of pose 0 (primary + {hits} shadow rays), oracle C restatement, "
-                      f"{threads} threads, {dt:.1f} s"}
+            "sample": f"{frames} full {W}x{H} frames of the path ({rays} primary + shadow rays), oracle C "
+                      f"restatement of the reference tracer, {threads} threads, {dt:.1f} s"}
+
+
+def _pct(v, q):
+    import numpy as np
+    return float(np.percentile(np.asarray(v, np.float64), q)) if len(v) else None
+
+
+def edit_bench(args, dist):
+    """Batched-edit workload: 2^15 scene, edits with 50% sphere carve, 30%
+    sphere fill, 20% box fill, radius log-uniform in [4, 512], centred on
+    surface voxels (seed 3).  The plain form applies them one call per edit
+    (hd_edit_apply: host-driven levels, a sync per level); the batched form
+    runs them through hd_edit_batch (one captured graph per edit, launch
+    shape from hd_autotune_batch on the first 32 edits).  Both start from
+    the same freshly generated scene and must end on the same root."""
+    import hashdag_gb300 as hd
+    from hashdag_gb300 import workloads
+    depth, n = args.depth, args.edits
+    tuples = workloads.mixed_edits(depth, n, (4.0, 512.0), seed=workloads.SEED_EDITS)
+    eds = [hd.editor_from_tuple(e) for e in tuples]
+
+    def fresh():
+        d, _ = load_scene(depth, args.pool_pages)
+        return d
+
+    # plain: a warm-up context first (allocations, module load)
+    d = fresh()
+    for e in eds[:4]:
+        d.edit_threads(e)
+    d.free()
+    d = fresh()
+    t0 = time.perf_counter()
+    plain = [d.edit_threads(e) for e in eds]
+    plain_s = time.perf_counter() - t0
+    plain_root = d.firstNodeIndex
+    d.free()
+    # batched: tune on a copy, capture once, then the timed batch
+    d = fresh()
+    tuning, _ = d.autotune_batch(eds[:32])
+    d.edit_batch(eds[:2])
+    d.free()
+    d = fresh()
+    d.batch_tuning = tuning
+    d.edit_batch(eds[:1])  # capture on this context
+    d.free()
+    d = fresh()
+    d.batch_tuning = tuning
+    t0 = time.perf_counter()
+    total, per = d.edit_batch(eds, per_edit=True)
+    batch_s = time.perf_counter() - t0
+    batch_root = d.firstNodeIndex
+    fallbacks = d.batch_fallbacks()
+    d.free()
+    plain_s = dist.max(plain_s)
+    batch_s = dist.max(batch_s)
+    vox = sum(s.num_voxels for s in plain)
+    foa = sum(s.find_or_add_calls for s in plain)
+
+    def form(seconds, stats, extra):
+        lat = [s.device_ms for s in stats]
+        out = {"voxels_per_s": vox * dist.world / seconds, "find_or_add_per_s": foa * dist.world / seconds,
+               "edits_per_s": n * dist.world / seconds, "wall_s": seconds,
+               "p50_edit_ms": _pct(lat, 50), "p99_edit_ms": _pct(lat, 99), "max_edit_ms": max(lat)}
+        out.update(extra)
+        return out
+
+    res = {"workload": f"mixed_edits_d{depth}_{n}_r4-512", "edits": n, "num_voxels": vox, "find_or_add_calls": foa,
+           "nodes_added": sum(s.nodes_added for s in plain),
+           "plain": form(plain_s, plain, {"api": "hd_edit_apply per edit", "latency": "device time per edit"}),
+           "batched": form(batch_s, per, {"api": "hd_edit_batch (one CUDA graph launch per edit)",
+                                          "latency": "device time per edit inside the batch",
+                                          "p99_completion_ms": _pct([s.host_ms for s in per], 99),
+                                          "tuning": {"foa_warps": tuning.foa_warps,
+                                                     "probe_words": tuning.probe_words,
+                                                     "grid_blocks": tuning.grid_blocks},
+                                          "fallbacks": fallbacks}),
+           "same_root": bool(plain_root == batch_root)}
+    res["batched_over_plain_voxels_per_s"] = res["batched"]["voxels_per_s"] / res["plain"]["voxels_per_s"]
+    return res, tuples
+
+
+def edit_cpu_baseline(args, tuples):
+    """The oracle's C restatement of the reference editor (single thread) on
+    the same scene and edits, as many edits as fit the time budget."""
+    import hashdag_gb300 as hd
+    d, _ = load_scene(args.depth, args.pool_pages)
+    ot = oracle_from(d, args.depth, spare_pages=1 << 18)
+    d.free()
+    t0 = time.perf_counter()
+    vox = foa = k = 0
+    while k < len(tuples) and time.perf_counter() - t0 < args.edit_cpu_seconds:
+        s = ot.edit(*tuples[k])
+        vox += s.num_voxels
+        foa += s.find_or_add_calls
+        k += 1
+    dt = time.perf_counter() - t0
+    return {"voxels_per_s": vox / dt, "find_or_add_per_s": foa / dt, "edits_per_s": k / dt, "cores": 1,
+            "kind": "port", "sample": f"first {k} of the {len(tuples)} edits, oracle C editor, 1 thread, {dt:.1f} s"}
 
 
 def run_reference(args, dist):
@@ -354,11 +463,20 @@ def run_gpu(args, dist):
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         try:
             ot = oracle_from(dag, depth)
-            cpu = cpu_baseline(ot, poses, W, H, args.cpu_sample_rows)
+            cpu = cpu_baseline(ot, poses, W, H, args.cpu_seconds)
             del ot
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}
+    edits = None
+    if args.edits:
+        dag.free()
+        edits, tuples = edit_bench(args, dist)
+        if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+            try:
+                edits["cpu_baseline"] = edit_cpu_baseline(args, tuples)
+            except Exception as e:  # reported, never required
+                edits["cpu_baseline"] = {"value": None, "sample": f"failed: {e}"}
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": dist.world, "steps": K,
             "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -371,7 +489,7 @@ def run_gpu(args, dist):
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(_capi.Camera),
                     "d2h_bytes_per_step": W * H * 16 + W * H},
             "gpu_launches": 2 * K, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "wall_s": wall}
+            "wall_s": wall, "edits": edits}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dag.free()
