@@ -35,7 +35,13 @@ class Camera(C.Structure):
 
 
 class Edit(C.Structure):
-    _fields_ = [("tool", C.c_uint32), ("center", C.c_float * 3), ("radius", C.c_float)]
+    _fields_ = [("tool", C.c_uint32), ("center", C.c_float * 3), ("radius", C.c_float), ("rgb", C.c_uint32),
+                ("source", C.c_float * 3), ("dest", C.c_float * 3)]
+
+
+class Color(C.Structure):
+    _fields_ = [("color_bits", C.c_uint32), ("weight", C.c_uint8), ("bits_per_weight", C.c_uint8),
+                ("reserved", C.c_uint16)]
 
 
 class EditStats(C.Structure):

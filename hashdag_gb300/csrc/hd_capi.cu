@@ -182,14 +182,16 @@ hd_status hd_load_basic_dag(hd_ctx* c, const uint32_t* h_words, uint64_t n_words
     });
 }
 
-hd_status hd_generate_scene(hd_ctx* c, uint64_t seed)
+hd_status hd_generate_scene(hd_ctx* c, uint64_t seed) { return hd_generate_scene_ex(c, seed, 0); }
+
+hd_status hd_generate_scene_ex(hd_ctx* c, uint64_t seed, uint32_t flags)
 {
-    if (!c)
+    if (!c || (flags & ~uint32_t(HD_SCENE_SHELL)))
         return HD_ERR_INVALID;
     return guarded(c, [&] {
         uint32_t* words;
         uint64_t n;
-        generate_scene(c, seed, &words, &n);
+        generate_scene(c, seed, flags, &words, &n);
         c->scratch.release(); // the generator's buffers are large; start the ingest clean
         table_reset(c);
         import_basic_dag(c, words, n);

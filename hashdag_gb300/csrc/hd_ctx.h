@@ -48,7 +48,7 @@ void append_items(hd_ctx* c, uint32_t level, const uint32_t* content, uint64_t n
                   const uint32_t* next, const uint32_t* touched, const uint32_t* n_touched, uint32_t* out_addr);
 
 // hd_scene.cu
-void generate_scene(hd_ctx* c, uint64_t seed, uint32_t** d_words, uint64_t* n_words);
+void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words, uint64_t* n_words);
 
 // hd_edit.cu / hd_edit_batch.cu
 void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats);

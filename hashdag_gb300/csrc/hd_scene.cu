@@ -152,6 +152,65 @@ HD_D uint32_t classify(uint32_t depth, uint32_t level, uint32_t x, uint32_t y, u
     return 2;
 }
 
+// Shell scenes: a node holds no shell voxel when it holds no solid voxel or
+// when the node grown by one voxel on every side is solid throughout (single
+// source: the height field alone or one sphere alone; conservative).  *live
+// = spheres touching the grown node.  Returns 0 (empty) or 2 (mixed).
+HD_D uint32_t classify_shell(uint32_t depth, uint32_t level, uint32_t x, uint32_t y, uint32_t z, const int32_t* hmin,
+                             const int32_t* hmax, uint64_t parent_live, uint64_t* live)
+{
+    const uint32_t shift = depth - level;
+    const int64_t s = int64_t(1) << shift, E = int64_t(1) << depth;
+    const uint64_t m = uint64_t(1) << level;
+    const int64_t x0 = int64_t(x) << shift, y0 = int64_t(y) << shift, z0 = int64_t(z) << shift;
+    bool touched = y0 <= hmax[(uint64_t(x) << level) | z];
+    const bool inside = x0 > 0 && z0 > 0 && y0 > 0 && x0 + s < E && z0 + s < E && y0 + s < E;
+    bool full = false;
+    if (inside) {
+        int64_t lo = INT64_MAX;
+        for (int a = -1; a <= 1; a++)
+            for (int b = -1; b <= 1; b++) {
+                const int64_t v = hmin[uint64_t(int64_t(x) + a) * m + uint64_t(int64_t(z) + b)];
+                lo = v < lo ? v : lo;
+            }
+        full = y0 + s <= lo;
+    }
+    uint64_t out = 0;
+    uint64_t todo = parent_live;
+    while (todo) {
+        const uint32_t k = __ffsll(todo) - 1;
+        todo &= todo - 1;
+        const int64_t* sp = c_spheres + 4 * k;
+        const int64_t lo3[3] = {x0, y0, z0};
+        int64_t d2in = 0, d2near = 0, d2far = 0;
+        for (int a = 0; a < 3; a++) {
+            const int64_t c = sp[a], l = lo3[a], h = lo3[a] + s - 1;
+            const int64_t din = c < l ? l - c : (c > h ? c - h : 0);
+            const int64_t dn = c < l - 1 ? l - 1 - c : (c > h + 1 ? c - h - 1 : 0);
+            const int64_t df = (c - l + 1) > (h + 1 - c) ? (c - l + 1) : (h + 1 - c);
+            d2in += din * din;
+            d2near += dn * dn;
+            d2far += df * df;
+        }
+        const int64_t r2 = sp[3] * sp[3];
+        if (d2near <= r2)
+            out |= 1ull << k;
+        if (d2in <= r2)
+            touched = true;
+        if (inside && d2far <= r2)
+            full = true;
+    }
+    *live = out;
+    return (!touched || full) ? 0u : 2u;
+}
+
+HD_D uint32_t classify_any(bool shell, uint32_t depth, uint32_t level, uint32_t x, uint32_t y, uint32_t z,
+                           const int32_t* hmin, const int32_t* hmax, uint64_t parent_live, uint64_t* live)
+{
+    return shell ? classify_shell(depth, level, x, y, z, hmin, hmax, parent_live, live)
+                 : classify(depth, level, x, y, z, hmin, hmax, parent_live, live);
+}
+
 struct Frontier {
     uint32_t* x;
     uint32_t* y;
@@ -159,8 +218,9 @@ struct Frontier {
     uint64_t* live;
 };
 
-__global__ void k_classify_children(uint32_t depth, uint32_t level, Frontier f, uint32_t n, const int32_t* hmin,
-                                    const int32_t* hmax, uint32_t* __restrict__ cls2, uint32_t* __restrict__ nmixed)
+__global__ void k_classify_children(bool shell, uint32_t depth, uint32_t level, Frontier f, uint32_t n,
+                                    const int32_t* hmin, const int32_t* hmax, uint32_t* __restrict__ cls2,
+                                    uint32_t* __restrict__ nmixed)
 {
     HD_GRID_STRIDE(i, n)
     {
@@ -169,8 +229,8 @@ __global__ void k_classify_children(uint32_t depth, uint32_t level, Frontier f, 
         const uint64_t pl = f.live[i];
         for (uint32_t c = 0; c < 8; c++) {
             uint64_t live;
-            const uint32_t cls = classify(depth, level + 1, 2 * px + ((c >> 2) & 1), 2 * py + ((c >> 1) & 1),
-                                          2 * pz + (c & 1), hmin, hmax, pl, &live);
+            const uint32_t cls = classify_any(shell, depth, level + 1, 2 * px + ((c >> 2) & 1),
+                                              2 * py + ((c >> 1) & 1), 2 * pz + (c & 1), hmin, hmax, pl, &live);
             c2 |= cls << (2 * c);
             nm += cls == 2;
         }
@@ -179,8 +239,9 @@ __global__ void k_classify_children(uint32_t depth, uint32_t level, Frontier f, 
     }
 }
 
-__global__ void k_expand(uint32_t depth, uint32_t level, Frontier f, uint32_t n, const uint32_t* __restrict__ cls2,
-                         const uint32_t* __restrict__ coff, const int32_t* hmin, const int32_t* hmax, Frontier out)
+__global__ void k_expand(bool shell, uint32_t depth, uint32_t level, Frontier f, uint32_t n,
+                         const uint32_t* __restrict__ cls2, const uint32_t* __restrict__ coff, const int32_t* hmin,
+                         const int32_t* hmax, Frontier out)
 {
     HD_GRID_STRIDE(i, n)
     {
@@ -191,7 +252,7 @@ __global__ void k_expand(uint32_t depth, uint32_t level, Frontier f, uint32_t n,
                 continue;
             const uint32_t cx = 2 * f.x[i] + ((c >> 2) & 1), cy = 2 * f.y[i] + ((c >> 1) & 1), cz = 2 * f.z[i] + (c & 1);
             uint64_t live;
-            classify(depth, level + 1, cx, cy, cz, hmin, hmax, f.live[i], &live);
+            classify_any(shell, depth, level + 1, cx, cy, cz, hmin, hmax, f.live[i], &live);
             out.x[o] = cx;
             out.y[o] = cy;
             out.z[o] = cz;
@@ -229,6 +290,61 @@ __global__ void k_leaf_masks(uint64_t seed, uint32_t depth, Frontier f, uint32_t
                     }
                 }
             }
+        masks[i] = leaf;
+    }
+}
+
+// Shell leaves: solid voxels with an empty face neighbour; heights of the
+// 6x6 footprint around the leaf, outside the volume empty.
+HD_D bool shell_solid(const int64_t* h, uint64_t live, int64_t E, int64_t x0, int64_t z0, int64_t x, int64_t y,
+                      int64_t z)
+{
+    if (x < 0 || y < 0 || z < 0 || x >= E || y >= E || z >= E)
+        return false;
+    if (y <= h[(x - x0 + 1) * 6 + (z - z0 + 1)])
+        return true;
+    uint64_t todo = live;
+    while (todo) {
+        const uint32_t k = __ffsll(todo) - 1;
+        todo &= todo - 1;
+        const int64_t* sp = c_spheres + 4 * k;
+        const int64_t dx = x - sp[0], dy = y - sp[1], dz = z - sp[2];
+        if (dx * dx + dy * dy + dz * dz <= sp[3] * sp[3])
+            return true;
+    }
+    return false;
+}
+
+__global__ void k_leaf_masks_shell(uint64_t seed, uint32_t depth, Frontier f, uint32_t n, uint64_t* __restrict__ masks)
+{
+    const int64_t E = int64_t(1) << depth;
+    HD_GRID_STRIDE(i, n)
+    {
+        const int64_t x0 = int64_t(f.x[i]) << 2, y0 = int64_t(f.y[i]) << 2, z0 = int64_t(f.z[i]) << 2;
+        const uint64_t live = f.live[i];
+        int64_t h[36];
+        for (int a = 0; a < 6; a++)
+            for (int b = 0; b < 6; b++) {
+                const int64_t x = x0 + a - 1, z = z0 + b - 1;
+                h[a * 6 + b] = (x < 0 || z < 0 || x >= E || z >= E)
+                                   ? -1
+                                   : scene_height(seed, depth, uint32_t(x), uint32_t(z));
+            }
+        uint64_t leaf = 0;
+        for (uint32_t lx = 0; lx < 4; lx++)
+            for (uint32_t ly = 0; ly < 4; ly++)
+                for (uint32_t lz = 0; lz < 4; lz++) {
+                    const int64_t x = x0 + lx, y = y0 + ly, z = z0 + lz;
+                    if (!shell_solid(h, live, E, x0, z0, x, y, z))
+                        continue;
+                    if (shell_solid(h, live, E, x0, z0, x + 1, y, z) && shell_solid(h, live, E, x0, z0, x - 1, y, z) &&
+                        shell_solid(h, live, E, x0, z0, x, y + 1, z) && shell_solid(h, live, E, x0, z0, x, y - 1, z) &&
+                        shell_solid(h, live, E, x0, z0, x, y, z + 1) && shell_solid(h, live, E, x0, z0, x, y, z - 1))
+                        continue;
+                    const uint32_t c1 = ((lx >> 1) << 2) | ((ly >> 1) << 1) | (lz >> 1);
+                    const uint32_t c2 = ((lx & 1) << 2) | ((ly & 1) << 1) | (lz & 1);
+                    leaf |= 1ull << (c1 * 8 + c2);
+                }
         masks[i] = leaf;
     }
 }
@@ -463,8 +579,9 @@ __global__ void k_emit(uint32_t level, uint32_t T, bool leaf, const uint32_t* __
     }
 }
 
-void generate_scene(hd_ctx* c, uint64_t seed, uint32_t** d_words_out, uint64_t* n_words_out)
+void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words_out, uint64_t* n_words_out)
 {
+    const bool shell = (flags & HD_SCENE_SHELL) != 0;
     cudaStream_t st = c->stream;
     Scratch& s = c->scratch;
     const uint32_t D = c->g.depth, leafl = c->g.leaf_level, T = c->g.T;
@@ -531,20 +648,24 @@ void generate_scene(hd_ctx* c, uint64_t seed, uint32_t** d_words_out, uint64_t* 
         cls2[L] = s.get<uint32_t>(a, uint64_t(n) + 1);
         coff[L] = s.get<uint32_t>(b, uint64_t(n) + 1);
         uint32_t* nm = s.get<uint32_t>("scn_nm", uint64_t(n) + 1);
-        k_classify_children<<<grid_for(n, 128), 128, 0, st>>>(D, L, fr[L], n, hmin[L + 1], hmax[L + 1], cls2[L], nm);
+        k_classify_children<<<grid_for(n, 128), 128, 0, st>>>(shell, D, L, fr[L], n, hmin[L + 1], hmax[L + 1],
+                                                              cls2[L], nm);
         HD_LAUNCH_CHECK();
         exclusive_scan<uint32_t, uint32_t>(s, nm, coff[L], n, d_n, st);
         const uint32_t nn = read_scalar(d_n, st);
         fr[L + 1] = alloc_frontier(L + 1, nn);
         nf[L + 1] = nn;
-        k_expand<<<grid_for(n, 128), 128, 0, st>>>(D, L, fr[L], n, cls2[L], coff[L], hmin[L + 1], hmax[L + 1],
-                                                   fr[L + 1]);
+        k_expand<<<grid_for(n, 128), 128, 0, st>>>(shell, D, L, fr[L], n, cls2[L], coff[L], hmin[L + 1],
+                                                   hmax[L + 1], fr[L + 1]);
         HD_LAUNCH_CHECK();
     }
     // height bounds no longer needed past this point: free them for the dedup
     // leaf masks
     uint64_t* masks = s.get<uint64_t>("scn_masks", uint64_t(nf[leafl]) + 1);
-    k_leaf_masks<<<grid_for(nf[leafl], 128, 152 * 64), 128, 0, st>>>(seed, D, fr[leafl], nf[leafl], masks);
+    if (shell)
+        k_leaf_masks_shell<<<grid_for(nf[leafl], 128, 152 * 64), 128, 0, st>>>(seed, D, fr[leafl], nf[leafl], masks);
+    else
+        k_leaf_masks<<<grid_for(nf[leafl], 128, 152 * 64), 128, 0, st>>>(seed, D, fr[leafl], nf[leafl], masks);
     HD_LAUNCH_CHECK();
     // 3. bottom-up dedup
     std::vector<uint32_t*> ucont(leafl + 1);

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define HD_ABI_VERSION 2u
+#define HD_ABI_VERSION 3u
 #define HD_PAGE_SIZE 512u
 #define HD_MAX_DEPTH 20u
 /* Sentinel of the edit recursion (hash_dag_edits.h:17). */
@@ -74,18 +74,37 @@ typedef struct hd_camera {
 
 /* Edit tools (hash_dag_editors.h): sphere carve/fill (SphereEditor<bool>,
  * :272-313), box carve/fill (BoxEditor<bool>, :223-270). */
+/* The editors of hash_dag_editors.h: SphereEditor<false/true> (:272-313),
+ * BoxEditor<false/true> (:223-270), SpherePaintEditor (:315-330) and the
+ * copy tool (CopyEditorWithDecompression, :437-609, the reference's
+ * CopyEditor with its default build switches). */
 typedef enum hd_tool {
     HD_TOOL_SPHERE_REMOVE = 0,
     HD_TOOL_SPHERE_ADD = 1,
     HD_TOOL_BOX_REMOVE = 2,
-    HD_TOOL_BOX_ADD = 3
+    HD_TOOL_BOX_ADD = 3,
+    HD_TOOL_SPHERE_PAINT = 4,
+    HD_TOOL_COPY = 5
 } hd_tool;
 
 typedef struct hd_edit {
     uint32_t tool;      /* hd_tool */
-    float center[3];
+    float center[3];    /* sphere centre / box centre; copy: centre of the source region */
     float radius;       /* sphere radius, or box half extent */
+    uint32_t rgb;       /* paint: target colour r | g << 8 | b << 16 (the reference paints blue, 0xFF0000) */
+    float source[3];    /* copy: the region moves by dest - source (CopyEditor's source / dest) */
+    float dest[3];
 } hd_edit;
+
+/* CompressedColor (variable_weight_size_colors.h:86-155): 32 colour bits
+ * (rgb101210 when bits_per_weight == 0, else two rgb565 end points) and a
+ * weight of bits_per_weight bits. */
+typedef struct hd_color {
+    uint32_t color_bits;
+    uint8_t weight;
+    uint8_t bits_per_weight;
+    uint16_t reserved;
+} hd_color;
 
 /* Counters of one edit call (or a batch): the reference's EditStats
  * (hash_dag_edits.h:39-49) plus find-or-add work. */
@@ -136,6 +155,11 @@ hd_status hd_load_basic_dag(hd_ctx* ctx, const uint32_t* h_words, uint64_t n_wor
  * imported as hd_load_basic_dag does.  The words of the BasicDAG can be read
  * back with hd_export_basic_dag. */
 hd_status hd_generate_scene(hd_ctx* ctx, uint64_t seed);
+/* flags: HD_SCENE_SHELL keeps only the surface shell of the solid scene
+ * (solid voxels with an empty face neighbour; outside the volume counts as
+ * empty), the form the coloured scenes use. */
+#define HD_SCENE_SHELL 1u
+hd_status hd_generate_scene_ex(hd_ctx* ctx, uint64_t seed, uint32_t flags);
 hd_status hd_export_basic_dag(hd_ctx* ctx, uint32_t* h_words, uint64_t capacity, uint64_t* n_words);
 
 /* ---- traversal (DAGTracer, dag_tracer.cu:116-219) ---------------------- */

@@ -19,16 +19,18 @@ REF = "/root/reference"
 OUT = os.path.join(HERE, "_ref")
 
 
-def lib_path(depth, ctl, top_bits):
-    return os.path.join(OUT, f"libhdref_d{depth}_t{ctl}_b{top_bits}.so")
+def lib_path(depth, ctl, top_bits, colors=False):
+    return os.path.join(OUT, f"libhdref_d{depth}_t{ctl}_b{top_bits}{'_c' if colors else ''}.so")
 
 
 def available():
     return os.path.isdir(os.path.join(REF, "src"))
 
 
-def build(depth, ctl, top_bits, force=False):
-    out = lib_path(depth, ctl, top_bits)
+def build(depth, ctl, top_bits, force=False, colors=False):
+    """colors=True: EDITS_ENABLE_COLORS=1 and the colour entry points, linked
+    with the oracle library for the scene's colour field."""
+    out = lib_path(depth, ctl, top_bits, colors)
     if os.path.exists(out) and not force:
         return out
     if not available():
@@ -36,7 +38,8 @@ def build(depth, ctl, top_bits, force=False):
     os.makedirs(OUT, exist_ok=True)
     src = os.path.join(REF, "src")
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-w",
-           "-DBENCHMARK=1", "-DUSE_BLOOM_FILTER=0", "-DEDITS_ENABLE_COLORS=0", "-DEDITS_COUNTERS=1",
+           "-DBENCHMARK=1", "-DUSE_BLOOM_FILTER=0", f"-DEDITS_ENABLE_COLORS={1 if colors else 0}",
+           "-DEDITS_COUNTERS=1",
            "-DENABLE_CHECKS=0", "-DTRACK_GLOBAL_NEWDELETE=0",
            f"-DHARNESS_DEPTH={depth}", f"-DBUCKETS_BITS_FOR_TOP_LEVELS={top_bits}",
            f"-DC_colorTreeLevels=CTL_VALUE = {ctl}, CTL_IGNORED",
@@ -44,6 +47,10 @@ def build(depth, ctl, top_bits, force=False):
            "-I", src, "-I", os.path.join(src, "dags"), "-I", os.path.join(src, "dags", "hash_dag"),
            "-I", os.path.join(src, "gmath"), "-I", "/usr/local/cuda/include",
            os.path.join(HERE, "refharness", "ref_host.cpp"), "-o", out + ".tmp"]
+    if colors:
+        from oracle import build_oracle
+        lib = build_oracle.build()
+        cmd += ["-include", os.path.join(HERE, "hd_oracle.h"), lib, "-Wl,-rpath," + os.path.dirname(lib)]
     subprocess.check_call(cmd)
     os.replace(out + ".tmp", out)
     return out

@@ -543,6 +543,7 @@ typedef struct {
 typedef struct {
     uint64_t seed;
     uint32_t depth, leaf_level, T;
+    int shell; /* keep only solid voxels with an empty face neighbour */
     int32_t* hmin[HD_MAX_DEPTH]; /* min/max of the height over each node footprint, per level */
     int32_t* hmax[HD_MAX_DEPTH];
     int64_t spheres[256];
@@ -655,10 +656,126 @@ static uint32_t gen_full(gen_ctx* g, uint32_t level)
     return id;
 }
 
+/* Shell scenes: a node holds no shell voxel when it holds no solid voxel, or
+ * when the node grown by one voxel on every side is solid throughout (every
+ * voxel then has six solid neighbours).  Only single-source fullness is
+ * detected (the height field alone or one sphere alone), which is
+ * conservative.  live_out = spheres touching the grown node. */
+static int classify_shell(const gen_ctx* g, uint32_t level, uint32_t x0, uint32_t y0, uint32_t z0,
+                          const uint8_t* live, uint8_t* live_out)
+{
+    const uint32_t shift = g->depth - level;
+    const int64_t s = (int64_t)1 << shift, E = (int64_t)1 << g->depth;
+    const uint32_t m = 1u << level;
+    const uint32_t cx = x0 >> shift, cz = z0 >> shift;
+    int touched = (int64_t)y0 <= g->hmax[level][(uint64_t)cx * m + cz];
+    const int inside = x0 > 0 && z0 > 0 && y0 > 0 && (int64_t)x0 + s < E && (int64_t)z0 + s < E &&
+                       (int64_t)y0 + s < E;
+    int full = 0;
+    if (inside) {
+        int64_t lo = INT64_MAX;
+        for (int a = -1; a <= 1; a++)
+            for (int b = -1; b <= 1; b++) {
+                const int64_t v = g->hmin[level][(uint64_t)(cx + a) * m + (cz + b)];
+                lo = v < lo ? v : lo;
+            }
+        full = (int64_t)y0 + s <= lo;
+    }
+    for (int k = 0; k < 64; k++) {
+        live_out[k] = 0;
+        if (!live[k])
+            continue;
+        const int64_t* sp = g->spheres + 4 * k;
+        const int64_t lo3[3] = {x0, y0, z0};
+        int64_t d2in = 0, d2near = 0, d2far = 0;
+        for (int a = 0; a < 3; a++) {
+            const int64_t c = sp[a], l = lo3[a], h = lo3[a] + s - 1;
+            const int64_t din = c < l ? l - c : (c > h ? c - h : 0);
+            const int64_t dn = c < l - 1 ? l - 1 - c : (c > h + 1 ? c - h - 1 : 0);
+            const int64_t df = (c - l + 1) > (h + 1 - c) ? (c - l + 1) : (h + 1 - c);
+            d2in += din * din;
+            d2near += dn * dn;
+            d2far += df * df;
+        }
+        const int64_t r2 = sp[3] * sp[3];
+        if (d2near <= r2)
+            live_out[k] = 1;
+        if (d2in <= r2)
+            touched = 1;
+        if (inside && d2far <= r2)
+            full = 1;
+    }
+    if (!touched || full)
+        return 0;
+    return 2;
+}
+
+/* solid voxel test inside a leaf's neighbourhood: heights of the 6x6
+ * footprint around the leaf (h[(x - x0 + 1) * 6 + (z - z0 + 1)]) and the
+ * live spheres; outside the volume is empty */
+static int shell_solid(const gen_ctx* g, const int64_t* h, const uint8_t* live, uint32_t x0, uint32_t z0, int64_t x,
+                       int64_t y, int64_t z)
+{
+    const int64_t E = (int64_t)1 << g->depth;
+    if (x < 0 || y < 0 || z < 0 || x >= E || y >= E || z >= E)
+        return 0;
+    if (y <= h[(x - x0 + 1) * 6 + (z - z0 + 1)])
+        return 1;
+    for (int k = 0; k < 64; k++)
+        if (live[k] && in_sphere(g->spheres + 4 * k, x, y, z))
+            return 1;
+    return 0;
+}
+
+static uint64_t shell_leaf(const gen_ctx* g, uint32_t x0, uint32_t y0, uint32_t z0, const uint8_t* live)
+{
+    const int64_t E = (int64_t)1 << g->depth;
+    int64_t h[36];
+    for (int a = 0; a < 6; a++)
+        for (int b = 0; b < 6; b++) {
+            const int64_t x = (int64_t)x0 + a - 1, z = (int64_t)z0 + b - 1;
+            h[a * 6 + b] = (x < 0 || z < 0 || x >= E || z >= E) ? -1
+                                                                 : or_scene_height(g->seed, g->depth, (uint32_t)x,
+                                                                                   (uint32_t)z);
+        }
+    uint64_t leaf = 0;
+    for (uint32_t lx = 0; lx < 4; lx++)
+        for (uint32_t ly = 0; ly < 4; ly++)
+            for (uint32_t lz = 0; lz < 4; lz++) {
+                const int64_t x = x0 + lx, y = y0 + ly, z = z0 + lz;
+                if (!shell_solid(g, h, live, x0, z0, x, y, z))
+                    continue;
+                if (shell_solid(g, h, live, x0, z0, x + 1, y, z) && shell_solid(g, h, live, x0, z0, x - 1, y, z) &&
+                    shell_solid(g, h, live, x0, z0, x, y + 1, z) && shell_solid(g, h, live, x0, z0, x, y - 1, z) &&
+                    shell_solid(g, h, live, x0, z0, x, y, z + 1) && shell_solid(g, h, live, x0, z0, x, y, z - 1))
+                    continue;
+                const uint32_t c1 = ((lx >> 1) << 2) | ((ly >> 1) << 1) | (lz >> 1);
+                const uint32_t c2 = ((lx & 1) << 2) | ((ly & 1) << 1) | (lz & 1);
+                leaf |= 1ull << (c1 * 8 + c2);
+            }
+    return leaf;
+}
+
+int or_scene_shell(uint64_t seed, uint32_t depth, uint32_t x, uint32_t y, uint32_t z)
+{
+    const int64_t E = (int64_t)1 << depth;
+    const int64_t d[7][3] = {{0, 0, 0}, {1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+    int s[7];
+    for (int k = 0; k < 7; k++) {
+        const int64_t a = (int64_t)x + d[k][0], b = (int64_t)y + d[k][1], c = (int64_t)z + d[k][2];
+        s[k] = (a < 0 || b < 0 || c < 0 || a >= E || b >= E || c >= E)
+                   ? 0
+                   : or_scene_solid(seed, depth, (uint32_t)a, (uint32_t)b, (uint32_t)c);
+    }
+    return s[0] && !(s[1] && s[2] && s[3] && s[4] && s[5] && s[6]);
+}
+
 /* 0 = empty, 1 = full, 2 = maybe mixed */
 static int classify(const gen_ctx* g, uint32_t level, uint32_t x0, uint32_t y0, uint32_t z0,
                     const uint8_t* live, uint8_t* live_out)
 {
+    if (g->shell)
+        return classify_shell(g, level, x0, y0, z0, live, live_out);
     const uint32_t shift = g->depth - level;
     const int64_t s = (int64_t)1 << shift;
     const uint64_t cell = ((uint64_t)(x0 >> shift) << level) | (z0 >> shift);
@@ -707,6 +824,13 @@ static uint32_t gen_build(gen_ctx* g, uint32_t level, uint32_t x0, uint32_t y0, 
         *count = (uint64_t)1 << (3 * (g->depth - level));
         return gen_full(g, level);
     }
+    if (level == g->leaf_level && g->shell) {
+        const uint64_t leaf = shell_leaf(g, x0, y0, z0, live2);
+        *count = popc64(leaf);
+        if (!leaf)
+            return GEN_EMPTY;
+        return level_insert(&g->lv[level], 1, 0, *count, leaf, NULL);
+    }
     if (level == g->leaf_level) {
         uint64_t leaf = 0;
         for (uint32_t lx = 0; lx < 4; lx++)
@@ -754,10 +878,16 @@ static uint32_t gen_build(gen_ctx* g, uint32_t level, uint32_t x0, uint32_t y0, 
 
 uint32_t* or_generate_basic_dag(uint64_t seed, uint32_t depth, uint32_t T, uint64_t* n_words)
 {
+    return or_generate_basic_dag_ex(seed, depth, T, 0, n_words);
+}
+
+uint32_t* or_generate_basic_dag_ex(uint64_t seed, uint32_t depth, uint32_t T, uint32_t flags, uint64_t* n_words)
+{
     if (depth < 6 || depth > 16 || T > depth - 2)
         return NULL;
     gen_ctx* g = (gen_ctx*)calloc(1, sizeof(gen_ctx));
     g->seed = seed;
+    g->shell = (flags & HD_SCENE_SHELL) != 0;
     g->depth = depth;
     g->leaf_level = depth - 2;
     g->T = T;
@@ -1407,6 +1537,315 @@ void or_trace_frame_mt(const or_table* t, const hd_camera* cam, uint32_t W, uint
 }
 
 /* ======================================================================
+ * Colours: CompressedColor and the colour conversions (color_utils.h,
+ * variable_weight_size_colors.h:86-155), ColorLeafBuilder (:557-689),
+ * CompressedColorLeaf decoding (:343-551) with CFG_COLOR_SWAP_BYTE_ORDER=1
+ * (typedefs.h:516), the HashDAGColors tree (hash_dag_colors.h:24-55).
+ * ====================================================================== */
+
+#define CPM 16384u /* CColorsPerMacroBlock (variable_weight_size_colors.h:8) */
+#define LEAF_FLAG 0x80000000u /* Utils::set_flag (utils.h:37-51) */
+
+static float clampf(float f, float a, float b) { return f < a ? a : f > b ? b : f; }
+
+/* ColorUtils (color_utils.h:9-75) */
+static uint16_t f3_to_rgb565(f3 c)
+{
+    const float r = clampf(c.x, 0.f, 1.f), g = clampf(c.y, 0.f, 1.f), b = clampf(c.z, 0.f, 1.f);
+    return (uint16_t)(((uint16_t)(r * 31.0f) << 0) | ((uint16_t)(g * 63.0f) << 5) | ((uint16_t)(b * 31.0f) << 11));
+}
+static f3 rgb565_to_f3(uint16_t v)
+{
+    return (f3){(float)((v >> 0) & 0x1F) / 31.0f, (float)((v >> 5) & 0x3F) / 63.0f, (float)((v >> 11) & 0x1F) / 31.0f};
+}
+static uint32_t f3_to_rgb101210(f3 c)
+{
+    const float r = clampf(c.x, 0.f, 1.f), g = clampf(c.y, 0.f, 1.f), b = clampf(c.z, 0.f, 1.f);
+    return ((uint32_t)(r * 1023.0f) << 0) | ((uint32_t)(g * 4095.0f) << 10) | ((uint32_t)(b * 1023.0f) << 22);
+}
+static f3 rgb101210_to_f3(uint32_t v)
+{
+    return (f3){(float)((v >> 0) & 0x3FF) / 1023.0f, (float)((v >> 10) & 0xFFF) / 4095.0f,
+                (float)((v >> 22) & 0x3FF) / 1023.0f};
+}
+uint32_t or_f3_to_rgb888(float x, float y, float z)
+{
+    const float r = clampf(x, 0.f, 1.f), g = clampf(y, 0.f, 1.f), b = clampf(z, 0.f, 1.f);
+    return ((uint32_t)(r * 255.0f) << 0) | ((uint32_t)(g * 255.0f) << 8) | ((uint32_t)(b * 255.0f) << 16) |
+           0xff000000u;
+}
+/* CompressedColor::set_single_color / get_color (:127-154); lerp is
+ * a * (1 - f) + b * f (cuda_math.h:22) */
+static hd_color single_color(f3 c)
+{
+    hd_color k;
+    memset(&k, 0, sizeof(k));
+    k.color_bits = f3_to_rgb101210(c);
+    return k;
+}
+static f3 color_value(hd_color k)
+{
+    if (k.bits_per_weight == 0)
+        return rgb101210_to_f3(k.color_bits);
+    const f3 lo = rgb565_to_f3((uint16_t)(k.color_bits & 0xFFFF));
+    const f3 hi = rgb565_to_f3((uint16_t)((k.color_bits >> 16) & 0xFFFF));
+    const float w = (float)k.weight / (float)((1 << k.bits_per_weight) - 1);
+    return (f3){lo.x * (1 - w) + hi.x * w, lo.y * (1 - w) + hi.y * w, lo.z * (1 - w) + hi.z * w};
+}
+uint32_t or_color_rgb888(hd_color k)
+{
+    const f3 c = color_value(k);
+    return or_f3_to_rgb888(c.x, c.y, c.z);
+}
+
+/* Scene colours: RGB8 from a seeded value-noise field sampled on an aligned
+ * 8^3 grid (lattice period 16 cells, trilinear with integer weights), each
+ * voxel stored as set_single_color(rgb / 255). */
+static uint32_t color_lattice(uint64_t seed, uint32_t c, uint32_t i, uint32_t j, uint32_t k)
+{
+    return (uint32_t)(mix64(seed ^ mix64(((uint64_t)c << 60) ^ ((uint64_t)i << 40) ^ ((uint64_t)j << 20) ^ k)) >> 56);
+}
+uint32_t or_color_rgb8(uint64_t seed, uint32_t x, uint32_t y, uint32_t z)
+{
+    const uint32_t cx = x >> 3, cy = y >> 3, cz = z >> 3;
+    const uint32_t i = cx >> 4, j = cy >> 4, k = cz >> 4;
+    const uint32_t fx = cx & 15, fy = cy & 15, fz = cz & 15;
+    uint32_t out = 0;
+    for (uint32_t c = 0; c < 3; c++) {
+        uint32_t acc = 0;
+        for (uint32_t a = 0; a < 2; a++)
+            for (uint32_t b = 0; b < 2; b++)
+                for (uint32_t d = 0; d < 2; d++) {
+                    const uint32_t w = (a ? fx : 16 - fx) * (b ? fy : 16 - fy) * (d ? fz : 16 - fz);
+                    acc += color_lattice(seed, c, i + a, j + b, k + d) * w;
+                }
+        out |= ((acc + 2048) >> 12) << (8 * c);
+    }
+    return out;
+}
+hd_color or_voxel_color(uint64_t seed, uint32_t x, uint32_t y, uint32_t z)
+{
+    const uint32_t rgb = or_color_rgb8(seed, x, y, z);
+    return single_color((f3){(float)(rgb & 0xFF) / 255.0f, (float)((rgb >> 8) & 0xFF) / 255.0f,
+                             (float)((rgb >> 16) & 0xFF) / 255.0f});
+}
+
+/* CompressedColorLeaf, always unique here: blocks (colour bits << 32 |
+ * header), byte-swapped weight words, macro blocks (first block, weight
+ * offset) */
+typedef struct {
+    uint64_t* blocks;
+    uint64_t nb;
+    uint32_t* weights; /* + one padding word: extract_bits reads two bytes */
+    uint64_t nw;
+    uint64_t* macros; /* 2 words per macro block */
+    uint64_t nm;      /* words */
+} or_leaf;
+
+/* ColorLeafBuilder (:557-689) */
+typedef struct {
+    uint32_t bits, color_bits, weight_offset, index;
+} bblock;
+typedef struct {
+    uint32_t start_weight, start_block;
+} bmacro;
+typedef struct {
+    bblock* blocks;
+    uint64_t nb, cb;
+    uint32_t* weights;
+    uint64_t nw, cw;
+    bmacro* macros;
+    uint64_t nm, cm;
+    uint32_t num_weights, target_bit_pos, color_index, last_bits, last_color_bits, last_macro_color,
+        last_macro_weight;
+} or_builder;
+
+#define GROW(ptr, n, cap, T)                                                \
+    do {                                                                    \
+        if ((n) == (cap)) {                                                 \
+            (cap) = (cap) ? 2 * (cap) : 16;                                 \
+            (ptr) = (T*)realloc((ptr), (size_t)(cap) * sizeof(T));          \
+        }                                                                   \
+    } while (0)
+
+static void builder_free(or_builder* b)
+{
+    free(b->blocks);
+    free(b->weights);
+    free(b->macros);
+    memset(b, 0, sizeof(*b));
+}
+static void add_weight(or_builder* b, uint32_t weight, uint32_t bits)
+{
+    const uint32_t target = (b->target_bit_pos + 32 - bits) % 64;
+    const uint64_t ww = (uint64_t)weight << target;
+    if (target > (uint32_t)(32 - bits)) {
+        b->weights[b->nw - 1] |= (uint32_t)(ww >> 32);
+        b->target_bit_pos -= bits;
+    }
+    if (target < 32) {
+        GROW(b->weights, b->nw, b->cw, uint32_t);
+        b->weights[b->nw++] = (uint32_t)(ww & 0xFFFFFFFFu);
+        b->target_bit_pos = target;
+    }
+    b->num_weights += bits;
+}
+static void builder_add(or_builder* b, hd_color k)
+{
+    if (b->color_index % CPM == 0) {
+        b->last_macro_color = b->color_index;
+        b->last_macro_weight = b->num_weights;
+        GROW(b->macros, b->nm, b->cm, bmacro);
+        b->macros[b->nm++] = (bmacro){b->num_weights, (uint32_t)b->nb};
+    }
+    if (b->color_index % CPM == 0 || b->last_color_bits != k.color_bits || b->last_bits != k.bits_per_weight) {
+        b->last_color_bits = k.color_bits;
+        b->last_bits = k.bits_per_weight;
+        GROW(b->blocks, b->nb, b->cb, bblock);
+        b->blocks[b->nb++] = (bblock){k.bits_per_weight, k.color_bits, b->num_weights - b->last_macro_weight,
+                                      b->color_index - b->last_macro_color};
+    }
+    if (k.bits_per_weight > 0)
+        add_weight(b, k.weight, k.bits_per_weight);
+    b->color_index++;
+}
+/* add_large_single_color (:626-656) */
+static void builder_add_large(or_builder* b, f3 c, uint32_t n)
+{
+    const hd_color k = single_color(c);
+    uint32_t left = n;
+    while (left > 0) {
+        const uint32_t in_macro = CPM - (b->color_index % CPM);
+        const uint32_t add = in_macro < left ? in_macro : left;
+        left -= add;
+        builder_add(b, k);
+        b->color_index += add - 1;
+    }
+}
+static uint32_t swap32(uint32_t v)
+{
+    return ((v & 0xffu) << 24) | ((v & 0xff00u) << 8) | ((v & 0xff0000u) >> 8) | ((v & 0xff000000u) >> 24);
+}
+/* VariableColorsUtils::make_block_header (:31-52) */
+static uint32_t make_block_header(uint32_t weight_offset, uint32_t bits, uint32_t index)
+{
+    if (bits == 0)
+        weight_offset = 0xFFFF;
+    else
+        bits--;
+    return (weight_offset << 16) | (bits << 14) | index;
+}
+/* ColorLeafBuilder::build (:658-689) */
+static void builder_build(const or_builder* b, or_leaf* leaf)
+{
+    leaf->nb = b->nb;
+    leaf->blocks = (uint64_t*)malloc((b->nb + 1) * 8);
+    for (uint64_t i = 0; i < b->nb; i++)
+        leaf->blocks[i] = ((uint64_t)b->blocks[i].color_bits << 32) |
+                          make_block_header(b->blocks[i].weight_offset, b->blocks[i].bits, b->blocks[i].index);
+    leaf->nw = b->nw;
+    leaf->weights = (uint32_t*)calloc(b->nw + 1, 4);
+    for (uint64_t i = 0; i < b->nw; i++)
+        leaf->weights[i] = swap32(b->weights[i]);
+    leaf->nm = 2 * b->nm;
+    leaf->macros = (uint64_t*)malloc((leaf->nm + 1) * 8);
+    for (uint64_t i = 0; i < b->nm; i++) {
+        leaf->macros[2 * i + 0] = b->macros[i].start_block;
+        leaf->macros[2 * i + 1] = b->macros[i].start_weight;
+    }
+}
+
+/* VariableColorsUtils header fields (:10-30) */
+static uint32_t hdr_index(uint32_t h) { return h & (CPM - 1); }
+static uint32_t hdr_weight_offset(uint32_t h) { return h >> 16; }
+static uint32_t hdr_bits(uint32_t h) { return hdr_weight_offset(h) == 0xFFFF ? 0 : ((h >> 14) & 3) + 1; }
+
+/* ColorUtils::extract_bits, byte-swapped layout (color_utils.h:115-145) */
+static uint32_t extract_bits(uint32_t bits, const uint32_t* words, uint64_t bit_ptr)
+{
+    if (bits == 0)
+        return 0;
+    const uint8_t* bytes = (const uint8_t*)words;
+    const uint64_t byte = bit_ptr / 8;
+    uint16_t dst = (uint16_t)(bytes[byte] | ((uint16_t)bytes[byte + 1] << 8));
+    dst = (uint16_t)((dst << 8) | (dst >> 8));
+    const uint32_t shift = 16 - bits - (uint32_t)(bit_ptr % 8);
+    return (uint32_t)((dst >> shift) & ((1u << bits) - 1));
+}
+/* binary_search_blocks (:414-443) */
+static uint32_t leaf_search(const or_leaf* l, uint64_t ci)
+{
+    const uint32_t local = (uint32_t)(ci % CPM);
+    const uint64_t m = ci / CPM;
+    uint32_t lo = (uint32_t)l->macros[2 * m];
+    uint32_t hi = 2 * (m + 1) < l->nm ? (uint32_t)l->macros[2 * (m + 1)] - 1 : (uint32_t)(l->nb - 1);
+    uint32_t pos = (lo + hi) / 2;
+    uint32_t h = (uint32_t)l->blocks[pos];
+    while (hdr_index(h) != local && lo <= hi) {
+        if (hdr_index(h) > local)
+            hi = pos - 1;
+        else
+            lo = pos + 1;
+        pos = (lo + hi) / 2;
+        h = (uint32_t)l->blocks[pos];
+    }
+    return pos;
+}
+/* get_color_for_block / get_color (:445-486) */
+static hd_color leaf_color(const or_leaf* l, uint64_t ci)
+{
+    const uint32_t pos = leaf_search(l, ci);
+    const uint64_t block = l->blocks[pos];
+    const uint32_t h = (uint32_t)block;
+    hd_color k;
+    memset(&k, 0, sizeof(k));
+    k.color_bits = (uint32_t)(block >> 32);
+    k.bits_per_weight = (uint8_t)hdr_bits(h);
+    if (k.bits_per_weight) {
+        const uint64_t local = ci % CPM, m = ci / CPM;
+        const uint64_t wi = l->macros[2 * m + 1] + hdr_weight_offset(h) + (local - hdr_index(h)) * k.bits_per_weight;
+        k.weight = (uint8_t)extract_bits(k.bits_per_weight, l->weights, wi);
+    }
+    return k;
+}
+static int leaf_valid_index(const or_leaf* l, uint64_t ci) { return l && l->blocks && 2 * ci / CPM < l->nm; }
+
+/* HashDAGColors: interior colour nodes of 8 entries; an entry with
+ * LEAF_FLAG is a leaf index.  Every leaf here is unique (the reference's
+ * import shares one main leaf through offsets; decoded colours are the
+ * same). */
+struct or_colors {
+    uint32_t* nodes;
+    uint64_t n_nodes, cap_nodes;
+    or_leaf* leaves;
+    uint64_t n_leaves, cap_leaves;
+    /* HashDAGUndoRedo (hash_dag.h:20-212) */
+    struct frame {
+        uint32_t root;
+        uint32_t n;
+        uint32_t* index;
+        or_leaf* prev;
+        or_leaf* next;
+    } *undo, *redo;
+    uint64_t n_undo, cap_undo, n_redo, cap_redo;
+};
+
+static uint32_t colors_alloc_node(or_colors* c)
+{
+    for (int k = 0; k < 8; k++) {
+        GROW(c->nodes, c->n_nodes, c->cap_nodes, uint32_t);
+        c->nodes[c->n_nodes++] = 0;
+    }
+    return (uint32_t)(c->n_nodes - 8);
+}
+static uint32_t colors_alloc_leaf(or_colors* c)
+{
+    GROW(c->leaves, c->n_leaves, c->cap_leaves, or_leaf);
+    memset(&c->leaves[c->n_leaves], 0, sizeof(or_leaf));
+    return (uint32_t)(c->n_leaves++) | LEAF_FLAG;
+}
+
+/* ======================================================================
  * Editors (hash_dag_editors.h) and the edit recursion (hash_dag_edits.h)
  * ====================================================================== */
 
@@ -1415,6 +1854,14 @@ typedef struct {
     f3 c;        /* sphere centre */
     float r, r2; /* radius, radius * radius (SphereEditorBase, :99-110) */
     f3 bmin, bmax; /* box bounds (BoxEditorBase, :57-75) */
+    f3 paint;    /* SpherePaintEditor's target colour (the reference: blue) */
+    /* CopyEditorWithDecompression (:437-609): source / dest, the source
+     * region's lower corner (copyMin) and its occupancy and colours read
+     * before the edit (values / colors, size^3, x fastest) */
+    f3 src, dst, copy_min;
+    uint32_t size;
+    uint8_t* values;
+    hd_color* colors;
 } editor;
 
 static editor make_editor(const hd_edit* e)
@@ -1425,12 +1872,42 @@ static editor make_editor(const hd_edit* e)
     ed.c = (f3){e->center[0], e->center[1], e->center[2]};
     ed.r = e->radius;
     ed.r2 = e->radius * e->radius;
-    ed.bmin = (f3){e->center[0] - e->radius, e->center[1] - e->radius, e->center[2] - e->radius};
-    ed.bmax = (f3){e->center[0] + e->radius, e->center[1] + e->radius, e->center[2] + e->radius};
+    f3 bc = ed.c;
+    if (e->tool == HD_TOOL_COPY) {
+        /* BoxEditorBase(center - source + dest, radius) */
+        ed.src = (f3){e->source[0], e->source[1], e->source[2]};
+        ed.dst = (f3){e->dest[0], e->dest[1], e->dest[2]};
+        bc = (f3){ed.c.x - ed.src.x + ed.dst.x, ed.c.y - ed.src.y + ed.dst.y, ed.c.z - ed.src.z + ed.dst.z};
+        ed.copy_min = (f3){ed.c.x - ed.r, ed.c.y - ed.r, ed.c.z - ed.r};
+        ed.size = 2 * (uint32_t)ceilf(ed.r);
+    }
+    ed.bmin = (f3){bc.x - e->radius, bc.y - e->radius, bc.z - e->radius};
+    ed.bmax = (f3){bc.x + e->radius, bc.y + e->radius, bc.z + e->radius};
+    ed.paint = (f3){(float)(e->rgb & 0xFF) / 255.0f, (float)((e->rgb >> 8) & 0xFF) / 255.0f,
+                    (float)((e->rgb >> 16) & 0xFF) / 255.0f};
     return ed;
 }
-static int is_sphere(const editor* e) { return e->tool == HD_TOOL_SPHERE_ADD || e->tool == HD_TOOL_SPHERE_REMOVE; }
+static int is_sphere(const editor* e)
+{
+    return e->tool == HD_TOOL_SPHERE_ADD || e->tool == HD_TOOL_SPHERE_REMOVE || e->tool == HD_TOOL_SPHERE_PAINT;
+}
 static int is_adding(const editor* e) { return e->tool == HD_TOOL_SPHERE_ADD || e->tool == HD_TOOL_BOX_ADD; }
+/* is_full / is_empty exist for the sphere and box editors only (the base
+ * Editor returns false, :30-37) */
+static int has_shortcuts(const editor* e) { return e->tool <= HD_TOOL_BOX_ADD; }
+/* get_single_color (:256-259, :297-300) */
+static f3 single_of(const editor* e) { return is_sphere(e) ? (f3){1, 0, 0} : (f3){1, 0, 1}; }
+/* the copy tool's source index of a destination voxel, or -1 (:585-606) */
+static int64_t copy_index(const editor* e, f3 pos)
+{
+    const f3 q = {((pos.x - e->dst.x) + e->src.x) - e->copy_min.x, ((pos.y - e->dst.y) + e->src.y) - e->copy_min.y,
+                  ((pos.z - e->dst.z) + e->src.z) - e->copy_min.z};
+    const uint32_t px = (uint32_t)(q.x < 0 ? 0 : q.x), py = (uint32_t)(q.y < 0 ? 0 : q.y),
+                   pz = (uint32_t)(q.z < 0 ? 0 : q.z);
+    if (px >= e->size || py >= e->size || pz >= e->size)
+        return -1;
+    return (int64_t)px + (int64_t)e->size * py + (int64_t)e->size * e->size * pz;
+}
 
 static float sq(float f) { return f * f; }
 
@@ -1477,7 +1954,59 @@ typedef struct {
     or_table* t;
     editor ed;
     uint64_t num_voxels, num_nodes;
+    /* colours (NULL: off): the current task's builder, its old leaf and
+     * the running oldLeavesCount (LeafEditParameters, hash_dag_edits.h:67-78) */
+    or_colors* col;
+    or_builder* b;
+    const or_leaf* old;
+    uint64_t old_count;
+    /* rebuilt leaves of this edit, for the undo frame */
+    uint32_t n_diff, cap_diff;
+    uint32_t* diff_index;
+    or_leaf* diff_prev;
+    or_leaf* diff_next;
 } edit_job;
+
+static hd_color prev_color(edit_job* j, int prev)
+{
+    hd_color k;
+    memset(&k, 0, sizeof(k));
+    if (prev && j->old && leaf_valid_index(j->old, j->old_count))
+        k = leaf_color(j->old, j->old_count);
+    return k;
+}
+static int new_value(const editor* e, f3 pos, int prev)
+{
+    if (e->tool == HD_TOOL_SPHERE_PAINT)
+        return prev;
+    if (e->tool == HD_TOOL_COPY) {
+        if (prev)
+            return prev;
+        const int64_t i = copy_index(e, pos);
+        return i < 0 ? prev : e->values[i];
+    }
+    return is_adding(e);
+}
+/* get_new_color of each editor (:262-269, :302-312, :323-329, :595-608) */
+static hd_color new_color(edit_job* j, f3 pos, int prev, int nv)
+{
+    const editor* e = &j->ed;
+    if (e->tool == HD_TOOL_SPHERE_PAINT) {
+        const f3 old = color_value(prev_color(j, prev));
+        const f3 d = {pos.x - e->c.x, pos.y - e->c.y, pos.z - e->c.z};
+        const float len = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+        const float f = clampf(1 - len / e->r, 0.f, .1f);
+        return single_color((f3){old.x * (1 - f) + e->paint.x * f, old.y * (1 - f) + e->paint.y * f,
+                                 old.z * (1 - f) + e->paint.z * f});
+    }
+    if (e->tool == HD_TOOL_COPY) {
+        if (prev == nv || !nv)
+            return prev_color(j, prev);
+        const int64_t i = copy_index(e, pos);
+        return i < 0 ? prev_color(j, prev) : e->colors[i];
+    }
+    return single_color(single_of(e));
+}
 
 static void descend(const uint32_t in[3], uint32_t c, uint32_t out[3])
 {
@@ -1495,23 +2024,33 @@ static uint32_t edit_leaf(edit_job* j, uint32_t level, uint32_t index, const uin
     f3 mn, mx;
     node_box(path, D - level, &mn, &mx);
     const uint32_t full_count = 1u << (3 * (D - level));
+    uint32_t old_count = 0;
+    if (index != INVALID) {
+        const uint32_t* p = sys_ptr(t, index);
+        old_count = level < leafl ? p[0] >> 8 : popc32(p[0]) + popc32(p[1]);
+    }
     if (!should_edit_impl(&j->ed, mn, mx)) {
-        uint32_t count = 0;
-        if (index != INVALID) {
-            const uint32_t* p = sys_ptr(t, index);
-            count = level < leafl ? p[0] >> 8 : popc32(p[0]) + popc32(p[1]);
+        if (j->b && index != INVALID) { /* copy_colors (:380-392) */
+            for (uint32_t k = 0; k < old_count; k++)
+                builder_add(j->b, prev_color(j, 1)), j->old_count++;
         }
-        *count_out = count;
+        *count_out = old_count;
         return index;
     }
-    const int inside = inside_tool(&j->ed, mn, mx);
+    const int inside = has_shortcuts(&j->ed) && inside_tool(&j->ed, mn, mx);
     if (!is_adding(&j->ed) && inside) { /* is_empty */
         j->num_voxels += full_count;
+        if (j->b)
+            j->old_count += old_count;
         *count_out = 0;
         return INVALID;
     }
     if (is_adding(&j->ed) && inside) { /* is_full */
         j->num_voxels += full_count;
+        if (j->b) {
+            j->old_count += old_count;
+            builder_add_large(j->b, single_of(&j->ed), full_count);
+        }
         *count_out = full_count;
         return t->full[level];
     }
@@ -1533,8 +2072,13 @@ static uint32_t edit_leaf(edit_job* j, uint32_t level, uint32_t index, const uin
                 const uint64_t bit = 1ull << (c1 * 8 + c2);
                 const int se = should_edit_impl(&j->ed, pos, pos1);
                 const int prev = (leaf & bit) != 0;
-                const int nv = se ? is_adding(&j->ed) : prev;
+                const int nv = se ? new_value(&j->ed, pos, prev) : prev;
                 j->num_voxels += (uint64_t)se;
+                if (j->b) {
+                    if (nv)
+                        builder_add(j->b, se ? new_color(j, pos, prev, nv) : prev_color(j, prev));
+                    j->old_count += (uint64_t)prev;
+                }
                 if (prev != nv) {
                     if (nv)
                         leaf |= bit;
@@ -1594,19 +2138,42 @@ static uint32_t edit_leaf(edit_job* j, uint32_t level, uint32_t index, const uin
     return or_find_or_add_interior(t, level, n, node);
 }
 
+#define COLOR_IGNORE 0xFFFFFFFu /* HashDagEdits::C_IgnoreColorIndex (hash_dag_edits.h:15) */
+
+static void push_diff(edit_job* j, uint32_t leaf_ref, const or_leaf* prev, const or_leaf* next)
+{
+    if (j->n_diff == j->cap_diff) {
+        j->cap_diff = j->cap_diff ? 2 * j->cap_diff : 16;
+        j->diff_index = (uint32_t*)realloc(j->diff_index, j->cap_diff * 4);
+        j->diff_prev = (or_leaf*)realloc(j->diff_prev, j->cap_diff * sizeof(or_leaf));
+        j->diff_next = (or_leaf*)realloc(j->diff_next, j->cap_diff * sizeof(or_leaf));
+    }
+    j->diff_index[j->n_diff] = leaf_ref;
+    j->diff_prev[j->n_diff] = *prev;
+    j->diff_next[j->n_diff] = *next;
+    j->n_diff++;
+}
+
 /* HashDagEdits::edit_threaded (hash_dag_edits.h:106-333) with both passes
- * folded into one depth-first recursion (tasks run in depth-first order). */
-static uint32_t edit_top(edit_job* j, uint32_t level, uint32_t index, const uint32_t path[3])
+ * folded into one depth-first recursion (tasks run in depth-first order;
+ * each task owns one colour leaf, so running it in place is the same as
+ * running it between the passes).  cn: this node's colour node (0 = none,
+ * except at the root); *cn_out: the colour index reported to the parent. */
+static uint32_t edit_top(edit_job* j, uint32_t level, uint32_t index, const uint32_t path[3], uint32_t cn,
+                         uint32_t* cn_out)
 {
     or_table* t = j->t;
     const uint32_t D = t->cfg.depth, T = t->cfg.color_tree_levels;
+    or_colors* col = j->col;
     /* the reference runs this recursion twice (queue pass, build pass) and
      * counts the node in both (hash_dag_edits.h:120, hash_dag.h:287, :358) */
     j->num_nodes += 2;
     f3 mn, mx;
     node_box(path, D - level, &mn, &mx);
-    if (!should_edit_impl(&j->ed, mn, mx))
+    if (!should_edit_impl(&j->ed, mn, mx)) {
+        *cn_out = COLOR_IGNORE;
         return index;
+    }
     uint32_t mask = 0;
     const uint32_t* p = NULL;
     if (index != INVALID) {
@@ -1619,26 +2186,66 @@ static uint32_t edit_top(edit_job* j, uint32_t level, uint32_t index, const uint
         uint32_t np[3];
         descend(path, c, np);
         const uint32_t old = (mask & (1u << c)) ? p[off++] : INVALID;
+        uint32_t ccn = 0;
+        if (col && (level == 0 || cn > 0))
+            ccn = col->nodes[cn + c];
         uint32_t nk;
         if (level == T - 1) {
             f3 cmn, cmx;
             node_box(np, D - level - 1, &cmn, &cmx);
             if (should_edit_impl(&j->ed, cmn, cmx)) {
                 uint32_t cc;
-                nk = edit_leaf(j, T, old, np, &cc);
+                if (col) {
+                    or_builder b;
+                    memset(&b, 0, sizeof(b));
+                    const or_leaf* old_leaf = (ccn > 0 && (ccn & LEAF_FLAG)) ? &col->leaves[ccn & ~LEAF_FLAG] : NULL;
+                    or_leaf prev;
+                    memset(&prev, 0, sizeof(prev));
+                    if (old_leaf)
+                        prev = *old_leaf;
+                    j->b = &b;
+                    j->old = old_leaf ? &prev : NULL;
+                    j->old_count = 0;
+                    nk = edit_leaf(j, T, old, np, &cc);
+                    j->b = NULL;
+                    j->old = NULL;
+                    if (b.color_index > 0) { /* hash_dag_edits.h:218-241 */
+                        if (ccn == 0 || !(ccn & LEAF_FLAG)) {
+                            if (cn == 0)
+                                cn = colors_alloc_node(col);
+                            ccn = colors_alloc_leaf(col);
+                            col->nodes[cn + c] = ccn;
+                        }
+                        or_leaf next;
+                        builder_build(&b, &next);
+                        col->leaves[ccn & ~LEAF_FLAG] = next;
+                        push_diff(j, ccn, &prev, &next);
+                    }
+                    builder_free(&b);
+                } else {
+                    nk = edit_leaf(j, T, old, np, &cc);
+                }
             } else {
                 nk = old;
             }
         } else {
-            nk = edit_top(j, level + 1, old, np);
+            uint32_t child_cn;
+            nk = edit_top(j, level + 1, old, np, ccn, &child_cn);
+            if (col && child_cn != ccn && child_cn != COLOR_IGNORE) { /* :278-292 */
+                if (level > 0 && cn == 0)
+                    cn = colors_alloc_node(col);
+                col->nodes[cn + c] = child_cn;
+            }
         }
         if (t->error)
             return INVALID;
         changed |= old != nk;
         kids[c] = nk;
     }
-    if (!changed)
+    if (!changed) {
+        *cn_out = cn;
         return index;
+    }
     uint32_t node[9], n = 0;
     node[n++] = 0;
     for (uint32_t c = 0; c < 8; c++)
@@ -1646,8 +2253,11 @@ static uint32_t edit_top(edit_job* j, uint32_t level, uint32_t index, const uint
             node[n++] = kids[c];
             node[0] |= 1u << c;
         }
-    if ((node[0] & 0xffu) == 0)
+    if ((node[0] & 0xffu) == 0) {
+        *cn_out = COLOR_IGNORE;
         return INVALID;
+    }
+    *cn_out = cn;
     return or_find_or_add_interior(t, level, n, node);
 }
 
@@ -1659,12 +2269,14 @@ int or_edit(or_table* t, const hd_edit* e, hd_edit_stats* stats)
     j.ed = make_editor(e);
     t->foa_calls = t->nodes_added = t->words_scanned = 0;
     const uint32_t path[3] = {0, 0, 0};
-    uint32_t root;
+    uint32_t root, cn;
+    if (e->tool > HD_TOOL_BOX_ADD) /* paint and copy need colours */
+        return HD_ERR_INVALID;
     if (t->cfg.color_tree_levels == 0) {
         uint32_t cc;
         root = edit_leaf(&j, 0, t->root, path, &cc);
     } else {
-        root = edit_top(&j, 0, t->root, path);
+        root = edit_top(&j, 0, t->root, path, 0, &cn);
     }
     if (!t->error)
         t->root = root;
@@ -1677,6 +2289,257 @@ int or_edit(or_table* t, const hd_edit* e, hd_edit_stats* stats)
         stats->words_scanned = t->words_scanned;
     }
     return t->error;
+}
+
+/* ---- colour API ---------------------------------------------------- */
+
+or_colors* or_colors_create(void) { return (or_colors*)calloc(1, sizeof(or_colors)); }
+
+static void free_frames(struct frame* f, uint64_t n)
+{
+    for (uint64_t i = 0; i < n; i++) {
+        free(f[i].index);
+        free(f[i].prev);
+        free(f[i].next);
+    }
+}
+void or_colors_destroy(or_colors* c)
+{
+    if (!c)
+        return;
+    /* leaf arrays may be shared by undo frames and the tree; the oracle
+     * keeps every leaf it ever built until the process ends */
+    free_frames(c->undo, c->n_undo);
+    free_frames(c->redo, c->n_redo);
+    free(c->undo);
+    free(c->redo);
+    free(c->nodes);
+    free(c->leaves);
+    free(c);
+}
+
+static void leaf_voxels(const or_table* t, uint32_t level, uint32_t index, const uint32_t path[3], uint64_t seed,
+                        or_builder* b)
+{
+    const uint32_t* p = sys_ptr(t, index);
+    if (level == t->leaf_level) {
+        const uint64_t leaf = (uint64_t)p[0] | ((uint64_t)p[1] << 32);
+        for (uint32_t bit = 0; bit < 64; bit++) {
+            if (!((leaf >> bit) & 1))
+                continue;
+            const uint32_t c1 = bit >> 3, c2 = bit & 7;
+            const uint32_t x = (path[0] << 2) | (((c1 >> 2) & 1) << 1) | ((c2 >> 2) & 1);
+            const uint32_t y = (path[1] << 2) | (((c1 >> 1) & 1) << 1) | ((c2 >> 1) & 1);
+            const uint32_t z = (path[2] << 2) | ((c1 & 1) << 1) | (c2 & 1);
+            builder_add(b, or_voxel_color(seed, x, y, z));
+        }
+        return;
+    }
+    const uint32_t mask = p[0] & 0xffu;
+    uint32_t off = 1;
+    for (uint32_t c = 0; c < 8; c++) {
+        if (!(mask & (1u << c)))
+            continue;
+        uint32_t np[3];
+        descend(path, c, np);
+        leaf_voxels(t, level + 1, p[off++], np, seed, b);
+    }
+}
+static uint32_t colors_tree(const or_table* t, or_colors* col, uint32_t level, uint32_t index, const uint32_t path[3],
+                            uint64_t seed)
+{
+    const uint32_t T = t->cfg.color_tree_levels;
+    const uint32_t cn = colors_alloc_node(col);
+    const uint32_t* p = sys_ptr(t, index);
+    const uint32_t mask = p[0] & 0xffu;
+    uint32_t off = 1;
+    for (uint32_t c = 0; c < 8; c++) {
+        if (!(mask & (1u << c)))
+            continue;
+        const uint32_t child = sys_ptr(t, index)[off++];
+        uint32_t np[3];
+        descend(path, c, np);
+        if (level == T - 1) {
+            or_builder b;
+            memset(&b, 0, sizeof(b));
+            leaf_voxels(t, T, child, np, seed, &b);
+            const uint32_t ref = colors_alloc_leaf(col);
+            builder_build(&b, &col->leaves[ref & ~LEAF_FLAG]);
+            builder_free(&b);
+            col->nodes[cn + c] = ref;
+        } else {
+            const uint32_t sub = colors_tree(t, col, level + 1, child, np, seed);
+            col->nodes[cn + c] = sub;
+        }
+    }
+    return cn;
+}
+/* The colour tree of a freshly loaded scene: the tree's node layout of
+ * create_hash_dag_colors (hash_dag_factory.cpp:100-147), with one unique leaf
+ * per present level-T child holding its voxels' colours in depth-first
+ * order (leaf voxels in bit order). */
+int or_colors_from_scene(or_colors* col, const or_table* t, uint64_t color_seed)
+{
+    const uint32_t T = t->cfg.color_tree_levels;
+    if (!col || col->n_nodes || T == 0 || T >= t->leaf_level || t->root == INVALID)
+        return HD_ERR_INVALID;
+    const uint32_t path[3] = {0, 0, 0};
+    colors_tree(t, col, 0, t->root, path, color_seed);
+    return HD_OK;
+}
+
+/* DAGUtils::get_color (dag_utils.h:423-523) */
+hd_color or_get_color(const or_table* t, const or_colors* col, uint32_t x, uint32_t y, uint32_t z)
+{
+    hd_color none;
+    memset(&none, 0, sizeof(none));
+    const uint32_t D = t->cfg.depth, T = t->cfg.color_tree_levels, leafl = t->leaf_level;
+    uint64_t nof = 0;
+    uint32_t cn = 0;
+    const or_leaf* leaf = NULL;
+    uint32_t index = t->root;
+    if (index == INVALID)
+        return none;
+    for (uint32_t level = 0; level < leafl;) {
+        level++;
+        const uint32_t* p = sys_ptr(t, index);
+        const uint32_t mask = p[0] & 0xffu;
+        const uint32_t sh = D - level;
+        const uint32_t child = (((x >> sh) & 1) << 2) | (((y >> sh) & 1) << 1) | ((z >> sh) & 1);
+        if (!(mask & (1u << child)))
+            return none;
+        if (level - 1 < T) {
+            cn = col->nodes[cn + child];
+            if (level == T) {
+                leaf = (cn & LEAF_FLAG) ? &col->leaves[cn & ~LEAF_FLAG] : NULL;
+            } else if (!cn) {
+                return none;
+            }
+        }
+        if (level == leafl) {
+            for (uint32_t cb = 0; cb < child; cb++)
+                if (mask & (1u << cb)) {
+                    const uint32_t* lp = sys_ptr(t, p[child_offset(mask, cb)]);
+                    nof += popc32(lp[0]) + popc32(lp[1]);
+                }
+            const uint32_t* lp = sys_ptr(t, p[child_offset(mask, child)]);
+            const uint64_t bits = (uint64_t)lp[0] | ((uint64_t)lp[1] << 32);
+            const uint32_t bi = ((x & 1) ? 4 : 0) | ((y & 1) ? 2 : 0) | ((z & 1) ? 1 : 0) | ((x & 2) ? 32 : 0) |
+                                ((y & 2) ? 16 : 0) | ((z & 2) ? 8 : 0);
+            nof += popc64(bits & ((1ull << bi) - 1));
+            break;
+        }
+        if (level > T)
+            for (uint32_t cb = 0; cb < child; cb++)
+                if (mask & (1u << cb))
+                    nof += sys_ptr(t, p[child_offset(mask, cb)])[0] >> 8;
+        index = p[child_offset(mask, child)];
+    }
+    if (!leaf || !leaf_valid_index(leaf, nof))
+        return none;
+    return leaf_color(leaf, nof);
+}
+
+static void push_frame(struct frame** stack, uint64_t* n, uint64_t* cap, struct frame f)
+{
+    if (*n == *cap) {
+        *cap = *cap ? 2 * *cap : 16;
+        *stack = (struct frame*)realloc(*stack, *cap * sizeof(struct frame));
+    }
+    (*stack)[(*n)++] = f;
+}
+
+/* HashDAG::edit_threads (hash_dag.h:255-405) with colours: the edit, the
+ * colour leaves rebuilt, an undo frame recorded (HashDAGUndoRedo::add_frame
+ * drops the redo stack, :55-66). */
+int or_edit_colored(or_table* t, or_colors* col, const hd_edit* e, hd_edit_stats* stats)
+{
+    if (!col || !col->n_nodes || t->cfg.color_tree_levels == 0 || e->tool > HD_TOOL_COPY)
+        return HD_ERR_INVALID;
+    edit_job j;
+    memset(&j, 0, sizeof(j));
+    j.t = t;
+    j.col = col;
+    j.ed = make_editor(e);
+    if (e->tool == HD_TOOL_COPY) {
+        /* the source region read before the edit (:459-505, BENCHMARK).
+         * DAGUtils::get_values' overlap test compares inclusive node bounds
+         * with `boundsMax <= inMin` (dag_utils.h:264-283), so a voxel whose
+         * x, y or z equals the region's start is never written and keeps
+         * the memset 0. */
+        const uint32_t n = j.ed.size;
+        const uint32_t m0[3] = {(uint32_t)j.ed.copy_min.x, (uint32_t)j.ed.copy_min.y, (uint32_t)j.ed.copy_min.z};
+        const uint64_t n3 = (uint64_t)n * n * n;
+        j.ed.values = (uint8_t*)calloc(n3 + 1, 1);
+        j.ed.colors = (hd_color*)calloc(n3 + 1, sizeof(hd_color));
+        for (uint32_t z = 0; z < n; z++)
+            for (uint32_t y = 0; y < n; y++)
+                for (uint32_t x = 0; x < n; x++) {
+                    const uint64_t i = x + (uint64_t)n * y + (uint64_t)n * n * z;
+                    j.ed.values[i] = (x && y && z) ? (uint8_t)or_get_value(t, m0[0] + x, m0[1] + y, m0[2] + z) : 0;
+                    if (j.ed.values[i])
+                        j.ed.colors[i] = or_get_color(t, col, m0[0] + x, m0[1] + y, m0[2] + z);
+                }
+    }
+    t->foa_calls = t->nodes_added = t->words_scanned = 0;
+    const uint32_t path[3] = {0, 0, 0};
+    uint32_t cn;
+    const uint32_t before = t->root;
+    const uint32_t root = edit_top(&j, 0, t->root, path, 0, &cn);
+    free(j.ed.values);
+    free(j.ed.colors);
+    if (!t->error) {
+        t->root = root;
+        struct frame f = {before, j.n_diff, j.diff_index, j.diff_prev, j.diff_next};
+        free_frames(col->redo, col->n_redo);
+        col->n_redo = 0;
+        push_frame(&col->undo, &col->n_undo, &col->cap_undo, f);
+    }
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->num_voxels = j.num_voxels;
+        stats->num_nodes = j.num_nodes;
+        stats->find_or_add_calls = t->foa_calls;
+        stats->nodes_added = t->nodes_added;
+        stats->words_scanned = t->words_scanned;
+    }
+    return t->error;
+}
+
+/* HashDAGUndoRedo::undo / redo (hash_dag.h:67-120): swap the root, put the
+ * frame's leaves back, move the inverted frame to the other stack. */
+static int swap_frame(or_table* t, or_colors* col, struct frame** from, uint64_t* nf, struct frame** to, uint64_t* nt,
+                      uint64_t* capt)
+{
+    if (*nf == 0)
+        return 0;
+    struct frame f = (*from)[--(*nf)];
+    struct frame inv = {t->root, f.n, f.index, f.next, f.prev};
+    t->root = f.root;
+    for (uint32_t i = 0; i < f.n; i++)
+        col->leaves[f.index[i] & ~LEAF_FLAG] = f.prev[i];
+    push_frame(to, nt, capt, inv);
+    return 1;
+}
+int or_undo(or_table* t, or_colors* col)
+{
+    return swap_frame(t, col, &col->undo, &col->n_undo, &col->redo, &col->n_redo, &col->cap_redo);
+}
+int or_redo(or_table* t, or_colors* col)
+{
+    return swap_frame(t, col, &col->redo, &col->n_redo, &col->undo, &col->n_undo, &col->cap_undo);
+}
+
+void or_colors_stats(const or_colors* col, uint64_t* out /* nodes, leaves, blocks, weight words, macro words */)
+{
+    out[0] = col->n_nodes;
+    out[1] = col->n_leaves;
+    out[2] = out[3] = out[4] = 0;
+    for (uint64_t i = 0; i < col->n_leaves; i++) {
+        out[2] += col->leaves[i].nb;
+        out[3] += col->leaves[i].nw;
+        out[4] += col->leaves[i].nm;
+    }
 }
 
 /* ======================================================================

@@ -54,9 +54,14 @@ uint32_t or_read_word(const or_table* t, uint32_t vptr);
 int32_t or_scene_height(uint64_t seed, uint32_t depth, uint32_t x, uint32_t z);
 void or_scene_spheres(uint64_t seed, uint32_t depth, int64_t* out /* 64 x 4: cx cy cz r */);
 int or_scene_solid(uint64_t seed, uint32_t depth, uint32_t x, uint32_t y, uint32_t z);
+/* shell scene: solid voxels with an empty face neighbour (outside = empty) */
+int or_scene_shell(uint64_t seed, uint32_t depth, uint32_t x, uint32_t y, uint32_t z);
 /* Builds the BasicDAG words of the scene; returns malloc'd words. */
 uint32_t* or_generate_basic_dag(uint64_t seed, uint32_t depth, uint32_t color_tree_levels,
                                 uint64_t* n_words);
+/* flags: HD_SCENE_SHELL keeps only the surface shell of the solid scene */
+uint32_t* or_generate_basic_dag_ex(uint64_t seed, uint32_t depth, uint32_t color_tree_levels, uint32_t flags,
+                                   uint64_t* n_words);
 void or_free(void* p);
 
 /* ---- ingest: HashDAGFactory::load_from_DAG ---------------------------- */
@@ -86,6 +91,23 @@ void or_trace_frame_mt(const or_table* t, const hd_camera* cam, uint32_t width, 
 /* ---- edits (hash_dag_edits.h) and GC (hash_dag.h:407-547) ------------- */
 int or_edit(or_table* t, const hd_edit* edit, hd_edit_stats* stats);
 int or_gc(or_table* t, uint32_t* extra_roots, uint32_t n_extra);
+/* ---- colours (variable_weight_size_colors.h, hash_dag_colors.h) ------- */
+typedef struct or_colors or_colors;
+or_colors* or_colors_create(void);
+void or_colors_destroy(or_colors* c);
+/* colour tree + one leaf per level-T slot from the scene's colour field */
+int or_colors_from_scene(or_colors* c, const or_table* t, uint64_t color_seed);
+hd_color or_get_color(const or_table* t, const or_colors* c, uint32_t x, uint32_t y, uint32_t z);
+/* every tool incl. paint and copy; records an undo frame */
+int or_edit_colored(or_table* t, or_colors* c, const hd_edit* e, hd_edit_stats* stats);
+int or_undo(or_table* t, or_colors* c); /* 1 if a frame was applied */
+int or_redo(or_table* t, or_colors* c);
+void or_colors_stats(const or_colors* c, uint64_t* out);
+uint32_t or_color_rgb8(uint64_t seed, uint32_t x, uint32_t y, uint32_t z);
+hd_color or_voxel_color(uint64_t seed, uint32_t x, uint32_t y, uint32_t z);
+uint32_t or_color_rgb888(hd_color k);
+uint32_t or_f3_to_rgb888(float x, float y, float z);
+
 /* Debugging aid: log every find_or_add call (level, content, result). */
 void or_set_foa_log(const char* path);
 

@@ -27,7 +27,16 @@ class HdCamera(C.Structure):
 
 
 class HdEdit(C.Structure):
-    _fields_ = [("tool", C.c_uint32), ("center", C.c_float * 3), ("radius", C.c_float)]
+    _fields_ = [("tool", C.c_uint32), ("center", C.c_float * 3), ("radius", C.c_float), ("rgb", C.c_uint32),
+                ("source", C.c_float * 3), ("dest", C.c_float * 3)]
+
+
+class HdColor(C.Structure):
+    _fields_ = [("color_bits", C.c_uint32), ("weight", C.c_uint8), ("bits_per_weight", C.c_uint8),
+                ("reserved", C.c_uint16)]
+
+    def tuple(self):
+        return (self.color_bits, self.weight, self.bits_per_weight)
 
 
 class HdEditStats(C.Structure):
@@ -94,6 +103,10 @@ def lib():
         L.or_scene_spheres.argtypes = [u64, u32, np.ctypeslib.ndpointer(np.int64, flags="C")]
         L.or_generate_basic_dag.restype = C.POINTER(u32)
         L.or_generate_basic_dag.argtypes = [u64, u32, u32, C.POINTER(u64)]
+        L.or_generate_basic_dag_ex.restype = C.POINTER(u32)
+        L.or_generate_basic_dag_ex.argtypes = [u64, u32, u32, u32, C.POINTER(u64)]
+        L.or_scene_shell.restype = C.c_int
+        L.or_scene_shell.argtypes = [u64, u32, u32, u32, u32]
         L.or_free.argtypes = [P]
         L.or_load_basic_dag.argtypes = [P, pu32, u64]
         L.or_get_value.argtypes = [P, u32, u32, u32]
@@ -109,6 +122,21 @@ def lib():
         L.or_edit.argtypes = [P, C.POINTER(HdEdit), C.POINTER(HdEditStats)]
         L.or_gc.argtypes = [P, P, u32]
         L.or_set_foa_log.argtypes = [C.c_char_p]
+        L.or_colors_create.restype = P
+        L.or_colors_destroy.argtypes = [P]
+        L.or_colors_from_scene.argtypes = [P, P, u64]
+        L.or_get_color.restype = HdColor
+        L.or_get_color.argtypes = [P, P, u32, u32, u32]
+        L.or_edit_colored.argtypes = [P, P, C.POINTER(HdEdit), C.POINTER(HdEditStats)]
+        L.or_undo.argtypes = [P, P]
+        L.or_redo.argtypes = [P, P]
+        L.or_colors_stats.argtypes = [P, np.ctypeslib.ndpointer(np.uint64, flags="C")]
+        L.or_color_rgb8.restype = u32
+        L.or_color_rgb8.argtypes = [u64, u32, u32, u32]
+        L.or_voxel_color.restype = HdColor
+        L.or_voxel_color.argtypes = [u64, u32, u32, u32]
+        L.or_color_rgb888.restype = u32
+        L.or_color_rgb888.argtypes = [HdColor]
         _lib = L
     return _lib
 
@@ -135,9 +163,12 @@ def camera(cam):
     return c
 
 
-def generate_basic_dag(seed, depth, color_tree_levels):
+SCENE_SHELL = 1
+
+
+def generate_basic_dag(seed, depth, color_tree_levels, flags=0):
     n = C.c_uint64(0)
-    p = lib().or_generate_basic_dag(seed, depth, color_tree_levels, C.byref(n))
+    p = lib().or_generate_basic_dag_ex(seed, depth, color_tree_levels, flags, C.byref(n))
     if not p:
         raise RuntimeError("scene generation failed")
     words = np.ctypeslib.as_array(p, shape=(n.value,)).copy()
@@ -151,6 +182,10 @@ def scene_height(seed, depth, x, z):
 
 def scene_solid(seed, depth, x, y, z):
     return lib().or_scene_solid(seed, depth, x, y, z)
+
+
+def scene_shell(seed, depth, x, y, z):
+    return lib().or_scene_shell(seed, depth, x, y, z)
 
 
 def scene_spheres(seed, depth):
@@ -256,7 +291,7 @@ class Table:
         return paths.reshape(h, w, 4), mask.reshape(h, w)
 
     def edit(self, tool, center, radius):
-        e = HdEdit(tool, (C.c_float * 3)(*center), radius)
+        e = make_edit(tool, center, radius)
         s = HdEditStats()
         r = lib().or_edit(self.h, C.byref(e), C.byref(s))
         if r:
@@ -269,3 +304,54 @@ class Table:
         if r:
             raise RuntimeError(f"gc failed {r}")
         return [int(v) for v in arr[:len(extra_roots)]]
+
+
+def make_edit(tool, center, radius, rgb=0xFF0000, source=(0.0, 0.0, 0.0), dest=(0.0, 0.0, 0.0)):
+    return HdEdit(tool, (C.c_float * 3)(*center), radius, rgb, (C.c_float * 3)(*source), (C.c_float * 3)(*dest))
+
+
+class Colors:
+    """HashDAGColors of a Table: colour tree, leaves, undo/redo frames."""
+
+    def __init__(self, table):
+        self.t = table
+        self.h = lib().or_colors_create()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_colors_destroy(self.h)
+            self.h = None
+
+    def from_scene(self, color_seed):
+        if lib().or_colors_from_scene(self.h, self.t.h, color_seed):
+            raise RuntimeError("colour import failed")
+
+    def get_color(self, x, y, z):
+        return lib().or_get_color(self.t.h, self.h, x, y, z).tuple()
+
+    def edit(self, tool, center, radius, rgb=0xFF0000, source=(0.0, 0.0, 0.0), dest=(0.0, 0.0, 0.0)):
+        e = make_edit(tool, center, radius, rgb, source, dest)
+        s = HdEditStats()
+        r = lib().or_edit_colored(self.t.h, self.h, C.byref(e), C.byref(s))
+        if r:
+            raise RuntimeError(f"edit failed {r}")
+        return s
+
+    def undo(self):
+        return bool(lib().or_undo(self.t.h, self.h))
+
+    def redo(self):
+        return bool(lib().or_redo(self.t.h, self.h))
+
+    def stats(self):
+        out = np.zeros(5, np.uint64)
+        lib().or_colors_stats(self.h, out)
+        return dict(zip(("nodes", "leaves", "blocks", "weight_words", "macro_words"), (int(v) for v in out)))
+
+
+def voxel_color(seed, x, y, z):
+    return lib().or_voxel_color(seed, x, y, z).tuple()
+
+
+def color_rgb888(color_bits, weight=0, bits_per_weight=0):
+    return lib().or_color_rgb888(HdColor(color_bits, weight, bits_per_weight, 0))

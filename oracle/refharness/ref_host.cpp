@@ -240,3 +240,149 @@ extern "C" uint32 ref_level_size(uint32 level) { return g_dag.data.get_level_siz
 // Hash known-answer vectors (hash_table.h:80-89).
 extern "C" uint32 ref_hash_leaf(uint64 leaf) { return HashDagUtils::hash_leaf(leaf); }
 extern "C" uint32 ref_hash_interior(uint32 n, const uint32* node) { return HashDagUtils::hash_interior(n, node); }
+
+#if EDITS_ENABLE_COLORS
+// ---------------------------------------------------------------------------
+// Colours (built with EDITS_ENABLE_COLORS=1): the scene's voxel colours come
+// from the oracle's colour field (the test input, like the scene), packed
+// by the reference's own ColorLeafBuilder into a BasicDAGCompressedColors
+// main leaf and imported with HashDAGFactory::load_colors_from_DAG.
+// ---------------------------------------------------------------------------
+extern "C" hd_color or_voxel_color(uint64_t seed, uint32_t x, uint32_t y, uint32_t z);
+
+static void add_voxel_colors(const BasicDAG& dag, uint32 level, uint32 index, uint3 path, uint64 seed,
+                             ColorLeafBuilder& builder)
+{
+    if (level == C_leafLevel) {
+        const uint64 leaf = dag.get_leaf(index).to_64();
+        for (uint32 bit = 0; bit < 64; bit++) {
+            if (!((leaf >> bit) & 1))
+                continue;
+            const uint32 c1 = bit >> 3, c2 = bit & 7;
+            const uint32 x = (path.x << 2) | (((c1 >> 2) & 1) << 1) | ((c2 >> 2) & 1);
+            const uint32 y = (path.y << 2) | (((c1 >> 1) & 1) << 1) | ((c2 >> 1) & 1);
+            const uint32 z = (path.z << 2) | ((c1 & 1) << 1) | (c2 & 1);
+            const hd_color k = or_voxel_color(seed, x, y, z);
+            CompressedColor color;
+            color.colorBits = k.color_bits;
+            color.weight = k.weight;
+            color.bitsPerWeight = k.bits_per_weight;
+            builder.add(color);
+        }
+        return;
+    }
+    const uint32 node = dag.get_node(level, index);
+    const uint8 mask = Utils::child_mask(node);
+    for (uint8 c = 0; c < 8; c++)
+        if (mask & (1u << c))
+            add_voxel_colors(dag, level + 1, dag.get_child_index(level, index, mask, c),
+                             make_uint3((path.x << 1) | ((c >> 2) & 1), (path.y << 1) | ((c >> 1) & 1),
+                                        (path.z << 1) | (c & 1)),
+                             seed, builder);
+}
+
+// HashDAGFactory::load_from_DAG + load_colors_from_DAG (hash_dag_factory.cpp:
+// 150-197) on a BasicDAG and the colour field of `colorSeed`.
+extern "C" int ref_load_colored(const uint32* words, uint64 nWords, uint32 poolPages, uint64 colorSeed)
+{
+    if (g_loaded)
+        return 1;
+    BasicDAG basic;
+    basic.data = StaticArray<uint32>::allocate("basic dag", nWords, EMemoryType::CPU);
+    std::memcpy(basic.data.data(), words, nWords * sizeof(uint32));
+    HashDAGFactory::load_from_DAG(g_dag, basic, poolPages);
+    // enclosedLeaves: indexed by the upper header bits of the top levels
+    uint32 maxIndex = 0;
+    {
+        std::vector<std::pair<uint32, uint32>> stack{{0u, 0u}};
+        std::unordered_set<uint64> seen;
+        while (!stack.empty()) {
+            auto [level, index] = stack.back();
+            stack.pop_back();
+            if (level >= C_colorTreeLevels || !seen.insert((uint64(level) << 32) | index).second)
+                continue;
+            const uint32 node = basic.get_node(level, index);
+            maxIndex = std::max(maxIndex, node >> 8);
+            const uint8 mask = Utils::child_mask(node);
+            for (uint8 c = 0; c < 8; c++)
+                if (mask & (1u << c))
+                    stack.push_back({level + 1, basic.get_child_index(level, index, mask, c)});
+        }
+    }
+    BasicDAGCompressedColors colors;
+    colors.topLevels = C_colorTreeLevels;
+    colors.enclosedLeaves = StaticArray<EnclosedLeavesType>::allocate("enclosed leaves", maxIndex + 1, EMemoryType::CPU);
+    std::memset(colors.enclosedLeaves.data(), 0, (maxIndex + 1) * sizeof(EnclosedLeavesType));
+    DAGUtils::fix_enclosed_leaves(basic, colors.enclosedLeaves, C_colorTreeLevels);
+    ColorLeafBuilder builder;
+    add_voxel_colors(basic, 0, 0, make_uint3(0, 0, 0), colorSeed, builder);
+    builder.build(colors.leaf, true);
+    HashDAGFactory::load_colors_from_DAG(g_colors, basic, colors);
+    g_recorder = new StatsRecorder();
+    g_loaded = true;
+    return 0;
+}
+
+// HashDAG::edit_threads with colours (hash_dag.h:255-405), task order as in
+// run_edit, colour leaves rebuilt at the end (BENCHMARK: no undo frame).
+template<typename TEditor>
+static void run_edit_colored(const TEditor& editor, uint64* stats)
+{
+    HashDagEdits::ThreadedEditParameters parameters{ g_dag.data, g_colors, *g_recorder };
+    HashDagEdits::edit_threaded<true>(0, g_dag.firstNodeIndex, 0, Path(0, 0, 0), editor, parameters);
+    std::vector<std::pair<uint64, HashDagEdits::Thread*>> tasks;
+    for (auto& it : parameters.threads)
+        tasks.emplace_back(morton(it.first, C_colorTreeLevels), it.second.get());
+    std::sort(tasks.begin(), tasks.end(),
+              [](const std::pair<uint64, HashDagEdits::Thread*>& a, const std::pair<uint64, HashDagEdits::Thread*>& b) {
+                  return a.first < b.first;
+              });
+    for (auto& task : tasks)
+        task.second->lambda();
+    for (auto& it : parameters.threads)
+        parameters.stats += it.second->stats;
+    g_dag.firstNodeIndex =
+        HashDagEdits::edit_threaded<false>(0, g_dag.firstNodeIndex, 0, Path(0, 0, 0), editor, parameters).nodeIndex;
+    for (auto& colorToBuild : parameters.colorsToBuild) {
+        auto& leaf = g_colors.get_leaf_ref(colorToBuild.newLeafIndex);
+        colorToBuild.builder->build(leaf, true);
+    }
+    g_colors.upload_to_gpu(false);
+    stats[0] = parameters.stats.numVoxels;
+    stats[1] = parameters.stats.numNodes;
+}
+
+// tool: 0..3 as ref_edit, 4 SpherePaintEditor (blue), 5 CopyEditor
+// (identity transform, no swirl) moving center +- radius by dest - source
+extern "C" int ref_edit_colored(uint32 tool, const float* center, float radius, const float* source,
+                                const float* dest, uint64* stats)
+{
+    const float3 c = make_float3(center[0], center[1], center[2]);
+    switch (tool) {
+    case 0: run_edit_colored(SphereEditor<false>(c, radius), stats); break;
+    case 1: run_edit_colored(SphereEditor<true>(c, radius), stats); break;
+    case 2: run_edit_colored(BoxEditor<false>(c, radius), stats); break;
+    case 3: run_edit_colored(BoxEditor<true>(c, radius), stats); break;
+    case 4: run_edit_colored(SpherePaintEditor(c, radius), stats); break;
+    case 5: {
+        const Matrix3x3 identity = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        run_edit_colored(CopyEditor(g_dag, g_colors, make_float3(source[0], source[1], source[2]),
+                                    make_float3(dest[0], dest[1], dest[2]), c, radius, identity, *g_recorder, false,
+                                    0.0f),
+                         stats);
+        break;
+    }
+    default: return 1;
+    }
+    return 0;
+}
+
+// DAGUtils::get_color (dag_utils.h:423-523): colour bits, weight, bits per weight
+extern "C" void ref_get_color(uint32 x, uint32 y, uint32 z, uint32* out)
+{
+    const CompressedColor k = DAGUtils::get_color(g_dag, g_colors, Path(x, y, z));
+    out[0] = k.colorBits;
+    out[1] = k.weight;
+    out[2] = k.bitsPerWeight;
+}
+#endif

@@ -91,3 +91,75 @@ def test_oracle_volume_matches_scene_function():
     for _ in range(2000):
         x, y, z = (int(v) for v in rng.integers(0, e, 3))
         assert t.get_value(x, y, z) == po.scene_solid(1, depth, x, y, z)
+
+
+def _color_state(get_value, get_color, boxes, half):
+    rows = []
+    for (cx, cy, cz) in boxes:
+        for x in range(cx - half, cx + half):
+            for y in range(cy - half, cy + half):
+                for z in range(cz - half, cz + half):
+                    if get_value(x, y, z):
+                        rows.append((x, y, z) + tuple(get_color(x, y, z)))
+    rows = sorted(set(rows))
+    arr = np.array(rows, np.uint32).reshape(-1, 6)
+    return len(rows), hashlib.sha256(arr.tobytes()).hexdigest()
+
+
+def test_oracle_colors_match_reference_fixture():
+    """Shell scene with colours, an edit stream over all six tools and a GC:
+    roots, edit counters and the colour of every present voxel in boxes
+    around the edits equal what the reference computed (fixture made by
+    tests/golden/make_golden_colors.py)."""
+    fx = _load("ref_colors_d10.json")
+    depth, T = fx["depth"], fx["color_tree_levels"]
+    words = po.generate_basic_dag(fx["seed"], depth, T, flags=po.SCENE_SHELL)
+    assert hashlib.sha256(words.tobytes()).hexdigest() == fx["basic_dag_sha256"]
+    ot = po.Table(po.default_config(depth))
+    ot.load_basic_dag(words)
+    col = po.Colors(ot)
+    col.from_scene(fx["color_seed"])
+    boxes = [tuple(b) for b in fx["boxes"]]
+
+    def state():
+        return _color_state(ot.get_value, col.get_color, boxes, fx["half"])
+
+    step = fx["steps"][0]
+    assert ot.root == step["root"]
+    assert state() == (step["present"], step["digest"])
+    for i, (e, step) in enumerate(zip(fx["edits"], fx["steps"][1:])):
+        s = col.edit(e["tool"], e["center"], e["radius"], source=e["source"], dest=e["dest"])
+        assert ot.root == step["root"], i
+        assert (s.num_voxels, s.num_nodes) == (step["num_voxels"], step["num_nodes"]), i
+        assert state() == (step["present"], step["digest"]), i
+    ot.gc()
+    g = fx["gc"]
+    assert state() == (g["present"], g["digest"])
+
+
+def test_oracle_color_undo_redo_restores_state():
+    """HashDAGUndoRedo semantics on the oracle: undo gives back the root and
+    the colours before the edit, redo the ones after."""
+    fx = _load("ref_colors_d10.json")
+    depth, T = fx["depth"], fx["color_tree_levels"]
+    ot = po.Table(po.default_config(depth))
+    ot.load_basic_dag(po.generate_basic_dag(fx["seed"], depth, T, flags=po.SCENE_SHELL))
+    col = po.Colors(ot)
+    col.from_scene(fx["color_seed"])
+    boxes = [tuple(b) for b in fx["boxes"][:4]]
+
+    def state():
+        return ot.root, _color_state(ot.get_value, col.get_color, boxes, fx["half"])
+
+    states = [state()]
+    for e in fx["edits"][:4]:
+        col.edit(e["tool"], e["center"], e["radius"], source=e["source"], dest=e["dest"])
+        states.append(state())
+    for k in range(4, 0, -1):
+        assert col.undo()
+        assert state() == states[k - 1]
+    assert not col.undo()
+    for k in range(1, 5):
+        assert col.redo()
+        assert state() == states[k]
+    assert not col.redo()
