@@ -21,10 +21,12 @@ import numpy as np
 from . import _capi
 from ._capi import BatchTuning, Camera, Config, Edit, EditStats, HashDagError, LevelStats, lib
 
-__all__ = ["HashDAG", "DAGTracer", "SphereEditor", "BoxEditor", "BatchTuning", "Camera", "Config", "EditStats", "LevelStats",
+__all__ = ["HashDAG", "DAGTracer", "SphereEditor", "BoxEditor", "SpherePaintEditor", "CopyEditor", "BatchTuning", "Camera", "Config", "EditStats", "LevelStats",
            "HashDagError", "default_config"]
 
-TOOL_SPHERE_REMOVE, TOOL_SPHERE_ADD, TOOL_BOX_REMOVE, TOOL_BOX_ADD = 0, 1, 2, 3
+TOOL_SPHERE_REMOVE, TOOL_SPHERE_ADD, TOOL_BOX_REMOVE, TOOL_BOX_ADD, TOOL_SPHERE_PAINT, TOOL_COPY = range(6)
+SCENE_SHELL = 1
+GC_KEEP_HISTORY = 1
 
 
 def default_config(depth, **overrides):
@@ -44,13 +46,17 @@ def _torch():
 
 class _Editor:
     tool = None
+    rgb = 0xFF0000
+    source = (0.0, 0.0, 0.0)
+    dest = (0.0, 0.0, 0.0)
 
     def __init__(self, center, radius):
         self.center = tuple(float(np.float32(v)) for v in center)
         self.radius = float(np.float32(radius))
 
     def to_edit(self):
-        return Edit(self.tool, (C.c_float * 3)(*self.center), self.radius)
+        return Edit(self.tool, (C.c_float * 3)(*self.center), self.radius, self.rgb,
+                    (C.c_float * 3)(*self.source), (C.c_float * 3)(*self.dest))
 
 
 class SphereEditor(_Editor):
@@ -70,10 +76,37 @@ class BoxEditor(_Editor):
         self.tool = TOOL_BOX_ADD if adding else TOOL_BOX_REMOVE
 
 
+class SpherePaintEditor(_Editor):
+    """SpherePaintEditor (hash_dag_editors.h:315-330): voxels in the sphere
+    move their colour toward rgb (r | g << 8 | b << 16; the reference paints
+    blue, 0xFF0000) by clamp(1 - distance / radius, 0, 0.1)."""
+    tool = TOOL_SPHERE_PAINT
+
+    def __init__(self, center, radius, rgb=0xFF0000):
+        super().__init__(center, radius)
+        self.rgb = int(rgb)
+
+
+class CopyEditor(_Editor):
+    """The copy tool (CopyEditorWithDecompression, hash_dag_editors.h:437-609):
+    the region center +- radius, read before the edit, is OR-ed into the
+    region moved by dest - source, with its colours."""
+    tool = TOOL_COPY
+
+    def __init__(self, center, radius, source, dest):
+        super().__init__(center, radius)
+        self.source = tuple(float(np.float32(v)) for v in source)
+        self.dest = tuple(float(np.float32(v)) for v in dest)
+
+
 def editor_from_tuple(t):
-    tool, center, radius = t
+    tool, center, radius = t[:3]
     if tool in (TOOL_SPHERE_REMOVE, TOOL_SPHERE_ADD):
         return SphereEditor(center, radius, tool == TOOL_SPHERE_ADD)
+    if tool == TOOL_SPHERE_PAINT:
+        return SpherePaintEditor(center, radius, *(t[3:4] or ()))
+    if tool == TOOL_COPY:
+        return CopyEditor(center, radius, t[3], t[4])
     return BoxEditor(center, radius, tool == TOOL_BOX_ADD)
 
 
@@ -121,8 +154,55 @@ class HashDAG:
         words = np.ascontiguousarray(words, np.uint32)
         self._check(lib().hd_load_basic_dag(self._h, words.ctypes.data, words.size))
 
-    def generate_scene(self, seed):
-        self._check(lib().hd_generate_scene(self._h, seed))
+    def generate_scene(self, seed, shell=False):
+        """The seeded scene; shell=True keeps its surface shell (the form the
+        coloured scenes use)."""
+        self._check(lib().hd_generate_scene_ex(self._h, seed, SCENE_SHELL if shell else 0))
+
+    # -- colours -------------------------------------------------------------
+    def colors_from_scene(self, color_seed):
+        """HashDAGColors of the current scene from the seeded colour field."""
+        self._check(lib().hd_colors_from_scene(self._h, color_seed))
+
+    def get_colors(self, xyz):
+        """DAGUtils::get_color for n x 3 voxels: n x 3 array of (colour bits,
+        weight, bits per weight)."""
+        torch = _torch()
+        xyz = np.ascontiguousarray(xyz, np.uint32).reshape(-1, 3)
+        d_in = torch.from_numpy(xyz.view(np.int32)).cuda()
+        d_out = torch.empty(len(xyz) * 2, dtype=torch.int32, device="cuda")
+        self._check(lib().hd_get_colors(self._h, d_in.data_ptr(), len(xyz), d_out.data_ptr()))
+        raw = d_out.cpu().numpy().view(np.uint32).reshape(-1, 2)
+        return np.stack([raw[:, 0], raw[:, 1] & 0xFF, (raw[:, 1] >> 8) & 0xFF], axis=1)
+
+    def color_stats(self):
+        out = (C.c_uint64 * 5)()
+        self._check(lib().hd_color_stats(self._h, out))
+        return dict(zip(("nodes", "leaves", "blocks", "macro_words", "weight_words"), (int(v) for v in out)))
+
+    # -- undo / redo ---------------------------------------------------------
+    def undo(self):
+        """HashDAGUndoRedo::undo; False when there is nothing to undo."""
+        st = lib().hd_undo(self._h)
+        if st == _capi.HD_ERR_STATE:
+            return False
+        self._check(st)
+        return True
+
+    def redo(self):
+        st = lib().hd_redo(self._h)
+        if st == _capi.HD_ERR_STATE:
+            return False
+        self._check(st)
+        return True
+
+    def history(self):
+        u, r = C.c_uint32(), C.c_uint32()
+        self._check(lib().hd_history(self._h, C.byref(u), C.byref(r)))
+        return u.value, r.value
+
+    def set_undo_capacity(self, frames):
+        self._check(lib().hd_set_undo_capacity(self._h, int(frames)))
 
     def export_basic_dag(self):
         n = C.c_uint64()
@@ -228,12 +308,14 @@ class HashDAG:
         self._check(lib().hd_batch_fallbacks(self._h, C.byref(v)))
         return v.value
 
-    def remove_stale_nodes(self, extra_roots=()):
+    def remove_stale_nodes(self, extra_roots=(), keep_history=False):
         """HashDAG::remove_stale_nodes(levels - 2), marking from the root and
-        from extra_roots (kept undo states); returns the remapped extra
-        roots."""
+        from extra_roots; returns the remapped extra roots.  The undo / redo
+        history is dropped (as the reference's engine does) unless
+        keep_history, which keeps its states alive."""
         arr = np.array(list(extra_roots) + [0], np.uint32)
-        self._check(lib().hd_gc(self._h, arr.ctypes.data, len(extra_roots)))
+        self._check(lib().hd_gc_ex(self._h, arr.ctypes.data, len(extra_roots),
+                                   GC_KEEP_HISTORY if keep_history else 0))
         return [int(v) for v in arr[:len(extra_roots)]]
 
     def set_fp_mode(self, mode):
@@ -266,6 +348,16 @@ class DAGTracer:
                                          self.paths.data_ptr(), lt, float(shadow_bias),
                                          self.shadows.data_ptr(), C.byref(ms)))
         return ms.value
+
+    def resolve_colors(self, dag):
+        """The colour lookup of Tracer::trace_colors on the last paths:
+        uint32 RGBA8 per pixel (0 = miss), kept in self.colors."""
+        torch = _torch()
+        if getattr(self, "colors", None) is None:
+            self.colors = torch.zeros((self.height, self.width), dtype=torch.int32, device="cuda")
+        dag._check(lib().hd_trace_colors(dag.handle, self.paths.data_ptr(), self.width, self.height,
+                                         self.colors.data_ptr()))
+        return self.colors.cpu().numpy().view(np.uint32)
 
     def get_paths(self):
         return self.paths.cpu().numpy().view(np.uint32)

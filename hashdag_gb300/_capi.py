@@ -81,6 +81,16 @@ SIGNATURES = [
     ("hd_sync", C.c_int, [_P]),
     ("hd_load_basic_dag", C.c_int, [_P, _P, _u64]),
     ("hd_generate_scene", C.c_int, [_P, _u64]),
+    ("hd_generate_scene_ex", C.c_int, [_P, _u64, _u32]),
+    ("hd_colors_from_scene", C.c_int, [_P, _u64]),
+    ("hd_get_colors", C.c_int, [_P, _P, _u64, _P]),
+    ("hd_trace_colors", C.c_int, [_P, _P, _u32, _u32, _P]),
+    ("hd_color_stats", C.c_int, [_P, C.POINTER(_u64)]),
+    ("hd_undo", C.c_int, [_P]),
+    ("hd_redo", C.c_int, [_P]),
+    ("hd_set_undo_capacity", C.c_int, [_P, _u32]),
+    ("hd_history", C.c_int, [_P, C.POINTER(_u32), C.POINTER(_u32)]),
+    ("hd_gc_ex", C.c_int, [_P, _P, _u32, _u32]),
     ("hd_export_basic_dag", C.c_int, [_P, _P, _u64, C.POINTER(_u64)]),
     ("hd_trace_primary", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _P, C.POINTER(_f32)]),
     ("hd_trace_shadow", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _P, C.POINTER(_f32), _f32, _P,

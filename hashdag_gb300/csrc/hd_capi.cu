@@ -133,6 +133,7 @@ hd_status hd_destroy(hd_ctx* c)
         return HD_ERR_INVALID;
     cudaStreamSynchronize(c->stream);
     hd::batch_release(c);
+    hd::color_release(c);
     cudaFree(c->t.pool);
     cudaFree(c->t.page_table);
     cudaFree(c->t.bucket_sizes);

@@ -1,13 +1,23 @@
 // The context behind the opaque hd_ctx handle, shared by the .cu files.
 #pragma once
 
+#include <deque>
 #include <string>
+#include <vector>
 
+#include "hd_color.cuh"
 #include "hd_common.cuh"
 #include "hd_util.cuh"
 
 namespace hd {
 struct BatchGraph; // hd_edit_batch.cu
+// One undo step (HashDAGUndoRedo::Frame, hash_dag.h:28-45): the root before
+// the edit and the colour leaves it replaced.
+struct UndoFrame {
+    uint32_t root = 0;
+    std::vector<uint32_t> leaf;
+    std::vector<LeafDesc> prev, next;
+};
 }
 
 struct hd_ctx {
@@ -33,6 +43,14 @@ struct hd_ctx {
     hd_batch_tuning tuning{4, 4, 304};
     hd::BatchGraph* batch = nullptr;
     uint64_t batch_fallbacks = 0;
+    // colours: the table, host mirror of its counters
+    bool colors = false;
+    uint64_t color_seed = 0;
+    hd::ColorTable ct{};
+    uint64_t ctop[5] = {0, 0, 0, 0, 0};
+    // undo / redo history
+    std::deque<hd::UndoFrame> undo, redo;
+    size_t undo_capacity = 200;
 };
 
 namespace hd {
@@ -54,6 +72,20 @@ void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words
 void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats);
 void edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* per_edit, hd_edit_stats* total);
 void batch_release(hd_ctx* c);
+
+// hd_color.cu
+struct Editor;
+struct Level;
+void color_release(hd_ctx* c);
+void colors_from_scene(hd_ctx* c, uint64_t color_seed);
+void get_colors(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, hd_color* d_out);
+void trace_colors(hd_ctx* c, const uint32_t* d_paths, uint32_t w, uint32_t h, uint32_t* d_rgba);
+void copy_source(hd_ctx* c, Editor& ed);
+void color_spawn(hd_ctx* c, uint32_t level, uint32_t n, const Level& lv, const Level& next);
+void edit_colors(hd_ctx* c, const Editor& ed, std::vector<Level>& lv, const std::vector<uint32_t>& count,
+                 uint32_t deepest, UndoFrame& frame);
+bool undo_step(hd_ctx* c, bool redo);
+void push_undo(hd_ctx* c, UndoFrame&& f);
 
 // hd_trace.cu
 void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint32_t* d_paths,

@@ -11,6 +11,9 @@
 namespace hd {
 
 constexpr uint32_t kFoaWarps = 4;
+
+// the device error word without clearing it
+static uint32_t check_error_peek(hd_ctx* c) { return read_scalar(c->t.error, c->stream); }
 constexpr int kFoaProbe = 4;
 
 __global__ void k_edit_classify(Table t, Editor ed, uint32_t level, uint32_t n, Level lv, EditCounters* ctr)
@@ -102,7 +105,7 @@ struct EditBuffers {
     std::vector<uint32_t> cap;
 };
 
-static Level alloc_level(Scratch& s, uint32_t L, uint64_t n, bool leaf)
+static Level alloc_level(Scratch& s, uint32_t L, uint64_t n, bool leaf, bool colors)
 {
     char nm[48];
     auto buf = [&](const char* what, size_t bytes) {
@@ -121,6 +124,13 @@ static Level alloc_level(Scratch& s, uint32_t L, uint64_t n, bool leaf)
     l.exp = static_cast<uint32_t*>(buf("exp", n * 4));
     l.leaf = leaf ? static_cast<uint64_t*>(buf("leaf", n * 8)) : nullptr;
     l.cand = static_cast<uint32_t*>(buf("cand", n * 36));
+    if (colors) {
+        l.ocnt = static_cast<uint32_t*>(buf("ocnt", n * 4));
+        l.cn = static_cast<uint32_t*>(buf("cn", n * 4));
+        l.noff = static_cast<uint32_t*>(buf("noff", n * 4));
+        l.ooff = static_cast<uint32_t*>(buf("ooff", n * 4));
+        l.task = static_cast<uint32_t*>(buf("task", n * 4));
+    }
     return l;
 }
 
@@ -130,15 +140,22 @@ void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats)
     Scratch& s = c->scratch;
     const Geom& g = c->g;
     const uint32_t levels = g.leaf_level + 1;
-    const Editor ed = make_editor(e);
+    Editor ed = make_editor(e);
+    const bool colors = c->colors;
     const auto t0 = std::chrono::steady_clock::now();
     HD_CUDA(cudaEventRecord(c->ev0, st));
+    if (e.tool == HD_TOOL_COPY)
+        copy_source(c, ed); // the source region as it is before the edit
+    UndoFrame frame;
+    frame.root = c->root;
     EditCounters* ctr = s.get<EditCounters>("ed_ctr", 1);
     HD_CUDA(cudaMemsetAsync(ctr, 0, sizeof(EditCounters), st));
     uint32_t* d_n = s.get<uint32_t>("ed_n", 4);
     std::vector<Level> lv(levels);
     std::vector<uint32_t> count(levels, 0);
-    lv[0] = alloc_level(s, 0, 1, levels == 1);
+    lv[0] = alloc_level(s, 0, 1, levels == 1, colors);
+    if (colors)
+        HD_CUDA(cudaMemsetAsync(lv[0].cn, 0, 4, st));
     HD_CUDA(cudaMemsetAsync(lv[0].x, 0, 4, st));
     HD_CUDA(cudaMemsetAsync(lv[0].y, 0, 4, st));
     HD_CUDA(cudaMemsetAsync(lv[0].z, 0, 4, st));
@@ -158,9 +175,12 @@ void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats)
         if (ne == 0)
             break;
         count[L + 1] = 8 * ne;
-        lv[L + 1] = alloc_level(s, L + 1, count[L + 1], L + 1 == g.leaf_level);
+        lv[L + 1] = alloc_level(s, L + 1, count[L + 1], L + 1 == g.leaf_level, colors);
         k_edit_spawn<<<grid_for(n, 128), 128, 0, st>>>(c->t, n, lv[L], lv[L + 1]);
         HD_LAUNCH_CHECK();
+        if (colors && L < g.T) {
+            color_spawn(c, L, n, lv[L], lv[L + 1]);
+        }
     }
     // bottom-up
     uint32_t maxn = 1;
@@ -192,6 +212,8 @@ void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats)
             c->t, uint32_t(L), lv[L], keys, vals, starts, d_cnt + 1, d_cnt, ctr);
         HD_LAUNCH_CHECK();
     }
+    if (colors && !check_error_peek(c))
+        edit_colors(c, ed, lv, count, deepest, frame);
     k_edit_finish<<<1, 1, 0, st>>>(lv[0], c->d_root, c->t.error);
     HD_LAUNCH_CHECK();
     HD_CUDA(cudaEventRecord(c->ev1, st));
@@ -204,6 +226,7 @@ void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats)
                           err == kErrCapacity ? "edit would empty the whole scene"
                                               : "edit failed on the device (" + c->err_detail + ")"};
     c->root = read_scalar(c->d_root, st);
+    push_undo(c, std::move(frame));
     if (stats) {
         stats->num_voxels = h.num_voxels;
         stats->num_nodes = h.num_nodes;
@@ -221,7 +244,7 @@ extern "C" {
 
 hd_status hd_edit_apply(hd_ctx* c, const hd_edit* edit, hd_edit_stats* stats)
 {
-    if (!c || !edit || edit->tool > HD_TOOL_BOX_ADD || !(edit->radius >= 0.0f))
+    if (!c || !edit || edit->tool > HD_TOOL_COPY || !(edit->radius >= 0.0f))
         return HD_ERR_INVALID;
     try {
         hd::edit_one(c, *edit, stats);

@@ -32,12 +32,26 @@ constexpr uint32_t kNoBucket = 0xFFFFFFFFu;
 
 
 // ---- editors ----------------------------------------------------------------
+// SphereEditor / BoxEditor (hash_dag_editors.h:223-313), SpherePaintEditor
+// (:315-330) and the copy tool (CopyEditorWithDecompression, :437-609).
 struct Editor {
     uint32_t tool;
     float cx, cy, cz, r, r2;
     float bminx, bminy, bminz, bmaxx, bmaxy, bmaxz;
-    HD_HD bool sphere() const { return tool == HD_TOOL_SPHERE_ADD || tool == HD_TOOL_SPHERE_REMOVE; }
+    float paint_r, paint_g, paint_b; // paint target colour
+    // copy: source / dest, the source region's corner (copyMin) and size,
+    // its occupancy and colours read before the edit (x fastest)
+    float srcx, srcy, srcz, dstx, dsty, dstz, minx, miny, minz;
+    uint32_t size;
+    const uint8_t* values;
+    const uint64_t* colors;
+    HD_HD bool sphere() const
+    {
+        return tool == HD_TOOL_SPHERE_ADD || tool == HD_TOOL_SPHERE_REMOVE || tool == HD_TOOL_SPHERE_PAINT;
+    }
     HD_HD bool adding() const { return tool == HD_TOOL_SPHERE_ADD || tool == HD_TOOL_BOX_ADD; }
+    // is_full / is_empty exist for the sphere and box editors only
+    HD_HD bool shortcuts() const { return tool <= HD_TOOL_BOX_ADD; }
 };
 
 HD_HD Editor make_editor(const hd_edit& e)
@@ -49,13 +63,58 @@ HD_HD Editor make_editor(const hd_edit& e)
     ed.cz = e.center[2];
     ed.r = e.radius;
     ed.r2 = e.radius * e.radius;
-    ed.bminx = e.center[0] - e.radius;
-    ed.bminy = e.center[1] - e.radius;
-    ed.bminz = e.center[2] - e.radius;
-    ed.bmaxx = e.center[0] + e.radius;
-    ed.bmaxy = e.center[1] + e.radius;
-    ed.bmaxz = e.center[2] + e.radius;
+    float bx = e.center[0], by = e.center[1], bz = e.center[2];
+    if (e.tool == HD_TOOL_COPY) {
+        // BoxEditorBase(center - source + dest, radius)
+        ed.srcx = e.source[0];
+        ed.srcy = e.source[1];
+        ed.srcz = e.source[2];
+        ed.dstx = e.dest[0];
+        ed.dsty = e.dest[1];
+        ed.dstz = e.dest[2];
+        bx = e.center[0] - e.source[0] + e.dest[0];
+        by = e.center[1] - e.source[1] + e.dest[1];
+        bz = e.center[2] - e.source[2] + e.dest[2];
+        ed.minx = e.center[0] - e.radius;
+        ed.miny = e.center[1] - e.radius;
+        ed.minz = e.center[2] - e.radius;
+        ed.size = 2 * uint32_t(ceilf(e.radius));
+    }
+    ed.bminx = bx - e.radius;
+    ed.bminy = by - e.radius;
+    ed.bminz = bz - e.radius;
+    ed.bmaxx = bx + e.radius;
+    ed.bmaxy = by + e.radius;
+    ed.bmaxz = bz + e.radius;
+    ed.paint_r = float(e.rgb & 0xFF) / 255.0f;
+    ed.paint_g = float((e.rgb >> 8) & 0xFF) / 255.0f;
+    ed.paint_b = float((e.rgb >> 16) & 0xFF) / 255.0f;
     return ed;
+}
+
+// the copy tool's source index of a destination voxel, or -1 (:585-606)
+HD_HD int64_t copy_index(const Editor& e, float px, float py, float pz)
+{
+    const float qx = ((px - e.dstx) + e.srcx) - e.minx, qy = ((py - e.dsty) + e.srcy) - e.miny,
+                qz = ((pz - e.dstz) + e.srcz) - e.minz;
+    const uint32_t ix = uint32_t(qx < 0 ? 0.0f : qx), iy = uint32_t(qy < 0 ? 0.0f : qy),
+                   iz = uint32_t(qz < 0 ? 0.0f : qz);
+    if (ix >= e.size || iy >= e.size || iz >= e.size)
+        return -1;
+    return int64_t(ix) + int64_t(e.size) * iy + int64_t(e.size) * e.size * iz;
+}
+// get_new_value of each editor
+HD_HD bool new_value(const Editor& e, float px, float py, float pz, bool prev)
+{
+    if (e.tool == HD_TOOL_SPHERE_PAINT)
+        return prev;
+    if (e.tool == HD_TOOL_COPY) {
+        if (prev)
+            return prev;
+        const int64_t i = copy_index(e, px, py, pz);
+        return i < 0 ? prev : e.values[i] != 0;
+    }
+    return e.adding();
 }
 
 HD_D float sqr(float f) { return f * f; }
@@ -120,6 +179,12 @@ struct Level {
     uint32_t* exp;   // exclusive scan of flag
     uint64_t* leaf;  // new leaf masks (leaf level only)
     uint32_t* cand;  // candidate content, 9 words per entry
+    // colours (allocated only when the context has colours)
+    uint32_t* ocnt;  // voxel count of the old node (levels >= T)
+    uint32_t* cn;    // levels < T: colour node; level T: the slot's leaf reference
+    uint32_t* noff;  // offset in the task's new colour sequence (levels >= T)
+    uint32_t* ooff;  // offset in the task's old leaf
+    uint32_t* task;  // level-T entry the entry belongs to
 };
 
 struct EditCounters {
@@ -167,7 +232,7 @@ HD_D void classify_entry(const Table& t, const Editor& ed, uint32_t level, const
                     const uint32_t* p = t.sys(old);
                     cnt = level < leafl ? (p[0] >> 8) : popc32(p[0]) + popc32(p[1]);
                 }
-            } else if (inside_tool(ed, mnx, mny, mnz, mxx, mxy, mxz)) {
+            } else if (ed.shortcuts() && inside_tool(ed, mnx, mny, mnz, mxx, mxy, mxz)) {
                 const uint32_t full_count = 1u << (3 * depth);
                 voxels = full_count;
                 if (ed.adding()) {
@@ -195,7 +260,7 @@ HD_D void classify_entry(const Table& t, const Editor& ed, uint32_t level, const
                         if (should_edit_impl(ed, px, py, pz, px + 1.0f, py + 1.0f, pz + 1.0f)) {
                             edited++;
                             const uint64_t bit = 1ull << (c1 * 8 + c2);
-                            leaf = ed.adding() ? (leaf | bit) : (leaf & ~bit);
+                            leaf = new_value(ed, px, py, pz, (leaf & bit) != 0) ? (leaf | bit) : (leaf & ~bit);
                         }
                     }
                 voxels = edited;
@@ -209,6 +274,14 @@ HD_D void classify_entry(const Table& t, const Editor& ed, uint32_t level, const
     lv.res[i] = res;
     lv.cnt[i] = cnt;
     lv.flag[i] = state == kDescend;
+    if (lv.ocnt && level >= T) {
+        uint32_t oc = 0;
+        if (old != kInvalid) {
+            const uint32_t* p = t.sys(old);
+            oc = level < leafl ? (p[0] >> 8) : popc32(p[0]) + popc32(p[1]);
+        }
+        lv.ocnt[i] = oc;
+    }
 }
 
 // A descended entry spawns its 8 children (child order) at 8 * exp[i] on the

@@ -602,6 +602,31 @@ void edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* per_
     const auto t0 = std::chrono::steady_clock::now();
     cudaStream_t st = c->stream;
     hd_edit_stats sum{};
+    bool plain = c->colors;
+    for (uint32_t i = 0; i < n && !plain; i++)
+        plain = edits[i].tool > HD_TOOL_BOX_ADD;
+    if (plain) {
+        // colours, paint and copy take the one-edit path, edit by edit
+        float at = 0;
+        for (uint32_t i = 0; i < n; i++) {
+            hd_edit_stats s{};
+            edit_one(c, edits[i], &s);
+            at += s.device_ms;
+            s.host_ms = at;
+            if (per_edit)
+                per_edit[i] = s;
+            sum.num_voxels += s.num_voxels;
+            sum.num_nodes += s.num_nodes;
+            sum.find_or_add_calls += s.find_or_add_calls;
+            sum.nodes_added += s.nodes_added;
+            sum.words_scanned += s.words_scanned;
+        }
+        sum.device_ms = at;
+        sum.host_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (total)
+            *total = sum;
+        return;
+    }
     if (!c->batch)
         c->batch = new BatchGraph();
     BatchGraph& bg = *c->batch;
@@ -646,6 +671,14 @@ void edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* per_
         const uint32_t ok = fin.idx; // edits applied in this round
         if (ok) {
             HD_CUDA(cudaMemcpy(ctr.data() + done, b.ctr, sizeof(EditCounters) * ok, cudaMemcpyDeviceToHost));
+            std::vector<uint32_t> roots(ok);
+            HD_CUDA(cudaMemcpy(roots.data(), b.roots, 4ull * ok, cudaMemcpyDeviceToHost));
+            for (uint32_t k = 0; k < ok; k++) {
+                UndoFrame f;
+                f.root = c->root;
+                push_undo(c, std::move(f));
+                c->root = roots[k];
+            }
             for (uint32_t k = 0; k < ok; k++) {
                 float a = 0, d = 0;
                 HD_CUDA(cudaEventElapsedTime(&a, bg.events[0], bg.events[k + 1]));
@@ -669,6 +702,7 @@ void edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* per_
                               "edit " + std::to_string(done) + " failed on the device (" + c->err_detail + ")"};
         }
         // capacity: this edit with the one-edit path, then resume
+        c->root = read_scalar(c->d_root, st);
         hd_edit_stats s{};
         edit_one(c, edits[done], &s);
         ctr[done].num_voxels = s.num_voxels;
@@ -736,7 +770,7 @@ hd_status guarded_call(hd_ctx* c, F&& f)
 bool valid_edits(const hd_edit* edits, uint32_t n)
 {
     for (uint32_t i = 0; i < n; i++)
-        if (edits[i].tool > HD_TOOL_BOX_ADD || !(edits[i].radius >= 0.0f))
+        if (edits[i].tool > HD_TOOL_COPY || !(edits[i].radius >= 0.0f))
             return false;
     return true;
 }

@@ -182,19 +182,37 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots)
 
 } // namespace hd
 
-extern "C" hd_status hd_gc(hd_ctx* c, uint32_t* extra, uint32_t n)
+extern "C" hd_status hd_gc_ex(hd_ctx* c, uint32_t* extra, uint32_t n, uint32_t flags)
 {
-    if (!c || (n && !extra))
+    if (!c || (n && !extra) || (flags & ~uint32_t(HD_GC_KEEP_HISTORY)))
         return HD_ERR_INVALID;
     try {
         std::vector<uint32_t> roots(1 + n);
         roots[0] = hd::read_scalar(c->d_root, c->stream);
         for (uint32_t i = 0; i < n; i++)
             roots[1 + i] = extra[i];
+        if (flags & HD_GC_KEEP_HISTORY) {
+            // the roots of the undo / redo frames stay alive and are remapped
+            for (auto& f : c->undo)
+                roots.push_back(f.root);
+            for (auto& f : c->redo)
+                roots.push_back(f.root);
+        } else {
+            // the engine frees its undo history with the GC (engine.cpp:178-185)
+            c->undo.clear();
+            c->redo.clear();
+        }
         hd::gc(c, roots);
         // the remapped extra roots go back to the caller
         for (uint32_t i = 0; i < n; i++)
             extra[i] = roots[1 + i];
+        size_t k = 1 + n;
+        if (flags & HD_GC_KEEP_HISTORY) {
+            for (auto& f : c->undo)
+                f.root = roots[k++];
+            for (auto& f : c->redo)
+                f.root = roots[k++];
+        }
         return HD_OK;
     } catch (const hd::StatusError& e) {
         c->err = e.msg;
@@ -204,3 +222,5 @@ extern "C" hd_status hd_gc(hd_ctx* c, uint32_t* extra, uint32_t n)
         return HD_ERR_CUDA;
     }
 }
+
+extern "C" hd_status hd_gc(hd_ctx* c, uint32_t* extra, uint32_t n) { return hd_gc_ex(c, extra, n, 0); }

@@ -19,10 +19,6 @@
 
 namespace hd {
 
-struct F3 {
-    float x, y, z;
-};
-
 HD_D float fmax_r(float a, float b) { return a > b ? a : b; } // constexpr_max (cuda_math.h:13)
 HD_D float fmin_r(float a, float b) { return a < b ? a : b; }
 

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define HD_ABI_VERSION 3u
+#define HD_ABI_VERSION 4u
 #define HD_PAGE_SIZE 512u
 #define HD_MAX_DEPTH 20u
 /* Sentinel of the edit recursion (hash_dag_edits.h:17). */
@@ -246,6 +246,37 @@ hd_status hd_autotune_batch(hd_ctx* ctx, const hd_edit* sample, uint32_t n, hd_b
  * its bound), since the context was created. */
 hd_status hd_batch_fallbacks(hd_ctx* ctx, uint64_t* count);
 
+/* ---- colours (HashDAGColors, hash_dag_colors.h; variable_weight_size_colors.h) */
+
+/* Builds the colour tree of the current scene: one colour node per path above
+ * C_colorTreeLevels, one compressed colour leaf per path at
+ * C_colorTreeLevels with its voxels' colours in depth-first order (the
+ * seeded colour field of color_seed: RGB8 of a value-noise field on an
+ * aligned 8^3 grid, stored as set_single_color(rgb / 255)).  From then on
+ * every edit rebuilds the colour leaves it touches (all six tools). */
+hd_status hd_colors_from_scene(hd_ctx* ctx, uint64_t color_seed);
+/* DAGUtils::get_color (dag_utils.h:423-523) for n voxels (d_xyz: 3 uint32
+ * per voxel, device); CompressedColor{} for empty voxels outside any leaf. */
+hd_status hd_get_colors(hd_ctx* ctx, const uint32_t* d_xyz, uint64_t n, hd_color* d_out);
+/* The colour lookup of Tracer::trace_colors (tracer.cu:254-451) on the paths
+ * of hd_trace_primary: RGB888 | 0xff000000 of the hit voxel's colour
+ * (CompressedColor::get_color, float3_to_rgb888), 0 for a miss.  Headless:
+ * no shading or debug colour modes. */
+hd_status hd_trace_colors(hd_ctx* ctx, const uint32_t* d_paths, uint32_t width, uint32_t height,
+                          uint32_t* d_rgba);
+/* colour-tree nodes (entries), leaves, blocks, macro words, weight words */
+hd_status hd_color_stats(hd_ctx* ctx, uint64_t* out5);
+
+/* ---- undo / redo (HashDAGUndoRedo, hash_dag.h:20-212) ------------------- */
+
+/* Every successful edit records a frame (the root before it and the colour
+ * leaves it replaced); undo restores them, redo re-applies; a new edit drops
+ * the redo frames.  At most `capacity` undo frames are kept (default 200). */
+hd_status hd_undo(hd_ctx* ctx); /* HD_ERR_STATE when there is nothing to undo */
+hd_status hd_redo(hd_ctx* ctx);
+hd_status hd_set_undo_capacity(hd_ctx* ctx, uint32_t frames);
+hd_status hd_history(hd_ctx* ctx, uint32_t* undo_frames, uint32_t* redo_frames);
+
 /* ---- garbage collection (HashDAG::remove_stale_nodes, hash_dag.h:407-547) */
 
 /* Marks the nodes reachable from the root and from the n extra roots, then
@@ -254,6 +285,12 @@ hd_status hd_batch_fallbacks(hd_ctx* ctx, uint64_t* count);
  * remapped.  Pages stay mapped (the reference never unmaps them).  The root
  * and h_extra_roots (in/out) are rewritten to their new addresses. */
 hd_status hd_gc(hd_ctx* ctx, uint32_t* h_extra_roots, uint32_t n_extra);
+/* hd_gc with flags: HD_GC_KEEP_HISTORY keeps the undo / redo frames (their
+ * roots stay alive and are remapped); without it the history is dropped, as
+ * the reference's engine frees its HashDAGUndoRedo after a GC
+ * (engine.cpp:178-185). */
+#define HD_GC_KEEP_HISTORY 1u
+hd_status hd_gc_ex(hd_ctx* ctx, uint32_t* h_extra_roots, uint32_t n_extra, uint32_t flags);
 
 /* ---- state and statistics ---------------------------------------------- */
 
