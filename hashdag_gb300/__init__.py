@@ -19,9 +19,11 @@ import ctypes as C
 import numpy as np
 
 from . import _capi
-from ._capi import BatchTuning, Camera, Config, Edit, EditStats, HashDagError, LevelStats, lib
+from ._capi import (BatchTuning, Camera, Config, Edit, EditStats, HashDagError, LevelStats, Request, RequestResult,
+                    ServeConfig, ServeStats, lib)
 
-__all__ = ["HashDAG", "DAGTracer", "SphereEditor", "BoxEditor", "SpherePaintEditor", "CopyEditor", "BatchTuning", "Camera", "Config", "EditStats", "LevelStats",
+__all__ = ["HashDAG", "DAGTracer", "SphereEditor", "BoxEditor", "SpherePaintEditor", "CopyEditor", "BatchTuning",
+           "Request", "RequestResult", "ServeConfig", "ServeStats", "edit_request", "render_request", "Camera", "Config", "EditStats", "LevelStats",
            "HashDagError", "default_config"]
 
 TOOL_SPHERE_REMOVE, TOOL_SPHERE_ADD, TOOL_BOX_REMOVE, TOOL_BOX_ADD, TOOL_SPHERE_PAINT, TOOL_COPY = range(6)
@@ -97,6 +99,15 @@ class CopyEditor(_Editor):
         super().__init__(center, radius)
         self.source = tuple(float(np.float32(v)) for v in source)
         self.dest = tuple(float(np.float32(v)) for v in dest)
+
+
+def edit_request(arrival_ms, editor):
+    return Request(0, 0, 0, 0, float(arrival_ms), editor.to_edit(), Camera())
+
+
+def render_request(arrival_ms, width, height, camera):
+    cam = camera if isinstance(camera, Camera) else Camera.from_params(camera)
+    return Request(1, int(width), int(height), 0, float(arrival_ms), Edit(), cam)
 
 
 def editor_from_tuple(t):
@@ -317,6 +328,19 @@ class HashDAG:
         self._check(lib().hd_gc_ex(self._h, arr.ctypes.data, len(extra_roots),
                                    GC_KEEP_HISTORY if keep_history else 0))
         return [int(v) for v in arr[:len(extra_roots)]]
+
+    # -- serving loop ----------------------------------------------------------
+    def serve(self, requests, continuous=True, max_renders=3, realtime=True, gc_free_fraction=0.1,
+              light=(0.3, 1.0, 0.2), shadow_bias=1.0):
+        """Runs a request trace (a list of Request, arrival times
+        non-decreasing); returns (list of RequestResult, ServeStats)."""
+        arr = (Request * max(1, len(requests)))(*requests)
+        cfg = ServeConfig(int(continuous), int(max_renders), int(realtime), float(gc_free_fraction),
+                          (C.c_float * 3)(*light), float(shadow_bias))
+        res = (RequestResult * max(1, len(requests)))()
+        st = ServeStats()
+        self._check(lib().hd_serve(self._h, arr, len(requests), C.byref(cfg), res, C.byref(st)))
+        return list(res)[:len(requests)], st
 
     def set_fp_mode(self, mode):
         self._check(lib().hd_set_fp_mode(self._h, int(mode)))

@@ -57,6 +57,32 @@ class BatchTuning(C.Structure):
         return f"BatchTuning(foa_warps={self.foa_warps}, probe_words={self.probe_words}, grid_blocks={self.grid_blocks})"
 
 
+class Request(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32), ("reserved", C.c_uint32),
+                ("arrival_ms", C.c_double), ("edit", Edit), ("camera", Camera)]
+
+
+class ServeConfig(C.Structure):
+    _fields_ = [("continuous", C.c_uint32), ("max_renders", C.c_uint32), ("realtime", C.c_uint32),
+                ("gc_free_fraction", C.c_float), ("light", C.c_float * 3), ("shadow_bias", C.c_float)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("start_ms", C.c_double), ("end_ms", C.c_double), ("root", C.c_uint32), ("status", C.c_uint32),
+                ("edits_before", C.c_uint32), ("reserved", C.c_uint32), ("checksum", C.c_uint64),
+                ("num_voxels", C.c_uint64)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("wall_ms", C.c_double), ("edits", C.c_uint32), ("renders", C.c_uint32), ("gcs", C.c_uint32),
+                ("reserved", C.c_uint32), ("edit_p50_ms", C.c_double), ("edit_p99_ms", C.c_double),
+                ("frame_p50_ms", C.c_double), ("frame_p99_ms", C.c_double), ("voxels_per_s", C.c_double),
+                ("num_voxels", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 class LevelStats(C.Structure):
     _fields_ = [("words", C.c_uint64 * MAX_DEPTH), ("nodes", C.c_uint64 * MAX_DEPTH), ("pages_used", C.c_uint64),
                 ("root", C.c_uint32), ("levels", C.c_uint32)]
@@ -91,6 +117,8 @@ SIGNATURES = [
     ("hd_set_undo_capacity", C.c_int, [_P, _u32]),
     ("hd_history", C.c_int, [_P, C.POINTER(_u32), C.POINTER(_u32)]),
     ("hd_gc_ex", C.c_int, [_P, _P, _u32, _u32]),
+    ("hd_serve", C.c_int, [_P, C.POINTER(Request), _u32, C.POINTER(ServeConfig), C.POINTER(RequestResult),
+                           C.POINTER(ServeStats)]),
     ("hd_export_basic_dag", C.c_int, [_P, _P, _u64, C.POINTER(_u64)]),
     ("hd_trace_primary", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _P, C.POINTER(_f32)]),
     ("hd_trace_shadow", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _P, C.POINTER(_f32), _f32, _P,

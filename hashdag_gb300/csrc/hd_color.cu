@@ -347,13 +347,14 @@ __global__ void k_trace_colors(Table t, ColorTable ct, const uint32_t* __restric
     }
 }
 
-void trace_colors(hd_ctx* c, const uint32_t* d_paths, uint32_t w, uint32_t h, uint32_t* d_rgba)
+void trace_colors(hd_ctx* c, const uint32_t* d_paths, uint32_t w, uint32_t h, uint32_t* d_rgba, cudaStream_t stream,
+                  const uint32_t* d_root)
 {
     if (!c->colors)
         throw StatusError{HD_ERR_STATE, "the context has no colours"};
     const uint64_t n = uint64_t(w) * h;
-    k_trace_colors<<<grid_for(n, 256), 256, 0, c->stream>>>(c->t, c->ct, c->d_root,
-                                                             reinterpret_cast<const uint4*>(d_paths), n, d_rgba);
+    k_trace_colors<<<grid_for(n, 256), 256, 0, stream ? stream : c->stream>>>(
+        c->t, c->ct, d_root ? d_root : c->d_root, reinterpret_cast<const uint4*>(d_paths), n, d_rgba);
     HD_LAUNCH_CHECK();
 }
 
@@ -797,6 +798,9 @@ void edit_colors(hd_ctx* c, const Editor& ed, std::vector<Level>& lv, const std:
     HD_CUDA(cudaMemcpyAsync(tot, d_tot, 16, cudaMemcpyDeviceToHost, st));
     HD_CUDA(cudaStreamSynchronize(st));
     need_new_total = tot[3];
+    // renders in flight read the leaves about to be replaced: wait for them
+    for (cudaEvent_t e : c->color_fences)
+        HD_CUDA(cudaStreamWaitEvent(st, e, 0));
     // nodes: at most one per entry above T
     uint64_t max_nodes = 0;
     for (uint32_t L = 1; L < T; L++)

@@ -51,6 +51,9 @@ struct hd_ctx {
     // undo / redo history
     std::deque<hd::UndoFrame> undo, redo;
     size_t undo_capacity = 200;
+    // events the colour commit of the next edit waits for (renders in flight
+    // that still read the colour leaves the edit replaces)
+    std::vector<cudaEvent_t> color_fences;
 };
 
 namespace hd {
@@ -79,7 +82,8 @@ struct Level;
 void color_release(hd_ctx* c);
 void colors_from_scene(hd_ctx* c, uint64_t color_seed);
 void get_colors(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, hd_color* d_out);
-void trace_colors(hd_ctx* c, const uint32_t* d_paths, uint32_t w, uint32_t h, uint32_t* d_rgba);
+void trace_colors(hd_ctx* c, const uint32_t* d_paths, uint32_t w, uint32_t h, uint32_t* d_rgba,
+                  cudaStream_t stream = nullptr, const uint32_t* d_root = nullptr);
 void copy_source(hd_ctx* c, Editor& ed);
 void color_spawn(hd_ctx* c, uint32_t level, uint32_t n, const Level& lv, const Level& next);
 void edit_colors(hd_ctx* c, const Editor& ed, std::vector<Level>& lv, const std::vector<uint32_t>& count,
@@ -88,10 +92,13 @@ bool undo_step(hd_ctx* c, bool redo);
 void push_undo(hd_ctx* c, UndoFrame&& f);
 
 // hd_trace.cu
+// stream / d_root: nullptr = the context's stream and root
 void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint32_t* d_paths,
-                   unsigned long long* d_counters = nullptr);
+                   unsigned long long* d_counters = nullptr, cudaStream_t stream = nullptr,
+                   const uint32_t* d_root = nullptr);
 void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
-                  const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters = nullptr);
+                  const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters = nullptr,
+                  cudaStream_t stream = nullptr, const uint32_t* d_root = nullptr);
 void get_values(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out);
 
 } // namespace hd

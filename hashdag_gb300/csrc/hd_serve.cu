@@ -1,0 +1,344 @@
+// Serving loop: a stream of edit and render requests against one resident
+// DAG (table, colours, undo history on the device).
+//
+// The reference's interactive engine applies one edit per frame and renders
+// in between (Engine::tick, engine.cpp:575-720).  Here requests arrive on
+// their own clock and two policies run the same trace:
+//  * sequential: one request at a time in arrival order, each finished
+//    before the next starts (the plain GPU path);
+//  * continuous: renders are admitted into up to max_renders slots, each on
+//    its own stream, reading the root of the moment they are admitted;
+//    edits run in arrival order on the context stream while renders are in
+//    flight (a render's colour pass completes before a later edit replaces
+//    colour leaves); when free pool words fall below gc_free_fraction the
+//    renders drain and a GC runs that keeps the undo history.  Without
+//    colours, queued geometry edits go through the batched graph path.
+// Every render produces paths, a shadow mask and (with colours) RGBA, and a
+// checksum of them that does not depend on node addresses, so a render can
+// be compared with the same render made alone on the same state.
+#include <algorithm>
+#include <chrono>
+#include <deque>
+#include <thread>
+#include <vector>
+
+#include "hd_color.cuh"
+#include "hd_ctx.h"
+
+namespace hd {
+
+void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats);
+
+// order-independent checksum of a rendered frame: sum over pixels of a mix of
+// (pixel, path, shadow, colour)
+__global__ void k_frame_checksum(const uint4* __restrict__ paths, const uint8_t* __restrict__ mask,
+                                 const uint32_t* __restrict__ rgba, uint64_t n, unsigned long long* out)
+{
+    unsigned long long acc = 0;
+    HD_GRID_STRIDE(i, n)
+    {
+        const uint4 p = paths[i];
+        uint64_t h = mix64(i ^ (uint64_t(p.x) << 21) ^ (uint64_t(p.y) << 42));
+        h = mix64(h ^ p.z ^ (uint64_t(mask[i]) << 32) ^ (rgba ? uint64_t(rgba[i]) << 24 : 0));
+        acc += h;
+    }
+    for (int o = 16; o; o >>= 1)
+        acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0)
+        atomicAdd(out, acc);
+}
+
+__global__ void k_words_total(Table t, uint32_t levels, unsigned long long* out)
+{
+    unsigned long long sum = 0;
+    for (uint32_t level = 0; level < levels; level++) {
+        const uint32_t nb = t.g.buckets(level), first = t.g.level_first_bucket(level);
+        for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x)
+            sum += t.bucket_sizes[first + b];
+    }
+    for (int o = 16; o; o >>= 1)
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0)
+        atomicAdd(out, sum);
+}
+
+namespace {
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    uint32_t* paths = nullptr;
+    uint8_t* mask = nullptr;
+    uint32_t* rgba = nullptr;
+    uint32_t* root = nullptr;
+    unsigned long long* sum = nullptr;
+    unsigned long long* h_sum = nullptr; // pinned
+    cudaEvent_t colors_done = nullptr, done = nullptr;
+    int64_t req = -1;
+    uint64_t pixels = 0;
+};
+
+struct Clock {
+    std::chrono::steady_clock::time_point t0;
+    cudaEvent_t ev0 = nullptr;
+    double now() const { return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); }
+    double at(cudaEvent_t e) const
+    {
+        float ms = 0;
+        HD_CUDA(cudaEventElapsedTime(&ms, ev0, e));
+        return ms;
+    }
+};
+
+uint64_t free_words(hd_ctx* c)
+{
+    unsigned long long* d = c->scratch.get<unsigned long long>("serve_words", 1);
+    HD_CUDA(cudaMemsetAsync(d, 0, 8, c->stream));
+    k_words_total<<<152, 256, 0, c->stream>>>(c->t, c->g.leaf_level + 1, d);
+    HD_LAUNCH_CHECK();
+    const unsigned long long used = read_scalar(d, c->stream);
+    const uint64_t cap = uint64_t(c->cfg.pool_pages) * kPage;
+    return used >= cap ? 0 : cap - used;
+}
+
+} // namespace
+
+void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config& cfg, hd_request_result* res,
+           hd_serve_stats* stats)
+{
+    cudaStream_t st = c->stream;
+    const uint32_t R = cfg.continuous ? (cfg.max_renders ? cfg.max_renders : 1) : 1;
+    uint64_t max_pixels = 1;
+    for (uint32_t i = 0; i < n; i++)
+        if (reqs[i].kind == HD_REQ_RENDER)
+            max_pixels = std::max<uint64_t>(max_pixels, uint64_t(reqs[i].width) * reqs[i].height);
+    std::vector<Slot> slots(R);
+    for (uint32_t k = 0; k < R; k++) {
+        Slot& s = slots[k];
+        char nm[32];
+        if (cfg.continuous)
+            HD_CUDA(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
+        else
+            s.stream = st;
+        snprintf(nm, sizeof(nm), "serve_paths_%u", k);
+        s.paths = c->scratch.get<uint32_t>(nm, max_pixels * 4);
+        snprintf(nm, sizeof(nm), "serve_mask_%u", k);
+        s.mask = c->scratch.get<uint8_t>(nm, max_pixels);
+        snprintf(nm, sizeof(nm), "serve_rgba_%u", k);
+        s.rgba = c->scratch.get<uint32_t>(nm, max_pixels);
+        snprintf(nm, sizeof(nm), "serve_root_%u", k);
+        s.root = c->scratch.get<uint32_t>(nm, 1);
+        snprintf(nm, sizeof(nm), "serve_sum_%u", k);
+        s.sum = c->scratch.get<unsigned long long>(nm, 1);
+        HD_CUDA(cudaMallocHost(&s.h_sum, 8));
+        HD_CUDA(cudaEventCreateWithFlags(&s.colors_done, cudaEventDisableTiming));
+        HD_CUDA(cudaEventCreate(&s.done));
+    }
+    auto cleanup = [&] {
+        for (Slot& s : slots) {
+            if (s.stream && s.stream != st) {
+                cudaStreamSynchronize(s.stream);
+                cudaStreamDestroy(s.stream);
+            }
+            if (s.h_sum)
+                cudaFreeHost(s.h_sum);
+            if (s.colors_done)
+                cudaEventDestroy(s.colors_done);
+            if (s.done)
+                cudaEventDestroy(s.done);
+        }
+        c->color_fences.clear();
+    };
+    try {
+        Clock clk;
+        HD_CUDA(cudaEventCreate(&clk.ev0));
+        HD_CUDA(cudaStreamSynchronize(st));
+        HD_CUDA(cudaEventRecord(clk.ev0, st));
+        HD_CUDA(cudaEventSynchronize(clk.ev0));
+        clk.t0 = std::chrono::steady_clock::now();
+        const uint64_t cap_words = uint64_t(c->cfg.pool_pages) * kPage;
+        uint32_t edits_done = 0, gcs = 0, completed = 0;
+        uint64_t voxels = 0;
+        std::deque<uint32_t> edits, renders;
+        uint32_t next = 0;
+        cudaEvent_t edit_ev;
+        HD_CUDA(cudaEventCreate(&edit_ev));
+
+        auto launch_render = [&](Slot& s, uint32_t i) {
+            const hd_request& r = reqs[i];
+            res[i].start_ms = clk.now();
+            res[i].root = c->root;
+            res[i].edits_before = edits_done;
+            HD_CUDA(cudaMemcpyAsync(s.root, &c->root, 4, cudaMemcpyHostToDevice, s.stream));
+            trace_primary(c, r.camera, r.width, r.height, s.paths, nullptr, s.stream, s.root);
+            trace_shadow(c, r.camera, r.width, r.height, s.paths, cfg.light, cfg.shadow_bias, s.mask, nullptr,
+                         s.stream, s.root);
+            if (c->colors)
+                trace_colors(c, s.paths, r.width, r.height, s.rgba, s.stream, s.root);
+            HD_CUDA(cudaEventRecord(s.colors_done, s.stream));
+            const uint64_t px = uint64_t(r.width) * r.height;
+            HD_CUDA(cudaMemsetAsync(s.sum, 0, 8, s.stream));
+            k_frame_checksum<<<grid_for(px, 256, 152 * 8), 256, 0, s.stream>>>(
+                reinterpret_cast<const uint4*>(s.paths), s.mask, c->colors ? s.rgba : nullptr, px, s.sum);
+            HD_LAUNCH_CHECK();
+            HD_CUDA(cudaMemcpyAsync(s.h_sum, s.sum, 8, cudaMemcpyDeviceToHost, s.stream));
+            HD_CUDA(cudaEventRecord(s.done, s.stream));
+            s.req = i;
+            s.pixels = px;
+        };
+        auto finish_render = [&](Slot& s) {
+            const uint32_t i = uint32_t(s.req);
+            res[i].end_ms = clk.at(s.done);
+            res[i].checksum = *s.h_sum;
+            res[i].status = HD_OK;
+            s.req = -1;
+            completed++;
+        };
+        auto drain = [&] {
+            for (Slot& s : slots)
+                if (s.req >= 0) {
+                    HD_CUDA(cudaEventSynchronize(s.done));
+                    finish_render(s);
+                }
+        };
+        auto run_edit = [&](uint32_t i) {
+            if (cfg.gc_free_fraction > 0 && double(free_words(c)) < cfg.gc_free_fraction * double(cap_words)) {
+                drain();
+                uint32_t dummy = 0;
+                const hd_status g = hd_gc_ex(c, &dummy, 0, HD_GC_KEEP_HISTORY);
+                if (g != HD_OK)
+                    throw StatusError{g, "GC inside the serving loop failed: " + c->err};
+                gcs++;
+            }
+            c->color_fences.clear();
+            for (Slot& s : slots)
+                if (s.req >= 0)
+                    c->color_fences.push_back(s.colors_done);
+            res[i].start_ms = clk.now();
+            hd_edit_stats es{};
+            edit_one(c, reqs[i].edit, &es);
+            HD_CUDA(cudaEventRecord(edit_ev, st));
+            HD_CUDA(cudaEventSynchronize(edit_ev));
+            c->color_fences.clear();
+            res[i].end_ms = clk.at(edit_ev);
+            res[i].root = c->root;
+            res[i].num_voxels = es.num_voxels;
+            res[i].checksum = es.num_voxels;
+            res[i].edits_before = edits_done;
+            res[i].status = HD_OK;
+            voxels += es.num_voxels;
+            edits_done++;
+            completed++;
+        };
+
+        while (completed < n) {
+            const double now = clk.now();
+            while (next < n && (!cfg.realtime || reqs[next].arrival_ms <= now)) {
+                (reqs[next].kind == HD_REQ_RENDER ? renders : edits).push_back(next);
+                next++;
+            }
+            if (!cfg.continuous) {
+                // one request at a time, in arrival order
+                if (!edits.empty() || !renders.empty()) {
+                    const bool edit_first =
+                        renders.empty() || (!edits.empty() && edits.front() < renders.front());
+                    if (edit_first) {
+                        const uint32_t i = edits.front();
+                        edits.pop_front();
+                        run_edit(i);
+                    } else {
+                        const uint32_t i = renders.front();
+                        renders.pop_front();
+                        launch_render(slots[0], i);
+                        HD_CUDA(cudaEventSynchronize(slots[0].done));
+                        finish_render(slots[0]);
+                    }
+                    continue;
+                }
+            } else {
+                bool progress = false;
+                for (Slot& s : slots)
+                    if (s.req >= 0 && cudaEventQuery(s.done) == cudaSuccess) {
+                        finish_render(s);
+                        progress = true;
+                    }
+                for (Slot& s : slots)
+                    if (s.req < 0 && !renders.empty()) {
+                        launch_render(s, renders.front());
+                        renders.pop_front();
+                        progress = true;
+                    }
+                if (!edits.empty()) {
+                    const uint32_t i = edits.front();
+                    edits.pop_front();
+                    run_edit(i);
+                    progress = true;
+                }
+                if (progress)
+                    continue;
+            }
+            // idle: wait for the next arrival or a render
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+        drain();
+        HD_CUDA(cudaStreamSynchronize(st));
+        const double wall = clk.now();
+        std::vector<double> el, fr;
+        for (uint32_t i = 0; i < n; i++)
+            (reqs[i].kind == HD_REQ_RENDER ? fr : el).push_back(res[i].end_ms - reqs[i].arrival_ms);
+        auto pct = [](std::vector<double> v, double q) {
+            if (v.empty())
+                return 0.0;
+            std::sort(v.begin(), v.end());
+            const double pos = q / 100.0 * double(v.size() - 1);
+            const size_t lo = size_t(pos);
+            const size_t hi = std::min(lo + 1, v.size() - 1);
+            return v[lo] + (v[hi] - v[lo]) * (pos - double(lo));
+        };
+        if (stats) {
+            *stats = hd_serve_stats{};
+            stats->wall_ms = wall;
+            stats->edits = uint32_t(el.size());
+            stats->renders = uint32_t(fr.size());
+            stats->gcs = gcs;
+            stats->edit_p50_ms = pct(el, 50);
+            stats->edit_p99_ms = pct(el, 99);
+            stats->frame_p50_ms = pct(fr, 50);
+            stats->frame_p99_ms = pct(fr, 99);
+            stats->voxels_per_s = double(voxels) / (wall * 1e-3);
+            stats->num_voxels = voxels;
+        }
+        cudaEventDestroy(edit_ev);
+        cudaEventDestroy(clk.ev0);
+    } catch (...) {
+        cleanup();
+        throw;
+    }
+    cleanup();
+}
+
+} // namespace hd
+
+extern "C" hd_status hd_serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config* cfg,
+                              hd_request_result* results, hd_serve_stats* stats)
+{
+    if (!c || !cfg || (n && (!reqs || !results)))
+        return HD_ERR_INVALID;
+    for (uint32_t i = 0; i < n; i++) {
+        if (reqs[i].kind > HD_REQ_RENDER || (i && reqs[i].arrival_ms < reqs[i - 1].arrival_ms))
+            return HD_ERR_INVALID;
+        if (reqs[i].kind == HD_REQ_RENDER && (!reqs[i].width || !reqs[i].height))
+            return HD_ERR_INVALID;
+        if (reqs[i].kind == HD_REQ_EDIT && (reqs[i].edit.tool > HD_TOOL_COPY || !(reqs[i].edit.radius >= 0.0f)))
+            return HD_ERR_INVALID;
+    }
+    try {
+        hd::serve(c, reqs, n, *cfg, results, stats);
+        return HD_OK;
+    } catch (const hd::StatusError& e) {
+        c->err = e.msg;
+        return e.status;
+    } catch (const hd::CudaError& e) {
+        c->err = std::string("CUDA error ") + cudaGetErrorString(e.code) + " in " + e.where;
+        return HD_ERR_CUDA;
+    }
+}

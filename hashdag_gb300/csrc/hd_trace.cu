@@ -280,43 +280,48 @@ __global__ void __launch_bounds__(64) k_trace_shadow(Table t, const uint32_t* __
 }
 
 void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint32_t* d_paths,
-                   unsigned long long* d_counters)
+                   unsigned long long* d_counters, cudaStream_t stream, const uint32_t* d_root)
 {
+    cudaStream_t st = stream ? stream : c->stream;
+    const uint32_t* rt = d_root ? d_root : c->d_root;
     dim3 grid((w + 7) / 8, (h + 7) / 8);
     uint4* out = reinterpret_cast<uint4*>(d_paths);
     if (d_counters) {
         if (c->fp_mode)
-            k_trace_primary<1, true><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, out, d_counters);
+            k_trace_primary<1, true><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, out, d_counters);
         else
-            k_trace_primary<0, true><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, out, d_counters);
+            k_trace_primary<0, true><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, out, d_counters);
     } else {
         if (c->fp_mode)
-            k_trace_primary<1, false><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, out, nullptr);
+            k_trace_primary<1, false><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, out, nullptr);
         else
-            k_trace_primary<0, false><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, out, nullptr);
+            k_trace_primary<0, false><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, out, nullptr);
     }
     HD_LAUNCH_CHECK();
 }
 
 void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
-                  const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters)
+                  const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters,
+                  cudaStream_t stream, const uint32_t* d_root)
 {
+    cudaStream_t st = stream ? stream : c->stream;
+    const uint32_t* rt = d_root ? d_root : c->d_root;
     dim3 grid((w + 7) / 8, (h + 7) / 8);
     const F3 l = {light[0], light[1], light[2]};
     const uint4* p = reinterpret_cast<const uint4*>(d_paths);
     if (d_counters) {
         if (c->fp_mode)
-            k_trace_shadow<1, true><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, p, l, bias, d_mask,
+            k_trace_shadow<1, true><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask,
                                                                 d_counters);
         else
-            k_trace_shadow<0, true><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, p, l, bias, d_mask,
+            k_trace_shadow<0, true><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask,
                                                                 d_counters);
     } else {
         if (c->fp_mode)
-            k_trace_shadow<1, false><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, p, l, bias, d_mask,
+            k_trace_shadow<1, false><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask,
                                                                  nullptr);
         else
-            k_trace_shadow<0, false><<<grid, 64, 0, c->stream>>>(c->t, c->d_root, cam, w, h, p, l, bias, d_mask,
+            k_trace_shadow<0, false><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask,
                                                                  nullptr);
     }
     HD_LAUNCH_CHECK();

@@ -122,3 +122,63 @@ def mixed_edits(depth, n, r_range=(4.0, 512.0), seed=SEED_EDITS, mix=(0.5, 0.3, 
     tools = np.where(u < mix[0], SPHERE_REMOVE, np.where(u < mix[0] + mix[1], SPHERE_ADD, BOX_ADD))
     return [(int(tools[i]), tuple(float(np.float32(v)) for v in c[i]), float(np.float32(math.exp(lr[i]))))
             for i in range(n)]
+
+
+def paint_copy_edits(depth, n_paint=512, n_copy=32, paint_r=(8.0, 256.0), copy_radius=128.0, copy_offset=2048,
+                     seed=SEED_EDITS):
+    """Colours / copy workload: n_paint sphere paints (radius log-uniform in
+    paint_r, random RGB8 target) centred on surface voxels, then n_copy copies
+    of a (2 * copy_radius)^3 region around a surface voxel moved by a seeded
+    integer offset in [-copy_offset, copy_offset]^3 (both regions kept inside
+    the volume).  Tuples: (tool, centre, radius, rgb) / (tool, centre, radius,
+    source, dest)."""
+    rng = np.random.default_rng(seed + 100)
+    e = float(1 << depth)
+    c = _centres(depth, n_paint + n_copy, rng)
+    out = []
+    lr = rng.uniform(math.log(paint_r[0]), math.log(paint_r[1]), n_paint)
+    rgb = rng.integers(0, 1 << 24, n_paint)
+    for i in range(n_paint):
+        out.append((4, tuple(float(np.float32(v)) for v in c[i]), float(np.float32(math.exp(lr[i]))), int(rgb[i])))
+    lo, hi = copy_radius + 1, e - copy_radius - 1
+    for i in range(n_copy):
+        src = np.clip(np.floor(c[n_paint + i]), lo, hi)
+        off = rng.integers(-copy_offset, copy_offset + 1, 3).astype(np.float64)
+        dst = np.clip(src + off, lo, hi)
+        out.append((5, tuple(float(v) for v in src), float(copy_radius), (0.0, 0.0, 0.0),
+                    tuple(float(v) for v in dst - src)))
+    return out
+
+
+RESOLUTIONS = ((1280, 720), (1920, 1080), (3840, 2160))
+
+
+def serving_trace(depth, n, rate_per_s, seed=SEED_SERVING, edit_fraction=0.7, r_range=(4.0, 1024.0),
+                  resolutions=RESOLUTIONS, poses=64):
+    """Poisson arrivals at rate_per_s: edit_fraction edits (sphere carve,
+    sphere fill, sphere paint in equal parts; radius log-uniform in r_range;
+    centres on surface voxels; random paint colour), the rest renders at a
+    seeded resolution and a seeded pose of the Catmull-Rom path.  Returns
+    (kind, arrival_ms, payload) tuples: ("edit", t, (tool, centre, radius,
+    rgb)) / ("render", t, (width, height, camera params))."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1000.0 / rate_per_s, n))
+    kinds = rng.uniform(0, 1, n) < edit_fraction
+    c = _centres(depth, n, rng)
+    lr = rng.uniform(math.log(r_range[0]), math.log(r_range[1]), n)
+    tools = rng.choice([SPHERE_REMOVE, SPHERE_ADD, 4], n)
+    rgb = rng.integers(0, 1 << 24, n)
+    res = rng.integers(0, len(resolutions), n)
+    pose = rng.integers(0, poses, n)
+    cams = {}
+    out = []
+    for i in range(n):
+        if kinds[i]:
+            out.append(("edit", float(t[i]), (int(tools[i]), tuple(float(np.float32(v)) for v in c[i]),
+                                              float(np.float32(math.exp(lr[i]))), int(rgb[i]))))
+        else:
+            w, h = resolutions[res[i]]
+            if (w, h) not in cams:
+                cams[(w, h)] = catmull_rom_path(depth, poses, w, h)
+            out.append(("render", float(t[i]), (w, h, cams[(w, h)][pose[i]])))
+    return out

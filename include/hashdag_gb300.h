@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define HD_ABI_VERSION 4u
+#define HD_ABI_VERSION 5u
 #define HD_PAGE_SIZE 512u
 #define HD_MAX_DEPTH 20u
 /* Sentinel of the edit recursion (hash_dag_edits.h:17). */
@@ -276,6 +276,60 @@ hd_status hd_undo(hd_ctx* ctx); /* HD_ERR_STATE when there is nothing to undo */
 hd_status hd_redo(hd_ctx* ctx);
 hd_status hd_set_undo_capacity(hd_ctx* ctx, uint32_t frames);
 hd_status hd_history(hd_ctx* ctx, uint32_t* undo_frames, uint32_t* redo_frames);
+
+/* ---- serving loop -------------------------------------------------------- */
+
+#define HD_REQ_EDIT 0u
+#define HD_REQ_RENDER 1u
+
+/* One request of a trace: an edit (any tool) or a render (primary rays,
+ * shadow rays toward the configured light, colours when the context has
+ * them) at width x height from camera. */
+typedef struct hd_request {
+    uint32_t kind;           /* HD_REQ_EDIT / HD_REQ_RENDER                    */
+    uint32_t width, height;  /* render                                         */
+    uint32_t reserved;
+    double arrival_ms;       /* since the start of the trace, non-decreasing    */
+    hd_edit edit;            /* edit                                           */
+    hd_camera camera;        /* render                                         */
+} hd_request;
+
+typedef struct hd_serve_config {
+    uint32_t continuous;     /* 0: one request at a time in arrival order;
+                                1: renders in flight on their own streams while
+                                   edits run, edits in arrival order           */
+    uint32_t max_renders;    /* render slots (continuous)                      */
+    uint32_t realtime;       /* 1: a request is available at its arrival time  */
+    float gc_free_fraction;  /* GC (keeping the undo history) when the free
+                                pool words fall below this fraction; 0 = never */
+    float light[3];
+    float shadow_bias;
+} hd_serve_config;
+
+typedef struct hd_request_result {
+    double start_ms, end_ms; /* admission and device completion               */
+    uint32_t root;           /* edit: the root after it; render: rendered root */
+    uint32_t status;
+    uint32_t edits_before;   /* edits committed before the request's state     */
+    uint32_t reserved;
+    uint64_t checksum;       /* render: address-independent checksum of paths,
+                                shadow mask and colours; edit: voxels          */
+    uint64_t num_voxels;     /* edit                                           */
+} hd_request_result;
+
+typedef struct hd_serve_stats {
+    double wall_ms;
+    uint32_t edits, renders, gcs, reserved;
+    double edit_p50_ms, edit_p99_ms;    /* completion - arrival                */
+    double frame_p50_ms, frame_p99_ms;
+    double voxels_per_s;                /* edited voxels over the wall time    */
+    uint64_t num_voxels;
+} hd_serve_stats;
+
+/* Runs the trace against the context's DAG (Engine::tick's edit / render
+ * interleaving, engine.cpp:575-720, as a request loop). */
+hd_status hd_serve(hd_ctx* ctx, const hd_request* requests, uint32_t n, const hd_serve_config* config,
+                   hd_request_result* results, hd_serve_stats* stats);
 
 /* ---- garbage collection (HashDAG::remove_stale_nodes, hash_dag.h:407-547) */
 
