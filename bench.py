@@ -25,6 +25,10 @@ radius log-uniform in [4, 512]) applied plainly (hd_edit_apply per edit) and
 batched (hd_edit_batch, autotuned): edited voxels/s, find-or-add/s, p50/p99
 per-edit device latency of both forms, and the oracle's single-thread CPU
 editor on a bounded sample of the same edits.
+"colors": the 2^15 shell scene with colours, 512 paints, 32 copies of 256^3
+regions, one GC.  "serving": a Poisson request trace on the 2^16 coloured
+scene, sequential vs continuous policy (p50/p99 edit and frame latency,
+edited voxels/s).
 """
 import argparse
 import ctypes as C
@@ -60,6 +64,11 @@ def parse():
     p.add_argument("--pool-pages", type=int, default=0, help="physical pool pages (0 = library default)")
     p.add_argument("--edits", type=int, default=256, help="edits of the edit benchmark (0 = skip it)")
     p.add_argument("--edit-cpu-seconds", type=float, default=12.0, help="budget of the CPU edit sample")
+    p.add_argument("--no-colors", action="store_true", help="skip the colours / copy / GC workload")
+    p.add_argument("--no-serving", action="store_true", help="skip the serving-loop workload")
+    p.add_argument("--serving-depth", type=int, default=16)
+    p.add_argument("--serving-requests", type=int, default=300)
+    p.add_argument("--serving-rate", type=float, default=400.0, help="requests per second")
     return p.parse_args()
 
 
@@ -310,6 +319,85 @@ def edit_cpu_baseline(args, tuples):
             "kind": "port", "sample": f"first {k} of the {len(tuples)} edits, oracle C editor, 1 thread, {dt:.1f} s"}
 
 
+def colors_bench(args):
+    """Colours, copy and GC: the 2^15 shell scene with per-voxel colours,
+    512 sphere paints (radius log-uniform in [8, 256], random RGB8), 32 copies
+    of a 256^3 region moved by a seeded offset in [-2048, 2048]^3, then one
+    GC (hd_edit_apply per edit, colour leaves rebuilt on the device)."""
+    import hashdag_gb300 as hd
+    from hashdag_gb300 import workloads
+    depth = args.depth
+    d = hd.HashDAG(depth)
+    t0 = time.perf_counter()
+    d.generate_scene(workloads.SEED_SCENE, shell=True)
+    t1 = time.perf_counter()
+    d.colors_from_scene(workloads.SEED_COLORS)
+    t2 = time.perf_counter()
+    edits = workloads.paint_copy_edits(depth)
+    lat = {4: [], 5: []}
+    vox = {4: 0, 5: 0}
+    t3 = time.perf_counter()
+    for e in edits:
+        s = d.edit_threads(hd.editor_from_tuple(e))
+        lat[e[0]].append(s.device_ms)
+        vox[e[0]] += s.num_voxels
+    t4 = time.perf_counter()
+    pages_before = d.level_stats().pages_used
+    t5 = time.perf_counter()
+    d.remove_stale_nodes()
+    d.sync()
+    t6 = time.perf_counter()
+    st = d.level_stats()
+    out = {"workload": f"paint_copy_gc_d{depth}_shell", "scene_gen_s": t1 - t0, "color_import_s": t2 - t1,
+           "edits_s": t4 - t3, "edits_per_s": len(edits) / (t4 - t3),
+           "voxels_per_s": (vox[4] + vox[5]) / (t4 - t3),
+           "paint": {"n": len(lat[4]), "p50_ms": _pct(lat[4], 50), "p99_ms": _pct(lat[4], 99), "voxels": vox[4]},
+           "copy": {"n": len(lat[5]), "p50_ms": _pct(lat[5], 50), "p99_ms": _pct(lat[5], 99), "voxels": vox[5]},
+           "gc_s": t6 - t5, "pages_before_gc": int(pages_before), "pages_after_gc": int(st.pages_used),
+           "nodes_after_gc": [int(v) for v in st.nodes[:depth - 1]], "color_table": d.color_stats()}
+    d.free()
+    return out
+
+
+def serving_bench(args):
+    """Serving loop: the 2^16 shell scene with colours (2^17 does not fit the
+    table's 32-bit virtual addresses), a Poisson trace (70% sphere carve /
+    fill / paint with radius log-uniform in [4, 1024], 30% renders at 720p,
+    1080p or 4K), replayed in real time by the sequential policy (one request
+    at a time) and by the continuous one (renders in flight while edits run,
+    GC when free pool words fall below 10%)."""
+    import hashdag_gb300 as hd
+    from hashdag_gb300 import workloads
+    depth, n, rate = args.serving_depth, args.serving_requests, args.serving_rate
+    trace = workloads.serving_trace(depth, n, rate)
+
+    def requests():
+        out = []
+        for kind, t, p in trace:
+            if kind == "edit":
+                tool, centre, radius, rgb = p
+                ed = hd.SpherePaintEditor(centre, radius, rgb) if tool == 4 else \
+                    hd.editor_from_tuple((tool, centre, radius))
+                out.append(hd.edit_request(t, ed))
+            else:
+                out.append(hd.render_request(t, p[0], p[1], p[2]))
+        return out
+
+    out = {"workload": f"serving_d{depth}_shell_{n}req_{rate:.0f}per_s", "requests": n, "rate_per_s": rate}
+    for name, continuous in (("sequential", False), ("continuous", True)):
+        d = hd.HashDAG(depth)
+        t0 = time.perf_counter()
+        d.generate_scene(workloads.SEED_SCENE, shell=True)
+        d.colors_from_scene(workloads.SEED_COLORS)
+        setup = time.perf_counter() - t0
+        res, st = d.serve(requests(), continuous=continuous, max_renders=3, realtime=True, gc_free_fraction=0.1)
+        out[name] = dict(st.as_dict(), setup_s=setup)
+        d.free()
+    out["continuous_over_sequential_voxels_per_s"] = (out["continuous"]["voxels_per_s"] /
+                                                      max(1e-9, out["sequential"]["voxels_per_s"]))
+    return out
+
+
 def run_reference(args, dist):
     """The CPU arm: the oracle's restatement of the reference tracer."""
     if dist.rank != 0:
@@ -477,6 +565,11 @@ def run_gpu(args, dist):
                 edits["cpu_baseline"] = edit_cpu_baseline(args, tuples)
             except Exception as e:  # reported, never required
                 edits["cpu_baseline"] = {"value": None, "sample": f"failed: {e}"}
+    colors = serving = None
+    if not args.no_colors:
+        colors = colors_bench(args)
+    if not args.no_serving:
+        serving = serving_bench(args)
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": dist.world, "steps": K,
             "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -489,7 +582,7 @@ def run_gpu(args, dist):
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(_capi.Camera),
                     "d2h_bytes_per_step": W * H * 16 + W * H},
             "gpu_launches": 2 * K, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "wall_s": wall, "edits": edits}
+            "wall_s": wall, "edits": edits, "colors": colors, "serving": serving}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dag.free()

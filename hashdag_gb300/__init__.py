@@ -186,6 +186,11 @@ class HashDAG:
         raw = d_out.cpu().numpy().view(np.uint32).reshape(-1, 2)
         return np.stack([raw[:, 0], raw[:, 1] & 0xFF, (raw[:, 1] >> 8) & 0xFF], axis=1)
 
+    def memory_stats(self):
+        out = (C.c_uint64 * 4)()
+        self._check(lib().hd_memory_stats(self._h, out))
+        return dict(zip(("table", "colors", "scratch", "generation_peak"), (int(v) for v in out)))
+
     def color_stats(self):
         out = (C.c_uint64 * 5)()
         self._check(lib().hd_color_stats(self._h, out))

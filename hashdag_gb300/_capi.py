@@ -112,6 +112,7 @@ SIGNATURES = [
     ("hd_get_colors", C.c_int, [_P, _P, _u64, _P]),
     ("hd_trace_colors", C.c_int, [_P, _P, _u32, _u32, _P]),
     ("hd_color_stats", C.c_int, [_P, C.POINTER(_u64)]),
+    ("hd_memory_stats", C.c_int, [_P, C.POINTER(_u64)]),
     ("hd_undo", C.c_int, [_P]),
     ("hd_redo", C.c_int, [_P]),
     ("hd_set_undo_capacity", C.c_int, [_P, _u32]),

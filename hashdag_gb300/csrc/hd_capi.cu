@@ -59,7 +59,8 @@ void check_device_error(hd_ctx* c, const char* what)
 {
     const uint32_t e = check_error(c);
     if (e)
-        throw StatusError{e == kErrCapacity ? HD_ERR_INVALID : hd_status(e), std::string(what) + " failed on the device"};
+        throw StatusError{e == kErrCapacity ? HD_ERR_INVALID : hd_status(e),
+                          std::string(what) + " failed on the device (" + c->err_detail + ")"};
 }
 
 } // namespace
@@ -73,8 +74,8 @@ void hd_default_config(uint32_t depth, hd_config* out)
     out->depth = depth;
     out->color_tree_levels = depth >= 15 ? 10 : (depth > 5 ? depth - 5 : 0);
     out->top_levels = 9;
-    out->top_bucket_bits = depth <= 10 ? 10 : 12;
-    out->low_bucket_bits = 16;
+    out->top_bucket_bits = depth <= 10 ? 10 : (depth <= 15 ? 12 : 14);
+    out->low_bucket_bits = depth <= 15 ? 16 : 17;
     out->top_bucket_size = 1024;
     out->low_bucket_size = 4096;
     // enough pages for every bucket of the table
@@ -350,6 +351,19 @@ hd_status hd_get_level_stats(hd_ctx* c, hd_level_stats* out)
         out->root = c->root;
         out->levels = c->cfg.depth;
     });
+}
+
+hd_status hd_memory_stats(hd_ctx* c, uint64_t* out)
+{
+    if (!c || !out)
+        return HD_ERR_INVALID;
+    out[0] = uint64_t(c->cfg.pool_pages) * HD_PAGE_SIZE * 4 + c->g.total_vpages * 4 + c->g.total_buckets * 4;
+    const ColorTable& ct = c->ct;
+    out[1] = ct.cap_nodes * 4 + ct.cap_leaves * sizeof(LeafDesc) + ct.cap_blocks * 8 + ct.cap_macros * 8 +
+             ct.cap_weights * 4;
+    out[2] = c->scratch.total();
+    out[3] = c->gen_scratch_peak;
+    return HD_OK;
 }
 
 hd_status hd_table_sizes(hd_ctx* c, uint64_t* n_buckets, uint64_t* n_vpages, uint64_t* n_pool_pages_used)

@@ -54,6 +54,7 @@ struct hd_ctx {
     // events the colour commit of the next edit waits for (renders in flight
     // that still read the colour leaves the edit replaces)
     std::vector<cudaEvent_t> color_fences;
+    size_t gen_scratch_peak = 0; // bytes of scratch the last scene generation held at most
 };
 
 namespace hd {

@@ -71,18 +71,31 @@ static void scene_spheres(uint64_t seed, uint32_t depth, int64_t* out)
 }
 
 // ---- 1. height bounds ------------------------------------------------------
-__global__ void k_height_leaf(uint64_t seed, uint32_t depth, uint32_t n, int32_t* __restrict__ hmin,
+// hmax: the maximum height over the 4x4 columns of a leaf footprint.  hmin:
+// the minimum over the same columns, or with `grown` over the footprint grown
+// by one column on every side (6x6; a column outside the volume counts as
+// -infinity), which makes the shell scenes' height-field fullness test exact.
+__global__ void k_height_leaf(uint64_t seed, uint32_t depth, uint32_t n, bool grown, int32_t* __restrict__ hmin,
                               int32_t* __restrict__ hmax)
 {
+    const int64_t E = int64_t(1) << depth;
     HD_GRID_STRIDE(idx, uint64_t(n) * n)
     {
         const uint32_t cx = uint32_t(idx / n), cz = uint32_t(idx % n);
         int64_t lo = INT64_MAX, hi = INT64_MIN;
-        for (uint32_t a = 0; a < 4; a++)
-            for (uint32_t b = 0; b < 4; b++) {
-                const int64_t h = scene_height(seed, depth, 4 * cx + a, 4 * cz + b);
+        const int r = grown ? 1 : 0;
+        for (int a = -r; a < 4 + r; a++)
+            for (int b = -r; b < 4 + r; b++) {
+                const int64_t x = int64_t(4 * cx) + a, z = int64_t(4 * cz) + b;
+                const bool in = a >= 0 && a < 4 && b >= 0 && b < 4;
+                if (x < 0 || z < 0 || x >= E || z >= E) {
+                    lo = INT32_MIN;
+                    continue;
+                }
+                const int64_t h = scene_height(seed, depth, uint32_t(x), uint32_t(z));
                 lo = h < lo ? h : lo;
-                hi = h > hi ? h : hi;
+                if (in)
+                    hi = h > hi ? h : hi;
             }
         hmin[idx] = int32_t(lo);
         hmax[idx] = int32_t(hi);
@@ -165,16 +178,8 @@ HD_D uint32_t classify_shell(uint32_t depth, uint32_t level, uint32_t x, uint32_
     const int64_t x0 = int64_t(x) << shift, y0 = int64_t(y) << shift, z0 = int64_t(z) << shift;
     bool touched = y0 <= hmax[(uint64_t(x) << level) | z];
     const bool inside = x0 > 0 && z0 > 0 && y0 > 0 && x0 + s < E && z0 + s < E && y0 + s < E;
-    bool full = false;
-    if (inside) {
-        int64_t lo = INT64_MAX;
-        for (int a = -1; a <= 1; a++)
-            for (int b = -1; b <= 1; b++) {
-                const int64_t v = hmin[uint64_t(int64_t(x) + a) * m + uint64_t(int64_t(z) + b)];
-                lo = v < lo ? v : lo;
-            }
-        full = y0 + s <= lo;
-    }
+    // hmin holds the minimum over the grown footprint in shell scenes
+    bool full = inside && y0 + s <= hmin[uint64_t(x) * m + z];
     uint64_t out = 0;
     uint64_t todo = parent_live;
     while (todo) {
@@ -604,7 +609,8 @@ void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words
     }
     {
         const uint32_t n = 1u << leafl;
-        k_height_leaf<<<grid_for(uint64_t(n) * n, 256, 152 * 64), 256, 0, st>>>(seed, D, n, hmin[leafl], hmax[leafl]);
+        k_height_leaf<<<grid_for(uint64_t(n) * n, 256, 152 * 64), 256, 0, st>>>(seed, D, n, shell, hmin[leafl],
+                                                                                hmax[leafl]);
         HD_LAUNCH_CHECK();
         for (int32_t L = int32_t(leafl) - 1; L >= 0; L--) {
             const uint32_t m = 1u << L;
@@ -627,6 +633,14 @@ void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words
         Frontier f{s.get<uint32_t>(nx, n + 1), s.get<uint32_t>(ny, n + 1), s.get<uint32_t>(nz, n + 1),
                    s.get<uint64_t>(nl, n + 1)};
         return f;
+    };
+    auto drop_frontier = [&](uint32_t L) {
+        const char* names[4] = {"scn_fx_%u", "scn_fy_%u", "scn_fz_%u", "scn_fl_%u"};
+        for (const char* f : names) {
+            char nm[32];
+            snprintf(nm, 32, f, L);
+            s.drop(nm);
+        }
     };
     fr[0] = alloc_frontier(0, 1);
     {
@@ -658,6 +672,8 @@ void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words
         k_expand<<<grid_for(n, 128), 128, 0, st>>>(shell, D, L, fr[L], n, cls2[L], coff[L], hmin[L + 1],
                                                    hmax[L + 1], fr[L + 1]);
         HD_LAUNCH_CHECK();
+        // this level's paths are no longer needed (the dedup reads cls2 / coff)
+        drop_frontier(L);
     }
     // height bounds no longer needed past this point: free them for the dedup
     // leaf masks
@@ -667,6 +683,14 @@ void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words
     else
         k_leaf_masks<<<grid_for(nf[leafl], 128, 152 * 64), 128, 0, st>>>(seed, D, fr[leafl], nf[leafl], masks);
     HD_LAUNCH_CHECK();
+    drop_frontier(leafl);
+    for (uint32_t L = 0; L <= leafl; L++) {
+        char a[32], b[32];
+        snprintf(a, 32, "scn_hmin_%u", L);
+        snprintf(b, 32, "scn_hmax_%u", L);
+        s.drop(a);
+        s.drop(b);
+    }
     // 3. bottom-up dedup
     std::vector<uint32_t*> ucont(leafl + 1);
     std::vector<uint64_t*> ucount(leafl + 1);
@@ -775,7 +799,14 @@ void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words
     if (c->d_basic)
         cudaFree(c->d_basic);
     c->d_basic = nullptr;
-    HD_CUDA(cudaMalloc(&c->d_basic, n_words * 4));
+    if (cudaMalloc(&c->d_basic, n_words * 4) != cudaSuccess) {
+        cudaGetLastError();
+        size_t fr = 0, tot = 0;
+        cudaMemGetInfo(&fr, &tot);
+        throw StatusError{HD_ERR_OOM, "BasicDAG allocation of " + std::to_string(n_words) + " words failed (" +
+                                          std::to_string(fr >> 20) + " MiB free, scratch " +
+                                          std::to_string(c->scratch.total() >> 20) + " MiB)"};
+    }
     c->n_basic = n_words;
     uint64_t enclosed = 0;
     for (uint32_t L = 0; L <= leafl; L++) {
@@ -790,6 +821,7 @@ void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words
         throw StatusError{HD_ERR_INVALID, "scene header overflow (count or enclosed index >= 2^24)"};
     *d_words_out = c->d_basic;
     *n_words_out = n_words;
+    c->gen_scratch_peak = s.peak();
 }
 
 } // namespace hd

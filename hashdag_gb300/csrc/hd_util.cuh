@@ -48,9 +48,11 @@ public:
             size_t want = bytes + bytes / 4 + 256;
             if (cudaMalloc(&b.ptr, want) != cudaSuccess) {
                 cudaGetLastError();
-                throw StatusError{HD_ERR_OOM, std::string("scratch allocation failed: ") + name};
+                throw StatusError{HD_ERR_OOM, std::string("scratch allocation failed: ") + name + " (" +
+                                                  std::to_string(want >> 20) + " MiB)"};
             }
             b.bytes = want;
+            note_peak();
         }
         return b.ptr;
     }
@@ -58,6 +60,22 @@ public:
     T* get(const char* name, size_t count)
     {
         return static_cast<T*>(get(name, count * sizeof(T)));
+    }
+    // frees one buffer (synchronises the device, as cudaFree does)
+    void drop(const char* name)
+    {
+        auto it = bufs_.find(name);
+        if (it == bufs_.end())
+            return;
+        if (it->second.ptr)
+            cudaFree(it->second.ptr);
+        bufs_.erase(it);
+    }
+    size_t peak() const { return peak_; }
+    void note_peak()
+    {
+        const size_t t = total();
+        peak_ = t > peak_ ? t : peak_;
     }
     void release()
     {
@@ -80,6 +98,7 @@ private:
         size_t bytes = 0;
     };
     std::unordered_map<std::string, Buf> bufs_;
+    size_t peak_ = 0;
 };
 
 // ----------------------------------------------------------------- scan ---

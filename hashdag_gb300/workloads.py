@@ -24,8 +24,16 @@ def color_tree_levels(depth):
 
 def top_bucket_bits(depth):
     """BUCKETS_BITS_FOR_TOP_LEVELS: the reference's 10, raised to 12 on scenes
-    of depth 11 and more whose level 8 holds over 10^5 nodes."""
-    return 10 if depth <= 10 else 12
+    of depth 11 to 15 whose level 8 holds over 10^5 nodes, and to 14 from depth
+    16 (over 5 * 10^5 nodes at level 8)."""
+    return 10 if depth <= 10 else (12 if depth <= 15 else 14)
+
+
+def low_bucket_bits(depth):
+    """BUCKETS_BITS_FOR_LOW_LEVELS: the reference's 16, raised to 17 from depth
+    16, where the shell scene's lowest interior level would average more
+    than the 4096 words a bucket holds."""
+    return 16 if depth <= 15 else 17
 
 
 # ---------------------------------------------------------------- cameras --

@@ -352,6 +352,10 @@ hd_status hd_get_root(hd_ctx* ctx, uint32_t* root);
 hd_status hd_set_root(hd_ctx* ctx, uint32_t root);
 hd_status hd_get_config(hd_ctx* ctx, hd_config* cfg);
 hd_status hd_get_level_stats(hd_ctx* ctx, hd_level_stats* out);
+/* Device bytes held: [0] table (pool, page table, bucket sizes), [1] colour
+ * table, [2] scratch buffers, [3] the peak scratch of the last scene
+ * generation. */
+hd_status hd_memory_stats(hd_ctx* ctx, uint64_t* out4);
 /* Copies the table to the host.  Arrays sized by hd_table_sizes: bucket
  * sizes (total buckets), page table (virtual pages), pool (pages_used + 1
  * pages of 512 words; page 0 is the reserved null page), full-node indices

@@ -149,8 +149,8 @@ def default_config(depth, color_tree_levels=None, pool_pages=None):
         color_tree_levels = min(10, depth - 5)
     if pool_pages is None:
         pool_pages = 1 << 20
-    top_bits = 10 if depth <= 10 else 12
-    return HdConfig(depth, color_tree_levels, 9, top_bits, 16, 1024, 4096, pool_pages)
+    top_bits = 10 if depth <= 10 else (12 if depth <= 15 else 14)
+    return HdConfig(depth, color_tree_levels, 9, top_bits, 16 if depth <= 15 else 17, 1024, 4096, pool_pages)
 
 
 def camera(cam):
