@@ -4,13 +4,15 @@
 Workload (Catmull-Rom traversal of the 2^15 scene): the seeded procedural
 scene at depth 15 generated and ingested on the device before timing; 64
 camera poses on a seeded Catmull-Rom path at 1920x1080 (90 degree FOV); one
-step = one pose: a primary ray per pixel and, on a hit, one shadow ray toward
-normalize(0.3, 1, 0.2) with bias 1.  Metric: Mrays/s (primary + shadow).
+step = --views poses (default 16; 4 steps cover the path) traced by
+hd_trace_views: a primary ray per pixel of every view in one launch, then,
+for every hit, one shadow ray toward normalize(0.3, 1, 0.2) with bias 1 in
+one launch.  Metric: Mrays/s (primary + shadow).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
-value  = device throughput (CUDA events around the two launches of each
-         step; L2 flushed with a 512 MB write before every timed step).
+value  = device throughput (CUDA events around each step's call; L2
+         flushed with a 512 MB write before every timed step).
 e2e    = the same metric through the C ABI with host buffers: camera from
          host memory, paths + shadow mask copied back to pinned host memory
          every step.
@@ -51,13 +53,14 @@ BIAS = 1.0
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=64)
+    p.add_argument("--steps", type=int, default=4)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     p.add_argument("--depth", type=int, default=15)
     p.add_argument("--width", type=int, default=1920)
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--poses", type=int, default=64)
+    p.add_argument("--views", type=int, default=16, help="poses traced per step (one primary and one shadow launch)")
     p.add_argument("--ref-rows", type=int, default=192, help="rows per step of the CPU reference arm")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the traversal cpu_baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -453,39 +456,42 @@ def run_gpu(args, dist):
     lstats = dag.level_stats()
     poses = workloads.catmull_rom_path(depth, args.poses, W, H)
     cams = [_capi.Camera.from_params(p) for p in poses]
-    paths = torch.zeros(W * H * 4, dtype=torch.int32, device="cuda")
-    mask = torch.zeros(W * H, dtype=torch.uint8, device="cuda")
+    V = args.views
+    paths = torch.zeros(V * W * H * 4, dtype=torch.int32, device="cuda")
+    mask = torch.zeros(V * W * H, dtype=torch.uint8, device="cuda")
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     light = (C.c_float * 3)(*LIGHT)
     h = dag.handle
 
-    def pose(k):
-        return cams[(k + dist.rank * 7) % len(cams)]
+    def step_poses(k):
+        return [(k * V + j + dist.rank * 7) % len(cams) for j in range(V)]
+
+    def step_cams(k):
+        return (_capi.Camera * V)(*[cams[i] for i in step_poses(k)])
 
     # traversal counters of every pose the timed steps render (outside timing)
     counts = [0] * 6
     per_pose = {}
     for k in range(K):
-        i = (k + dist.rank * 7) % len(cams)
-        if i not in per_pose:
-            out = (C.c_uint64 * 6)()
-            dag._check(L.hd_trace_counters(h, C.byref(cams[i]), W, H, light, BIAS, paths.data_ptr(),
-                                           mask.data_ptr(), out))
-            per_pose[i] = list(out)
-        counts = [a + b for a, b in zip(counts, per_pose[i])]
+        for i in step_poses(k):
+            if i not in per_pose:
+                out = (C.c_uint64 * 6)()
+                dag._check(L.hd_trace_counters(h, C.byref(cams[i]), W, H, light, BIAS, paths.data_ptr(),
+                                               mask.data_ptr(), out))
+                per_pose[i] = list(out)
+            counts = [a + b for a, b in zip(counts, per_pose[i])]
     rays_total = counts[0] + counts[3]
     prim_bytes, shad_bytes = algorithmic_bytes(counts)
+    step_arrays = [step_cams(k) for k in range(max(K, args.warmup))]
 
-    def launch(k):
-        cam = pose(k)
-        dag._check(L.hd_trace_primary(h, C.byref(cam), W, H, paths.data_ptr(), None))
-        dag._check(L.hd_trace_shadow(h, C.byref(cam), W, H, paths.data_ptr(), light, BIAS, mask.data_ptr(), None))
+    def launch(k, ms=None):
+        dag._check(L.hd_trace_views(h, step_arrays[k], V, W, H, paths.data_ptr(), light, BIAS, mask.data_ptr(), ms))
 
     for k in range(args.warmup):
         launch(k)
     torch.cuda.synchronize()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-            torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    split = [(C.c_float * 2)() for _ in range(K)]
     clocks = ClockSampler(torch.cuda.current_device())
     dist.barrier()
     torch.cuda.synchronize()
@@ -494,34 +500,31 @@ def run_gpu(args, dist):
     wall0 = time.perf_counter()
     for k in range(K):
         flush.fill_(k & 0xff)  # writes 512 MB: evicts the 129 MB L2
-        e0, e1, e2 = evs[k]
+        e0, e1 = evs[k]
         e0.record()
-        cam = pose(k)
-        dag._check(L.hd_trace_primary(h, C.byref(cam), W, H, paths.data_ptr(), None))
+        launch(k, split[k])
         e1.record()
-        dag._check(L.hd_trace_shadow(h, C.byref(cam), W, H, paths.data_ptr(), light, BIAS, mask.data_ptr(), None))
-        e2.record()
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     dist.barrier()
     clk = clocks.stop()
-    ms_p = sum(e0.elapsed_time(e1) for e0, e1, _ in evs)
-    ms_s = sum(e1.elapsed_time(e2) for _, e1, e2 in evs)
-    total_ms = dist.max(ms_p + ms_s)
+    step_ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+    ms_p = sum(sp[0] for sp in split)
+    ms_s = sum(sp[1] for sp in split)
+    total_ms = dist.max(step_ms)
     rays_all = dist.sum(rays_total)
     value = rays_all / (total_ms * 1e-3) / 1e6
 
-    # end to end through the C ABI with host buffers
-    h_paths = torch.empty(W * H * 4, dtype=torch.int32, pin_memory=True)
-    h_mask = torch.empty(W * H, dtype=torch.uint8, pin_memory=True)
-    host_cam = [_capi.Camera.from_params(poses[(k + dist.rank * 7) % len(cams)]) for k in range(K)]
+    # end to end through the C ABI with host buffers: cameras up, every view's
+    # paths and shadow mask down, every step
+    h_paths = torch.empty(V * W * H * 4, dtype=torch.int32, pin_memory=True)
+    h_mask = torch.empty(V * W * H, dtype=torch.uint8, pin_memory=True)
     torch.cuda.synchronize()
     dist.barrier()
     t0 = time.perf_counter()
     for k in range(K):
         flush.fill_(k & 0xff)
-        dag._check(L.hd_trace_frame(h, C.byref(host_cam[k]), W, H, light, BIAS, paths.data_ptr(), mask.data_ptr(),
-                                    None, None))
+        launch(k)
         h_paths.copy_(paths, non_blocking=True)
         h_mask.copy_(mask, non_blocking=True)
         torch.cuda.synchronize()
@@ -574,14 +577,15 @@ def run_gpu(args, dist):
             "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload, "depth": depth, "width": W, "height": H, "poses": args.poses,
-                       "light": list(LIGHT), "shadow_bias": BIAS, "l2": "flushed (512 MB write) before every step",
+                       "views_per_step": V, "light": list(LIGHT), "shadow_bias": BIAS,
+                       "l2": "flushed (512 MB write) before every step",
                        "scene_gen_s": round(gen_s, 2), "rays_per_step": rays_total / K,
                        "scene_pages_used": int(lstats.pages_used),
                        "scene_nodes": int(sum(lstats.nodes[:depth - 1])),
                        "parallelism": f"replicas x{dist.world}"},
-            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(_capi.Camera),
-                    "d2h_bytes_per_step": W * H * 16 + W * H},
-            "gpu_launches": 2 * K, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": V * C.sizeof(_capi.Camera),
+                    "d2h_bytes_per_step": V * (W * H * 16 + W * H)},
+            "gpu_launches": 4 * K, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "wall_s": wall, "edits": edits, "colors": colors, "serving": serving}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)

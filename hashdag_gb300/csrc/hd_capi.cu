@@ -148,6 +148,8 @@ hd_status hd_destroy(hd_ctx* c)
         cudaEventDestroy(c->ev0);
     if (c->ev1)
         cudaEventDestroy(c->ev1);
+    if (c->ev_mid)
+        cudaEventDestroy(c->ev_mid);
     c->scratch.release();
     delete c;
     return HD_OK;
@@ -252,6 +254,27 @@ hd_status hd_trace_shadow(hd_ctx* c, const hd_camera* cam, uint32_t w, uint32_t 
     if (!c || !cam || !d_paths || !d_mask || !light || !w || !h)
         return HD_ERR_INVALID;
     return timed(c, ms, [&] { trace_shadow(c, *cam, w, h, d_paths, light, bias, d_mask); });
+}
+
+hd_status hd_trace_views(hd_ctx* c, const hd_camera* cams, uint32_t n_views, uint32_t width, uint32_t height,
+                         uint32_t* d_paths, const float* light, float bias, uint8_t* d_mask, float* ms)
+{
+    if (!c || !cams || !n_views || !width || !height || !d_paths || !light || !d_mask)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        hd_camera* d_cams = c->scratch.get<hd_camera>("views_cams", n_views);
+        HD_CUDA(cudaMemcpyAsync(d_cams, cams, sizeof(hd_camera) * n_views, cudaMemcpyHostToDevice, c->stream));
+        if (!c->ev_mid)
+            HD_CUDA(cudaEventCreate(&c->ev_mid));
+        HD_CUDA(cudaEventRecord(c->ev0, c->stream));
+        trace_views(c, d_cams, n_views, width, height, d_paths, light, bias, d_mask, nullptr, nullptr, c->ev_mid);
+        HD_CUDA(cudaEventRecord(c->ev1, c->stream));
+        HD_CUDA(cudaEventSynchronize(c->ev1));
+        if (ms) {
+            HD_CUDA(cudaEventElapsedTime(ms, c->ev0, c->ev_mid));
+            HD_CUDA(cudaEventElapsedTime(ms + 1, c->ev_mid, c->ev1));
+        }
+    });
 }
 
 hd_status hd_trace_frame(hd_ctx* c, const hd_camera* cam, uint32_t w, uint32_t h, const float light[3], float bias,

@@ -34,7 +34,7 @@ struct hd_ctx {
     // BasicDAG of the last generated scene (device), kept for export
     uint32_t* d_basic = nullptr;
     uint64_t n_basic = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_mid = nullptr;
     // bucket list heads of the edit path stay all-empty between calls
     bool edit_head_ready = false;
     uint32_t* edit_head_ptr = nullptr;
@@ -97,9 +97,15 @@ void push_undo(hd_ctx* c, UndoFrame&& f);
 void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint32_t* d_paths,
                    unsigned long long* d_counters = nullptr, cudaStream_t stream = nullptr,
                    const uint32_t* d_root = nullptr);
+// d_list: w * h + 1 words for the list of hit pixels (nullptr = context
+// scratch, not for concurrent calls)
 void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
                   const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters = nullptr,
-                  cudaStream_t stream = nullptr, const uint32_t* d_root = nullptr);
+                  cudaStream_t stream = nullptr, const uint32_t* d_root = nullptr, uint32_t* d_list = nullptr);
 void get_values(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out);
+// mid (optional): recorded between the primary and the shadow launches
+void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t w, uint32_t h, uint32_t* d_paths,
+                 const float light[3], float bias, uint8_t* d_mask, cudaStream_t stream = nullptr,
+                 uint32_t* d_list = nullptr, cudaEvent_t mid = nullptr);
 
 } // namespace hd

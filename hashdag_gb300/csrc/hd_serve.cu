@@ -70,6 +70,7 @@ struct Slot {
     uint8_t* mask = nullptr;
     uint32_t* rgba = nullptr;
     uint32_t* root = nullptr;
+    uint32_t* list = nullptr; // hit pixels of the shadow pass
     unsigned long long* sum = nullptr;
     unsigned long long* h_sum = nullptr; // pinned
     cudaEvent_t colors_done = nullptr, done = nullptr;
@@ -127,6 +128,8 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
         s.rgba = c->scratch.get<uint32_t>(nm, max_pixels);
         snprintf(nm, sizeof(nm), "serve_root_%u", k);
         s.root = c->scratch.get<uint32_t>(nm, 1);
+        snprintf(nm, sizeof(nm), "serve_list_%u", k);
+        s.list = c->scratch.get<uint32_t>(nm, max_pixels + 1);
         snprintf(nm, sizeof(nm), "serve_sum_%u", k);
         s.sum = c->scratch.get<unsigned long long>(nm, 1);
         HD_CUDA(cudaMallocHost(&s.h_sum, 8));
@@ -171,7 +174,7 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
             HD_CUDA(cudaMemcpyAsync(s.root, &c->root, 4, cudaMemcpyHostToDevice, s.stream));
             trace_primary(c, r.camera, r.width, r.height, s.paths, nullptr, s.stream, s.root);
             trace_shadow(c, r.camera, r.width, r.height, s.paths, cfg.light, cfg.shadow_bias, s.mask, nullptr,
-                         s.stream, s.root);
+                         s.stream, s.root, s.list);
             if (c->colors)
                 trace_colors(c, s.paths, r.width, r.height, s.rgba, s.stream, s.root);
             HD_CUDA(cudaEventRecord(s.colors_done, s.stream));

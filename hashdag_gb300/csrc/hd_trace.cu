@@ -15,6 +15,8 @@
 #include <mutex>
 #include <string>
 
+#include <algorithm>
+
 #include "hd_ctx.h"
 
 namespace hd {
@@ -208,6 +210,23 @@ HD_D void add_counts(unsigned long long* counters, uint32_t rays, uint32_t desce
 }
 
 template <int FMA, bool COUNT>
+HD_D void primary_ray(const Table& t, uint32_t root, const hd_camera& cam, uint32_t W, uint32_t H, uint32_t x,
+                      uint32_t y, uint4* __restrict__ out, unsigned long long* counters)
+{
+    double dd[3];
+    camera_dir<FMA>(cam, double(x), double(y), dd);
+    const F3 d = {float(dd[0]), float(dd[1]), float(dd[2])};
+    const F3 inv = inverse_dir(d);
+    const F3 o = {float(cam.position[0]), float(cam.position[1]), float(cam.position[2])};
+    const uint32_t order = (d.x < 0.f ? 4u : 0u) + (d.y < 0.f ? 2u : 0u) + (d.z < 0.f ? 1u : 0u);
+    uint32_t hit[3], descents = 0, leaves = 0;
+    walk<FMA, false>(t, root, o, d, inv, order, hit, descents, leaves);
+    out[uint64_t(H - 1 - y) * W + x] = make_uint4(hit[0], hit[1], hit[2], 0);
+    if (COUNT)
+        add_counts(counters, 1, descents, leaves);
+}
+
+template <int FMA, bool COUNT>
 __global__ void __launch_bounds__(64) k_trace_primary(Table t, const uint32_t* __restrict__ d_root, hd_camera cam,
                                                       uint32_t W, uint32_t H, uint4* __restrict__ out,
                                                       unsigned long long* counters)
@@ -216,36 +235,34 @@ __global__ void __launch_bounds__(64) k_trace_primary(Table t, const uint32_t* _
     const uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 3);
     if (x >= W || y >= H)
         return;
-    double dd[3];
-    camera_dir<FMA>(cam, double(x), double(y), dd);
-    const F3 d = {float(dd[0]), float(dd[1]), float(dd[2])};
-    const F3 inv = inverse_dir(d);
-    const F3 o = {float(cam.position[0]), float(cam.position[1]), float(cam.position[2])};
-    const uint32_t order = (d.x < 0.f ? 4u : 0u) + (d.y < 0.f ? 2u : 0u) + (d.z < 0.f ? 1u : 0u);
-    uint32_t hit[3], descents = 0, leaves = 0;
-    walk<FMA, false>(t, *d_root, o, d, inv, order, hit, descents, leaves);
-    out[uint64_t(H - 1 - y) * W + x] = make_uint4(hit[0], hit[1], hit[2], 0);
-    if (COUNT)
-        add_counts(counters, 1, descents, leaves);
+    primary_ray<FMA, COUNT>(t, *d_root, cam, W, H, x, y, out, counters);
 }
 
-// Rows are output rows (the layout of the paths image).
-template <int FMA, bool COUNT>
-__global__ void __launch_bounds__(64) k_trace_shadow(Table t, const uint32_t* __restrict__ d_root, hd_camera cam,
-                                                     uint32_t W, uint32_t H, const uint4* __restrict__ paths,
-                                                     F3 light, float bias, uint8_t* __restrict__ mask,
-                                                     unsigned long long* counters)
+// Several views in one launch: blockIdx.z is the view; view v writes its
+// paths at out + v * W * H (the single-view layout).
+template <int FMA>
+__global__ void __launch_bounds__(64) k_trace_primary_views(Table t, const uint32_t* __restrict__ d_root,
+                                                            const hd_camera* __restrict__ cams, uint32_t W, uint32_t H,
+                                                            uint4* __restrict__ out)
 {
     const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7);
-    const uint32_t r = blockIdx.y * 8 + (threadIdx.x >> 3);
-    if (x >= W || r >= H)
+    const uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 3);
+    if (x >= W || y >= H)
         return;
-    const uint64_t i = uint64_t(r) * W + x;
+    const hd_camera cam = cams[blockIdx.z];
+    primary_ray<FMA, false>(t, *d_root, cam, W, H, x, y, out + uint64_t(blockIdx.z) * W * H, nullptr);
+}
+
+// One shadow ray from the hit of output pixel i (tracer.cu:589-697 reduced to
+// the hit test): the exact hit point on the hit voxel's box
+// (ray_box_intersection, :574-587) plus bias * light, any-hit toward light.
+template <int FMA, bool COUNT>
+HD_D void shadow_ray(const Table& t, uint32_t root, const hd_camera& cam, uint32_t W, uint32_t H,
+                     const uint4* __restrict__ paths, F3 light, float bias, uint8_t* __restrict__ mask, uint64_t i,
+                     unsigned long long* counters)
+{
+    const uint32_t x = uint32_t(i % W), r = uint32_t(i / W);
     const uint4 p = paths[i];
-    if (p.x == 0 && p.y == 0 && p.z == 0) {
-        mask[i] = 2;
-        return;
-    }
     // sun_direction(): normalize in float (tracer.cu:546-549)
     const float dot = FMA ? __fmaf_rn(light.z, light.z, __fmaf_rn(light.y, light.y, light.x * light.x))
                           : (light.x * light.x + light.y * light.y) + light.z * light.z;
@@ -274,11 +291,111 @@ __global__ void __launch_bounds__(64) k_trace_shadow(Table t, const uint32_t* __
         o = {start.x + bias * dir.x, start.y + bias * dir.y, start.z + bias * dir.z};
     }
     uint32_t hit[3], descents = 0, leaves = 0;
-    mask[i] = walk<FMA, true>(t, *d_root, o, dir, inverse_dir(dir), 0, hit, descents, leaves) ? 1 : 0;
+    mask[i] = walk<FMA, true>(t, root, o, dir, inverse_dir(dir), 0, hit, descents, leaves) ? 1 : 0;
     if (COUNT)
         add_counts(counters, 1, descents, leaves);
 }
 
+// Shadow rays start only at hit pixels (a path of (0, 0, 0) is a miss,
+// tracer.cu:644-648).  The hit pixels of each 8x8 tile are appended to a
+// list, tile by tile, so that the shadow kernel runs full warps of rays from
+// neighbouring pixels; misses get mask 2 here.  Rows are output rows (the
+// layout of the paths image).
+__global__ void __launch_bounds__(64) k_shadow_list(uint32_t W, uint32_t H, const uint4* __restrict__ paths,
+                                                    uint8_t* __restrict__ mask, uint32_t* __restrict__ list,
+                                                    uint32_t* __restrict__ count)
+{
+    __shared__ uint32_t warp_base[2];
+    const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7);
+    const uint32_t r = blockIdx.y * 8 + (threadIdx.x >> 3);
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool in = x < W && r < H;
+    const uint64_t i = uint64_t(r) * W + x;
+    bool hit = false;
+    if (in) {
+        const uint4 p = paths[i];
+        hit = (p.x | p.y | p.z) != 0;
+        if (!hit)
+            mask[i] = 2;
+    }
+    const uint32_t b = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0)
+        warp_base[warp] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t n0 = warp_base[0], n1 = warp_base[1];
+        const uint32_t base = (n0 + n1) ? atomicAdd(count, n0 + n1) : 0u;
+        warp_base[0] = base;
+        warp_base[1] = base + n0;
+    }
+    __syncthreads();
+    if (hit)
+        list[warp_base[warp] + __popc(b & ((1u << lane) - 1u))] = uint32_t(i);
+}
+
+// The hit pixels of several views (blockIdx.z = view) into one list of
+// view * W * H + pixel indices.
+__global__ void __launch_bounds__(64) k_shadow_list_views(uint32_t W, uint32_t H, const uint4* __restrict__ paths,
+                                                          uint8_t* __restrict__ mask, uint32_t* __restrict__ list,
+                                                          uint32_t* __restrict__ count)
+{
+    __shared__ uint32_t warp_base[2];
+    const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7);
+    const uint32_t r = blockIdx.y * 8 + (threadIdx.x >> 3);
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool in = x < W && r < H;
+    const uint64_t i = uint64_t(blockIdx.z) * W * H + uint64_t(r) * W + x;
+    bool hit = false;
+    if (in) {
+        const uint4 p = paths[i];
+        hit = (p.x | p.y | p.z) != 0;
+        if (!hit)
+            mask[i] = 2;
+    }
+    const uint32_t b = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0)
+        warp_base[warp] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t n0 = warp_base[0], n1 = warp_base[1];
+        const uint32_t base = (n0 + n1) ? atomicAdd(count, n0 + n1) : 0u;
+        warp_base[0] = base;
+        warp_base[1] = base + n0;
+    }
+    __syncthreads();
+    if (hit)
+        list[warp_base[warp] + __popc(b & ((1u << lane) - 1u))] = uint32_t(i);
+}
+
+template <int FMA>
+__global__ void __launch_bounds__(128) k_trace_shadow_views(Table t, const uint32_t* __restrict__ d_root,
+                                                            const hd_camera* __restrict__ cams, uint32_t W, uint32_t H,
+                                                            const uint4* __restrict__ paths, F3 light, float bias,
+                                                            uint8_t* __restrict__ mask, const uint32_t* __restrict__ list,
+                                                            const uint32_t* __restrict__ count)
+{
+    const uint32_t n = *count;
+    const uint64_t frame = uint64_t(W) * H;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t g = list[j];
+        const uint32_t v = uint32_t(g / frame);
+        const hd_camera cam = cams[v];
+        shadow_ray<FMA, false>(t, *d_root, cam, W, H, paths + v * frame, light, bias, mask + v * frame, g - v * frame,
+                               nullptr);
+    }
+}
+
+template <int FMA, bool COUNT>
+__global__ void __launch_bounds__(128) k_trace_shadow(Table t, const uint32_t* __restrict__ d_root, hd_camera cam,
+                                                      uint32_t W, uint32_t H, const uint4* __restrict__ paths,
+                                                      F3 light, float bias, uint8_t* __restrict__ mask,
+                                                      const uint32_t* __restrict__ list,
+                                                      const uint32_t* __restrict__ count, unsigned long long* counters)
+{
+    const uint32_t n = *count;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        shadow_ray<FMA, COUNT>(t, *d_root, cam, W, H, paths, light, bias, mask, list[j], counters);
+}
 void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint32_t* d_paths,
                    unsigned long long* d_counters, cudaStream_t stream, const uint32_t* d_root)
 {
@@ -302,28 +419,70 @@ void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint
 
 void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
                   const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters,
-                  cudaStream_t stream, const uint32_t* d_root)
+                  cudaStream_t stream, const uint32_t* d_root, uint32_t* d_list)
 {
     cudaStream_t st = stream ? stream : c->stream;
     const uint32_t* rt = d_root ? d_root : c->d_root;
-    dim3 grid((w + 7) / 8, (h + 7) / 8);
-    const F3 l = {light[0], light[1], light[2]};
+    const uint64_t px = uint64_t(w) * h;
+    uint32_t* list = d_list ? d_list : c->scratch.get<uint32_t>("shadow_list", px + 1);
+    uint32_t* count = list + px;
+    HD_CUDA(cudaMemsetAsync(count, 0, 4, st));
+    dim3 tiles((w + 7) / 8, (h + 7) / 8);
     const uint4* p = reinterpret_cast<const uint4*>(d_paths);
+    k_shadow_list<<<tiles, 64, 0, st>>>(w, h, p, d_mask, list, count);
+    HD_LAUNCH_CHECK();
+    const F3 l = {light[0], light[1], light[2]};
+    const uint32_t blocks = uint32_t(std::min<uint64_t>((px + 127) / 128, 152 * 16));
     if (d_counters) {
         if (c->fp_mode)
-            k_trace_shadow<1, true><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask,
-                                                                d_counters);
+            k_trace_shadow<1, true><<<blocks, 128, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask, list, count,
+                                                            d_counters);
         else
-            k_trace_shadow<0, true><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask,
-                                                                d_counters);
+            k_trace_shadow<0, true><<<blocks, 128, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask, list, count,
+                                                            d_counters);
     } else {
         if (c->fp_mode)
-            k_trace_shadow<1, false><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask,
-                                                                 nullptr);
+            k_trace_shadow<1, false><<<blocks, 128, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask, list, count,
+                                                             nullptr);
         else
-            k_trace_shadow<0, false><<<grid, 64, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask,
-                                                                 nullptr);
+            k_trace_shadow<0, false><<<blocks, 128, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask, list, count,
+                                                             nullptr);
     }
+    HD_LAUNCH_CHECK();
+}
+
+// n_views frames in two launches: primary rays of every view, then the
+// shadow rays of every hit pixel of every view.
+void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t w, uint32_t h, uint32_t* d_paths,
+                 const float light[3], float bias, uint8_t* d_mask, cudaStream_t stream, uint32_t* d_list,
+                 cudaEvent_t mid)
+{
+    cudaStream_t st = stream ? stream : c->stream;
+    const uint64_t px = uint64_t(w) * h * n_views;
+    if (px >= 0xFFFFFFFFull)
+        throw StatusError{HD_ERR_INVALID, "views x width x height must stay below 2^32 pixels"};
+    dim3 tiles((w + 7) / 8, (h + 7) / 8, n_views);
+    uint4* out = reinterpret_cast<uint4*>(d_paths);
+    if (c->fp_mode)
+        k_trace_primary_views<1><<<tiles, 64, 0, st>>>(c->t, c->d_root, d_cams, w, h, out);
+    else
+        k_trace_primary_views<0><<<tiles, 64, 0, st>>>(c->t, c->d_root, d_cams, w, h, out);
+    HD_LAUNCH_CHECK();
+    if (mid)
+        HD_CUDA(cudaEventRecord(mid, st));
+    uint32_t* list = d_list ? d_list : c->scratch.get<uint32_t>("shadow_list", px + 1);
+    uint32_t* count = list + px;
+    HD_CUDA(cudaMemsetAsync(count, 0, 4, st));
+    k_shadow_list_views<<<tiles, 64, 0, st>>>(w, h, out, d_mask, list, count);
+    HD_LAUNCH_CHECK();
+    const F3 l = {light[0], light[1], light[2]};
+    const uint32_t blocks = uint32_t(std::min<uint64_t>((px + 127) / 128, 152 * 16));
+    if (c->fp_mode)
+        k_trace_shadow_views<1><<<blocks, 128, 0, st>>>(c->t, c->d_root, d_cams, w, h, out, l, bias, d_mask, list,
+                                                        count);
+    else
+        k_trace_shadow_views<0><<<blocks, 128, 0, st>>>(c->t, c->d_root, d_cams, w, h, out, l, bias, d_mask, list,
+                                                        count);
     HD_LAUNCH_CHECK();
 }
 

@@ -179,6 +179,14 @@ hd_status hd_trace_primary(hd_ctx* ctx, const hd_camera* cam, uint32_t width, ui
 hd_status hd_trace_shadow(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint32_t height,
                           const uint32_t* d_paths, const float light[3], float bias,
                           uint8_t* d_mask, float* ms);
+/* n_views frames in one primary launch and one shadow launch (rays from many
+ * views batched, so that the long shadow rays of one view overlap the work
+ * of the others): view v's paths at d_paths + v * width * height * 4 and its
+ * mask at d_mask + v * width * height, each equal to what hd_trace_primary /
+ * hd_trace_shadow give for that view.  cams: host array; ms (optional, 2
+ * floats): device time of the primary launch and of the shadow pass. */
+hd_status hd_trace_views(hd_ctx* ctx, const hd_camera* cams, uint32_t n_views, uint32_t width, uint32_t height,
+                         uint32_t* d_paths, const float* light, float bias, uint8_t* d_mask, float* ms);
 /* Primary + shadow in one call: the per-frame traversal step. */
 hd_status hd_trace_frame(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint32_t height,
                          const float light[3], float bias, uint32_t* d_paths, uint8_t* d_mask,

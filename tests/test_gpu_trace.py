@@ -142,3 +142,31 @@ def test_trace_depth15_rows_match_oracle(gpu):
     out_rows = slice(H - rows[1], H - rows[0])
     assert np.array_equal(paths[out_rows], opaths[out_rows])
     assert np.array_equal(shadows[out_rows], omask[out_rows])
+
+
+def test_trace_views_equals_single_views(gpu):
+    """hd_trace_views (several views per launch) gives each view the paths
+    and shadow mask of hd_trace_primary / hd_trace_shadow."""
+    import ctypes as C
+    import torch
+    from hashdag_gb300 import _capi
+    depth, W, H, V = 12, 640, 360, 5
+    d = hd.HashDAG(depth)
+    d.generate_scene(1)
+    poses = workloads.catmull_rom_path(depth, V, W, H)
+    cams = (_capi.Camera * V)(*[_capi.Camera.from_params(p) for p in poses])
+    paths = torch.zeros(V * W * H * 4, dtype=torch.int32, device="cuda")
+    mask = torch.zeros(V * W * H, dtype=torch.uint8, device="cuda")
+    light = (C.c_float * 3)(0.3, 1.0, 0.2)
+    ms = (C.c_float * 2)()
+    d._check(_capi.lib().hd_trace_views(d.handle, cams, V, W, H, paths.data_ptr(), light, 1.0, mask.data_ptr(), ms))
+    tr = hd.DAGTracer(W, H)
+    for v in range(V):
+        tr.resolve_paths(poses[v], d)
+        tr.resolve_shadows(poses[v], d)
+        got_p = paths[v * W * H * 4:(v + 1) * W * H * 4].cpu().numpy().view(np.uint32).reshape(H, W, 4)
+        got_m = mask[v * W * H:(v + 1) * W * H].cpu().numpy().reshape(H, W)
+        assert np.array_equal(got_p, tr.get_paths().reshape(H, W, 4)), v
+        assert np.array_equal(got_m, tr.get_shadows()), v
+    assert ms[0] > 0 and ms[1] > 0
+    d.free()
