@@ -166,15 +166,17 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
-def traffic_from_profiles(workload):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
-    summary, when it covers this workload."""
+def traffic_from_profiles(workload, kernel, views):
+    """DRAM bytes of one launch of the dominant kernel: the per-view traffic
+    of the committed ncu capture for this workload times the views of a
+    launch (traffic grows with the views traced)."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
-        return d.get(workload, {}).get("bytes_per_launch")
-    except (OSError, ValueError, AttributeError):
+        per_view = d[workload]["per_view"][kernel]
+        return per_view * views
+    except (OSError, ValueError, KeyError, TypeError):
         return None
 
 
@@ -547,7 +549,7 @@ def run_gpu(args, dist):
     workload = f"catmull_rom_d{depth}_{W}x{H}"
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": dom_bytes, "traffic": traffic_from_profiles(workload),
+                "algorithmic_bytes_per_launch": dom_bytes, "traffic": traffic_from_profiles(workload, dominant, V),
                 "primary_ms_per_launch": ms_p / K, "shadow_ms_per_launch": ms_s / K,
                 "primary_bytes_per_launch": prim_bytes / K, "shadow_bytes_per_launch": shad_bytes / K}
     cpu = None
