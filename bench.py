@@ -90,11 +90,15 @@ class Dist:
         if self.pg:
             self.pg.barrier()
 
+    def _device(self):
+        # gloo reduces host tensors, NCCL device tensors
+        return "cpu" if self.pg.get_backend() == "gloo" else "cuda"
+
     def max(self, v):
         if not self.pg:
             return v
         import torch
-        t = torch.tensor([float(v)], device="cuda")
+        t = torch.tensor([float(v)], dtype=torch.float64, device=self._device())
         self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
         return float(t.item())
 
@@ -102,7 +106,7 @@ class Dist:
         if not self.pg:
             return v
         import torch
-        t = torch.tensor([float(v)], device="cuda")
+        t = torch.tensor([float(v)], dtype=torch.float64, device=self._device())
         self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
         return float(t.item())
 
@@ -189,6 +193,12 @@ def algorithmic_bytes(counts):
     prim = 8 * counts[0] + 16 * counts[1] + 20 * counts[2] + 16 * counts[0]
     shad = 8 * counts[3] + 16 * counts[4] + 20 * counts[5] + 17 * counts[3]
     return prim, shad
+
+
+def replica_poses(step, views, rank, n_poses):
+    """Poses of one step on one rank: replicas render their own poses (rank r
+    starts 7 r poses further along the path); no data crosses ranks."""
+    return [(step * views + j + rank * 7) % n_poses for j in range(views)]
 
 
 def load_scene(depth, pool_pages=0):
@@ -466,7 +476,7 @@ def run_gpu(args, dist):
     h = dag.handle
 
     def step_poses(k):
-        return [(k * V + j + dist.rank * 7) % len(cams) for j in range(V)]
+        return replica_poses(k, V, dist.rank, len(cams))
 
     def step_cams(k):
         return (_capi.Camera * V)(*[cams[i] for i in step_poses(k)])
