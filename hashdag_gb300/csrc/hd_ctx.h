@@ -99,6 +99,9 @@ void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint
                    const uint32_t* d_root = nullptr);
 // d_list: w * h + 1 words for the list of hit pixels (nullptr = context
 // scratch, not for concurrent calls)
+// 32-bit words of a shadow-ray list buffer for px pixels: 16 bytes per ray
+// and a 4-word head (ray count, two work counters).
+inline uint64_t shadow_list_words(uint64_t px) { return 4 * px + 4; }
 void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
                   const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters = nullptr,
                   cudaStream_t stream = nullptr, const uint32_t* d_root = nullptr, uint32_t* d_list = nullptr);

@@ -129,7 +129,7 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
         snprintf(nm, sizeof(nm), "serve_root_%u", k);
         s.root = c->scratch.get<uint32_t>(nm, 1);
         snprintf(nm, sizeof(nm), "serve_list_%u", k);
-        s.list = c->scratch.get<uint32_t>(nm, max_pixels + 1);
+        s.list = c->scratch.get<uint32_t>(nm, shadow_list_words(max_pixels));
         snprintf(nm, sizeof(nm), "serve_sum_%u", k);
         s.sum = c->scratch.get<unsigned long long>(nm, 1);
         HD_CUDA(cudaMallocHost(&s.h_sum, 8));

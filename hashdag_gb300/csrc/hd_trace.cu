@@ -12,6 +12,7 @@
 // expression is rounded operation by operation in source order; FMA = 1
 // places explicit fused multiply-adds where the reference's default nvcc
 // build contracts a product into the following add.
+#include <map>
 #include <mutex>
 #include <string>
 
@@ -238,39 +239,59 @@ __global__ void __launch_bounds__(64) k_trace_primary(Table t, const uint32_t* _
     primary_ray<FMA, COUNT>(t, *d_root, cam, W, H, x, y, out, counters);
 }
 
-// Several views in one launch: blockIdx.z is the view; view v writes its
-// paths at out + v * W * H (the single-view layout).
+// Several views in one launch, as persistent warps: each warp takes 8x4
+// pixel tiles from a counter (view-major, then tile rows), so warps whose
+// rays end early take more tiles and every resident warp stays busy to the
+// end of the launch.  The next tile is fetched before the current one is
+// traced.  View v writes its paths at out + v * W * H (the single-view
+// layout).
 template <int FMA>
-__global__ void __launch_bounds__(64) k_trace_primary_views(Table t, const uint32_t* __restrict__ d_root,
-                                                            const hd_camera* __restrict__ cams, uint32_t W, uint32_t H,
-                                                            uint4* __restrict__ out)
+__global__ void __launch_bounds__(128, 16) k_trace_primary_views(Table t, const uint32_t* __restrict__ d_root,
+                                                             const hd_camera* __restrict__ cams, uint32_t W,
+                                                             uint32_t H, uint32_t n_views, uint4* __restrict__ out,
+                                                             uint32_t* __restrict__ next_tile)
 {
-    const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7);
-    const uint32_t y = blockIdx.y * 8 + (threadIdx.x >> 3);
-    if (x >= W || y >= H)
-        return;
-    const hd_camera cam = cams[blockIdx.z];
-    primary_ray<FMA, false>(t, *d_root, cam, W, H, x, y, out + uint64_t(blockIdx.z) * W * H, nullptr);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t tx = (W + 7) / 8, ty = (H + 3) / 4;
+    const uint32_t per_view = tx * ty, n_tiles = per_view * n_views;
+    const uint32_t root = *d_root;
+    uint32_t tile = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(next_tile, 1u) : 0u, 0);
+    while (tile < n_tiles) {
+        const uint32_t next = lane == 0 ? atomicAdd(next_tile, 1u) : 0u;
+        const uint32_t v = tile / per_view, k = tile - v * per_view;
+        const uint32_t x = (k % tx) * 8 + (lane & 7), y = (k / tx) * 4 + (lane >> 3);
+        if (x < W && y < H)
+            primary_ray<FMA, false>(t, root, cams[v], W, H, x, y, out + uint64_t(v) * W * H, nullptr);
+        tile = __shfl_sync(0xffffffffu, next, 0);
+    }
 }
 
-// One shadow ray from the hit of output pixel i (tracer.cu:589-697 reduced to
-// the hit test): the exact hit point on the hit voxel's box
-// (ray_box_intersection, :574-587) plus bias * light, any-hit toward light.
-template <int FMA, bool COUNT>
-HD_D void shadow_ray(const Table& t, uint32_t root, const hd_camera& cam, uint32_t W, uint32_t H,
-                     const uint4* __restrict__ paths, F3 light, float bias, uint8_t* __restrict__ mask, uint64_t i,
-                     unsigned long long* counters)
+// A shadow ray of the compacted list: the output pixel (view * W * H +
+// pixel) and its origin.
+struct ShadowRay {
+    uint32_t idx;
+    float ox, oy, oz;
+};
+
+// sun_direction(): the light normalised in float (tracer.cu:546-549)
+template <int FMA>
+HD_D F3 light_dir(F3 light)
 {
-    const uint32_t x = uint32_t(i % W), r = uint32_t(i / W);
-    const uint4 p = paths[i];
-    // sun_direction(): normalize in float (tracer.cu:546-549)
     const float dot = FMA ? __fmaf_rn(light.z, light.z, __fmaf_rn(light.y, light.y, light.x * light.x))
                           : (light.x * light.x + light.y * light.y) + light.z * light.z;
     const float il = 1.0f / sqrtf(dot);
-    const F3 dir = {il * light.x, il * light.y, il * light.z};
+    return F3{il * light.x, il * light.y, il * light.z};
+}
+
+// Origin of the shadow ray of output pixel (x, row r) whose primary ray hit
+// voxel p (tracer.cu:589-697 reduced to the hit test): the exact hit point on
+// the hit voxel's box (ray_box_intersection, :574-587, in double) plus
+// bias * light.
+template <int FMA>
+HD_D F3 shadow_origin(const hd_camera& cam, uint32_t H, uint32_t x, uint32_t r, uint4 p, F3 dir, float bias)
+{
     double cd[3];
     camera_dir<FMA>(cam, double(x), double(H - 1 - r), cd);
-    // ray_box_intersection with the hit voxel's box
     const double bmin[3] = {double(float(p.x)), double(float(p.y)), double(float(p.z))};
     double real_min[3];
 #pragma unroll
@@ -290,54 +311,20 @@ HD_D void shadow_ray(const Table& t, uint32_t root, const hd_camera& cam, uint32
                  float(cam.position[2] + cd[2] * maxmin)};
         o = {start.x + bias * dir.x, start.y + bias * dir.y, start.z + bias * dir.z};
     }
-    uint32_t hit[3], descents = 0, leaves = 0;
-    mask[i] = walk<FMA, true>(t, root, o, dir, inverse_dir(dir), 0, hit, descents, leaves) ? 1 : 0;
-    if (COUNT)
-        add_counts(counters, 1, descents, leaves);
+    return o;
 }
 
 // Shadow rays start only at hit pixels (a path of (0, 0, 0) is a miss,
-// tracer.cu:644-648).  The hit pixels of each 8x8 tile are appended to a
-// list, tile by tile, so that the shadow kernel runs full warps of rays from
-// neighbouring pixels; misses get mask 2 here.  Rows are output rows (the
-// layout of the paths image).
-__global__ void __launch_bounds__(64) k_shadow_list(uint32_t W, uint32_t H, const uint4* __restrict__ paths,
-                                                    uint8_t* __restrict__ mask, uint32_t* __restrict__ list,
+// tracer.cu:644-648).  The hit pixels of each 8x8 tile (blockIdx.z = view)
+// are appended to one list, tile by tile, with their ray origins, so that
+// the traversal kernel runs full warps of rays from neighbouring pixels and
+// carries none of the double-precision set-up; misses get mask 2 here.  Rows
+// are output rows (the layout of the paths image).
+template <int FMA>
+__global__ void __launch_bounds__(64) k_shadow_list(const hd_camera* __restrict__ cams, hd_camera cam0, uint32_t W,
+                                                    uint32_t H, const uint4* __restrict__ paths, F3 light, float bias,
+                                                    uint8_t* __restrict__ mask, ShadowRay* __restrict__ list,
                                                     uint32_t* __restrict__ count)
-{
-    __shared__ uint32_t warp_base[2];
-    const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7);
-    const uint32_t r = blockIdx.y * 8 + (threadIdx.x >> 3);
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const bool in = x < W && r < H;
-    const uint64_t i = uint64_t(r) * W + x;
-    bool hit = false;
-    if (in) {
-        const uint4 p = paths[i];
-        hit = (p.x | p.y | p.z) != 0;
-        if (!hit)
-            mask[i] = 2;
-    }
-    const uint32_t b = __ballot_sync(0xffffffffu, hit);
-    if (lane == 0)
-        warp_base[warp] = __popc(b);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const uint32_t n0 = warp_base[0], n1 = warp_base[1];
-        const uint32_t base = (n0 + n1) ? atomicAdd(count, n0 + n1) : 0u;
-        warp_base[0] = base;
-        warp_base[1] = base + n0;
-    }
-    __syncthreads();
-    if (hit)
-        list[warp_base[warp] + __popc(b & ((1u << lane) - 1u))] = uint32_t(i);
-}
-
-// The hit pixels of several views (blockIdx.z = view) into one list of
-// view * W * H + pixel indices.
-__global__ void __launch_bounds__(64) k_shadow_list_views(uint32_t W, uint32_t H, const uint4* __restrict__ paths,
-                                                          uint8_t* __restrict__ mask, uint32_t* __restrict__ list,
-                                                          uint32_t* __restrict__ count)
 {
     __shared__ uint32_t warp_base[2];
     const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7);
@@ -346,8 +333,9 @@ __global__ void __launch_bounds__(64) k_shadow_list_views(uint32_t W, uint32_t H
     const bool in = x < W && r < H;
     const uint64_t i = uint64_t(blockIdx.z) * W * H + uint64_t(r) * W + x;
     bool hit = false;
+    uint4 p = make_uint4(0, 0, 0, 0);
     if (in) {
-        const uint4 p = paths[i];
+        p = paths[i];
         hit = (p.x | p.y | p.z) != 0;
         if (!hit)
             mask[i] = 2;
@@ -363,39 +351,61 @@ __global__ void __launch_bounds__(64) k_shadow_list_views(uint32_t W, uint32_t H
         warp_base[1] = base + n0;
     }
     __syncthreads();
-    if (hit)
-        list[warp_base[warp] + __popc(b & ((1u << lane) - 1u))] = uint32_t(i);
-}
-
-template <int FMA>
-__global__ void __launch_bounds__(128) k_trace_shadow_views(Table t, const uint32_t* __restrict__ d_root,
-                                                            const hd_camera* __restrict__ cams, uint32_t W, uint32_t H,
-                                                            const uint4* __restrict__ paths, F3 light, float bias,
-                                                            uint8_t* __restrict__ mask, const uint32_t* __restrict__ list,
-                                                            const uint32_t* __restrict__ count)
-{
-    const uint32_t n = *count;
-    const uint64_t frame = uint64_t(W) * H;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-        const uint32_t g = list[j];
-        const uint32_t v = uint32_t(g / frame);
-        const hd_camera cam = cams[v];
-        shadow_ray<FMA, false>(t, *d_root, cam, W, H, paths + v * frame, light, bias, mask + v * frame, g - v * frame,
-                               nullptr);
+    if (hit) {
+        const hd_camera cam = cams ? cams[blockIdx.z] : cam0;
+        const F3 o = shadow_origin<FMA>(cam, H, x, r, p, light_dir<FMA>(light), bias);
+        list[warp_base[warp] + __popc(b & ((1u << lane) - 1u))] = ShadowRay{uint32_t(i), o.x, o.y, o.z};
     }
 }
 
+// The any-hit walk of every ray of the list toward the light
+// (intersect_ray_node_out_of_order, tracer.cu:453-543), as persistent warps
+// taking 32 rays at a time from a counter.
 template <int FMA, bool COUNT>
-__global__ void __launch_bounds__(128) k_trace_shadow(Table t, const uint32_t* __restrict__ d_root, hd_camera cam,
-                                                      uint32_t W, uint32_t H, const uint4* __restrict__ paths,
-                                                      F3 light, float bias, uint8_t* __restrict__ mask,
-                                                      const uint32_t* __restrict__ list,
-                                                      const uint32_t* __restrict__ count, unsigned long long* counters)
+__global__ void __launch_bounds__(128) k_trace_shadow(Table t, const uint32_t* __restrict__ d_root, F3 light,
+                                                      uint8_t* __restrict__ mask, const ShadowRay* __restrict__ list,
+                                                      uint32_t* __restrict__ head, unsigned long long* counters)
 {
-    const uint32_t n = *count;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        shadow_ray<FMA, COUNT>(t, *d_root, cam, W, H, paths, light, bias, mask, list[j], counters);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t n = head[0];
+    const uint32_t root = *d_root;
+    const F3 dir = light_dir<FMA>(light);
+    const F3 inv = inverse_dir(dir);
+    uint32_t base = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(head + 2, 32u) : 0u, 0);
+    while (base < n) {
+        const uint32_t next = lane == 0 ? atomicAdd(head + 2, 32u) : 0u;
+        const uint32_t j = base + lane;
+        if (j < n) {
+            const ShadowRay ray = list[j];
+            uint32_t hit[3], descents = 0, leaves = 0;
+            mask[ray.idx] =
+                walk<FMA, true>(t, root, F3{ray.ox, ray.oy, ray.oz}, dir, inv, 0, hit, descents, leaves) ? 1 : 0;
+            if (COUNT)
+                add_counts(counters, 1, descents, leaves);
+        }
+        base = __shfl_sync(0xffffffffu, next, 0);
+    }
 }
+
+// Blocks of a persistent launch of `kernel` with `threads` threads: as many
+// as stay resident on every SM (queried once per kernel).
+static uint32_t resident_blocks(const void* kernel, int threads)
+{
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, uint32_t> known;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = known.find({kernel, threads});
+    if (it != known.end())
+        return it->second;
+    int dev = 0, sms = 0, per_sm = 0;
+    HD_CUDA(cudaGetDevice(&dev));
+    HD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    HD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0));
+    const uint32_t n = uint32_t(std::max(1, sms * std::max(1, per_sm)));
+    known[{kernel, threads}] = n;
+    return n;
+}
+
 void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint32_t* d_paths,
                    unsigned long long* d_counters, cudaStream_t stream, const uint32_t* d_root)
 {
@@ -417,38 +427,50 @@ void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint
     HD_LAUNCH_CHECK();
 }
 
+// Shadow pass of n_views frames (cams: device cameras, or nullptr for the one
+// camera cam0): the hit list with origins, then the any-hit walks.
+static void shadow_pass(hd_ctx* c, const hd_camera* d_cams, const hd_camera& cam0, uint32_t n_views, uint32_t w,
+                        uint32_t h, const uint32_t* d_paths, const float light[3], float bias, uint8_t* d_mask,
+                        unsigned long long* d_counters, cudaStream_t st, const uint32_t* rt, uint32_t* d_list)
+{
+    const uint64_t px = uint64_t(w) * h * n_views;
+    uint32_t* buf = d_list ? d_list : c->scratch.get<uint32_t>("shadow_list", shadow_list_words(px));
+    ShadowRay* list = reinterpret_cast<ShadowRay*>(buf);
+    uint32_t* count = buf + 4 * px;
+    HD_CUDA(cudaMemsetAsync(count, 0, 16, st));
+    dim3 tiles((w + 7) / 8, (h + 7) / 8, n_views);
+    const uint4* p = reinterpret_cast<const uint4*>(d_paths);
+    const F3 l = {light[0], light[1], light[2]};
+    if (c->fp_mode)
+        k_shadow_list<1><<<tiles, 64, 0, st>>>(d_cams, cam0, w, h, p, l, bias, d_mask, list, count);
+    else
+        k_shadow_list<0><<<tiles, 64, 0, st>>>(d_cams, cam0, w, h, p, l, bias, d_mask, list, count);
+    HD_LAUNCH_CHECK();
+    auto launch = [&](auto kernel, unsigned long long* counters) {
+        const uint32_t blocks =
+            uint32_t(std::min<uint64_t>((px + 127) / 128, resident_blocks(reinterpret_cast<const void*>(kernel), 128)));
+        kernel<<<blocks, 128, 0, st>>>(c->t, rt, l, d_mask, list, count, counters);
+    };
+    if (d_counters) {
+        if (c->fp_mode)
+            launch(k_trace_shadow<1, true>, d_counters);
+        else
+            launch(k_trace_shadow<0, true>, d_counters);
+    } else {
+        if (c->fp_mode)
+            launch(k_trace_shadow<1, false>, nullptr);
+        else
+            launch(k_trace_shadow<0, false>, nullptr);
+    }
+    HD_LAUNCH_CHECK();
+}
+
 void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
                   const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters,
                   cudaStream_t stream, const uint32_t* d_root, uint32_t* d_list)
 {
-    cudaStream_t st = stream ? stream : c->stream;
-    const uint32_t* rt = d_root ? d_root : c->d_root;
-    const uint64_t px = uint64_t(w) * h;
-    uint32_t* list = d_list ? d_list : c->scratch.get<uint32_t>("shadow_list", px + 1);
-    uint32_t* count = list + px;
-    HD_CUDA(cudaMemsetAsync(count, 0, 4, st));
-    dim3 tiles((w + 7) / 8, (h + 7) / 8);
-    const uint4* p = reinterpret_cast<const uint4*>(d_paths);
-    k_shadow_list<<<tiles, 64, 0, st>>>(w, h, p, d_mask, list, count);
-    HD_LAUNCH_CHECK();
-    const F3 l = {light[0], light[1], light[2]};
-    const uint32_t blocks = uint32_t(std::min<uint64_t>((px + 127) / 128, 152 * 16));
-    if (d_counters) {
-        if (c->fp_mode)
-            k_trace_shadow<1, true><<<blocks, 128, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask, list, count,
-                                                            d_counters);
-        else
-            k_trace_shadow<0, true><<<blocks, 128, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask, list, count,
-                                                            d_counters);
-    } else {
-        if (c->fp_mode)
-            k_trace_shadow<1, false><<<blocks, 128, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask, list, count,
-                                                             nullptr);
-        else
-            k_trace_shadow<0, false><<<blocks, 128, 0, st>>>(c->t, rt, cam, w, h, p, l, bias, d_mask, list, count,
-                                                             nullptr);
-    }
-    HD_LAUNCH_CHECK();
+    shadow_pass(c, nullptr, cam, 1, w, h, d_paths, light, bias, d_mask, d_counters, stream ? stream : c->stream,
+                d_root ? d_root : c->d_root, d_list);
 }
 
 // n_views frames in two launches: primary rays of every view, then the
@@ -461,29 +483,24 @@ void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t 
     const uint64_t px = uint64_t(w) * h * n_views;
     if (px >= 0xFFFFFFFFull)
         throw StatusError{HD_ERR_INVALID, "views x width x height must stay below 2^32 pixels"};
-    dim3 tiles((w + 7) / 8, (h + 7) / 8, n_views);
+    uint32_t* buf = d_list ? d_list : c->scratch.get<uint32_t>("shadow_list", shadow_list_words(px));
+    uint32_t* next_tile = buf + 4 * px + 1;
+    HD_CUDA(cudaMemsetAsync(next_tile, 0, 4, st));
     uint4* out = reinterpret_cast<uint4*>(d_paths);
+    const uint64_t tiles = uint64_t((w + 7) / 8) * ((h + 3) / 4);
+    auto launch = [&](auto kernel) {
+        const uint32_t blocks = uint32_t(
+            std::min<uint64_t>((tiles * n_views + 3) / 4, resident_blocks(reinterpret_cast<const void*>(kernel), 128)));
+        kernel<<<blocks, 128, 0, st>>>(c->t, c->d_root, d_cams, w, h, n_views, out, next_tile);
+    };
     if (c->fp_mode)
-        k_trace_primary_views<1><<<tiles, 64, 0, st>>>(c->t, c->d_root, d_cams, w, h, out);
+        launch(k_trace_primary_views<1>);
     else
-        k_trace_primary_views<0><<<tiles, 64, 0, st>>>(c->t, c->d_root, d_cams, w, h, out);
+        launch(k_trace_primary_views<0>);
     HD_LAUNCH_CHECK();
     if (mid)
         HD_CUDA(cudaEventRecord(mid, st));
-    uint32_t* list = d_list ? d_list : c->scratch.get<uint32_t>("shadow_list", px + 1);
-    uint32_t* count = list + px;
-    HD_CUDA(cudaMemsetAsync(count, 0, 4, st));
-    k_shadow_list_views<<<tiles, 64, 0, st>>>(w, h, out, d_mask, list, count);
-    HD_LAUNCH_CHECK();
-    const F3 l = {light[0], light[1], light[2]};
-    const uint32_t blocks = uint32_t(std::min<uint64_t>((px + 127) / 128, 152 * 16));
-    if (c->fp_mode)
-        k_trace_shadow_views<1><<<blocks, 128, 0, st>>>(c->t, c->d_root, d_cams, w, h, out, l, bias, d_mask, list,
-                                                        count);
-    else
-        k_trace_shadow_views<0><<<blocks, 128, 0, st>>>(c->t, c->d_root, d_cams, w, h, out, l, bias, d_mask, list,
-                                                        count);
-    HD_LAUNCH_CHECK();
+    shadow_pass(c, d_cams, hd_camera{}, n_views, w, h, d_paths, light, bias, d_mask, nullptr, st, c->d_root, d_list);
 }
 
 // DAGUtils::get_value
