@@ -135,8 +135,12 @@ struct Entry {
 };
 
 // The stack walk shared by the primary ray (nearest hit, children in the
-// ray's octant order) and the shadow ray (any hit, children highest first).
-template <int FMA, bool ANY_HIT>
+// ray's octant order) and the shadow ray (any hit).  The reference's shadow
+// walk takes children highest first; whether a ray hits anything does not
+// depend on the order (the walk visits every crossed child until a voxel is
+// reached), so OCTANT shadow walks take the ray's front-to-back order as
+// primary rays do and meet the nearest occluders first.
+template <int FMA, bool ANY_HIT, bool OCTANT = !ANY_HIT>
 HD_D bool walk(const Table& t, uint32_t root, const F3& o, const F3& d, const F3& inv, uint32_t order, uint32_t* hit,
                uint32_t& descents, uint32_t& leaves)
 {
@@ -164,7 +168,7 @@ HD_D bool walk(const Table& t, uint32_t root, const F3& o, const F3& d, const F3
         py >>= up;
         pz >>= up;
         level = nl;
-        const uint32_t nc = ANY_HIT ? 31u - __clz(visit) : next_child(order, visit);
+        const uint32_t nc = OCTANT ? next_child(order, visit) : 31u - __clz(visit);
         visit &= ~(1u << nc);
         px = (px << 1) | ((nc >> 2) & 1);
         py = (py << 1) | ((nc >> 1) & 1);
@@ -371,6 +375,7 @@ __global__ void __launch_bounds__(128) k_trace_shadow(Table t, const uint32_t* _
     const uint32_t root = *d_root;
     const F3 dir = light_dir<FMA>(light);
     const F3 inv = inverse_dir(dir);
+    const uint32_t order = (dir.x < 0.f ? 4u : 0u) + (dir.y < 0.f ? 2u : 0u) + (dir.z < 0.f ? 1u : 0u);
     uint32_t base = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(head + 2, 32u) : 0u, 0);
     while (base < n) {
         const uint32_t next = lane == 0 ? atomicAdd(head + 2, 32u) : 0u;
@@ -379,7 +384,8 @@ __global__ void __launch_bounds__(128) k_trace_shadow(Table t, const uint32_t* _
             const ShadowRay ray = list[j];
             uint32_t hit[3], descents = 0, leaves = 0;
             mask[ray.idx] =
-                walk<FMA, true>(t, root, F3{ray.ox, ray.oy, ray.oz}, dir, inv, 0, hit, descents, leaves) ? 1 : 0;
+                walk<FMA, true, true>(t, root, F3{ray.ox, ray.oy, ray.oz}, dir, inv, order, hit, descents, leaves) ? 1
+                                                                                                                    : 0;
             if (COUNT)
                 add_counts(counters, 1, descents, leaves);
         }
