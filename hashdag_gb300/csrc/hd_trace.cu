@@ -15,6 +15,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 
 #include <algorithm>
 
@@ -129,10 +130,36 @@ HD_D uint32_t next_child(uint32_t order, uint32_t mask) // next_child (tracer.cu
     return (__ffs(permuted) - 1) ^ order;
 }
 
-struct Entry {
-    uint32_t index;
-    uint32_t masks; // child mask | visit mask << 8
+// The walk's stack: per level the node and its child mask | visit mask << 8.
+struct LocalStack {
+    struct {
+        uint32_t index, masks;
+    } e[HD_MAX_DEPTH];
+    HD_D void set(uint32_t l, uint32_t index, uint32_t masks) { e[l] = {index, masks}; }
+    HD_D uint32_t index(uint32_t l) const { return e[l].index; }
+    HD_D uint32_t masks(uint32_t l) const { return e[l].masks; }
 };
+// The same stack in shared memory: level l of thread k at [l * stride + k],
+// node indices and 16-bit masks in two arrays (6 bytes a level).
+struct SharedStack {
+    uint32_t* idx;
+    uint16_t* msk;
+    uint32_t stride;
+    HD_D void set(uint32_t l, uint32_t index, uint32_t masks)
+    {
+        idx[l * stride] = index;
+        msk[l * stride] = uint16_t(masks);
+    }
+    HD_D uint32_t index(uint32_t l) const { return idx[l * stride]; }
+    HD_D uint32_t masks(uint32_t l) const { return msk[l * stride]; }
+};
+// Shared bytes of a SharedStack for `threads` threads and depth D.
+HD_HD uint32_t shared_stack_bytes(uint32_t threads, uint32_t D) { return threads * D * 6; }
+HD_D SharedStack shared_stack(uint32_t* smem, uint32_t D)
+{
+    return SharedStack{smem + threadIdx.x, reinterpret_cast<uint16_t*>(smem + blockDim.x * D) + threadIdx.x,
+                       blockDim.x};
+}
 
 // The stack walk shared by the primary ray (nearest hit, children in the
 // ray's octant order) and the shadow ray (any hit).  The reference's shadow
@@ -140,24 +167,24 @@ struct Entry {
 // depend on the order (the walk visits every crossed child until a voxel is
 // reached), so OCTANT shadow walks take the ray's front-to-back order as
 // primary rays do and meet the nearest occluders first.
-template <int FMA, bool ANY_HIT, bool OCTANT = !ANY_HIT>
+template <int FMA, bool ANY_HIT, bool OCTANT = !ANY_HIT, typename Stack = LocalStack>
 HD_D bool walk(const Table& t, uint32_t root, const F3& o, const F3& d, const F3& inv, uint32_t order, uint32_t* hit,
-               uint32_t& descents, uint32_t& leaves)
+               uint32_t& descents, uint32_t& leaves, Stack stack = Stack{})
 {
     const uint32_t D = t.g.depth, leafl = t.g.leaf_level;
-    Entry stack[HD_MAX_DEPTH];
     uint32_t level = 0, px = 0, py = 0, pz = 0;
     uint32_t index = root;
-    uint32_t child_mask = __ldg(t.sys(root)) & 0xffu;
+    uint32_t child_mask = *(t.sys_ld(root)) & 0xffu;
     uint32_t visit = child_mask & intersection_mask<FMA>(D, true, 0, 0, 0, 0, o, d, inv);
     uint32_t leaf_lo = 0, leaf_hi = 0;
     for (;;) {
         uint32_t nl = level;
         while (nl > 0 && !visit) {
             nl--;
-            index = stack[nl].index;
-            child_mask = stack[nl].masks & 0xffu;
-            visit = stack[nl].masks >> 8;
+            index = stack.index(nl);
+            const uint32_t m = stack.masks(nl);
+            child_mask = m & 0xffu;
+            visit = m >> 8;
         }
         if (nl == 0 && !visit) {
             hit[0] = hit[1] = hit[2] = 0;
@@ -173,7 +200,7 @@ HD_D bool walk(const Table& t, uint32_t root, const F3& o, const F3& d, const F3
         px = (px << 1) | ((nc >> 2) & 1);
         py = (py << 1) | ((nc >> 1) & 1);
         pz = (pz << 1) | (nc & 1);
-        stack[level] = {index, child_mask | (visit << 8)};
+        stack.set(level, index, child_mask | (visit << 8));
         level++;
         if (level == D) {
             hit[0] = px;
@@ -182,12 +209,12 @@ HD_D bool walk(const Table& t, uint32_t root, const F3& o, const F3& d, const F3
             return true;
         }
         if (level < leafl) {
-            index = __ldg(t.sys(index + child_offset(child_mask, nc)));
-            child_mask = __ldg(t.sys(index)) & 0xffu;
+            index = *(t.sys_ld(index + child_offset(child_mask, nc)));
+            child_mask = *(t.sys_ld(index)) & 0xffu;
             descents++;
         } else if (level == leafl) {
-            const uint32_t addr = __ldg(t.sys(index + child_offset(child_mask, nc)));
-            const uint2 lf = __ldg(reinterpret_cast<const uint2*>(t.sys(addr)));
+            const uint32_t addr = *(t.sys_ld(index + child_offset(child_mask, nc)));
+            const uint2 lf = *(reinterpret_cast<const uint2*>(t.sys_ld(addr)));
             leaf_lo = lf.x;
             leaf_hi = lf.y;
             child_mask = first_child_mask(leaf_lo, leaf_hi);
@@ -199,10 +226,19 @@ HD_D bool walk(const Table& t, uint32_t root, const F3& o, const F3& d, const F3
     }
 }
 
-HD_D F3 inverse_dir(const F3& d)
-{
-    return {float(1.0 / double(d.x)), float(1.0 / double(d.y)), float(1.0 / double(d.z))};
-}
+// The child order of a ray: children visited as child ^ octant, 0..7, run
+// front to back along d (rayChildOrder, tracer.cu:161-164).
+HD_D uint32_t octant(const F3& d) { return (d.x < 0.f ? 4u : 0u) + (d.y < 0.f ? 2u : 0u) + (d.z < 0.f ? 1u : 0u); }
+
+// The reference takes float(1.0 / double(x)) (tracer.cu:160): the double
+// quotient rounded again to float.  Rounding a quotient first to a p'-bit
+// and then to a p-bit significand equals rounding it once to p bits when
+// p' >= 2p + 2 (S. Figueroa, "When is double rounding innocuous?", SIGNUM
+// Newsletter 30(3), 1995); double (53) and float (24) qualify.  So the
+// correctly rounded float reciprocal (__frcp_rn) gives the same bits with no
+// double-precision work, which the GB300's small FP64 pipe would otherwise
+// spend on every ray.
+HD_D F3 inverse_dir(const F3& d) { return {__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z)}; }
 
 // 8x8 pixel tiles per 64-thread block; a warp covers 8x4 pixels.
 // Traversal work counters (COUNT instances only): rays, interior descents,
@@ -214,18 +250,18 @@ HD_D void add_counts(unsigned long long* counters, uint32_t rays, uint32_t desce
     atomicAdd(counters + 2, leaves);
 }
 
-template <int FMA, bool COUNT>
+template <int FMA, bool COUNT, typename Stack = LocalStack>
 HD_D void primary_ray(const Table& t, uint32_t root, const hd_camera& cam, uint32_t W, uint32_t H, uint32_t x,
-                      uint32_t y, uint4* __restrict__ out, unsigned long long* counters)
+                      uint32_t y, uint4* __restrict__ out, unsigned long long* counters, Stack stack = Stack{})
 {
     double dd[3];
     camera_dir<FMA>(cam, double(x), double(y), dd);
     const F3 d = {float(dd[0]), float(dd[1]), float(dd[2])};
     const F3 inv = inverse_dir(d);
     const F3 o = {float(cam.position[0]), float(cam.position[1]), float(cam.position[2])};
-    const uint32_t order = (d.x < 0.f ? 4u : 0u) + (d.y < 0.f ? 2u : 0u) + (d.z < 0.f ? 1u : 0u);
+    const uint32_t order = octant(d);
     uint32_t hit[3], descents = 0, leaves = 0;
-    walk<FMA, false>(t, root, o, d, inv, order, hit, descents, leaves);
+    walk<FMA, false, true, Stack>(t, root, o, d, inv, order, hit, descents, leaves, stack);
     out[uint64_t(H - 1 - y) * W + x] = make_uint4(hit[0], hit[1], hit[2], 0);
     if (COUNT)
         add_counts(counters, 1, descents, leaves);
@@ -258,6 +294,8 @@ __global__ void __launch_bounds__(128, 16) k_trace_primary_views(Table t, const 
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t tx = (W + 7) / 8, ty = (H + 3) / 4;
     const uint32_t per_view = tx * ty, n_tiles = per_view * n_views;
+    extern __shared__ uint32_t smem[];
+    const SharedStack stack = shared_stack(smem, t.g.depth);
     const uint32_t root = *d_root;
     uint32_t tile = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(next_tile, 1u) : 0u, 0);
     while (tile < n_tiles) {
@@ -265,7 +303,7 @@ __global__ void __launch_bounds__(128, 16) k_trace_primary_views(Table t, const 
         const uint32_t v = tile / per_view, k = tile - v * per_view;
         const uint32_t x = (k % tx) * 8 + (lane & 7), y = (k / tx) * 4 + (lane >> 3);
         if (x < W && y < H)
-            primary_ray<FMA, false>(t, root, cams[v], W, H, x, y, out + uint64_t(v) * W * H, nullptr);
+            primary_ray<FMA, false>(t, root, cams[v], W, H, x, y, out + uint64_t(v) * W * H, nullptr, stack);
         tile = __shfl_sync(0xffffffffu, next, 0);
     }
 }
@@ -300,9 +338,21 @@ HD_D F3 shadow_origin(const hd_camera& cam, uint32_t H, uint32_t x, uint32_t r, 
     double real_min[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        const double t0 = (bmin[a] - cam.position[a]) / cd[a];
-        const double t1 = ((bmin[a] + 1.0) - cam.position[a]) / cd[a];
-        real_min[a] = t0 < t1 ? t0 : t1;
+        // min(t0, t1) with t0 = (bmin - pos) / cd, t1 = (bmin + 1 - pos) / cd:
+        // the numerators are ordered (bmin + 1 is exact, rounding is
+        // monotonic), so for cd > 0 the minimum is t0 and for cd < 0 it is t1
+        // (equal quotients give the same value either way); only cd = 0 needs
+        // both.
+        const double n0 = bmin[a] - cam.position[a];
+        const double n1 = (bmin[a] + 1.0) - cam.position[a];
+        if (cd[a] > 0.0) {
+            real_min[a] = n0 / cd[a];
+        } else if (cd[a] < 0.0) {
+            real_min[a] = n1 / cd[a];
+        } else {
+            const double t0 = n0 / cd[a], t1 = n1 / cd[a];
+            real_min[a] = t0 < t1 ? t0 : t1;
+        }
     }
     const double maxmin = fmax(fmax(real_min[0], real_min[1]), real_min[2]);
     F3 start, o;
@@ -375,7 +425,9 @@ __global__ void __launch_bounds__(128) k_trace_shadow(Table t, const uint32_t* _
     const uint32_t root = *d_root;
     const F3 dir = light_dir<FMA>(light);
     const F3 inv = inverse_dir(dir);
-    const uint32_t order = (dir.x < 0.f ? 4u : 0u) + (dir.y < 0.f ? 2u : 0u) + (dir.z < 0.f ? 1u : 0u);
+    const uint32_t order = octant(dir);
+    extern __shared__ uint32_t smem[];
+    const SharedStack stack = shared_stack(smem, t.g.depth);
     uint32_t base = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(head + 2, 32u) : 0u, 0);
     while (base < n) {
         const uint32_t next = lane == 0 ? atomicAdd(head + 2, 32u) : 0u;
@@ -384,8 +436,10 @@ __global__ void __launch_bounds__(128) k_trace_shadow(Table t, const uint32_t* _
             const ShadowRay ray = list[j];
             uint32_t hit[3], descents = 0, leaves = 0;
             mask[ray.idx] =
-                walk<FMA, true, true>(t, root, F3{ray.ox, ray.oy, ray.oz}, dir, inv, order, hit, descents, leaves) ? 1
-                                                                                                                    : 0;
+                walk<FMA, true, true>(t, root, F3{ray.ox, ray.oy, ray.oz}, dir, inv, order, hit, descents, leaves,
+                                      stack)
+                    ? 1
+                    : 0;
             if (COUNT)
                 add_counts(counters, 1, descents, leaves);
         }
@@ -394,21 +448,23 @@ __global__ void __launch_bounds__(128) k_trace_shadow(Table t, const uint32_t* _
 }
 
 // Blocks of a persistent launch of `kernel` with `threads` threads: as many
-// as stay resident on every SM (queried once per kernel).
-static uint32_t resident_blocks(const void* kernel, int threads)
+// as stay resident on every SM with smem_bytes of dynamic shared memory
+// (queried once per kernel and size).
+static uint32_t resident_blocks(const void* kernel, int threads, uint32_t smem_bytes)
 {
     static std::mutex mu;
-    static std::map<std::pair<const void*, int>, uint32_t> known;
+    static std::map<std::tuple<const void*, int, uint32_t>, uint32_t> known;
     std::lock_guard<std::mutex> lock(mu);
-    auto it = known.find({kernel, threads});
+    const auto key = std::make_tuple(kernel, threads, smem_bytes);
+    auto it = known.find(key);
     if (it != known.end())
         return it->second;
     int dev = 0, sms = 0, per_sm = 0;
     HD_CUDA(cudaGetDevice(&dev));
     HD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    HD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0));
+    HD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem_bytes));
     const uint32_t n = uint32_t(std::max(1, sms * std::max(1, per_sm)));
-    known[{kernel, threads}] = n;
+    known[key] = n;
     return n;
 }
 
@@ -453,9 +509,10 @@ static void shadow_pass(hd_ctx* c, const hd_camera* d_cams, const hd_camera& cam
         k_shadow_list<0><<<tiles, 64, 0, st>>>(d_cams, cam0, w, h, p, l, bias, d_mask, list, count);
     HD_LAUNCH_CHECK();
     auto launch = [&](auto kernel, unsigned long long* counters) {
-        const uint32_t blocks =
-            uint32_t(std::min<uint64_t>((px + 127) / 128, resident_blocks(reinterpret_cast<const void*>(kernel), 128)));
-        kernel<<<blocks, 128, 0, st>>>(c->t, rt, l, d_mask, list, count, counters);
+        const uint32_t smem = shared_stack_bytes(128, c->t.g.depth);
+        const uint32_t blocks = uint32_t(
+            std::min<uint64_t>((px + 127) / 128, resident_blocks(reinterpret_cast<const void*>(kernel), 128, smem)));
+        kernel<<<blocks, 128, smem, st>>>(c->t, rt, l, d_mask, list, count, counters);
     };
     if (d_counters) {
         if (c->fp_mode)
@@ -495,9 +552,10 @@ void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t 
     uint4* out = reinterpret_cast<uint4*>(d_paths);
     const uint64_t tiles = uint64_t((w + 7) / 8) * ((h + 3) / 4);
     auto launch = [&](auto kernel) {
-        const uint32_t blocks = uint32_t(
-            std::min<uint64_t>((tiles * n_views + 3) / 4, resident_blocks(reinterpret_cast<const void*>(kernel), 128)));
-        kernel<<<blocks, 128, 0, st>>>(c->t, c->d_root, d_cams, w, h, n_views, out, next_tile);
+        const uint32_t smem = shared_stack_bytes(128, c->t.g.depth);
+        const uint32_t blocks = uint32_t(std::min<uint64_t>(
+            (tiles * n_views + 3) / 4, resident_blocks(reinterpret_cast<const void*>(kernel), 128, smem)));
+        kernel<<<blocks, 128, smem, st>>>(c->t, c->d_root, d_cams, w, h, n_views, out, next_tile);
     };
     if (c->fp_mode)
         launch(k_trace_primary_views<1>);
@@ -599,7 +657,7 @@ __global__ void __launch_bounds__(64) k_trace_primary_partials(Table t, const ui
         camera_dir<FMA>(cam, double(x), double(y), dd);
         const F3 d = {float(dd[0]), float(dd[1]), float(dd[2])};
         const F3 o = {float(cam.position[0]), float(cam.position[1]), float(cam.position[2])};
-        const uint32_t order = (d.x < 0.f ? 4u : 0u) + (d.y < 0.f ? 2u : 0u) + (d.z < 0.f ? 1u : 0u);
+        const uint32_t order = octant(d);
         uint32_t hit[3];
         walk<FMA, false>(t, *d_root, o, d, inverse_dir(d), order, hit, descents, leaves);
         out[uint64_t(H - 1 - y) * W + x] = make_uint4(hit[0], hit[1], hit[2], 0);
@@ -624,34 +682,13 @@ __global__ void __launch_bounds__(64) k_trace_shadow_partials(Table t, const uin
         if (p.x == 0 && p.y == 0 && p.z == 0) {
             mask[i] = 2;
         } else {
-            const float dot = FMA ? __fmaf_rn(light.z, light.z, __fmaf_rn(light.y, light.y, light.x * light.x))
-                                  : (light.x * light.x + light.y * light.y) + light.z * light.z;
-            const float il = 1.0f / sqrtf(dot);
-            const F3 dir = {il * light.x, il * light.y, il * light.z};
-            double cd[3];
-            camera_dir<FMA>(cam, double(x), double(H - 1 - r), cd);
-            const double bmin[3] = {double(float(p.x)), double(float(p.y)), double(float(p.z))};
-            double real_min[3];
-            for (int a = 0; a < 3; a++) {
-                const double t0 = (bmin[a] - cam.position[a]) / cd[a];
-                const double t1 = ((bmin[a] + 1.0) - cam.position[a]) / cd[a];
-                real_min[a] = t0 < t1 ? t0 : t1;
-            }
-            const double maxmin = fmax(fmax(real_min[0], real_min[1]), real_min[2]);
-            F3 start, o;
-            if (FMA) {
-                start = {float(__fma_rn(cd[0], maxmin, cam.position[0])),
-                         float(__fma_rn(cd[1], maxmin, cam.position[1])),
-                         float(__fma_rn(cd[2], maxmin, cam.position[2]))};
-                o = {__fmaf_rn(bias, dir.x, start.x), __fmaf_rn(bias, dir.y, start.y),
-                     __fmaf_rn(bias, dir.z, start.z)};
-            } else {
-                start = {float(cam.position[0] + cd[0] * maxmin), float(cam.position[1] + cd[1] * maxmin),
-                         float(cam.position[2] + cd[2] * maxmin)};
-                o = {start.x + bias * dir.x, start.y + bias * dir.y, start.z + bias * dir.z};
-            }
+            // the same origin and front-to-back order as the shadow pass
+            const F3 dir = light_dir<FMA>(light);
+            const F3 o = shadow_origin<FMA>(cam, H, x, r, p, dir, bias);
+            const uint32_t order = octant(dir);
             uint32_t hit[3];
-            mask[i] = walk<FMA, true>(t, *d_root, o, dir, inverse_dir(dir), 0, hit, descents, leaves) ? 1 : 0;
+            mask[i] = walk<FMA, true, true>(t, *d_root, o, dir, inverse_dir(dir), order, hit, descents, leaves) ? 1
+                                                                                                                : 0;
             rays = 1;
         }
     }
