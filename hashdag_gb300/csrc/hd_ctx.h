@@ -109,6 +109,6 @@ void get_values(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out);
 // mid (optional): recorded between the primary and the shadow launches
 void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t w, uint32_t h, uint32_t* d_paths,
                  const float light[3], float bias, uint8_t* d_mask, cudaStream_t stream = nullptr,
-                 uint32_t* d_list = nullptr, cudaEvent_t mid = nullptr);
+                 uint32_t* d_list = nullptr, cudaEvent_t mid = nullptr, const uint32_t* d_root = nullptr);
 
 } // namespace hd

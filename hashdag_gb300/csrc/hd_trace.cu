@@ -251,8 +251,8 @@ HD_D void add_counts(unsigned long long* counters, uint32_t rays, uint32_t desce
 }
 
 template <int FMA, bool COUNT, typename Stack = LocalStack>
-HD_D void primary_ray(const Table& t, uint32_t root, const hd_camera& cam, uint32_t W, uint32_t H, uint32_t x,
-                      uint32_t y, uint4* __restrict__ out, unsigned long long* counters, Stack stack = Stack{})
+HD_D uint4 primary_ray(const Table& t, uint32_t root, const hd_camera& cam, uint32_t W, uint32_t H, uint32_t x,
+                       uint32_t y, uint4* __restrict__ out, unsigned long long* counters, Stack stack = Stack{})
 {
     double dd[3];
     camera_dir<FMA>(cam, double(x), double(y), dd);
@@ -262,9 +262,11 @@ HD_D void primary_ray(const Table& t, uint32_t root, const hd_camera& cam, uint3
     const uint32_t order = octant(d);
     uint32_t hit[3], descents = 0, leaves = 0;
     walk<FMA, false, true, Stack>(t, root, o, d, inv, order, hit, descents, leaves, stack);
-    out[uint64_t(H - 1 - y) * W + x] = make_uint4(hit[0], hit[1], hit[2], 0);
+    const uint4 path = make_uint4(hit[0], hit[1], hit[2], 0);
+    out[uint64_t(H - 1 - y) * W + x] = path;
     if (COUNT)
         add_counts(counters, 1, descents, leaves);
+    return path;
 }
 
 template <int FMA, bool COUNT>
@@ -277,35 +279,6 @@ __global__ void __launch_bounds__(64) k_trace_primary(Table t, const uint32_t* _
     if (x >= W || y >= H)
         return;
     primary_ray<FMA, COUNT>(t, *d_root, cam, W, H, x, y, out, counters);
-}
-
-// Several views in one launch, as persistent warps: each warp takes 8x4
-// pixel tiles from a counter (view-major, then tile rows), so warps whose
-// rays end early take more tiles and every resident warp stays busy to the
-// end of the launch.  The next tile is fetched before the current one is
-// traced.  View v writes its paths at out + v * W * H (the single-view
-// layout).
-template <int FMA>
-__global__ void __launch_bounds__(128, 16) k_trace_primary_views(Table t, const uint32_t* __restrict__ d_root,
-                                                             const hd_camera* __restrict__ cams, uint32_t W,
-                                                             uint32_t H, uint32_t n_views, uint4* __restrict__ out,
-                                                             uint32_t* __restrict__ next_tile)
-{
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t tx = (W + 7) / 8, ty = (H + 3) / 4;
-    const uint32_t per_view = tx * ty, n_tiles = per_view * n_views;
-    extern __shared__ uint32_t smem[];
-    const SharedStack stack = shared_stack(smem, t.g.depth);
-    const uint32_t root = *d_root;
-    uint32_t tile = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(next_tile, 1u) : 0u, 0);
-    while (tile < n_tiles) {
-        const uint32_t next = lane == 0 ? atomicAdd(next_tile, 1u) : 0u;
-        const uint32_t v = tile / per_view, k = tile - v * per_view;
-        const uint32_t x = (k % tx) * 8 + (lane & 7), y = (k / tx) * 4 + (lane >> 3);
-        if (x < W && y < H)
-            primary_ray<FMA, false>(t, root, cams[v], W, H, x, y, out + uint64_t(v) * W * H, nullptr, stack);
-        tile = __shfl_sync(0xffffffffu, next, 0);
-    }
 }
 
 // A shadow ray of the compacted list: the output pixel (view * W * H +
@@ -368,15 +341,63 @@ HD_D F3 shadow_origin(const hd_camera& cam, uint32_t H, uint32_t x, uint32_t r, 
     return o;
 }
 
+// Several views in one launch, as persistent warps: each warp takes 8x4
+// pixel tiles from a counter (view-major, then tile rows), so warps whose
+// rays end early take more tiles and every resident warp stays busy to the
+// end of the launch; the next tile is fetched before the current one is
+// traced.  View v writes its paths at out + v * W * H (the single-view
+// layout).  The shadow pass's set-up is fused in: a pixel whose primary ray
+// hit appends its shadow ray (origin on the hit voxel, as shadow_origin) to
+// the list, warp by warp; a miss gets mask 2 at once.
+template <int FMA>
+__global__ void __launch_bounds__(128, 16)
+    k_trace_views(Table t, const uint32_t* __restrict__ d_root, const hd_camera* __restrict__ cams, uint32_t W,
+                  uint32_t H, uint32_t n_views, uint4* __restrict__ out, F3 light, float bias,
+                  uint8_t* __restrict__ mask, ShadowRay* __restrict__ list, uint32_t* __restrict__ head)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t tx = (W + 7) / 8, ty = (H + 3) / 4;
+    const uint32_t per_view = tx * ty, n_tiles = per_view * n_views;
+    extern __shared__ uint32_t smem[];
+    const SharedStack stack = shared_stack(smem, t.g.depth);
+    const uint32_t root = *d_root;
+    uint32_t* next_tile = head + 1;
+    uint32_t tile = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(next_tile, 1u) : 0u, 0);
+    while (tile < n_tiles) {
+        const uint32_t next = lane == 0 ? atomicAdd(next_tile, 1u) : 0u;
+        const uint32_t v = tile / per_view, k = tile - v * per_view;
+        const uint32_t x = (k % tx) * 8 + (lane & 7), y = (k / tx) * 4 + (lane >> 3);
+        const uint64_t i = uint64_t(v) * W * H + uint64_t(H - 1 - y) * W + x;
+        bool hit = false;
+        uint4 p = make_uint4(0, 0, 0, 0);
+        if (x < W && y < H) {
+            p = primary_ray<FMA, false>(t, root, cams[v], W, H, x, y, out + uint64_t(v) * W * H, nullptr, stack);
+            hit = (p.x | p.y | p.z) != 0;
+            if (!hit)
+                mask[i] = 2;
+        }
+        const uint32_t b = __ballot_sync(0xffffffffu, hit);
+        if (b) {
+            const uint32_t base =
+                __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(head, uint32_t(__popc(b))) : 0u, 0);
+            if (hit) {
+                const F3 o = shadow_origin<FMA>(cams[v], H, x, H - 1 - y, p, light_dir<FMA>(light), bias);
+                list[base + __popc(b & ((1u << lane) - 1u))] = ShadowRay{uint32_t(i), o.x, o.y, o.z};
+            }
+        }
+        tile = __shfl_sync(0xffffffffu, next, 0);
+    }
+}
+
 // Shadow rays start only at hit pixels (a path of (0, 0, 0) is a miss,
-// tracer.cu:644-648).  The hit pixels of each 8x8 tile (blockIdx.z = view)
-// are appended to one list, tile by tile, with their ray origins, so that
+// tracer.cu:644-648).  The hit pixels of each 8x8 tile are appended to the
+// list, tile by tile, with their ray origins, so that
 // the traversal kernel runs full warps of rays from neighbouring pixels and
 // carries none of the double-precision set-up; misses get mask 2 here.  Rows
 // are output rows (the layout of the paths image).
 template <int FMA>
-__global__ void __launch_bounds__(64) k_shadow_list(const hd_camera* __restrict__ cams, hd_camera cam0, uint32_t W,
-                                                    uint32_t H, const uint4* __restrict__ paths, F3 light, float bias,
+__global__ void __launch_bounds__(64) k_shadow_list(hd_camera cam, uint32_t W, uint32_t H,
+                                                    const uint4* __restrict__ paths, F3 light, float bias,
                                                     uint8_t* __restrict__ mask, ShadowRay* __restrict__ list,
                                                     uint32_t* __restrict__ count)
 {
@@ -385,7 +406,7 @@ __global__ void __launch_bounds__(64) k_shadow_list(const hd_camera* __restrict_
     const uint32_t r = blockIdx.y * 8 + (threadIdx.x >> 3);
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool in = x < W && r < H;
-    const uint64_t i = uint64_t(blockIdx.z) * W * H + uint64_t(r) * W + x;
+    const uint64_t i = uint64_t(r) * W + x;
     bool hit = false;
     uint4 p = make_uint4(0, 0, 0, 0);
     if (in) {
@@ -406,7 +427,6 @@ __global__ void __launch_bounds__(64) k_shadow_list(const hd_camera* __restrict_
     }
     __syncthreads();
     if (hit) {
-        const hd_camera cam = cams ? cams[blockIdx.z] : cam0;
         const F3 o = shadow_origin<FMA>(cam, H, x, r, p, light_dir<FMA>(light), bias);
         list[warp_base[warp] + __popc(b & ((1u << lane) - 1u))] = ShadowRay{uint32_t(i), o.x, o.y, o.z};
     }
@@ -489,30 +509,18 @@ void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint
     HD_LAUNCH_CHECK();
 }
 
-// Shadow pass of n_views frames (cams: device cameras, or nullptr for the one
-// camera cam0): the hit list with origins, then the any-hit walks.
-static void shadow_pass(hd_ctx* c, const hd_camera* d_cams, const hd_camera& cam0, uint32_t n_views, uint32_t w,
-                        uint32_t h, const uint32_t* d_paths, const float light[3], float bias, uint8_t* d_mask,
-                        unsigned long long* d_counters, cudaStream_t st, const uint32_t* rt, uint32_t* d_list)
+// The any-hit walks of a shadow-ray list (head: ray count, two work
+// counters) over px pixels.
+static void shadow_walks(hd_ctx* c, uint64_t px, const float light[3], uint8_t* d_mask,
+                         unsigned long long* d_counters, cudaStream_t st, const uint32_t* rt, const ShadowRay* list,
+                         uint32_t* head)
 {
-    const uint64_t px = uint64_t(w) * h * n_views;
-    uint32_t* buf = d_list ? d_list : c->scratch.get<uint32_t>("shadow_list", shadow_list_words(px));
-    ShadowRay* list = reinterpret_cast<ShadowRay*>(buf);
-    uint32_t* count = buf + 4 * px;
-    HD_CUDA(cudaMemsetAsync(count, 0, 16, st));
-    dim3 tiles((w + 7) / 8, (h + 7) / 8, n_views);
-    const uint4* p = reinterpret_cast<const uint4*>(d_paths);
     const F3 l = {light[0], light[1], light[2]};
-    if (c->fp_mode)
-        k_shadow_list<1><<<tiles, 64, 0, st>>>(d_cams, cam0, w, h, p, l, bias, d_mask, list, count);
-    else
-        k_shadow_list<0><<<tiles, 64, 0, st>>>(d_cams, cam0, w, h, p, l, bias, d_mask, list, count);
-    HD_LAUNCH_CHECK();
     auto launch = [&](auto kernel, unsigned long long* counters) {
         const uint32_t smem = shared_stack_bytes(128, c->t.g.depth);
         const uint32_t blocks = uint32_t(
             std::min<uint64_t>((px + 127) / 128, resident_blocks(reinterpret_cast<const void*>(kernel), 128, smem)));
-        kernel<<<blocks, 128, smem, st>>>(c->t, rt, l, d_mask, list, count, counters);
+        kernel<<<blocks, 128, smem, st>>>(c->t, rt, l, d_mask, list, head, counters);
     };
     if (d_counters) {
         if (c->fp_mode)
@@ -528,43 +536,68 @@ static void shadow_pass(hd_ctx* c, const hd_camera* d_cams, const hd_camera& cam
     HD_LAUNCH_CHECK();
 }
 
+// Shadow pass of one frame from its paths: the hit list with origins, then
+// the any-hit walks.
+static void shadow_pass(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
+                        const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters,
+                        cudaStream_t st, const uint32_t* rt, uint32_t* d_list)
+{
+    const uint64_t px = uint64_t(w) * h;
+    uint32_t* buf = d_list ? d_list : c->scratch.get<uint32_t>("shadow_list", shadow_list_words(px));
+    ShadowRay* list = reinterpret_cast<ShadowRay*>(buf);
+    uint32_t* head = buf + 4 * px;
+    HD_CUDA(cudaMemsetAsync(head, 0, 16, st));
+    dim3 tiles((w + 7) / 8, (h + 7) / 8);
+    const uint4* p = reinterpret_cast<const uint4*>(d_paths);
+    const F3 l = {light[0], light[1], light[2]};
+    if (c->fp_mode)
+        k_shadow_list<1><<<tiles, 64, 0, st>>>(cam, w, h, p, l, bias, d_mask, list, head);
+    else
+        k_shadow_list<0><<<tiles, 64, 0, st>>>(cam, w, h, p, l, bias, d_mask, list, head);
+    HD_LAUNCH_CHECK();
+    shadow_walks(c, px, light, d_mask, d_counters, st, rt, list, head);
+}
+
 void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
                   const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters,
                   cudaStream_t stream, const uint32_t* d_root, uint32_t* d_list)
 {
-    shadow_pass(c, nullptr, cam, 1, w, h, d_paths, light, bias, d_mask, d_counters, stream ? stream : c->stream,
+    shadow_pass(c, cam, w, h, d_paths, light, bias, d_mask, d_counters, stream ? stream : c->stream,
                 d_root ? d_root : c->d_root, d_list);
 }
 
-// n_views frames in two launches: primary rays of every view, then the
-// shadow rays of every hit pixel of every view.
+// n_views frames in two launches: primary rays of every view with the
+// shadow-ray list, then the shadow rays of every hit pixel of every view.
 void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t w, uint32_t h, uint32_t* d_paths,
                  const float light[3], float bias, uint8_t* d_mask, cudaStream_t stream, uint32_t* d_list,
-                 cudaEvent_t mid)
+                 cudaEvent_t mid, const uint32_t* d_root)
 {
     cudaStream_t st = stream ? stream : c->stream;
+    const uint32_t* rt = d_root ? d_root : c->d_root;
     const uint64_t px = uint64_t(w) * h * n_views;
     if (px >= 0xFFFFFFFFull)
         throw StatusError{HD_ERR_INVALID, "views x width x height must stay below 2^32 pixels"};
     uint32_t* buf = d_list ? d_list : c->scratch.get<uint32_t>("shadow_list", shadow_list_words(px));
-    uint32_t* next_tile = buf + 4 * px + 1;
-    HD_CUDA(cudaMemsetAsync(next_tile, 0, 4, st));
+    ShadowRay* list = reinterpret_cast<ShadowRay*>(buf);
+    uint32_t* head = buf + 4 * px;
+    HD_CUDA(cudaMemsetAsync(head, 0, 16, st));
     uint4* out = reinterpret_cast<uint4*>(d_paths);
     const uint64_t tiles = uint64_t((w + 7) / 8) * ((h + 3) / 4);
+    const F3 l = {light[0], light[1], light[2]};
     auto launch = [&](auto kernel) {
         const uint32_t smem = shared_stack_bytes(128, c->t.g.depth);
         const uint32_t blocks = uint32_t(std::min<uint64_t>(
             (tiles * n_views + 3) / 4, resident_blocks(reinterpret_cast<const void*>(kernel), 128, smem)));
-        kernel<<<blocks, 128, smem, st>>>(c->t, c->d_root, d_cams, w, h, n_views, out, next_tile);
+        kernel<<<blocks, 128, smem, st>>>(c->t, rt, d_cams, w, h, n_views, out, l, bias, d_mask, list, head);
     };
     if (c->fp_mode)
-        launch(k_trace_primary_views<1>);
+        launch(k_trace_views<1>);
     else
-        launch(k_trace_primary_views<0>);
+        launch(k_trace_views<0>);
     HD_LAUNCH_CHECK();
     if (mid)
         HD_CUDA(cudaEventRecord(mid, st));
-    shadow_pass(c, d_cams, hd_camera{}, n_views, w, h, d_paths, light, bias, d_mask, nullptr, st, c->d_root, d_list);
+    shadow_walks(c, px, light, d_mask, nullptr, st, rt, list, head);
 }
 
 // DAGUtils::get_value
