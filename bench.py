@@ -597,7 +597,7 @@ def run_gpu(args, dist):
                        "parallelism": f"replicas x{dist.world}"},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": V * C.sizeof(_capi.Camera),
                     "d2h_bytes_per_step": V * (W * H * 16 + W * H)},
-            "gpu_launches": 3 * K, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": 2 * K, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "wall_s": wall, "edits": edits, "colors": colors, "serving": serving}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)

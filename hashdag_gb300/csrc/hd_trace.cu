@@ -26,11 +26,10 @@ namespace hd {
 HD_D float fmax_r(float a, float b) { return a > b ? a : b; } // constexpr_max (cuda_math.h:13)
 HD_D float fmin_r(float a, float b) { return a < b ? a : b; }
 
-// normalize(ray_min + px * ddx + py * ddy - position), double
+// ray_min + px * ddx + py * ddy - position and its squared length, double
 template <int FMA>
-HD_D void camera_dir(const hd_camera& cam, double px, double py, double out[3])
+HD_D double camera_vec(const hd_camera& cam, double px, double py, double v[3])
 {
-    double v[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         double t;
@@ -43,12 +42,84 @@ HD_D void camera_dir(const hd_camera& cam, double px, double py, double out[3])
         }
         v[a] = t - cam.position[a];
     }
-    const double dot = FMA ? __fma_rn(v[2], v[2], __fma_rn(v[1], v[1], v[0] * v[0]))
-                           : (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+    return FMA ? __fma_rn(v[2], v[2], __fma_rn(v[1], v[1], v[0] * v[0])) : (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+}
+
+// normalize(ray_min + px * ddx + py * ddy - position), double
+template <int FMA>
+HD_D void camera_dir(const hd_camera& cam, double px, double py, double out[3])
+{
+    double v[3];
+    const double dot = camera_vec<FMA>(cam, px, py, v);
     const double inv = 1.0 / sqrt(dot);
     out[0] = inv * v[0];
     out[1] = inv * v[1];
     out[2] = inv * v[2];
+}
+
+// Exact double of a 32-bit unsigned integer, built from its bits.
+HD_D double u32_to_double(uint32_t u)
+{
+    if (u == 0)
+        return 0.0;
+    const uint32_t e = 31 - __clz(u);
+    const uint64_t frac = (uint64_t(u) << (52 - e)) & ((1ull << 52) - 1);
+    return __longlong_as_double((long long)((uint64_t(1023 + e) << 52) | frac));
+}
+
+// v rounded to the nearest float (ties to even excepted), from its bits.
+// False when v lies within `margin` double ulps of a point halfway between
+// two floats (margin 0: exactly on it) or outside [2^-125, 2^126].
+HD_D bool round_to_float(double v, uint32_t margin, float& out)
+{
+    const uint64_t b = (uint64_t)__double_as_longlong(v);
+    const uint32_t sign = uint32_t(b >> 32) & 0x80000000u;
+    const uint64_t mag = b & 0x7FFFFFFFFFFFFFFFull;
+    if (mag == 0) {
+        out = __uint_as_float(sign);
+        return true;
+    }
+    const int32_t e = int32_t(mag >> 52) - 1023 + 127;
+    if (e < 2 || e > 253)
+        return false;
+    const uint32_t rem = uint32_t(mag) & ((1u << 29) - 1), mid = 1u << 28;
+    if ((rem > mid ? rem - mid : mid - rem) <= margin)
+        return false;
+    out = __uint_as_float(sign | ((uint32_t(e) << 23) + (uint32_t(mag >> 29) & 0x7FFFFFu) + (rem > mid ? 1u : 0u)));
+    return true;
+}
+
+// float(normalize(...)) of camera_dir with a third of its double-precision
+// work (the GB300's FP64 pipe is narrow, and every primary ray pays for
+// this).  The reference rounds 1 / sqrt(dot) twice and the product once more
+// (relative error below 2^-51.4 against the exact v / |v|); here a float
+// rsqrtf seed (2 ulp; the seed's argument rounded from dot, 2^-24) takes
+// one Newton-Raphson step in double, y1 = y0 + y0 (1 - dot y0^2) / 2, whose
+// error is 1.5 e0^2 plus roundings, below 2^-43, and y1 * v is rounded once.
+// The two doubles differ by less than 2^-42.9 relative, about 1,100 ulps of
+// the double; where a component lies more than 8,192 ulps from a float
+// rounding midpoint both round to the same float.  False (for about one ray
+// in ten thousand) sends the ray to the exact path.
+template <int FMA>
+HD_D bool camera_dir_float(const hd_camera& cam, uint32_t x, uint32_t y, F3& d)
+{
+    double v[3];
+    const double dot = camera_vec<FMA>(cam, u32_to_double(x), u32_to_double(y), v);
+    if (!(dot >= 0x1p-100 && dot <= 0x1p100))
+        return false;
+    // dot rounded to float by its bits (the carry of the rounding bit
+    // reaches the exponent when it must)
+    const uint64_t db = (uint64_t)__double_as_longlong(dot);
+    const uint32_t fb = ((uint32_t(db >> 52) - 1023 + 127) << 23) + ((uint32_t(db >> 29) & 0x7FFFFFu)) +
+                        uint32_t((db >> 28) & 1);
+    const uint32_t yb = __float_as_uint(rsqrtf(__uint_as_float(fb)));
+    const double y0 = __longlong_as_double(
+        (long long)((uint64_t(((yb >> 23) & 0xFF) - 127 + 1023) << 52) | (uint64_t(yb & 0x7FFFFFu) << 29)));
+    const double h = dot * y0;
+    const double e = __fma_rn(-h, y0, 1.0);
+    const double y1 = __fma_rn(y0 * e, 0.5, y0);
+    return round_to_float(y1 * v[0], 8192, d.x) && round_to_float(y1 * v[1], 8192, d.y) &&
+           round_to_float(y1 * v[2], 8192, d.z);
 }
 
 // compute_intersection_mask: children of node `path` at `level` crossed by
@@ -254,11 +325,17 @@ template <int FMA, bool COUNT, typename Stack = LocalStack>
 HD_D uint4 primary_ray(const Table& t, uint32_t root, const hd_camera& cam, uint32_t W, uint32_t H, uint32_t x,
                        uint32_t y, uint4* __restrict__ out, unsigned long long* counters, Stack stack = Stack{})
 {
-    double dd[3];
-    camera_dir<FMA>(cam, double(x), double(y), dd);
-    const F3 d = {float(dd[0]), float(dd[1]), float(dd[2])};
+    F3 d;
+    if (!camera_dir_float<FMA>(cam, x, y, d)) {
+        double dd[3];
+        camera_dir<FMA>(cam, double(x), double(y), dd);
+        d = {float(dd[0]), float(dd[1]), float(dd[2])};
+    }
     const F3 inv = inverse_dir(d);
-    const F3 o = {float(cam.position[0]), float(cam.position[1]), float(cam.position[2])};
+    F3 o;
+    if (!(round_to_float(cam.position[0], 0, o.x) && round_to_float(cam.position[1], 0, o.y) &&
+          round_to_float(cam.position[2], 0, o.z)))
+        o = {float(cam.position[0]), float(cam.position[1]), float(cam.position[2])};
     const uint32_t order = octant(d);
     uint32_t hit[3], descents = 0, leaves = 0;
     walk<FMA, false, true, Stack>(t, root, o, d, inv, order, hit, descents, leaves, stack);
