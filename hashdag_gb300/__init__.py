@@ -15,6 +15,7 @@ C ABI of libhashdag_gb300.so:
 Every call runs sm_103a kernels; there is no CPU path.
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -219,6 +220,53 @@ class HashDAG:
 
     def set_undo_capacity(self, frames):
         self._check(lib().hd_set_undo_capacity(self._h, int(frames)))
+
+    # -- files (serializer.h) ------------------------------------------------
+    @staticmethod
+    def _info(info):
+        if info is None:
+            return None
+        if isinstance(info, _capi.DagInfo):
+            return C.byref(info)
+        lo, hi = info
+        d = _capi.DagInfo()
+        d.aabb_min[:] = [float(v) for v in lo]
+        d.aabb_max[:] = [float(v) for v in hi]
+        return C.byref(d)
+
+    @staticmethod
+    def _info_tuple(d):
+        return tuple(d.aabb_min), tuple(d.aabb_max)
+
+    def load_dag_from_file(self, path):
+        """BasicDAGFactory::load_dag_from_file + load_from_DAG; returns the
+        file's DAGInfo as ((min), (max))."""
+        d = _capi.DagInfo()
+        self._check(lib().hd_load_basic_dag_file(self._h, os.fsencode(path), C.byref(d)))
+        return self._info_tuple(d)
+
+    def save_dag_to_file(self, path, info=None):
+        """BasicDAGFactory::save_dag_to_file of the last imported or
+        generated BasicDAG."""
+        self._check(lib().hd_save_basic_dag_file(self._h, os.fsencode(path), self._info(info)))
+
+    def load_compressed_colors_from_file(self, path, enclosed_leaves_compat32=False):
+        """BasicDAGFactory::load_compressed_colors_from_file +
+        HashDAGFactory::load_colors_from_DAG on the loaded scene."""
+        flags = _capi.COLORS_ENCLOSED_32 if enclosed_leaves_compat32 else 0
+        self._check(lib().hd_load_colors_file(self._h, os.fsencode(path), flags))
+
+    def save_snapshot(self, path, info=None):
+        """The table (and colours) in the reference's hash-DAG file format
+        plus bucket sizes, full nodes and colours."""
+        self._check(lib().hd_save_snapshot(self._h, os.fsencode(path), self._info(info)))
+
+    def load_snapshot(self, path):
+        """A snapshot, or a hash-DAG file the reference wrote (then edits wait
+        for remove_stale_nodes); returns the DAGInfo."""
+        d = _capi.DagInfo()
+        self._check(lib().hd_load_snapshot(self._h, os.fsencode(path), C.byref(d)))
+        return self._info_tuple(d)
 
     def export_basic_dag(self):
         n = C.c_uint64()

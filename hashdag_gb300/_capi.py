@@ -8,9 +8,10 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libhashdag_gb300.so")
 
 HD_OK, HD_ERR_INVALID, HD_ERR_CUDA, HD_ERR_POOL_FULL, HD_ERR_BUCKET_FULL, HD_ERR_TIMEOUT, HD_ERR_OOM, \
-    HD_ERR_STATE = range(8)
+    HD_ERR_STATE, HD_ERR_IO = range(9)
 STATUS_NAMES = {0: "HD_OK", 1: "HD_ERR_INVALID", 2: "HD_ERR_CUDA", 3: "HD_ERR_POOL_FULL", 4: "HD_ERR_BUCKET_FULL",
-                5: "HD_ERR_TIMEOUT", 6: "HD_ERR_OOM", 7: "HD_ERR_STATE"}
+                5: "HD_ERR_TIMEOUT", 6: "HD_ERR_OOM", 7: "HD_ERR_STATE", 8: "HD_ERR_IO"}
+COLORS_ENCLOSED_32 = 1
 MAX_DEPTH = 20
 INVALID_NODE = 0xDFFFFFF
 
@@ -20,6 +21,11 @@ class Config(C.Structure):
                 ("top_bucket_bits", C.c_uint32), ("low_bucket_bits", C.c_uint32),
                 ("top_bucket_size", C.c_uint32), ("low_bucket_size", C.c_uint32),
                 ("pool_pages", C.c_uint32)]
+
+
+class DagInfo(C.Structure):
+    """DAGInfo (dag_info.h:6-10): the scene's bounding box."""
+    _fields_ = [("aabb_min", C.c_double * 3), ("aabb_max", C.c_double * 3)]
 
 
 class Camera(C.Structure):
@@ -121,6 +127,11 @@ SIGNATURES = [
     ("hd_serve", C.c_int, [_P, C.POINTER(Request), _u32, C.POINTER(ServeConfig), C.POINTER(RequestResult),
                            C.POINTER(ServeStats)]),
     ("hd_export_basic_dag", C.c_int, [_P, _P, _u64, C.POINTER(_u64)]),
+    ("hd_load_basic_dag_file", C.c_int, [_P, C.c_char_p, C.POINTER(DagInfo)]),
+    ("hd_save_basic_dag_file", C.c_int, [_P, C.c_char_p, C.POINTER(DagInfo)]),
+    ("hd_load_colors_file", C.c_int, [_P, C.c_char_p, _u32]),
+    ("hd_save_snapshot", C.c_int, [_P, C.c_char_p, C.POINTER(DagInfo)]),
+    ("hd_load_snapshot", C.c_int, [_P, C.c_char_p, C.POINTER(DagInfo)]),
     ("hd_trace_primary", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _P, C.POINTER(_f32)]),
     ("hd_trace_shadow", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _P, C.POINTER(_f32), _f32, _P,
                                   C.POINTER(_f32)]),

@@ -11,27 +11,6 @@ using namespace hd;
 
 namespace {
 
-template <typename F>
-hd_status guarded(hd_ctx* c, F&& f)
-{
-    try {
-        f();
-        return HD_OK;
-    } catch (const StatusError& e) {
-        if (c)
-            c->err = e.msg;
-        return e.status;
-    } catch (const CudaError& e) {
-        if (c)
-            c->err = std::string("CUDA error ") + cudaGetErrorString(e.code) + " in " + e.where;
-        return e.code == cudaErrorMemoryAllocation ? HD_ERR_OOM : HD_ERR_CUDA;
-    } catch (const std::bad_alloc&) {
-        if (c)
-            c->err = "host allocation failed";
-        return HD_ERR_OOM;
-    }
-}
-
 bool valid_config(const hd_config& c, std::string& why)
 {
     if (c.depth < 4 || c.depth > HD_MAX_DEPTH)
@@ -179,10 +158,10 @@ hd_status hd_load_basic_dag(hd_ctx* c, const uint32_t* h_words, uint64_t n_words
     if (!c || !h_words || n_words < 2)
         return HD_ERR_INVALID;
     return guarded(c, [&] {
-        uint32_t* d = c->scratch.get<uint32_t>("basic_in", n_words);
-        HD_CUDA(cudaMemcpyAsync(d, h_words, n_words * 4, cudaMemcpyHostToDevice, c->stream));
+        keep_basic(c, h_words, n_words);
         table_reset(c);
-        import_basic_dag(c, d, n_words);
+        import_basic_dag(c, c->d_basic, n_words);
+        c->needs_gc = false;
     });
 }
 
@@ -200,6 +179,7 @@ hd_status hd_generate_scene_ex(hd_ctx* c, uint64_t seed, uint32_t flags)
         table_reset(c);
         import_basic_dag(c, words, n);
         c->scratch.release();
+        c->needs_gc = false;
     });
 }
 
@@ -444,6 +424,7 @@ hd_status hd_import_table(hd_ctx* c, const uint32_t* bs, const uint32_t* pt, con
         HD_CUDA(cudaMemcpyAsync(c->d_root, &root, 4, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaStreamSynchronize(st));
         c->root = root;
+        c->needs_gc = false;
     });
 }
 

@@ -100,6 +100,28 @@ struct PathLevel {
     uint32_t* z;
     uint32_t* nkids; // present children
     uint32_t* first; // exclusive scan of nkids
+    uint64_t* base;  // leavesCount of create_hash_dag_colors at the path (file import only)
+};
+
+// Leaves under a node (BasicDAGColorsBase::get_leaves_count, basic_dag.h:
+// 60-74): an index into enclosedLeaves above topLevels, the count itself
+// below.  An index past the array sets *bad.
+struct LeavesCount {
+    const uint64_t* enclosed;
+    uint64_t n_enclosed;
+    uint32_t top_levels;
+    uint32_t* bad;
+    HD_D uint64_t operator()(uint32_t level, uint32_t header) const
+    {
+        const uint32_t upper = header >> 8;
+        if (level >= top_levels)
+            return upper;
+        if (upper >= n_enclosed) {
+            atomicExch(bad, 1u);
+            return 0;
+        }
+        return enclosed[upper];
+    }
 };
 
 __global__ void k_path_children(Table t, PathLevel lv, uint32_t n)
@@ -110,18 +132,26 @@ __global__ void k_path_children(Table t, PathLevel lv, uint32_t n)
 // children of the level's paths, in child order; colour-tree entries of the
 // level: nodes[8 * (node_base + i) + c] = child's colour node, or at level
 // T - 1 the leaf of the child (leaf_base + its index at level T)
+// With leaves counts (the file import), each child also gets its base: the
+// path's base plus the leaves of its earlier siblings (the running
+// leavesCount of create_hash_dag_colors, hash_dag_factory.cpp:100-147).
 __global__ void k_path_expand(Table t, ColorTable ct, PathLevel lv, uint32_t n, PathLevel next, uint64_t node_base,
-                              uint64_t next_node_base, bool last_tree_level)
+                              uint64_t next_node_base, bool last_tree_level, uint32_t level, LeavesCount count)
 {
     HD_GRID_STRIDE(i, n)
     {
         const uint32_t* p = t.sys(lv.node[i]);
         const uint32_t mask = p[0] & 0xffu;
         uint32_t o = lv.first[i], k = 1;
+        uint64_t running = lv.base ? lv.base[i] : 0;
         for (uint32_t c = 0; c < 8; c++) {
             if (!(mask & (1u << c)))
                 continue;
             next.node[o] = p[k++];
+            if (lv.base) {
+                next.base[o] = running;
+                running += count(level + 1, t.sys(next.node[o])[0]);
+            }
             next.x[o] = (lv.x[i] << 1) | ((c >> 2) & 1);
             next.y[o] = (lv.y[i] << 1) | ((c >> 1) & 1);
             next.z[o] = (lv.z[i] << 1) | (c & 1);
@@ -224,23 +254,19 @@ __global__ void k_slot_write(Table t, ColorTable ct, PathLevel lv, uint32_t n, u
     }
 }
 
-// The colour tree of the context's current scene: one colour node per path
-// above C_colorTreeLevels (layout of create_hash_dag_colors,
-// hash_dag_factory.cpp:100-147, in breadth-first order), one leaf per path at
-// C_colorTreeLevels with its voxels' colours from the colour field.
-void colors_from_scene(hd_ctx* c, uint64_t color_seed)
+// The colour tree above C_colorTreeLevels of the context's current scene: one
+// colour node per path (layout of create_hash_dag_colors,
+// hash_dag_factory.cpp:100-147, in breadth-first order) whose level T - 1
+// entries name the leaves 0.. of the level-T paths, returned in lv[T] (with
+// their bases when `count` has leaves counts).
+static uint64_t color_tree(hd_ctx* c, std::vector<PathLevel>& lv, std::vector<uint32_t>& n, const LeavesCount& count)
 {
     cudaStream_t st = c->stream;
     Scratch& s = c->scratch;
-    const Geom& g = c->g;
-    const uint32_t T = g.T;
-    if (T == 0 || T >= g.leaf_level)
-        throw StatusError{HD_ERR_INVALID, "colours need 0 < C_colorTreeLevels < leaf level"};
-    if (c->root == kInvalid)
-        throw StatusError{HD_ERR_STATE, "empty scene"};
-    color_release(c);
-    std::vector<PathLevel> lv(T + 1);
-    std::vector<uint32_t> n(T + 1, 0);
+    const uint32_t T = c->g.T;
+    const bool with_base = count.bad != nullptr;
+    lv.assign(T + 1, PathLevel{});
+    n.assign(T + 1, 0);
     uint32_t* d_n = s.get<uint32_t>("col_n", 4);
     auto alloc = [&](uint32_t L, uint64_t cnt) {
         char a[32];
@@ -251,6 +277,10 @@ void colors_from_scene(hd_ctx* c, uint64_t color_seed)
             snprintf(a, sizeof(a), "col_%s_%u", names[k], L);
             *f[k] = s.get<uint32_t>(a, cnt + 1);
         }
+        if (with_base) {
+            snprintf(a, sizeof(a), "col_base_%u", L);
+            p.base = s.get<uint64_t>(a, cnt + 1);
+        }
         return p;
     };
     lv[0] = alloc(0, 1);
@@ -259,6 +289,8 @@ void colors_from_scene(hd_ctx* c, uint64_t color_seed)
     HD_CUDA(cudaMemcpyAsync(lv[0].x, &zero, 4, cudaMemcpyHostToDevice, st));
     HD_CUDA(cudaMemcpyAsync(lv[0].y, &zero, 4, cudaMemcpyHostToDevice, st));
     HD_CUDA(cudaMemcpyAsync(lv[0].z, &zero, 4, cudaMemcpyHostToDevice, st));
+    if (with_base)
+        HD_CUDA(cudaMemsetAsync(lv[0].base, 0, 8, st));
     n[0] = 1;
     std::vector<uint64_t> node_base(T + 1, 0);
     for (uint32_t L = 0; L < T; L++) {
@@ -272,10 +304,28 @@ void colors_from_scene(hd_ctx* c, uint64_t color_seed)
         const uint64_t add[5] = {8 * node_base[L + 1], L + 1 == T ? n[T] : 0, 0, 0, 0};
         color_reserve(c, add);
         k_path_expand<<<grid_for(n[L], 256), 256, 0, st>>>(c->t, c->ct, lv[L], n[L], lv[L + 1], node_base[L],
-                                                            node_base[L + 1], L + 1 == T);
+                                                            node_base[L + 1], L + 1 == T, L, count);
         HD_LAUNCH_CHECK();
     }
-    const uint64_t tree_nodes = node_base[T];
+    return node_base[T];
+}
+
+// The colour tree of the context's current scene with one leaf per path at
+// C_colorTreeLevels holding its voxels' colours from the colour field.
+void colors_from_scene(hd_ctx* c, uint64_t color_seed)
+{
+    cudaStream_t st = c->stream;
+    Scratch& s = c->scratch;
+    const Geom& g = c->g;
+    const uint32_t T = g.T;
+    if (T == 0 || T >= g.leaf_level)
+        throw StatusError{HD_ERR_INVALID, "colours need 0 < C_colorTreeLevels < leaf level"};
+    if (c->root == kInvalid)
+        throw StatusError{HD_ERR_STATE, "empty scene"};
+    color_release(c);
+    std::vector<PathLevel> lv;
+    std::vector<uint32_t> n;
+    const uint64_t tree_nodes = color_tree(c, lv, n, LeavesCount{});
     // slot leaves
     const uint32_t ns = n[T];
     uint32_t* nb = s.get<uint32_t>("col_nb", uint64_t(ns) + 1);
@@ -301,6 +351,76 @@ void colors_from_scene(hd_ctx* c, uint64_t color_seed)
         c->ctop[k] = tops[k];
     c->colors = true;
     c->color_seed = color_seed;
+}
+
+// Slot leaves as views of the main leaf: colour i of slot k is colour
+// base[k] + i of the main leaf.
+__global__ void k_slot_shared(ColorTable ct, PathLevel lv, uint32_t n, uint32_t nb, uint32_t nm, uint32_t nw)
+{
+    HD_GRID_STRIDE(i, n)
+    {
+        LeafDesc d{};
+        d.base = lv.base[i];
+        d.nb = nb;
+        d.nm = nm;
+        d.nw = nw;
+        ct.leaves[i] = d;
+    }
+}
+
+// HashDAGFactory::load_colors_from_DAG (hash_dag_factory.cpp:186-197) for a
+// BasicDAGCompressedColors main leaf (weights already byte-swapped as the
+// leaf decoder reads them) and its enclosedLeaves, on the table imported from
+// the same BasicDAG: the colour tree, and at C_colorTreeLevels a view of the
+// main leaf per path at the running leaves count.
+void colors_from_main_leaf(hd_ctx* c, uint32_t top_levels, const std::vector<uint64_t>& enclosed,
+                           const std::vector<uint32_t>& weights, const std::vector<uint64_t>& blocks,
+                           const std::vector<uint64_t>& macros)
+{
+    cudaStream_t st = c->stream;
+    Scratch& s = c->scratch;
+    const uint32_t T = c->g.T;
+    if (T == 0 || T >= c->g.leaf_level)
+        throw StatusError{HD_ERR_INVALID, "colours need 0 < C_colorTreeLevels < leaf level"};
+    if (top_levels > T)
+        throw StatusError{HD_ERR_INVALID, "C_colorTreeLevels is lower than the file's topLevels"};
+    if (c->root == kInvalid)
+        throw StatusError{HD_ERR_STATE, "empty scene"};
+    if (blocks.size() >= (1ull << 32) || macros.size() >= (1ull << 32) || weights.size() >= (1ull << 32))
+        throw StatusError{HD_ERR_INVALID, "colour leaf too large"};
+    color_release(c);
+    uint64_t* d_enc = s.get<uint64_t>("col_enclosed", enclosed.size() + 1);
+    if (!enclosed.empty())
+        HD_CUDA(cudaMemcpyAsync(d_enc, enclosed.data(), enclosed.size() * 8, cudaMemcpyHostToDevice, st));
+    uint32_t* bad = s.get<uint32_t>("col_bad", 1);
+    HD_CUDA(cudaMemsetAsync(bad, 0, 4, st));
+    std::vector<PathLevel> lv;
+    std::vector<uint32_t> n;
+    const uint64_t tree_nodes = color_tree(c, lv, n, LeavesCount{d_enc, enclosed.size(), top_levels, bad});
+    uint32_t h_bad = 0;
+    HD_CUDA(cudaMemcpyAsync(&h_bad, bad, 4, cudaMemcpyDeviceToHost, st));
+    HD_CUDA(cudaStreamSynchronize(st));
+    if (h_bad)
+        throw StatusError{HD_ERR_INVALID, "a node's enclosedLeaves index is past the file's array"};
+    const uint32_t ns = n[T];
+    const uint64_t add[5] = {8 * tree_nodes, ns, blocks.size(), macros.size(), weights.size()};
+    color_reserve(c, add);
+    if (!blocks.empty())
+        HD_CUDA(cudaMemcpyAsync(c->ct.blocks, blocks.data(), blocks.size() * 8, cudaMemcpyHostToDevice, st));
+    if (!macros.empty())
+        HD_CUDA(cudaMemcpyAsync(c->ct.macros, macros.data(), macros.size() * 8, cudaMemcpyHostToDevice, st));
+    if (!weights.empty())
+        HD_CUDA(cudaMemcpyAsync(c->ct.weights, weights.data(), weights.size() * 4, cudaMemcpyHostToDevice, st));
+    k_slot_shared<<<grid_for(ns, 256), 256, 0, st>>>(c->ct, lv[T], ns, uint32_t(blocks.size()),
+                                                     uint32_t(macros.size()), uint32_t(weights.size()));
+    HD_LAUNCH_CHECK();
+    const unsigned long long tops[5] = {8 * tree_nodes, ns, blocks.size(), macros.size(), weights.size()};
+    HD_CUDA(cudaMemcpyAsync(c->ct.top, tops, sizeof(tops), cudaMemcpyHostToDevice, st));
+    HD_CUDA(cudaStreamSynchronize(st));
+    for (int k = 0; k < 5; k++)
+        c->ctop[k] = tops[k];
+    c->colors = true;
+    c->color_seed = 0;
 }
 
 // ---- queries ----------------------------------------------------------------------

@@ -10,9 +10,10 @@
 // Layout: colour-tree nodes are 8 consecutive uint32 entries (0 = none; an
 // entry with bit 31 set is a leaf index); leaves are descriptors into three
 // append-only pools (blocks: colour bits << 32 | header; macro blocks: first
-// block, weight bit offset; weight words).  Every leaf is unique (the
-// reference's import shares one main leaf through offsets; decoded colours
-// are the same).
+// block, weight bit offset; weight words).  A descriptor with base = 0 is a
+// unique leaf; base > 0 makes it a view of a shared leaf whose colour i is the
+// shared leaf's colour base + i (CompressedColorLeaf::set_as_shared, :235-259:
+// the scenes loaded from a compressed-colours file share one main leaf).
 #pragma once
 
 #include "hd_common.cuh"
@@ -26,6 +27,7 @@ struct LeafDesc {
     uint64_t blocks;  // pool offsets
     uint64_t macros;
     uint64_t weights;
+    uint64_t base;    // colour index offset into a shared leaf (0: unique)
     uint32_t nb;      // blocks
     uint32_t nm;      // macro words (2 per macro block)
     uint32_t nw;      // weight words
@@ -147,9 +149,11 @@ HD_D uint32_t extract_bits(uint32_t bits, const uint32_t* words, uint64_t bit_pt
     return (dst >> shift) & ((1u << bits) - 1);
 }
 
-// binary_search_blocks (:414-443) + get_color_for_block (:445-480)
+// binary_search_blocks (:414-443) + get_color_for_block (:445-480); a shared
+// leaf adds its offset first (:405-410)
 HD_D uint64_t leaf_color(const ColorTable& ct, const LeafDesc& l, uint64_t ci)
 {
+    ci += l.base;
     const uint64_t* blocks = ct.blocks + l.blocks;
     const uint64_t* macros = ct.macros + l.macros;
     const uint32_t local = uint32_t(ci % kColorsPerMacro);
@@ -176,8 +180,12 @@ HD_D uint64_t leaf_color(const ColorTable& ct, const LeafDesc& l, uint64_t ci)
     }
     return pack_color(uint32_t(block >> 32), weight, bpw);
 }
-// is_valid_index (:247-254): 2 * index / CColorsPerMacroBlock < macro words
-HD_D bool leaf_valid_index(const LeafDesc& l, uint64_t ci) { return l.nb && 2 * ci / kColorsPerMacro < l.nm; }
+// is_valid_index (:255-262): 2 * (index + offset) / CColorsPerMacroBlock <
+// macro words
+HD_D bool leaf_valid_index(const LeafDesc& l, uint64_t ci)
+{
+    return l.nb && 2 * (ci + l.base) / kColorsPerMacro < l.nm;
+}
 
 // DAGUtils::get_color (dag_utils.h:423-523); 0 = CompressedColor{}.
 HD_D uint64_t get_color(const Table& t, const ColorTable& ct, uint32_t root, uint32_t x, uint32_t y, uint32_t z)

@@ -55,9 +55,35 @@ struct hd_ctx {
     // that still read the colour leaves the edit replaces)
     std::vector<cudaEvent_t> color_fences;
     size_t gen_scratch_peak = 0; // bytes of scratch the last scene generation held at most
+    // a table loaded from a hash-DAG file without bucket sizes: traversal
+    // works, edits wait for a GC to rebuild the buckets
+    bool needs_gc = false;
 };
 
 namespace hd {
+
+// Runs f, turning the errors it throws into a status and the context's
+// message.
+template <typename F>
+hd_status guarded(hd_ctx* c, F&& f)
+{
+    try {
+        f();
+        return HD_OK;
+    } catch (const StatusError& e) {
+        if (c)
+            c->err = e.msg;
+        return e.status;
+    } catch (const CudaError& e) {
+        if (c)
+            c->err = std::string("CUDA error ") + cudaGetErrorString(e.code) + " in " + e.where;
+        return e.code == cudaErrorMemoryAllocation ? HD_ERR_OOM : HD_ERR_CUDA;
+    } catch (const std::bad_alloc&) {
+        if (c)
+            c->err = "host allocation failed";
+        return HD_ERR_OOM;
+    }
+}
 
 // hd_table.cu
 void table_reset(hd_ctx* c);
@@ -72,6 +98,9 @@ void append_items(hd_ctx* c, uint32_t level, const uint32_t* content, uint64_t n
 // hd_scene.cu
 void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words, uint64_t* n_words);
 
+// hd_io.cu: keeps a copy of the BasicDAG words (host or device pointer)
+void keep_basic(hd_ctx* c, const uint32_t* words, uint64_t n);
+
 // hd_edit.cu / hd_edit_batch.cu
 void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats);
 void edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* per_edit, hd_edit_stats* total);
@@ -82,6 +111,10 @@ struct Editor;
 struct Level;
 void color_release(hd_ctx* c);
 void colors_from_scene(hd_ctx* c, uint64_t color_seed);
+void colors_from_main_leaf(hd_ctx* c, uint32_t top_levels, const std::vector<uint64_t>& enclosed,
+                           const std::vector<uint32_t>& weights, const std::vector<uint64_t>& blocks,
+                           const std::vector<uint64_t>& macros);
+void color_reserve(hd_ctx* c, const uint64_t add[5]);
 void get_colors(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, hd_color* d_out);
 void trace_colors(hd_ctx* c, const uint32_t* d_paths, uint32_t w, uint32_t h, uint32_t* d_rgba,
                   cudaStream_t stream = nullptr, const uint32_t* d_root = nullptr);

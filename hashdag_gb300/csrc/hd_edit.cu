@@ -136,6 +136,8 @@ static Level alloc_level(Scratch& s, uint32_t L, uint64_t n, bool leaf, bool col
 
 void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats)
 {
+    if (c->needs_gc)
+        throw StatusError{HD_ERR_STATE, "the table was loaded without bucket sizes; run hd_gc before editing"};
     cudaStream_t st = c->stream;
     Scratch& s = c->scratch;
     const Geom& g = c->g;

@@ -599,6 +599,8 @@ static void capture(hd_ctx* c, BatchGraph& bg, const BatchBuffers& b, uint32_t n
 // the batch started (host_ms, device clock).
 void edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* per_edit, hd_edit_stats* total)
 {
+    if (c->needs_gc)
+        throw StatusError{HD_ERR_STATE, "the table was loaded without bucket sizes; run hd_gc before editing"};
     const auto t0 = std::chrono::steady_clock::now();
     cudaStream_t st = c->stream;
     hd_edit_stats sum{};

@@ -203,6 +203,7 @@ extern "C" hd_status hd_gc_ex(hd_ctx* c, uint32_t* extra, uint32_t n, uint32_t f
             c->redo.clear();
         }
         hd::gc(c, roots);
+        c->needs_gc = false; // the buckets are rebuilt
         // the remapped extra roots go back to the caller
         for (uint32_t i = 0; i < n; i++)
             extra[i] = roots[1 + i];

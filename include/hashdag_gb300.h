@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define HD_ABI_VERSION 5u
+#define HD_ABI_VERSION 6u
 #define HD_PAGE_SIZE 512u
 #define HD_MAX_DEPTH 20u
 /* Sentinel of the edit recursion (hash_dag_edits.h:17). */
@@ -43,7 +43,8 @@ typedef enum hd_status {
     HD_ERR_BUCKET_FULL = 4, /* a bucket ran past its virtual range      */
     HD_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up       */
     HD_ERR_OOM = 6,         /* device allocation failed                 */
-    HD_ERR_STATE = 7        /* call not valid in the context's state    */
+    HD_ERR_STATE = 7,       /* call not valid in the context's state    */
+    HD_ERR_IO = 8           /* a file could not be read or written      */
 } hd_status;
 
 /* Table geometry.  The defaults are the reference's compile-time macros
@@ -353,6 +354,44 @@ hd_status hd_gc(hd_ctx* ctx, uint32_t* h_extra_roots, uint32_t n_extra);
  * (engine.cpp:178-185). */
 #define HD_GC_KEEP_HISTORY 1u
 hd_status hd_gc_ex(hd_ctx* ctx, uint32_t* h_extra_roots, uint32_t n_extra, uint32_t flags);
+
+/* ---- files (serializer.h:11-121) ---------------------------------------- */
+
+/* DAGInfo (dag_info.h:6-10): the scene's bounding box, carried by the files. */
+typedef struct hd_dag_info {
+    double aabb_min[3];
+    double aabb_max[3];
+} hd_dag_info;
+
+/* BasicDAGFactory::load_dag_from_file (basic_dag.cpp:105-117) followed by
+ * load_from_DAG (as hd_load_basic_dag).  The file's level count must equal
+ * the context's depth.  info may be NULL. */
+hd_status hd_load_basic_dag_file(hd_ctx* ctx, const char* path, hd_dag_info* info);
+/* BasicDAGFactory::save_dag_to_file (basic_dag.cpp:94-103) of the BasicDAG
+ * the context last imported or generated (HD_ERR_STATE when there is none).
+ * info may be NULL (zeros are written). */
+hd_status hd_save_basic_dag_file(hd_ctx* ctx, const char* path, const hd_dag_info* info);
+/* BasicDAGFactory::load_compressed_colors_from_file (basic_dag.cpp:49-92)
+ * followed by HashDAGFactory::load_colors_from_DAG (hash_dag_factory.cpp:
+ * 186-197) on the scene the context holds (loaded from the matching BasicDAG
+ * file): one main colour leaf shared by every level-C_colorTreeLevels slot at
+ * its running leaves count.  HD_COLORS_ENCLOSED_32 reads an old file whose
+ * enclosedLeaves are uint32 (the reference then zeroes them). */
+#define HD_COLORS_ENCLOSED_32 1u
+hd_status hd_load_colors_file(hd_ctx* ctx, const char* path, uint32_t flags);
+/* Snapshot: HashDAGFactory::save_dag_to_file's format (hash_dag_factory.cpp:
+ * 199-222: DAGInfo, levels, firstNodeIndex, poolMaxSize, pageTableSize,
+ * poolTop, the pool's first poolTop pages, the page table), which the
+ * reference's load_dag_from_file reads as is, followed by what that format
+ * leaves out: the table geometry, bucket sizes, full-node indices, per-level
+ * node counts and the colour table.  Undo history is not saved. */
+hd_status hd_save_snapshot(hd_ctx* ctx, const char* path, const hd_dag_info* info);
+/* Loads a snapshot, or a hash-DAG file the reference wrote
+ * (load_dag_from_file, :224-246).  The page table size must match the
+ * context's geometry.  A reference file carries no bucket sizes: the table
+ * can be traced, and edits return HD_ERR_STATE until hd_gc has rebuilt the
+ * buckets. */
+hd_status hd_load_snapshot(hd_ctx* ctx, const char* path, hd_dag_info* info);
 
 /* ---- state and statistics ---------------------------------------------- */
 

@@ -2388,6 +2388,125 @@ int or_colors_from_scene(or_colors* col, const or_table* t, uint64_t color_seed)
     return HD_OK;
 }
 
+/* ---- the compressed colours that ship beside a BasicDAG ------------------ */
+
+typedef struct {
+    const uint32_t* words;
+    uint32_t leaf_level, top_levels;
+    uint64_t* enclosed;
+    uint64_t n_enclosed;
+    uint64_t seed;
+    or_builder* b;
+} main_leaf_ctx;
+
+/* DAGUtils::fix_enclosed_leaves_impl (dag_utils.h:525-616): the leaves under
+ * a BasicDAG node; nodes above top_levels store theirs in enclosed[upper
+ * header bits].  The scenes built here carry their counts at and below
+ * top_levels, so the header patch of the reference's count-0 branch never
+ * happens (returns 0 if it would). */
+static uint64_t enclosed_count(main_leaf_ctx* m, uint32_t level, uint32_t index)
+{
+    const uint32_t* w = m->words;
+    if (level == m->leaf_level)
+        return (uint64_t)popc64((uint64_t)w[index] | ((uint64_t)w[index + 1] << 32));
+    const uint32_t node = w[index], upper = node >> 8, mask = node & 0xffu;
+    if (level >= m->top_levels)
+        return upper;
+    if (upper >= m->n_enclosed)
+        return 0;
+    if (m->enclosed[upper])
+        return m->enclosed[upper];
+    uint64_t count = 0;
+    uint32_t off = 1;
+    for (uint32_t c = 0; c < 8; c++)
+        if (mask & (1u << c))
+            count += enclosed_count(m, level + 1, w[index + off++]);
+    m->enclosed[upper] = count;
+    return count;
+}
+/* largest upper-bits index of the nodes above top_levels */
+static uint32_t max_enclosed_index(const main_leaf_ctx* m, uint32_t level, uint32_t index)
+{
+    if (level >= m->top_levels)
+        return 0;
+    const uint32_t node = m->words[index], mask = node & 0xffu;
+    uint32_t mx = node >> 8, off = 1;
+    for (uint32_t c = 0; c < 8; c++)
+        if (mask & (1u << c)) {
+            const uint32_t k = max_enclosed_index(m, level + 1, m->words[index + off++]);
+            mx = k > mx ? k : mx;
+        }
+    return mx;
+}
+/* every voxel's colour in depth-first order (children in order, leaf bits in
+ * index order) */
+static void main_leaf_voxels(main_leaf_ctx* m, uint32_t level, uint32_t index, const uint32_t path[3])
+{
+    const uint32_t* w = m->words;
+    if (level == m->leaf_level) {
+        const uint64_t leaf = (uint64_t)w[index] | ((uint64_t)w[index + 1] << 32);
+        for (uint32_t bit = 0; bit < 64; bit++) {
+            if (!((leaf >> bit) & 1))
+                continue;
+            const uint32_t c1 = bit >> 3, c2 = bit & 7;
+            const uint32_t x = (path[0] << 2) | (((c1 >> 2) & 1) << 1) | ((c2 >> 2) & 1);
+            const uint32_t y = (path[1] << 2) | (((c1 >> 1) & 1) << 1) | ((c2 >> 1) & 1);
+            const uint32_t z = (path[2] << 2) | ((c1 & 1) << 1) | (c2 & 1);
+            builder_add(m->b, or_voxel_color(m->seed, x, y, z));
+        }
+        return;
+    }
+    const uint32_t mask = w[index] & 0xffu;
+    uint32_t off = 1;
+    for (uint32_t c = 0; c < 8; c++) {
+        if (!(mask & (1u << c)))
+            continue;
+        uint32_t np[3];
+        descend(path, c, np);
+        main_leaf_voxels(m, level + 1, w[index + off++], np);
+    }
+}
+
+/* BasicDAGCompressedColors of a BasicDAG (root at word 0) and the colour
+ * field of `seed`: enclosedLeaves (fix_enclosed_leaves over the nodes above
+ * top_levels, sized by their largest index + 1) and the main leaf (one
+ * ColorLeafBuilder fed every voxel; weights in the leaf's in-memory order).
+ * Every output array is malloc'd; or_free releases it. */
+int or_main_leaf(const uint32_t* words, uint64_t n_words, uint32_t depth, uint32_t top_levels, uint64_t seed,
+                 uint64_t** enclosed, uint64_t* n_enclosed, uint64_t** blocks, uint64_t* nb, uint64_t** macros,
+                 uint64_t* nm, uint32_t** weights, uint64_t* nw)
+{
+    if (!words || n_words < 2 || depth < 4 || top_levels >= depth - 2)
+        return HD_ERR_INVALID;
+    main_leaf_ctx m;
+    memset(&m, 0, sizeof(m));
+    m.words = words;
+    m.leaf_level = depth - 2;
+    m.top_levels = top_levels;
+    m.seed = seed;
+    m.n_enclosed = top_levels ? (uint64_t)max_enclosed_index(&m, 0, 0) + 1 : 0;
+    m.enclosed = (uint64_t*)calloc(m.n_enclosed + 1, 8);
+    if (top_levels)
+        enclosed_count(&m, 0, 0);
+    or_builder b;
+    memset(&b, 0, sizeof(b));
+    m.b = &b;
+    const uint32_t path[3] = {0, 0, 0};
+    main_leaf_voxels(&m, 0, 0, path);
+    or_leaf leaf;
+    builder_build(&b, &leaf);
+    builder_free(&b);
+    *enclosed = m.enclosed;
+    *n_enclosed = m.n_enclosed;
+    *blocks = leaf.blocks;
+    *nb = leaf.nb;
+    *macros = leaf.macros;
+    *nm = leaf.nm;
+    *weights = leaf.weights;
+    *nw = leaf.nw;
+    return HD_OK;
+}
+
 /* DAGUtils::get_color (dag_utils.h:423-523) */
 hd_color or_get_color(const or_table* t, const or_colors* col, uint32_t x, uint32_t y, uint32_t z)
 {

@@ -103,6 +103,11 @@ int or_edit_colored(or_table* t, or_colors* c, const hd_edit* e, hd_edit_stats* 
 int or_undo(or_table* t, or_colors* c); /* 1 if a frame was applied */
 int or_redo(or_table* t, or_colors* c);
 void or_colors_stats(const or_colors* c, uint64_t* out);
+/* The BasicDAGCompressedColors shipped beside a BasicDAG (enclosedLeaves and
+ * one main leaf for the colour field of `seed`); arrays malloc'd, or_free. */
+int or_main_leaf(const uint32_t* words, uint64_t n_words, uint32_t depth, uint32_t top_levels, uint64_t seed,
+                 uint64_t** enclosed, uint64_t* n_enclosed, uint64_t** blocks, uint64_t* nb, uint64_t** macros,
+                 uint64_t* nm, uint32_t** weights, uint64_t* nw);
 uint32_t or_color_rgb8(uint64_t seed, uint32_t x, uint32_t y, uint32_t z);
 hd_color or_voxel_color(uint64_t seed, uint32_t x, uint32_t y, uint32_t z);
 uint32_t or_color_rgb888(hd_color k);

@@ -137,6 +137,9 @@ def lib():
         L.or_voxel_color.argtypes = [u64, u32, u32, u32]
         L.or_color_rgb888.restype = u32
         L.or_color_rgb888.argtypes = [HdColor]
+        PP = C.POINTER(C.c_void_p)
+        L.or_main_leaf.argtypes = [pu32, u64, u32, u32, u64, PP, C.POINTER(u64), PP, C.POINTER(u64), PP,
+                                   C.POINTER(u64), PP, C.POINTER(u64)]
         _lib = L
     return _lib
 
@@ -355,3 +358,68 @@ def voxel_color(seed, x, y, z):
 
 def color_rgb888(color_bits, weight=0, bits_per_weight=0):
     return lib().or_color_rgb888(HdColor(color_bits, weight, bits_per_weight, 0))
+
+
+# ---- on-disk formats (FileWriter, serializer.h:11-121) ------------------------
+# Raw little-endian values; an array is its uint64 element count, then its
+# elements; a DAGInfo is six doubles (AABB min, then max).
+
+def _array(a, dtype):
+    a = np.ascontiguousarray(a, dtype)
+    return np.uint64(a.size).tobytes() + a.tobytes()
+
+
+def _info(info):
+    lo, hi = info
+    return np.array(list(lo) + list(hi), np.float64).tobytes()
+
+
+def basic_dag_file(words, depth, info):
+    """BasicDAGFactory::save_dag_to_file (basic_dag.cpp:94-103): DAGInfo,
+    uint32 levels, the node words."""
+    return _info(info) + np.uint32(depth).tobytes() + _array(words, np.uint32)
+
+
+def main_leaf(words, depth, top_levels, seed):
+    """enclosedLeaves and the main leaf (blocks, macro words, weights in the
+    leaf's in-memory order) of the colour field of `seed` on a BasicDAG."""
+    words = np.ascontiguousarray(words, np.uint32)
+    ptr = [C.c_void_p() for _ in range(4)]
+    cnt = [C.c_uint64() for _ in range(4)]
+    r = lib().or_main_leaf(words, words.size, depth, top_levels, seed, C.byref(ptr[0]), C.byref(cnt[0]),
+                           C.byref(ptr[1]), C.byref(cnt[1]), C.byref(ptr[2]), C.byref(cnt[2]),
+                           C.byref(ptr[3]), C.byref(cnt[3]))
+    if r:
+        raise RuntimeError(f"main leaf failed: {r}")
+    out = []
+    for (p_, n_), dt in zip(zip(ptr, cnt), (np.uint64, np.uint64, np.uint64, np.uint32)):
+        arr = np.ctypeslib.as_array(C.cast(p_, C.POINTER(C.c_uint64 if dt == np.uint64 else C.c_uint32)),
+                                    shape=(max(1, n_.value),))[:n_.value].copy()
+        lib().or_free(p_)
+        out.append(arr.astype(dt))
+    enclosed, blocks, macros, weights = out
+    return dict(enclosed=enclosed, blocks=blocks, macros=macros, weights=weights)
+
+
+def swap_bytes(words):
+    """ColorUtils::swap_byte_order (color_utils.h:85-105) of uint32 words."""
+    return np.ascontiguousarray(words, np.uint32).byteswap()
+
+
+def compressed_colors_file(words, depth, top_levels, seed):
+    """BasicDAGFactory::save_compressed_colors_to_file (basic_dag.cpp:34-47):
+    uint32 topLevels, enclosedLeaves (uint64), the weights swapped back to
+    file order, blocks, macro blocks."""
+    m = main_leaf(words, depth, top_levels, seed)
+    return (np.uint32(top_levels).tobytes() + _array(m["enclosed"], np.uint64) +
+            _array(swap_bytes(m["weights"]), np.uint32) + _array(m["blocks"], np.uint64) +
+            _array(m["macros"], np.uint64))
+
+
+def hash_dag_file(table, info, pool_max):
+    """HashDAGFactory::save_dag_to_file (hash_dag_factory.cpp:199-222):
+    DAGInfo, uint32 levels, firstNodeIndex, poolMaxSize, pageTableSize,
+    poolTop, the pool's first poolTop pages, the page table."""
+    t = table.export()
+    head = np.array([table.cfg.depth, t["root"], pool_max, t["page_table"].size, table.pool_top], np.uint32)
+    return _info(info) + head.tobytes() + t["pool"].tobytes() + t["page_table"].tobytes()

@@ -67,6 +67,10 @@
 #include "hash_table.cpp"
 #include "stats.cpp"
 #include "hash_dag_factory.cpp"
+#if EDITS_ENABLE_COLORS
+// the BasicDAG / compressed-colour file writers and readers
+#include "dags/basic_dag/basic_dag.cpp"
+#endif
 
 #include <algorithm>
 #include <cstdlib>
@@ -283,11 +287,15 @@ static void add_voxel_colors(const BasicDAG& dag, uint32 level, uint32 index, ui
 
 // HashDAGFactory::load_from_DAG + load_colors_from_DAG (hash_dag_factory.cpp:
 // 150-197) on a BasicDAG and the colour field of `colorSeed`.
+// The BasicDAG and its compressed colours of the last ref_load_colored.
+static BasicDAG g_basic;
+static BasicDAGCompressedColors g_basic_colors;
+
 extern "C" int ref_load_colored(const uint32* words, uint64 nWords, uint32 poolPages, uint64 colorSeed)
 {
     if (g_loaded)
         return 1;
-    BasicDAG basic;
+    BasicDAG& basic = g_basic;
     basic.data = StaticArray<uint32>::allocate("basic dag", nWords, EMemoryType::CPU);
     std::memcpy(basic.data.data(), words, nWords * sizeof(uint32));
     HashDAGFactory::load_from_DAG(g_dag, basic, poolPages);
@@ -309,7 +317,7 @@ extern "C" int ref_load_colored(const uint32* words, uint64 nWords, uint32 poolP
                     stack.push_back({level + 1, basic.get_child_index(level, index, mask, c)});
         }
     }
-    BasicDAGCompressedColors colors;
+    BasicDAGCompressedColors& colors = g_basic_colors;
     colors.topLevels = C_colorTreeLevels;
     colors.enclosedLeaves = StaticArray<EnclosedLeavesType>::allocate("enclosed leaves", maxIndex + 1, EMemoryType::CPU);
     std::memset(colors.enclosedLeaves.data(), 0, (maxIndex + 1) * sizeof(EnclosedLeavesType));
@@ -374,6 +382,44 @@ extern "C" int ref_edit_colored(uint32 tool, const float* center, float radius, 
     }
     default: return 1;
     }
+    return 0;
+}
+
+// The reference's own file writers on the state of ref_load_colored (and the
+// edits since, for the hash-DAG file): BasicDAGFactory::save_dag_to_file,
+// save_compressed_colors_to_file (basic_dag.cpp:34-103) and
+// HashDAGFactory::save_dag_to_file (hash_dag_factory.cpp:199-222).  The
+// DAGInfo is the scene's cube [0, 2^depth].
+extern "C" int ref_save_files(const char* dagPath, const char* colorsPath, const char* hashPath)
+{
+    if (!g_loaded)
+        return 1;
+    DAGInfo info;
+    info.boundsAABBMin = Vector3(0, 0, 0);
+    info.boundsAABBMax = Vector3(double(1u << MAX_LEVELS), double(1u << MAX_LEVELS), double(1u << MAX_LEVELS));
+    if (dagPath)
+        BasicDAGFactory::save_dag_to_file(info, g_basic, dagPath);
+    if (colorsPath)
+        BasicDAGFactory::save_compressed_colors_to_file(g_basic_colors, colorsPath);
+    if (hashPath)
+        HashDAGFactory::save_dag_to_file(info, g_dag, hashPath);
+    return 0;
+}
+
+// The reference's loaders: BasicDAGFactory::load_dag_from_file and
+// load_compressed_colors_from_file, then load_from_DAG and
+// load_colors_from_DAG (a fresh process: the table is a singleton).
+extern "C" int ref_load_files(const char* dagPath, const char* colorsPath, uint32 poolPages)
+{
+    if (g_loaded)
+        return 1;
+    DAGInfo info;
+    BasicDAGFactory::load_dag_from_file(info, g_basic, dagPath);
+    BasicDAGFactory::load_compressed_colors_from_file(g_basic_colors, colorsPath);
+    HashDAGFactory::load_from_DAG(g_dag, g_basic, poolPages);
+    HashDAGFactory::load_colors_from_DAG(g_colors, g_basic, g_basic_colors);
+    g_recorder = new StatsRecorder();
+    g_loaded = true;
     return 0;
 }
 
