@@ -122,6 +122,83 @@ def editor_from_tuple(t):
     return BoxEditor(center, radius, tool == TOOL_BOX_ADD)
 
 
+REPLAY_TYPES = ("SetLocation", "SetRotation", "SetToolParameters", "EditSphere", "EditCube", "EditCopy",
+                "EditFill", "EditPaint", "Undo", "Redo", "EndFrame")
+
+
+class ReplayManager:
+    """ReplayManager (replay.h:462-635) over hd_replay: load_csv, write_csv,
+    replay_frame on a HashDAG (edits, undo / redo, the view), the frame's
+    camera back."""
+
+    def __init__(self, path=None, text=None):
+        self._h = C.c_void_p()
+        if path is not None:
+            st = lib().hd_replay_load(os.fsencode(path), C.byref(self._h))
+        else:
+            data = text.encode() if isinstance(text, str) else bytes(text)
+            st = lib().hd_replay_load_text(data, len(data), C.byref(self._h))
+        if st != _capi.HD_OK:
+            raise HashDagError(st, f"cannot load the replay {path if path is not None else '(text)'}")
+
+    def free(self):
+        if self._h:
+            lib().hd_replay_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def _info(self):
+        a, f, n = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        lib().hd_replay_info(self._h, C.byref(a), C.byref(f), C.byref(n))
+        return a.value, f.value, n.value
+
+    def num_frames(self):
+        return self._info()[1]
+
+    def __len__(self):
+        return self._info()[0]
+
+    def at_end(self):
+        a, _, n = self._info()
+        return n == a
+
+    def action(self, i):
+        """(type name, float cells, integer cells, boolean cell)."""
+        a = _capi.ReplayAction()
+        st = lib().hd_replay_get_action(self._h, i, C.byref(a))
+        if st != _capi.HD_OK:
+            raise HashDagError(st, f"no action {i}")
+        return (REPLAY_TYPES[a.type], [float(v) for v in a.floats[:a.n_floats]], [int(v) for v in a.ints[:a.n_ints]],
+                bool(a.flag))
+
+    def write_csv(self, path):
+        st = lib().hd_replay_write(self._h, os.fsencode(path))
+        if st != _capi.HD_OK:
+            raise HashDagError(st, f"cannot write {path}")
+
+    def reset_replay(self):
+        lib().hd_replay_reset(self._h)
+
+    def replay_frame(self, dag, replay_depth, width, height, info):
+        """Applies the next frame's actions to dag; returns (camera params
+        dict, edits applied)."""
+        cfg = _capi.ReplayConfig()
+        cfg.replay_depth, cfg.width, cfg.height = replay_depth, width, height
+        lo, hi = info
+        cfg.info.aabb_min[:] = [float(v) for v in lo]
+        cfg.info.aabb_max[:] = [float(v) for v in hi]
+        cam = Camera()
+        n = C.c_uint32()
+        _capi.check(dag.handle, lib().hd_replay_frame(dag.handle, self._h, C.byref(cfg), C.byref(cam), C.byref(n)))
+        return dict(position=list(cam.position), ray_min=list(cam.ray_min), ray_ddx=list(cam.ray_ddx),
+                    ray_ddy=list(cam.ray_ddy)), n.value
+
+
 class HashDAG:
     """A device-resident hash DAG (one hd_ctx)."""
 

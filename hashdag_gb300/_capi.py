@@ -28,6 +28,16 @@ class DagInfo(C.Structure):
     _fields_ = [("aabb_min", C.c_double * 3), ("aabb_max", C.c_double * 3)]
 
 
+class ReplayAction(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("flag", C.c_uint32), ("n_floats", C.c_uint32), ("n_ints", C.c_uint32),
+                ("floats", C.c_float * 20), ("ints", C.c_uint32 * 10)]
+
+
+class ReplayConfig(C.Structure):
+    _fields_ = [("replay_depth", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("reserved", C.c_uint32), ("info", DagInfo)]
+
+
 class Camera(C.Structure):
     _fields_ = [("position", C.c_double * 3), ("ray_min", C.c_double * 3), ("ray_ddx", C.c_double * 3),
                 ("ray_ddy", C.c_double * 3)]
@@ -131,6 +141,14 @@ SIGNATURES = [
     ("hd_save_basic_dag_file", C.c_int, [_P, C.c_char_p, C.POINTER(DagInfo)]),
     ("hd_load_colors_file", C.c_int, [_P, C.c_char_p, _u32]),
     ("hd_save_snapshot", C.c_int, [_P, C.c_char_p, C.POINTER(DagInfo)]),
+    ("hd_replay_load", C.c_int, [C.c_char_p, C.POINTER(_P)]),
+    ("hd_replay_load_text", C.c_int, [C.c_char_p, _u64, C.POINTER(_P)]),
+    ("hd_replay_free", C.c_int, [_P]),
+    ("hd_replay_info", C.c_int, [_P, C.POINTER(_u64), C.POINTER(_u64), C.POINTER(_u64)]),
+    ("hd_replay_get_action", C.c_int, [_P, _u64, C.POINTER(ReplayAction)]),
+    ("hd_replay_write", C.c_int, [_P, C.c_char_p]),
+    ("hd_replay_reset", C.c_int, [_P]),
+    ("hd_replay_frame", C.c_int, [_P, _P, C.POINTER(ReplayConfig), C.POINTER(Camera), C.POINTER(_u32)]),
     ("hd_load_snapshot", C.c_int, [_P, C.c_char_p, C.POINTER(DagInfo)]),
     ("hd_trace_primary", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _P, C.POINTER(_f32)]),
     ("hd_trace_shadow", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _P, C.POINTER(_f32), _f32, _P,

@@ -85,7 +85,10 @@ typedef enum hd_tool {
     HD_TOOL_BOX_REMOVE = 2,
     HD_TOOL_BOX_ADD = 3,
     HD_TOOL_SPHERE_PAINT = 4,
-    HD_TOOL_COPY = 5
+    HD_TOOL_COPY = 5,
+    HD_TOOL_NOISE_REMOVE = 6, /* SphereNoiseEditor(isAdding = false), :712-760 */
+    HD_TOOL_NOISE_ADD = 7,    /* SphereNoiseEditor(isAdding = true)           */
+    HD_TOOL_FILL = 8          /* FillEditorColors (flood fill), :624-710      */
 } hd_tool;
 
 typedef struct hd_edit {
@@ -392,6 +395,66 @@ hd_status hd_save_snapshot(hd_ctx* ctx, const char* path, const hd_dag_info* inf
  * can be traced, and edits return HD_ERR_STATE until hd_gc has rebuilt the
  * buckets. */
 hd_status hd_load_snapshot(hd_ctx* ctx, const char* path, hd_dag_info* info);
+
+/* ---- replays (ReplayManager, replay.h:462-635; replay.cpp:5-100) ------- */
+
+/* EReplayActionType (replay.h:12-25) */
+typedef enum hd_replay_type {
+    HD_REPLAY_SET_LOCATION = 0,
+    HD_REPLAY_SET_ROTATION = 1,
+    HD_REPLAY_SET_TOOL_PARAMETERS = 2,
+    HD_REPLAY_EDIT_SPHERE = 3,
+    HD_REPLAY_EDIT_CUBE = 4,
+    HD_REPLAY_EDIT_COPY = 5,
+    HD_REPLAY_EDIT_FILL = 6,
+    HD_REPLAY_EDIT_PAINT = 7,
+    HD_REPLAY_UNDO = 8,
+    HD_REPLAY_REDO = 9,
+    HD_REPLAY_END_FRAME = 10
+} hd_replay_type;
+
+typedef struct hd_replay hd_replay;
+
+/* One parsed action: its float cells and (uint32)stoi integer cells in line
+ * order, and the boolean cell (add, or the copy's swirl flag). */
+typedef struct hd_replay_action {
+    uint32_t type;
+    uint32_t flag;
+    uint32_t n_floats;
+    uint32_t n_ints;
+    float floats[20];
+    uint32_t ints[10];
+} hd_replay_action;
+
+/* replay_depth: REPLAY_DEPTH, the depth the replay was recorded on (positions
+ * and radii scale by 2^depth / 2^replay_depth); width, height: the image of
+ * the frame cameras; info: the scene's DAGInfo (world to voxel space). */
+typedef struct hd_replay_config {
+    uint32_t replay_depth;
+    uint32_t width;
+    uint32_t height;
+    uint32_t reserved;
+    hd_dag_info info;
+} hd_replay_config;
+
+/* ReplayManager::load_csv (replay.h:526-567): HD_ERR_INVALID names the first
+ * line that does not parse. */
+hd_status hd_replay_load(const char* path, hd_replay** out);
+hd_status hd_replay_load_text(const char* text, uint64_t n_bytes, hd_replay** out);
+hd_status hd_replay_free(hd_replay* replay);
+hd_status hd_replay_info(const hd_replay* replay, uint64_t* n_actions, uint64_t* n_frames, uint64_t* next_action);
+hd_status hd_replay_get_action(const hd_replay* replay, uint64_t index, hd_replay_action* out);
+/* ReplayManager::write_csv (replay.h:504-520) */
+hd_status hd_replay_write(const hd_replay* replay, const char* path);
+/* ReplayManager::reset_replay */
+hd_status hd_replay_reset(hd_replay* replay);
+/* ReplayManager::replay_frame (replay.h:479-495): applies the actions up to
+ * and including the next EndFrame to the context (edits, undo / redo, the
+ * view) and returns the frame's camera (get_trace_params of the view,
+ * dag_tracer.cu:71-113) and the number of edits applied.  HD_ERR_STATE when
+ * the replay is at its end. */
+hd_status hd_replay_frame(hd_ctx* ctx, hd_replay* replay, const hd_replay_config* config, hd_camera* camera,
+                          uint32_t* edits);
 
 /* ---- state and statistics ---------------------------------------------- */
 

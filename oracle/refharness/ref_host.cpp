@@ -68,8 +68,9 @@
 #include "stats.cpp"
 #include "hash_dag_factory.cpp"
 #if EDITS_ENABLE_COLORS
-// the BasicDAG / compressed-colour file writers and readers
+// the BasicDAG / compressed-colour file writers and readers, replays
 #include "dags/basic_dag/basic_dag.cpp"
+#include "replay.h"
 #endif
 
 #include <algorithm>
@@ -421,6 +422,98 @@ extern "C" int ref_load_files(const char* dagPath, const char* colorsPath, uint3
     g_recorder = new StatsRecorder();
     g_loaded = true;
     return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Replays: the reference's ReplayManager (replay.h, header only) reading and
+// writing CSV.  The actions' apply() bodies live in replay.cpp with the
+// engine; parsing and writing never call them, so they are empty here.
+// ---------------------------------------------------------------------------
+void ReplayActionUndo::apply() {}
+void ReplayActionRedo::apply() {}
+void ReplayActionSetLocation::apply() {}
+void ReplayActionSetRotation::apply() {}
+void ReplayActionSetToolParameters::apply() {}
+void ReplayActionSphere::apply() {}
+void ReplayActionCube::apply() {}
+void ReplayActionCopy::apply() {}
+void ReplayActionFill::apply() {}
+void ReplayActionPaint::apply() {}
+static ReplayManager g_replay;
+
+extern "C" int ref_replay_load(const char* path)
+{
+    g_replay.load_csv(path);
+    return 0;
+}
+extern "C" int ref_replay_write(const char* path)
+{
+    std::ofstream os(path, std::ios::binary);
+    g_replay.write_csv(os);
+    return os.good() ? 0 : 1;
+}
+extern "C" uint64 ref_replay_count() { return g_replay.actions.size(); }
+extern "C" uint64 ref_replay_frames() { return g_replay.numFrames; }
+// Action i as its type and its fields as doubles in declaration order
+// (booleans as 0 / 1, uint3 and uint32 fields as their values).
+extern "C" uint32 ref_replay_action(uint64 i, double* v, uint32* n)
+{
+    IReplayAction* a = g_replay.actions[i].get();
+    uint32 k = 0;
+    auto put = [&](double x) { v[k++] = x; };
+    switch (a->type) {
+    case EReplayActionType::SetLocation: {
+        auto& b = static_cast<ReplayActionSetLocation&>(*a);
+        put(b.location.X), put(b.location.Y), put(b.location.Z);
+        break;
+    }
+    case EReplayActionType::SetRotation: {
+        auto& b = static_cast<ReplayActionSetRotation&>(*a);
+        const Matrix3x3& m = b.rotation;
+        put(m.D00), put(m.D01), put(m.D02), put(m.D10), put(m.D11), put(m.D12), put(m.D20), put(m.D21), put(m.D22);
+        break;
+    }
+    case EReplayActionType::SetToolParameters: {
+        auto& b = static_cast<ReplayActionSetToolParameters&>(*a);
+        put(b.path.x), put(b.path.y), put(b.path.z), put(b.copySourcePath.x), put(b.copySourcePath.y),
+            put(b.copySourcePath.z), put(b.copyDestPath.x), put(b.copyDestPath.y), put(b.copyDestPath.z),
+            put(b.radius), put(b.tool);
+        break;
+    }
+    case EReplayActionType::EditSphere: {
+        auto& b = static_cast<ReplayActionSphere&>(*a);
+        put(b.location.x), put(b.location.y), put(b.location.z), put(b.radius), put(b.add);
+        break;
+    }
+    case EReplayActionType::EditCube: {
+        auto& b = static_cast<ReplayActionCube&>(*a);
+        put(b.location.x), put(b.location.y), put(b.location.z), put(b.radius), put(b.add);
+        break;
+    }
+    case EReplayActionType::EditCopy: {
+        auto& b = static_cast<ReplayActionCopy&>(*a);
+        put(b.location.x), put(b.location.y), put(b.location.z), put(b.src.x), put(b.src.y), put(b.src.z),
+            put(b.dest.x), put(b.dest.y), put(b.dest.z), put(b.radius);
+        const Matrix3x3& m = b.transform;
+        put(m.D00), put(m.D01), put(m.D02), put(m.D10), put(m.D11), put(m.D12), put(m.D20), put(m.D21), put(m.D22);
+        put(b.enableSwirl), put(b.swirlPeriod);
+        break;
+    }
+    case EReplayActionType::EditFill: {
+        auto& b = static_cast<ReplayActionFill&>(*a);
+        put(b.location.x), put(b.location.y), put(b.location.z), put(b.radius);
+        break;
+    }
+    case EReplayActionType::EditPaint: {
+        auto& b = static_cast<ReplayActionPaint&>(*a);
+        put(b.location.x), put(b.location.y), put(b.location.z), put(b.radius);
+        break;
+    }
+    default:
+        break;
+    }
+    *n = k;
+    return uint32(a->type);
 }
 
 // DAGUtils::get_color (dag_utils.h:423-523): colour bits, weight, bits per weight
