@@ -1862,7 +1862,18 @@ typedef struct {
     uint32_t size;
     uint8_t* values;
     hd_color* colors;
+    /* BufferEditor (:129-221) tools (noise, fill): the buffer's lower corner
+     * (BoxEditorBase::min), its radius (BoxEditorBase::radius: 1.5 r for the
+     * noise tool), the EValues of the size^3 buffer (x fastest), the table
+     * it reads (get_value at get_world_path) and, for the fill, the colour of
+     * each set voxel */
+    f3 buf_min;
+    float buf_r;
+    uint8_t* state;
+    const or_table* dag;
 } editor;
+
+static int make_buffers(editor* e, const or_table* t, const or_colors* col);
 
 static editor make_editor(const hd_edit* e)
 {
@@ -1881,8 +1892,16 @@ static editor make_editor(const hd_edit* e)
         ed.copy_min = (f3){ed.c.x - ed.r, ed.c.y - ed.r, ed.c.z - ed.r};
         ed.size = 2 * (uint32_t)ceilf(ed.r);
     }
-    ed.bmin = (f3){bc.x - e->radius, bc.y - e->radius, bc.z - e->radius};
-    ed.bmax = (f3){bc.x + e->radius, bc.y + e->radius, bc.z + e->radius};
+    float br = e->radius;
+    if (e->tool == HD_TOOL_NOISE_ADD || e->tool == HD_TOOL_NOISE_REMOVE)
+        br = 1.5f * e->radius; /* BufferEditor(dag, center, 1.5f * radius) (:716) */
+    if (e->tool >= HD_TOOL_NOISE_REMOVE) {
+        ed.buf_r = br;
+        ed.buf_min = (f3){bc.x - br, bc.y - br, bc.z - br};
+        ed.size = 2 * (uint32_t)ceilf(br);
+    }
+    ed.bmin = (f3){bc.x - br, bc.y - br, bc.z - br};
+    ed.bmax = (f3){bc.x + br, bc.y + br, bc.z + br};
     ed.paint = (f3){(float)(e->rgb & 0xFF) / 255.0f, (float)((e->rgb >> 8) & 0xFF) / 255.0f,
                     (float)((e->rgb >> 16) & 0xFF) / 255.0f};
     return ed;
@@ -1975,8 +1994,55 @@ static hd_color prev_color(edit_job* j, int prev)
         k = leaf_color(j->old, j->old_count);
     return k;
 }
+/* truncate(float3) (cuda_math.h:80) of a float that may be negative, as the
+ * reference's x86-64 build converts it: to a 64-bit integer toward zero,
+ * then its low 32 bits (so (-1, 0) gives 0 and anything below -1 a huge
+ * index) */
+static uint32_t trunc_u32(float f) { return (uint32_t)(int64_t)f; }
+
+/* BufferEditor's EValues (:134-141) */
+enum { EV_UNKNOWN = 0, EV_LOADED_TRUE = 1, EV_LOADED_FALSE = 2, EV_SET_TRUE = 3, EV_SET_FALSE = 4 };
+
+static uint64_t buf_index(const editor* e, uint32_t x, uint32_t y, uint32_t z)
+{
+    return (uint64_t)x + (uint64_t)e->size * y + (uint64_t)e->size * e->size * z;
+}
+/* BufferEditor::get_world_path (:159-164) */
+static void buf_world(const editor* e, uint32_t x, uint32_t y, uint32_t z, uint32_t w[3])
+{
+    w[0] = (uint32_t)(e->buf_min.x + (float)x);
+    w[1] = (uint32_t)(e->buf_min.y + (float)y);
+    w[2] = (uint32_t)(e->buf_min.z + (float)z);
+}
+/* BufferEditor::get_value (:185-195): Unknown loads the table's voxel */
+static int buf_get(const editor* e, uint32_t x, uint32_t y, uint32_t z)
+{
+    const uint64_t i = buf_index(e, x, y, z);
+    if (e->state[i] == EV_UNKNOWN) {
+        /* the table as it was when the editor was made: the root changes
+         * only once the edit is done */
+        uint32_t w[3];
+        buf_world(e, x, y, z, w);
+        e->state[i] = or_get_value(e->dag, w[0], w[1], w[2]) ? EV_LOADED_TRUE : EV_LOADED_FALSE;
+    }
+    return e->state[i] == EV_LOADED_TRUE || e->state[i] == EV_SET_TRUE;
+}
+/* BufferEditor::get_new_value (:211-220): `get_value(p) == EValues::Unknown`
+ * compares a bool with 0, so a voxel reads true only when set or loaded
+ * true, and a false one keeps its old value */
+static int buf_new_value(const editor* e, f3 pos, int prev)
+{
+    const uint32_t p[3] = {trunc_u32(pos.x - e->buf_min.x), trunc_u32(pos.y - e->buf_min.y),
+                           trunc_u32(pos.z - e->buf_min.z)};
+    if (p[0] >= e->size || p[1] >= e->size || p[2] >= e->size)
+        return prev;
+    return buf_get(e, p[0], p[1], p[2]) ? 1 : prev;
+}
+
 static int new_value(const editor* e, f3 pos, int prev)
 {
+    if (e->tool >= HD_TOOL_NOISE_REMOVE)
+        return buf_new_value(e, pos, prev);
     if (e->tool == HD_TOOL_SPHERE_PAINT)
         return prev;
     if (e->tool == HD_TOOL_COPY) {
@@ -2004,6 +2070,34 @@ static hd_color new_color(edit_job* j, f3 pos, int prev, int nv)
             return prev_color(j, prev);
         const int64_t i = copy_index(e, pos);
         return i < 0 ? prev_color(j, prev) : e->colors[i];
+    }
+    if (e->tool == HD_TOOL_NOISE_ADD || e->tool == HD_TOOL_NOISE_REMOVE) {
+        /* SphereNoiseEditor::get_new_color (:745-758) */
+        if (prev == nv)
+            return prev_color(j, prev);
+        hd_color k;
+        memset(&k, 0, sizeof(k));
+        k.bits_per_weight = 3;
+        k.color_bits = (uint32_t)f3_to_rgb565((f3){94 / 255.f, 30 / 255.f, 0 / 255.f}) |
+                       ((uint32_t)f3_to_rgb565((f3){125 / 255.f, 100 / 255.f, 89 / 255.f}) << 16);
+        const f3 d = {pos.x - e->c.x, pos.y - e->c.y, pos.z - e->c.z};
+        const float len = (float)sqrt((double)(d.x * d.x + d.y * d.y + d.z * d.z));
+        const int32_t w = (int32_t)((len / e->buf_r - 0.3f) * (float)((1 << 3) - 1));
+        k.weight = (uint8_t)(w < 0 ? 0 : w > 7 ? 7 : w);
+        return k;
+    }
+    if (e->tool == HD_TOOL_FILL) {
+        /* FillEditorColors::get_new_color (:693-709) */
+        if (nv && !prev) {
+            const uint32_t p[3] = {trunc_u32(pos.x - e->buf_min.x), trunc_u32(pos.y - e->buf_min.y),
+                                   trunc_u32(pos.z - e->buf_min.z)};
+            if (p[0] < e->size && p[1] < e->size && p[2] < e->size) {
+                const uint64_t i = buf_index(e, p[0], p[1], p[2]);
+                if (e->state[i] == EV_SET_TRUE)
+                    return e->colors[i];
+            }
+        }
+        return prev_color(j, prev);
     }
     return single_color(single_of(e));
 }
@@ -2270,7 +2364,9 @@ int or_edit(or_table* t, const hd_edit* e, hd_edit_stats* stats)
     t->foa_calls = t->nodes_added = t->words_scanned = 0;
     const uint32_t path[3] = {0, 0, 0};
     uint32_t root, cn;
-    if (e->tool > HD_TOOL_BOX_ADD) /* paint and copy need colours */
+    if (e->tool == HD_TOOL_SPHERE_PAINT || e->tool == HD_TOOL_COPY || e->tool > HD_TOOL_FILL)
+        return HD_ERR_INVALID; /* paint and copy need colours */
+    if (make_buffers(&j.ed, t, NULL))
         return HD_ERR_INVALID;
     if (t->cfg.color_tree_levels == 0) {
         uint32_t cc;
@@ -2278,6 +2374,8 @@ int or_edit(or_table* t, const hd_edit* e, hd_edit_stats* stats)
     } else {
         root = edit_top(&j, 0, t->root, path, 0, &cn);
     }
+    free(j.ed.state);
+    free(j.ed.colors);
     if (!t->error)
         t->root = root;
     if (stats) {
@@ -2568,18 +2666,244 @@ static void push_frame(struct frame** stack, uint64_t* n, uint64_t* cap, struct 
     (*stack)[(*n)++] = f;
 }
 
+/* ---- the noise and flood-fill buffers ------------------------------------ */
+
+/* std::mt19937_64 (the standard's 64-bit Mersenne Twister: Matsumoto and
+ * Nishimura's MT19937-64 parameters, seeded by the standard's recurrence) */
+typedef struct {
+    uint64_t mt[312];
+    uint32_t i;
+} mt64;
+static void mt64_seed(mt64* g, uint64_t seed)
+{
+    g->mt[0] = seed;
+    for (uint32_t i = 1; i < 312; i++)
+        g->mt[i] = 6364136223846793005ull * (g->mt[i - 1] ^ (g->mt[i - 1] >> 62)) + i;
+    g->i = 312;
+}
+static uint64_t mt64_next(mt64* g)
+{
+    if (g->i >= 312) {
+        for (uint32_t k = 0; k < 312; k++) {
+            const uint64_t x = (g->mt[k] & 0xFFFFFFFF80000000ull) | (g->mt[(k + 1) % 312] & 0x7FFFFFFFull);
+            uint64_t xa = x >> 1;
+            if (x & 1)
+                xa ^= 0xB5026F5AA96619E9ull;
+            g->mt[k] = g->mt[(k + 156) % 312] ^ xa;
+        }
+        g->i = 0;
+    }
+    uint64_t y = g->mt[g->i++];
+    y ^= (y >> 29) & 0x5555555555555555ull;
+    y ^= (y << 17) & 0x71D67FFFEDA60000ull;
+    y ^= (y << 37) & 0xFFF7EEE000000000ull;
+    y ^= y >> 43;
+    return y;
+}
+
+/* FastNoise's 3D gradient Perlin noise with an FBM fractal (the reference
+ * vendors FastNoise: FastNoise.cpp:207-225 SetSeed, :227-237 the fractal
+ * bounding, :760-793 GetPerlinFractal / SinglePerlinFractalFBM, :841-886
+ * SinglePerlin; float arithmetic, quintic interpolation, lacunarity 2, gain
+ * 0.5) */
+typedef struct {
+    uint8_t perm[512], perm12[512];
+    float frequency, bounding;
+    int octaves;
+} fnoise;
+static const float kGradX[12] = {1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+static const float kGradY[12] = {1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1};
+static const float kGradZ[12] = {0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+static void fn_seed(fnoise* n, int seed)
+{
+    mt64 g;
+    mt64_seed(&g, (uint64_t)(int64_t)seed);
+    for (int i = 0; i < 256; i++)
+        n->perm[i] = (uint8_t)i;
+    for (int j = 0; j < 256; j++) {
+        const int rng = (int)(mt64_next(&g) % (uint64_t)(256 - j));
+        const int k = rng + j;
+        const uint8_t l = n->perm[j];
+        n->perm[j] = n->perm[j + 256] = n->perm[k];
+        n->perm[k] = l;
+        n->perm12[j] = n->perm12[j + 256] = (uint8_t)(n->perm[j] % 12);
+    }
+}
+static void fn_octaves(fnoise* n, int octaves)
+{
+    n->octaves = octaves;
+    float amp = 0.5f, amp_fractal = 1.0f;
+    for (int i = 1; i < octaves; i++) {
+        amp_fractal += amp;
+        amp *= 0.5f;
+    }
+    n->bounding = 1.0f / amp_fractal;
+}
+static int fast_floor(float f) { return f >= 0 ? (int)f : (int)f - 1; }
+static float fn_lerp(float a, float b, float t) { return a + t * (b - a); }
+static float quintic(float t) { return t * t * t * (t * (t * 6 - 15) + 10); }
+static float grad3(const fnoise* n, uint8_t offset, int x, int y, int z, float xd, float yd, float zd)
+{
+    const uint8_t lut = n->perm12[(x & 0xff) + n->perm[(y & 0xff) + n->perm[(z & 0xff) + offset]]];
+    return xd * kGradX[lut] + yd * kGradY[lut] + zd * kGradZ[lut];
+}
+static float single_perlin(const fnoise* n, uint8_t offset, float x, float y, float z)
+{
+    const int x0 = fast_floor(x), y0 = fast_floor(y), z0 = fast_floor(z);
+    const int x1 = x0 + 1, y1 = y0 + 1, z1 = z0 + 1;
+    const float xs = quintic(x - (float)x0), ys = quintic(y - (float)y0), zs = quintic(z - (float)z0);
+    const float xd0 = x - (float)x0, yd0 = y - (float)y0, zd0 = z - (float)z0;
+    const float xd1 = xd0 - 1, yd1 = yd0 - 1, zd1 = zd0 - 1;
+    const float xf00 = fn_lerp(grad3(n, offset, x0, y0, z0, xd0, yd0, zd0), grad3(n, offset, x1, y0, z0, xd1, yd0, zd0), xs);
+    const float xf10 = fn_lerp(grad3(n, offset, x0, y1, z0, xd0, yd1, zd0), grad3(n, offset, x1, y1, z0, xd1, yd1, zd0), xs);
+    const float xf01 = fn_lerp(grad3(n, offset, x0, y0, z1, xd0, yd0, zd1), grad3(n, offset, x1, y0, z1, xd1, yd0, zd1), xs);
+    const float xf11 = fn_lerp(grad3(n, offset, x0, y1, z1, xd0, yd1, zd1), grad3(n, offset, x1, y1, z1, xd1, yd1, zd1), xs);
+    const float yf0 = fn_lerp(xf00, xf10, ys), yf1 = fn_lerp(xf01, xf11, ys);
+    return fn_lerp(yf0, yf1, zs);
+}
+static float perlin_fractal(const fnoise* n, float x, float y, float z)
+{
+    x *= n->frequency;
+    y *= n->frequency;
+    z *= n->frequency;
+    float sum = single_perlin(n, n->perm[0], x, y, z), amp = 1;
+    for (int i = 1; i < n->octaves; i++) {
+        x *= 2.0f;
+        y *= 2.0f;
+        z *= 2.0f;
+        amp *= 0.5f;
+        sum += single_perlin(n, n->perm[i], x, y, z) * amp;
+    }
+    return sum * n->bounding;
+}
+float or_perlin_fractal(int seed, float frequency, int octaves, float x, float y, float z)
+{
+    fnoise n;
+    fn_seed(&n, seed);
+    n.frequency = frequency;
+    fn_octaves(&n, octaves);
+    return perlin_fractal(&n, x, y, z);
+}
+
+/* SphereNoiseEditor's constructor (:716-744): a voxel of the buffer is set
+ * to isAdding where its distance to the centre, sqrt of the uint32 dot
+ * product of the (wrapping) uint3 difference, is below
+ * radius * (1 + noise) in double */
+static void noise_buffer(editor* e, int adding)
+{
+    const uint32_t n = e->size, ec = n / 2;
+    fnoise fn;
+    int seed = 1923 + (int32_t)e->c.x + 23 * (int32_t)e->c.y + 2938 * (int32_t)e->c.z;
+    fn_seed(&fn, seed < 0 ? -seed : seed);
+    fn.frequency = 1 / e->r;
+    fn_octaves(&fn, 3);
+    for (uint32_t x = 0; x < n; x++)
+        for (uint32_t y = 0; y < n; y++)
+            for (uint32_t z = 0; z < n; z++) {
+                const uint32_t dx = ec - x, dy = ec - y, dz = ec - z;
+                const double distance = sqrt((double)(dx * dx + dy * dy + dz * dz));
+                if (distance < (double)e->r * (1. + (double)perlin_fractal(&fn, (float)x, (float)y, (float)z)))
+                    e->state[buf_index(e, x, y, z)] = adding ? EV_SET_TRUE : EV_SET_FALSE;
+            }
+}
+
+/* FillEditorBase's constructor (:625-668): a depth-first flood from the
+ * buffer's centre through voxels that read false (get_value loads them
+ * from the table), 6-neighbours in the order -x, +x, -y, +y, -z, +z; every
+ * popped voxel is set; the bounds become min + the set voxels' box.  With
+ * colours, FillEditorColors (:679-705) then walks that box (x, then y, then
+ * z) carrying the colour of the last loaded-true voxel into every set voxel
+ * after it. */
+static void fill_buffer(editor* e, const or_colors* col)
+{
+    const uint32_t n = e->size;
+    uint32_t* stack = NULL;
+    uint64_t sn = 0, scap = 0;
+    const uint32_t ec = n / 2;
+    uint32_t mn[3] = {ec, ec, ec}, mx[3] = {ec, ec, ec};
+#define FILL_PUSH(a, b, c)                                                   \
+    do {                                                                     \
+        if (sn + 3 > scap) {                                                 \
+            scap = scap ? 2 * scap : 3 * 1024;                               \
+            stack = (uint32_t*)realloc(stack, scap * 4);                     \
+        }                                                                    \
+        stack[sn++] = (a);                                                   \
+        stack[sn++] = (b);                                                   \
+        stack[sn++] = (c);                                                   \
+    } while (0)
+    FILL_PUSH(ec, ec, ec);
+    while (sn) {
+        sn -= 3;
+        const uint32_t p[3] = {stack[sn], stack[sn + 1], stack[sn + 2]};
+        e->state[buf_index(e, p[0], p[1], p[2])] = EV_SET_TRUE;
+        for (int a = 0; a < 3; a++) {
+            mn[a] = p[a] < mn[a] ? p[a] : mn[a];
+            mx[a] = p[a] > mx[a] ? p[a] : mx[a];
+        }
+        static const int nb[6][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+        for (int k = 0; k < 6; k++) {
+            const uint32_t q[3] = {p[0] + (uint32_t)nb[k][0], p[1] + (uint32_t)nb[k][1], p[2] + (uint32_t)nb[k][2]};
+            if (q[0] < n && q[1] < n && q[2] < n && !buf_get(e, q[0], q[1], q[2]))
+                FILL_PUSH(q[0], q[1], q[2]);
+        }
+    }
+#undef FILL_PUSH
+    free(stack);
+    e->bmin = (f3){e->buf_min.x + (float)mn[0], e->buf_min.y + (float)mn[1], e->buf_min.z + (float)mn[2]};
+    e->bmax = (f3){e->buf_min.x + (float)mx[0], e->buf_min.y + (float)mx[1], e->buf_min.z + (float)mx[2]};
+    if (!col)
+        return;
+    hd_color color;
+    memset(&color, 0, sizeof(color));
+    for (uint32_t x = mn[0]; x <= mx[0]; x++)
+        for (uint32_t y = mn[1]; y <= mx[1]; y++)
+            for (uint32_t z = mn[2]; z <= mx[2]; z++) {
+                const uint64_t i = buf_index(e, x, y, z);
+                if (e->state[i] == EV_LOADED_TRUE) {
+                    uint32_t w[3];
+                    buf_world(e, x, y, z, w);
+                    color = or_get_color(e->dag, col, w[0], w[1], w[2]);
+                } else if (e->state[i] == EV_SET_TRUE) {
+                    e->colors[i] = color;
+                }
+            }
+}
+
+/* The buffers of the noise and fill editors, made before the edit as their
+ * constructors make them; 0, or HD_ERR_INVALID when the buffer would not
+ * fit. */
+static int make_buffers(editor* e, const or_table* t, const or_colors* col)
+{
+    if (e->tool < HD_TOOL_NOISE_REMOVE)
+        return 0;
+    const uint64_t n3 = (uint64_t)e->size * e->size * e->size;
+    if (n3 > (1ull << 31))
+        return HD_ERR_INVALID;
+    e->dag = t;
+    e->state = (uint8_t*)calloc(n3 + 1, 1);
+    if (e->tool == HD_TOOL_FILL) {
+        e->colors = (hd_color*)calloc(n3 + 1, sizeof(hd_color));
+        fill_buffer(e, col);
+    } else {
+        noise_buffer(e, e->tool == HD_TOOL_NOISE_ADD);
+    }
+    return 0;
+}
+
 /* HashDAG::edit_threads (hash_dag.h:255-405) with colours: the edit, the
  * colour leaves rebuilt, an undo frame recorded (HashDAGUndoRedo::add_frame
  * drops the redo stack, :55-66). */
 int or_edit_colored(or_table* t, or_colors* col, const hd_edit* e, hd_edit_stats* stats)
 {
-    if (!col || !col->n_nodes || t->cfg.color_tree_levels == 0 || e->tool > HD_TOOL_COPY)
+    if (!col || !col->n_nodes || t->cfg.color_tree_levels == 0 || e->tool > HD_TOOL_FILL)
         return HD_ERR_INVALID;
     edit_job j;
     memset(&j, 0, sizeof(j));
     j.t = t;
     j.col = col;
     j.ed = make_editor(e);
+    if (make_buffers(&j.ed, t, col))
+        return HD_ERR_INVALID;
     if (e->tool == HD_TOOL_COPY) {
         /* the source region read before the edit (:459-505, BENCHMARK).
          * DAGUtils::get_values' overlap test compares inclusive node bounds
@@ -2607,6 +2931,7 @@ int or_edit_colored(or_table* t, or_colors* col, const hd_edit* e, hd_edit_stats
     const uint32_t root = edit_top(&j, 0, t->root, path, 0, &cn);
     free(j.ed.values);
     free(j.ed.colors);
+    free(j.ed.state);
     if (!t->error) {
         t->root = root;
         struct frame f = {before, j.n_diff, j.diff_index, j.diff_prev, j.diff_next};

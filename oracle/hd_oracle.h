@@ -103,6 +103,8 @@ int or_edit_colored(or_table* t, or_colors* c, const hd_edit* e, hd_edit_stats* 
 int or_undo(or_table* t, or_colors* c); /* 1 if a frame was applied */
 int or_redo(or_table* t, or_colors* c);
 void or_colors_stats(const or_colors* c, uint64_t* out);
+/* FastNoise's GetPerlinFractal (FBM, quintic, lacunarity 2, gain 0.5) */
+float or_perlin_fractal(int seed, float frequency, int octaves, float x, float y, float z);
 /* The BasicDAGCompressedColors shipped beside a BasicDAG (enclosedLeaves and
  * one main leaf for the colour field of `seed`); arrays malloc'd, or_free. */
 int or_main_leaf(const uint32_t* words, uint64_t n_words, uint32_t depth, uint32_t top_levels, uint64_t seed,

@@ -137,6 +137,8 @@ def lib():
         L.or_voxel_color.argtypes = [u64, u32, u32, u32]
         L.or_color_rgb888.restype = u32
         L.or_color_rgb888.argtypes = [HdColor]
+        L.or_perlin_fractal.restype = C.c_float
+        L.or_perlin_fractal.argtypes = [C.c_int, C.c_float, C.c_int, C.c_float, C.c_float, C.c_float]
         PP = C.POINTER(C.c_void_p)
         L.or_main_leaf.argtypes = [pu32, u64, u32, u32, u64, PP, C.POINTER(u64), PP, C.POINTER(u64), PP,
                                    C.POINTER(u64), PP, C.POINTER(u64)]
@@ -423,3 +425,8 @@ def hash_dag_file(table, info, pool_max):
     t = table.export()
     head = np.array([table.cfg.depth, t["root"], pool_max, t["page_table"].size, table.pool_top], np.uint32)
     return _info(info) + head.tobytes() + t["pool"].tobytes() + t["page_table"].tobytes()
+
+
+def perlin_fractal(seed, frequency, octaves, x, y, z):
+    """FastNoise's GetPerlinFractal (FBM, quintic, lacunarity 2, gain 0.5)."""
+    return lib().or_perlin_fractal(seed, frequency, octaves, x, y, z)

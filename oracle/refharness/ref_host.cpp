@@ -67,6 +67,7 @@
 #include "hash_table.cpp"
 #include "stats.cpp"
 #include "hash_dag_factory.cpp"
+#include "FastNoise.cpp"
 #if EDITS_ENABLE_COLORS
 // the BasicDAG / compressed-colour file writers and readers, replays
 #include "dags/basic_dag/basic_dag.cpp"
@@ -242,6 +243,17 @@ extern "C" int ref_get_value(uint32 x, uint32 y, uint32 z) { return DAGUtils::ge
 // HashTable::get_level_size (hash_table.cpp:277-285)
 extern "C" uint32 ref_level_size(uint32 level) { return g_dag.data.get_level_size(level); }
 
+// FastNoise known answers: GetPerlinFractal with the seed, frequency and
+// octaves SphereNoiseEditor sets (hash_dag_editors.h:724-727).
+extern "C" float ref_perlin_fractal(int seed, float frequency, int octaves, float x, float y, float z)
+{
+    FastNoise noise;
+    noise.SetSeed(seed);
+    noise.SetFrequency(frequency);
+    noise.SetFractalOctaves(octaves);
+    return noise.GetPerlinFractal(x, y, z);
+}
+
 // Hash known-answer vectors (hash_table.h:80-89).
 extern "C" uint32 ref_hash_leaf(uint64 leaf) { return HashDagUtils::hash_leaf(leaf); }
 extern "C" uint32 ref_hash_interior(uint32 n, const uint32* node) { return HashDagUtils::hash_interior(n, node); }
@@ -362,7 +374,8 @@ static void run_edit_colored(const TEditor& editor, uint64* stats)
 }
 
 // tool: 0..3 as ref_edit, 4 SpherePaintEditor (blue), 5 CopyEditor
-// (identity transform, no swirl) moving center +- radius by dest - source
+// (identity transform, no swirl) moving center +- radius by dest - source,
+// 6 / 7 SphereNoiseEditor (isAdding false / true), 8 FillEditorColors
 extern "C" int ref_edit_colored(uint32 tool, const float* center, float radius, const float* source,
                                 const float* dest, uint64* stats)
 {
@@ -381,6 +394,9 @@ extern "C" int ref_edit_colored(uint32 tool, const float* center, float radius, 
                          stats);
         break;
     }
+    case 6: run_edit_colored(SphereNoiseEditor(g_dag, c, radius, false), stats); break;
+    case 7: run_edit_colored(SphereNoiseEditor(g_dag, c, radius, true), stats); break;
+    case 8: run_edit_colored(FillEditorColors(g_dag, g_colors, c, radius), stats); break;
     default: return 1;
     }
     return 0;
