@@ -23,11 +23,13 @@ from . import _capi
 from ._capi import (BatchTuning, Camera, Config, Edit, EditStats, HashDagError, LevelStats, Request, RequestResult,
                     ServeConfig, ServeStats, lib)
 
-__all__ = ["HashDAG", "DAGTracer", "SphereEditor", "BoxEditor", "SpherePaintEditor", "CopyEditor", "BatchTuning",
+__all__ = ["HashDAG", "DAGTracer", "SphereEditor", "BoxEditor", "SpherePaintEditor", "CopyEditor",
+           "SphereNoiseEditor", "FillEditorColors", "ReplayManager", "BatchTuning",
            "Request", "RequestResult", "ServeConfig", "ServeStats", "edit_request", "render_request", "Camera", "Config", "EditStats", "LevelStats",
            "HashDagError", "default_config"]
 
-TOOL_SPHERE_REMOVE, TOOL_SPHERE_ADD, TOOL_BOX_REMOVE, TOOL_BOX_ADD, TOOL_SPHERE_PAINT, TOOL_COPY = range(6)
+TOOL_SPHERE_REMOVE, TOOL_SPHERE_ADD, TOOL_BOX_REMOVE, TOOL_BOX_ADD, TOOL_SPHERE_PAINT, TOOL_COPY, \
+    TOOL_NOISE_REMOVE, TOOL_NOISE_ADD, TOOL_FILL = range(9)
 SCENE_SHELL = 1
 GC_KEEP_HISTORY = 1
 
@@ -102,6 +104,25 @@ class CopyEditor(_Editor):
         self.dest = tuple(float(np.float32(v)) for v in dest)
 
 
+class SphereNoiseEditor(_Editor):
+    """SphereNoiseEditor (hash_dag_editors.h:712-760): a sphere roughened by
+    FastNoise's Perlin FBM, in a buffer of 1.5 radius.  Carving (adding =
+    False) changes no voxel, as in the reference (BufferEditor::get_new_value
+    reads a voxel set false as its old value)."""
+
+    def __init__(self, center, radius, adding):
+        super().__init__(center, radius)
+        self.tool = TOOL_NOISE_ADD if adding else TOOL_NOISE_REMOVE
+
+
+class FillEditorColors(_Editor):
+    """FillEditorColors (hash_dag_editors.h:624-710): flood fill of the empty
+    voxels connected to the centre within center +- radius, each filled voxel
+    taking the colour of the last solid boundary voxel before it in x, y, z
+    order."""
+    tool = TOOL_FILL
+
+
 def edit_request(arrival_ms, editor):
     return Request(0, 0, 0, 0, float(arrival_ms), editor.to_edit(), Camera())
 
@@ -119,6 +140,10 @@ def editor_from_tuple(t):
         return SpherePaintEditor(center, radius, *(t[3:4] or ()))
     if tool == TOOL_COPY:
         return CopyEditor(center, radius, t[3], t[4])
+    if tool in (TOOL_NOISE_REMOVE, TOOL_NOISE_ADD):
+        return SphereNoiseEditor(center, radius, tool == TOOL_NOISE_ADD)
+    if tool == TOOL_FILL:
+        return FillEditorColors(center, radius)
     return BoxEditor(center, radius, tool == TOOL_BOX_ADD)
 
 

@@ -622,6 +622,27 @@ HD_D uint64_t new_color(const Editor& e, float px, float py, float pz, bool prev
         const int64_t i = copy_index(e, px, py, pz);
         return i < 0 ? prev_col : e.colors[i];
     }
+    if (e.tool == HD_TOOL_NOISE_ADD || e.tool == HD_TOOL_NOISE_REMOVE) {
+        // SphereNoiseEditor::get_new_color (:745-758): two rgb565 end points,
+        // 3-bit weight from the distance over BoxEditorBase::radius
+        if (prev == nv)
+            return prev_col;
+        const uint32_t bits = f3_to_rgb565(F3{94 / 255.f, 30 / 255.f, 0 / 255.f}) |
+                              (f3_to_rgb565(F3{125 / 255.f, 100 / 255.f, 89 / 255.f}) << 16);
+        const float dx = px - e.cx, dy = py - e.cy, dz = pz - e.cz;
+        const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+        const int32_t w = int32_t((len / e.buf_r - 0.3f) * float((1 << 3) - 1));
+        return pack_color(bits, uint32_t(w < 0 ? 0 : w > 7 ? 7 : w), 3);
+    }
+    if (e.tool == HD_TOOL_FILL) {
+        // FillEditorColors::get_new_color (:693-709)
+        if (nv && !prev) {
+            const int64_t i = buffer_index(e, px, py, pz);
+            if (i >= 0 && (e.values[i] & kBufSet))
+                return e.colors[i];
+        }
+        return prev_col;
+    }
     return single_color(e.sphere() ? F3{1, 0, 0} : F3{1, 0, 1});
 }
 

@@ -73,6 +73,11 @@ HD_HD F3 rgb101210_to_f3(uint32_t v)
     return F3{float((v >> 0) & 0x3FF) / 1023.0f, float((v >> 10) & 0xFFF) / 4095.0f,
               float((v >> 22) & 0x3FF) / 1023.0f};
 }
+HD_HD uint32_t f3_to_rgb565(F3 c)
+{
+    const float r = clampf(c.x, 0.f, 1.f), g = clampf(c.y, 0.f, 1.f), b = clampf(c.z, 0.f, 1.f);
+    return (uint32_t(r * 31.0f) << 0) | (uint32_t(g * 63.0f) << 5) | (uint32_t(b * 31.0f) << 11);
+}
 HD_HD F3 rgb565_to_f3(uint32_t v)
 {
     return F3{float((v >> 0) & 0x1F) / 31.0f, float((v >> 5) & 0x3F) / 63.0f, float((v >> 11) & 0x1F) / 31.0f};

@@ -119,6 +119,7 @@ void get_colors(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, hd_color* d_out);
 void trace_colors(hd_ctx* c, const uint32_t* d_paths, uint32_t w, uint32_t h, uint32_t* d_rgba,
                   cudaStream_t stream = nullptr, const uint32_t* d_root = nullptr);
 void copy_source(hd_ctx* c, Editor& ed);
+void tool_buffers(hd_ctx* c, Editor& ed); // hd_tools.cu
 void color_spawn(hd_ctx* c, uint32_t level, uint32_t n, const Level& lv, const Level& next);
 void edit_colors(hd_ctx* c, const Editor& ed, std::vector<Level>& lv, const std::vector<uint32_t>& count,
                  uint32_t deepest, UndoFrame& frame);

@@ -148,6 +148,8 @@ void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats)
     HD_CUDA(cudaEventRecord(c->ev0, st));
     if (e.tool == HD_TOOL_COPY)
         copy_source(c, ed); // the source region as it is before the edit
+    if (e.tool >= HD_TOOL_NOISE_REMOVE)
+        tool_buffers(c, ed); // the noise or fill buffer, made before the edit
     UndoFrame frame;
     frame.root = c->root;
     EditCounters* ctr = s.get<EditCounters>("ed_ctr", 1);
@@ -246,7 +248,7 @@ extern "C" {
 
 hd_status hd_edit_apply(hd_ctx* c, const hd_edit* edit, hd_edit_stats* stats)
 {
-    if (!c || !edit || edit->tool > HD_TOOL_COPY || !(edit->radius >= 0.0f))
+    if (!c || !edit || edit->tool > HD_TOOL_FILL || !(edit->radius >= 0.0f))
         return HD_ERR_INVALID;
     try {
         hd::edit_one(c, *edit, stats);

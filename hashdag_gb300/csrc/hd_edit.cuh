@@ -45,6 +45,11 @@ struct Editor {
     uint32_t size;
     const uint8_t* values;
     const uint64_t* colors;
+    // noise and fill (BufferEditor, :129-221): the buffer's corner
+    // (BoxEditorBase::min; minx.. above), its radius (1.5 r for the noise)
+    // and per voxel kBufNew (the voxel reads true) | kBufSet (set by the
+    // tool); the fill's colour of each set voxel in `colors`
+    float buf_r;
     HD_HD bool sphere() const
     {
         return tool == HD_TOOL_SPHERE_ADD || tool == HD_TOOL_SPHERE_REMOVE || tool == HD_TOOL_SPHERE_PAINT;
@@ -80,12 +85,22 @@ HD_HD Editor make_editor(const hd_edit& e)
         ed.minz = e.center[2] - e.radius;
         ed.size = 2 * uint32_t(ceilf(e.radius));
     }
-    ed.bminx = bx - e.radius;
-    ed.bminy = by - e.radius;
-    ed.bminz = bz - e.radius;
-    ed.bmaxx = bx + e.radius;
-    ed.bmaxy = by + e.radius;
-    ed.bmaxz = bz + e.radius;
+    float br = e.radius;
+    if (e.tool == HD_TOOL_NOISE_ADD || e.tool == HD_TOOL_NOISE_REMOVE)
+        br = 1.5f * e.radius; // BufferEditor(dag, center, 1.5f * radius) (:716)
+    if (e.tool >= HD_TOOL_NOISE_REMOVE) {
+        ed.buf_r = br;
+        ed.minx = bx - br;
+        ed.miny = by - br;
+        ed.minz = bz - br;
+        ed.size = 2 * uint32_t(ceilf(br));
+    }
+    ed.bminx = bx - br;
+    ed.bminy = by - br;
+    ed.bminz = bz - br;
+    ed.bmaxx = bx + br;
+    ed.bmaxy = by + br;
+    ed.bmaxz = bz + br;
     ed.paint_r = float(e.rgb & 0xFF) / 255.0f;
     ed.paint_g = float((e.rgb >> 8) & 0xFF) / 255.0f;
     ed.paint_b = float((e.rgb >> 16) & 0xFF) / 255.0f;
@@ -103,9 +118,33 @@ HD_HD int64_t copy_index(const Editor& e, float px, float py, float pz)
         return -1;
     return int64_t(ix) + int64_t(e.size) * iy + int64_t(e.size) * e.size * iz;
 }
+// Per-voxel flags of the noise and fill buffers
+constexpr uint8_t kBufNew = 1; // BufferEditor::get_value reads true (set, or loaded true)
+constexpr uint8_t kBufSet = 2; // EValues::SetTrue
+
+// truncate(float3) (cuda_math.h:80) of a float that may be negative, as the
+// reference's x86-64 build converts it: to a 64-bit integer toward zero, then
+// its low 32 bits ((-1, 0) gives 0, anything below -1 a huge index)
+HD_HD uint32_t trunc_u32(float f) { return uint32_t((long long)f); }
+
+// the buffer index of a voxel, or -1 (BufferEditor::get_new_value, :211-220)
+HD_HD int64_t buffer_index(const Editor& e, float px, float py, float pz)
+{
+    const uint32_t x = trunc_u32(px - e.minx), y = trunc_u32(py - e.miny), z = trunc_u32(pz - e.minz);
+    if (x >= e.size || y >= e.size || z >= e.size)
+        return -1;
+    return int64_t(x) + int64_t(e.size) * y + int64_t(e.size) * e.size * z;
+}
+
 // get_new_value of each editor
 HD_HD bool new_value(const Editor& e, float px, float py, float pz, bool prev)
 {
+    if (e.tool >= HD_TOOL_NOISE_REMOVE) {
+        // `get_value(p) == EValues::Unknown` compares a bool with 0: a
+        // voxel reads true when set or loaded true, else keeps its value
+        const int64_t i = buffer_index(e, px, py, pz);
+        return (i >= 0 && (e.values[i] & kBufNew)) ? true : prev;
+    }
     if (e.tool == HD_TOOL_SPHERE_PAINT)
         return prev;
     if (e.tool == HD_TOOL_COPY) {

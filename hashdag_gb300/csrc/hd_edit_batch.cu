@@ -772,7 +772,7 @@ hd_status guarded_call(hd_ctx* c, F&& f)
 bool valid_edits(const hd_edit* edits, uint32_t n)
 {
     for (uint32_t i = 0; i < n; i++)
-        if (edits[i].tool > HD_TOOL_COPY || !(edits[i].radius >= 0.0f))
+        if (edits[i].tool > HD_TOOL_FILL || !(edits[i].radius >= 0.0f))
             return false;
     return true;
 }

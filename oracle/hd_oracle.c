@@ -2010,9 +2010,9 @@ static uint64_t buf_index(const editor* e, uint32_t x, uint32_t y, uint32_t z)
 /* BufferEditor::get_world_path (:159-164) */
 static void buf_world(const editor* e, uint32_t x, uint32_t y, uint32_t z, uint32_t w[3])
 {
-    w[0] = (uint32_t)(e->buf_min.x + (float)x);
-    w[1] = (uint32_t)(e->buf_min.y + (float)y);
-    w[2] = (uint32_t)(e->buf_min.z + (float)z);
+    w[0] = trunc_u32(e->buf_min.x + (float)x);
+    w[1] = trunc_u32(e->buf_min.y + (float)y);
+    w[2] = trunc_u32(e->buf_min.z + (float)z);
 }
 /* BufferEditor::get_value (:185-195): Unknown loads the table's voxel */
 static int buf_get(const editor* e, uint32_t x, uint32_t y, uint32_t z)
