@@ -32,6 +32,10 @@ TOOL_SPHERE_REMOVE, TOOL_SPHERE_ADD, TOOL_BOX_REMOVE, TOOL_BOX_ADD, TOOL_SPHERE_
     TOOL_NOISE_REMOVE, TOOL_NOISE_ADD, TOOL_FILL = range(9)
 SCENE_SHELL = 1
 GC_KEEP_HISTORY = 1
+# EDebugColors (tracer.h:7-17) and the overlay's ETool (tracer.h:21-29)
+DEBUG_NONE, DEBUG_INDEX, DEBUG_POSITION, DEBUG_COLOR_TREE, DEBUG_COLOR_BITS, DEBUG_MIN_COLOR, DEBUG_MAX_COLOR, \
+    DEBUG_WEIGHT = range(8)
+OVERLAY_SPHERE, OVERLAY_SPHERE_PAINT, OVERLAY_SPHERE_NOISE, OVERLAY_CUBE, OVERLAY_CUBE_COPY, OVERLAY_CUBE_FILL = range(6)
 
 
 def default_config(depth, **overrides):
@@ -528,14 +532,25 @@ class DAGTracer:
                                          self.shadows.data_ptr(), C.byref(ms)))
         return ms.value
 
-    def resolve_colors(self, dag):
-        """The colour lookup of Tracer::trace_colors on the last paths:
-        uint32 RGBA8 per pixel (0 = miss), kept in self.colors."""
+    def resolve_colors(self, dag, debug_colors=DEBUG_NONE, debug_level=0, tool=None):
+        """Tracer::trace_colors on the last paths: uint32 RGBA8 per pixel,
+        kept in self.colors.  debug_colors: an EDebugColors view (DEBUG_*);
+        tool: the ToolInfo overlay as (overlay tool, position, radius,
+        copy source, copy dest), or None."""
         torch = _torch()
         if getattr(self, "colors", None) is None:
             self.colors = torch.zeros((self.height, self.width), dtype=torch.int32, device="cuda")
-        dag._check(lib().hd_trace_colors(dag.handle, self.paths.data_ptr(), self.width, self.height,
-                                         self.colors.data_ptr()))
+        q = _capi.TraceColorsParams()
+        q.debug_colors, q.debug_level = int(debug_colors), int(debug_level)
+        if tool is not None:
+            kind, pos, radius = tool[:3]
+            src, dst = (tool[3], tool[4]) if len(tool) > 3 else ((0, 0, 0), (0, 0, 0))
+            q.overlay.enabled, q.overlay.tool, q.overlay.radius = 1, int(kind), float(radius)
+            q.overlay.position[:] = [int(v) for v in pos]
+            q.overlay.copy_source[:] = [int(v) for v in src]
+            q.overlay.copy_dest[:] = [int(v) for v in dst]
+        dag._check(lib().hd_trace_colors_ex(dag.handle, self.paths.data_ptr(), self.width, self.height,
+                                            self.colors.data_ptr(), C.byref(q)))
         return self.colors.cpu().numpy().view(np.uint32)
 
     def get_paths(self):

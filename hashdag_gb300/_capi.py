@@ -38,6 +38,15 @@ class ReplayConfig(C.Structure):
                 ("reserved", C.c_uint32), ("info", DagInfo)]
 
 
+class ToolOverlay(C.Structure):
+    _fields_ = [("enabled", C.c_uint32), ("tool", C.c_uint32), ("position", C.c_uint32 * 3), ("radius", C.c_float),
+                ("copy_source", C.c_uint32 * 3), ("copy_dest", C.c_uint32 * 3)]
+
+
+class TraceColorsParams(C.Structure):
+    _fields_ = [("debug_colors", C.c_uint32), ("debug_level", C.c_uint32), ("overlay", ToolOverlay)]
+
+
 class Camera(C.Structure):
     _fields_ = [("position", C.c_double * 3), ("ray_min", C.c_double * 3), ("ray_ddx", C.c_double * 3),
                 ("ray_ddy", C.c_double * 3)]
@@ -127,6 +136,7 @@ SIGNATURES = [
     ("hd_colors_from_scene", C.c_int, [_P, _u64]),
     ("hd_get_colors", C.c_int, [_P, _P, _u64, _P]),
     ("hd_trace_colors", C.c_int, [_P, _P, _u32, _u32, _P]),
+    ("hd_trace_colors_ex", C.c_int, [_P, _P, _u32, _u32, _P, C.POINTER(TraceColorsParams)]),
     ("hd_color_stats", C.c_int, [_P, C.POINTER(_u64)]),
     ("hd_memory_stats", C.c_int, [_P, C.POINTER(_u64)]),
     ("hd_undo", C.c_int, [_P]),

@@ -451,30 +451,156 @@ void get_colors(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, hd_color* d_out)
     HD_LAUNCH_CHECK();
 }
 
-// Colour of each traced pixel: the hit voxel's colour as RGB888 (alpha 0xff),
-// 0 for a miss (a path of (0, 0, 0), tracer.cu:644-648).
-__global__ void k_trace_colors(Table t, ColorTable ct, const uint32_t* __restrict__ root, const uint4* paths,
-                               uint64_t n, uint32_t* rgba)
+// ToolInfo::strength (tracer.h:51-77): how close the pixel's voxel is to
+// the tool (> 0 inside)
+HD_D float sphere_strength(const uint32_t pos[3], uint4 p, float radius)
 {
-    const uint32_t r = *root;
-    HD_GRID_STRIDE(i, n)
-    {
-        const uint4 p = paths[i];
-        uint32_t out = 0;
-        if (p.x | p.y | p.z)
-            out = f3_to_rgb888(color_value(get_color(t, ct, r, p.x, p.y, p.z)));
-        rgba[i] = out;
+    const float dx = float(pos[0]) - float(p.x), dy = float(pos[1]) - float(p.y), dz = float(pos[2]) - float(p.z);
+    return 1 - sqrtf(dx * dx + dy * dy + dz * dz) / radius;
+}
+HD_D float cube_strength(const uint32_t pos[3], uint4 p, float radius)
+{
+    const float dx = fabsf(float(pos[0]) - float(p.x)), dy = fabsf(float(pos[1]) - float(p.y)),
+                dz = fabsf(float(pos[2]) - float(p.z));
+    const float m = dx > (dy > dz ? dy : dz) ? dx : (dy > dz ? dy : dz);
+    return 1 - m / radius;
+}
+HD_D float tool_strength(const hd_tool_overlay& o, uint4 p)
+{
+    switch (o.tool) {
+    case HD_OVERLAY_SPHERE:
+    case HD_OVERLAY_SPHERE_PAINT:
+    case HD_OVERLAY_SPHERE_NOISE:
+        return sphere_strength(o.position, p, o.radius);
+    case HD_OVERLAY_CUBE:
+        return cube_strength(o.position, p, o.radius);
+    default: {
+        const float a = sphere_strength(o.copy_source, p, 3), b = sphere_strength(o.copy_dest, p, 3);
+        const float m = a > b ? a : b, c = cube_strength(o.position, p, o.radius);
+        return m > c ? m : c;
+    }
     }
 }
 
+// Tracer::trace_colors (tracer.cu:254-451) for one pixel of the paths image:
+// the sky for a miss, 0xFF00FF where the path leaves the DAG, a checker for
+// a voxel without a valid colour, else the voxel's colour (or the debug
+// view), pulled toward red under the tool when the overlay is on.
+HD_D uint32_t trace_color(const Table& t, const ColorTable& ct, uint32_t root, uint4 p,
+                          const hd_trace_colors_params& q)
+{
+    if (!(p.x | p.y | p.z))
+        return f3_to_rgb888(F3{187 / 255.f, 242 / 255.f, 250 / 255.f});
+    const float strength = q.overlay.enabled ? tool_strength(q.overlay, p) : 0.f;
+    auto out = [&](uint32_t color) {
+        if (q.overlay.enabled && strength > 0) {
+            const F3 a = F3{float((color >> 0) & 0xFF) / 255.0f, float((color >> 8) & 0xFF) / 255.0f,
+                            float((color >> 16) & 0xFF) / 255.0f};
+            const float f = clampf(100 * strength, 0.f, .5f);
+            color = f3_to_rgb888(F3{a.x * (1 - f) + 1 * f, a.y * (1 - f) + 0 * f, a.z * (1 - f) + 0 * f});
+        }
+        return color;
+    };
+    auto invalid = [&]() {
+        const float b = float((p.x ^ p.y ^ p.z) & 1u);
+        return out(f3_to_rgb888(F3{1, b, 1.f - b}));
+    };
+    const uint32_t D = t.g.depth, T = t.g.T, leafl = t.g.leaf_level;
+    const bool tree_debug = q.debug_colors == HD_DEBUG_INDEX || q.debug_colors == HD_DEBUG_POSITION ||
+                            q.debug_colors == HD_DEBUG_COLOR_TREE;
+    uint64_t nof = 0;
+    uint32_t debug_index = 0, cn = 0;
+    const LeafDesc* leaf = nullptr;
+    uint32_t index = root;
+    for (uint32_t level = 0; level < leafl;) {
+        level++;
+        const uint32_t* node = t.sys(index);
+        const uint32_t mask = node[0] & 0xffu;
+        const uint32_t sh = D - level;
+        const uint32_t child = (((p.x >> sh) & 1) << 2) | (((p.y >> sh) & 1) << 1) | ((p.z >> sh) & 1);
+        if (!(mask & (1u << child)))
+            return out(0xFF00FFu);
+        if (level - 1 < T) {
+            cn = ct.nodes[cn + child];
+            if (level == T)
+                leaf = (cn & kLeafFlag) ? ct.leaves + (cn & ~kLeafFlag) : nullptr;
+            else if (!cn)
+                return invalid();
+        }
+        if (tree_debug) {
+            if (q.debug_colors == HD_DEBUG_INDEX && q.debug_level == level - 1)
+                debug_index = index;
+            if (level == leafl) {
+                if (q.debug_level == leafl)
+                    debug_index = node[child_offset(mask, child)];
+                if (q.debug_colors == HD_DEBUG_INDEX)
+                    return out(murmur32(debug_index)); // Utils::murmurhash32 (utils.h:68-76)
+                if (q.debug_colors == HD_DEBUG_POSITION) {
+                    float c = float((p.x ^ p.y ^ p.z) & 0x7FFu) / float(0x7FF);
+                    c = float((double(c) + 0.5) / 2);
+                    return out(f3_to_rgb888((index & kLeafFlag) ? F3{c, 0, 0} : F3{c, c, c}));
+                }
+                const uint32_t off = D - T;
+                const float c = float(((p.x >> off) ^ (p.y >> off) ^ (p.z >> off)) & 1u);
+                return out(f3_to_rgb888(F3{c, c, c}));
+            }
+            index = node[child_offset(mask, child)];
+            continue;
+        }
+        if (level == leafl) {
+            for (uint32_t cb = 0; cb < child; cb++)
+                if (mask & (1u << cb)) {
+                    const uint32_t* lp = t.sys(node[child_offset(mask, cb)]);
+                    nof += popc32(lp[0]) + popc32(lp[1]);
+                }
+            const uint32_t* lp = t.sys(node[child_offset(mask, child)]);
+            const uint64_t bits = uint64_t(lp[0]) | (uint64_t(lp[1]) << 32);
+            const uint32_t bi = ((p.x & 1) ? 4 : 0) | ((p.y & 1) ? 2 : 0) | ((p.z & 1) ? 1 : 0) | ((p.x & 2) ? 32 : 0) |
+                                ((p.y & 2) ? 16 : 0) | ((p.z & 2) ? 8 : 0);
+            nof += popc64(bits & ((1ull << bi) - 1));
+            break;
+        }
+        if (level > T)
+            for (uint32_t cb = 0; cb < child; cb++)
+                if (mask & (1u << cb))
+                    nof += t.sys(node[child_offset(mask, cb)])[0] >> 8;
+        index = node[child_offset(mask, child)];
+    }
+    if (!leaf || !leaf_valid_index(*leaf, nof))
+        return invalid();
+    const uint64_t col = leaf_color(ct, *leaf, nof);
+    switch (q.debug_colors) {
+    case HD_DEBUG_COLOR_BITS:
+        return out(0u); // get_debug_hash: 0 without COLOR_DEBUG (the benchmark build)
+    case HD_DEBUG_MIN_COLOR:
+        return out(f3_to_rgb888(rgb565_to_f3(pc_bits(col) & 0xFFFF)));
+    case HD_DEBUG_MAX_COLOR:
+        return out(f3_to_rgb888(rgb565_to_f3((pc_bits(col) >> 16) & 0xFFFF)));
+    case HD_DEBUG_WEIGHT: {
+        const float w = pc_bpw(col) ? float(pc_weight(col)) / float((1 << pc_bpw(col)) - 1) : 0.f;
+        return out(f3_to_rgb888(F3{w, w, w}));
+    }
+    default:
+        return out(f3_to_rgb888(color_value(col)));
+    }
+}
+
+__global__ void k_trace_colors(Table t, ColorTable ct, const uint32_t* __restrict__ root, const uint4* paths,
+                               uint64_t n, uint32_t* rgba, hd_trace_colors_params q)
+{
+    const uint32_t r = *root;
+    HD_GRID_STRIDE(i, n) rgba[i] = trace_color(t, ct, r, paths[i], q);
+}
+
 void trace_colors(hd_ctx* c, const uint32_t* d_paths, uint32_t w, uint32_t h, uint32_t* d_rgba, cudaStream_t stream,
-                  const uint32_t* d_root)
+                  const uint32_t* d_root, const hd_trace_colors_params* params)
 {
     if (!c->colors)
         throw StatusError{HD_ERR_STATE, "the context has no colours"};
     const uint64_t n = uint64_t(w) * h;
+    const hd_trace_colors_params q = params ? *params : hd_trace_colors_params{};
     k_trace_colors<<<grid_for(n, 256), 256, 0, stream ? stream : c->stream>>>(
-        c->t, c->ct, d_root ? d_root : c->d_root, reinterpret_cast<const uint4*>(d_paths), n, d_rgba);
+        c->t, c->ct, d_root ? d_root : c->d_root, reinterpret_cast<const uint4*>(d_paths), n, d_rgba, q);
     HD_LAUNCH_CHECK();
 }
 
@@ -1092,6 +1218,18 @@ hd_status hd_trace_colors(hd_ctx* c, const uint32_t* d_paths, uint32_t width, ui
         return HD_ERR_INVALID;
     return color_guard(c, [&] {
         hd::trace_colors(c, d_paths, width, height, d_rgba);
+        HD_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
+hd_status hd_trace_colors_ex(hd_ctx* c, const uint32_t* d_paths, uint32_t width, uint32_t height, uint32_t* d_rgba,
+                             const hd_trace_colors_params* params)
+{
+    if (!c || !d_paths || !d_rgba || !params || params->debug_colors > HD_DEBUG_WEIGHT ||
+        params->overlay.tool > HD_OVERLAY_CUBE_FILL)
+        return HD_ERR_INVALID;
+    return color_guard(c, [&] {
+        hd::trace_colors(c, d_paths, width, height, d_rgba, nullptr, nullptr, params);
         HD_CUDA(cudaStreamSynchronize(c->stream));
     });
 }

@@ -117,7 +117,8 @@ void colors_from_main_leaf(hd_ctx* c, uint32_t top_levels, const std::vector<uin
 void color_reserve(hd_ctx* c, const uint64_t add[5]);
 void get_colors(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, hd_color* d_out);
 void trace_colors(hd_ctx* c, const uint32_t* d_paths, uint32_t w, uint32_t h, uint32_t* d_rgba,
-                  cudaStream_t stream = nullptr, const uint32_t* d_root = nullptr);
+                  cudaStream_t stream = nullptr, const uint32_t* d_root = nullptr,
+                  const hd_trace_colors_params* params = nullptr);
 void copy_source(hd_ctx* c, Editor& ed);
 void tool_buffers(hd_ctx* c, Editor& ed); // hd_tools.cu
 void color_spawn(hd_ctx* c, uint32_t level, uint32_t n, const Level& lv, const Level& next);

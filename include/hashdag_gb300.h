@@ -270,12 +270,59 @@ hd_status hd_colors_from_scene(hd_ctx* ctx, uint64_t color_seed);
 /* DAGUtils::get_color (dag_utils.h:423-523) for n voxels (d_xyz: 3 uint32
  * per voxel, device); CompressedColor{} for empty voxels outside any leaf. */
 hd_status hd_get_colors(hd_ctx* ctx, const uint32_t* d_xyz, uint64_t n, hd_color* d_out);
-/* The colour lookup of Tracer::trace_colors (tracer.cu:254-451) on the paths
- * of hd_trace_primary: RGB888 | 0xff000000 of the hit voxel's colour
- * (CompressedColor::get_color, float3_to_rgb888), 0 for a miss.  Headless:
- * no shading or debug colour modes. */
+/* Tracer::trace_colors (tracer.cu:254-451) on the paths of
+ * hd_trace_primary, into a headless RGBA8 buffer (the reference writes a
+ * GL surface): float3_to_rgb888 of the hit voxel's colour
+ * (CompressedColor::get_color); the sky (187, 242, 250) for a miss; 0xFF00FF
+ * where the path leaves the DAG; the checker (1, b, 1 - b), b = (x ^ y ^ z)
+ * & 1, for a voxel without a valid colour.  hd_trace_colors is the
+ * EDebugColors::None view without the tool overlay. */
 hd_status hd_trace_colors(hd_ctx* ctx, const uint32_t* d_paths, uint32_t width, uint32_t height,
                           uint32_t* d_rgba);
+
+/* EDebugColors (tracer.h:7-17) */
+typedef enum hd_debug_colors {
+    HD_DEBUG_NONE = 0,
+    HD_DEBUG_INDEX = 1,      /* murmurhash32 of the node index at debug_level  */
+    HD_DEBUG_POSITION = 2,   /* grey checker of the voxel position             */
+    HD_DEBUG_COLOR_TREE = 3, /* parity of the colour-tree cell                 */
+    HD_DEBUG_COLOR_BITS = 4, /* the colour's debug hash: 0 (no COLOR_DEBUG)    */
+    HD_DEBUG_MIN_COLOR = 5,
+    HD_DEBUG_MAX_COLOR = 6,
+    HD_DEBUG_WEIGHT = 7
+} hd_debug_colors;
+
+/* ETool (tracer.h:21-29), for the overlay's ToolInfo::strength */
+typedef enum hd_overlay_tool {
+    HD_OVERLAY_SPHERE = 0,
+    HD_OVERLAY_SPHERE_PAINT = 1,
+    HD_OVERLAY_SPHERE_NOISE = 2,
+    HD_OVERLAY_CUBE = 3,
+    HD_OVERLAY_CUBE_COPY = 4,
+    HD_OVERLAY_CUBE_FILL = 5
+} hd_overlay_tool;
+
+/* ToolInfo (tracer.h:33-77) and TOOL_OVERLAY (typedefs.h:70-71, on in the
+ * interactive build): a pixel whose voxel has strength s > 0 moves toward
+ * red by clamp(100 s, 0, 0.5). */
+typedef struct hd_tool_overlay {
+    uint32_t enabled;
+    uint32_t tool; /* hd_overlay_tool */
+    uint32_t position[3];
+    float radius;
+    uint32_t copy_source[3];
+    uint32_t copy_dest[3];
+} hd_tool_overlay;
+
+typedef struct hd_trace_colors_params {
+    uint32_t debug_colors; /* hd_debug_colors */
+    uint32_t debug_level;  /* debugColorsIndexLevel of HD_DEBUG_INDEX */
+    hd_tool_overlay overlay;
+} hd_trace_colors_params;
+
+/* Tracer::trace_colors with a debug view and the tool overlay. */
+hd_status hd_trace_colors_ex(hd_ctx* ctx, const uint32_t* d_paths, uint32_t width, uint32_t height,
+                             uint32_t* d_rgba, const hd_trace_colors_params* params);
 /* colour-tree nodes (entries), leaves, blocks, macro words, weight words */
 hd_status hd_color_stats(hd_ctx* ctx, uint64_t* out5);
 

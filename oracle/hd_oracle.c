@@ -2657,6 +2657,149 @@ hd_color or_get_color(const or_table* t, const or_colors* col, uint32_t x, uint3
     return leaf_color(leaf, nof);
 }
 
+/* ToolInfo::strength (tracer.h:51-77) */
+static float sphere_strength(const uint32_t pos[3], const uint32_t p[3], float radius)
+{
+    const float dx = (float)pos[0] - (float)p[0], dy = (float)pos[1] - (float)p[1], dz = (float)pos[2] - (float)p[2];
+    return 1 - (float)sqrt((double)(dx * dx + dy * dy + dz * dz)) / radius;
+}
+static float cube_strength(const uint32_t pos[3], const uint32_t p[3], float radius)
+{
+    const float dx = fabsf((float)pos[0] - (float)p[0]), dy = fabsf((float)pos[1] - (float)p[1]),
+                dz = fabsf((float)pos[2] - (float)p[2]);
+    const float yz = dy > dz ? dy : dz;
+    return 1 - (dx > yz ? dx : yz) / radius;
+}
+static float tool_strength(const hd_tool_overlay* o, const uint32_t p[3])
+{
+    switch (o->tool) {
+    case HD_OVERLAY_SPHERE:
+    case HD_OVERLAY_SPHERE_PAINT:
+    case HD_OVERLAY_SPHERE_NOISE:
+        return sphere_strength(o->position, p, o->radius);
+    case HD_OVERLAY_CUBE:
+        return cube_strength(o->position, p, o->radius);
+    default: {
+        const float a = sphere_strength(o->copy_source, p, 3), b = sphere_strength(o->copy_dest, p, 3);
+        const float m = a > b ? a : b, c = cube_strength(o->position, p, o->radius);
+        return m > c ? m : c;
+    }
+    }
+}
+static uint32_t overlay(const hd_trace_colors_params* q, float strength, uint32_t color)
+{
+    if (q->overlay.enabled && strength > 0) {
+        const f3 a = {(float)((color >> 0) & 0xFF) / 255.0f, (float)((color >> 8) & 0xFF) / 255.0f,
+                      (float)((color >> 16) & 0xFF) / 255.0f};
+        const float f = clampf(100 * strength, 0.f, .5f);
+        color = or_f3_to_rgb888(a.x * (1 - f) + 1 * f, a.y * (1 - f) + 0 * f, a.z * (1 - f) + 0 * f);
+    }
+    return color;
+}
+/* Tracer::trace_colors (tracer.cu:254-451) for one hit path */
+static uint32_t trace_color(const or_table* t, const or_colors* col, const uint32_t p[3],
+                            const hd_trace_colors_params* q)
+{
+    if (!(p[0] | p[1] | p[2]))
+        return or_f3_to_rgb888(187 / 255.f, 242 / 255.f, 250 / 255.f);
+    const float s = q->overlay.enabled ? tool_strength(&q->overlay, p) : 0.f;
+    const float b = (float)((p[0] ^ p[1] ^ p[2]) & 1u);
+    const uint32_t invalid = overlay(q, s, or_f3_to_rgb888(1, b, 1.f - b));
+    const uint32_t D = t->cfg.depth, T = t->cfg.color_tree_levels, leafl = t->leaf_level;
+    const int tree_debug = q->debug_colors == HD_DEBUG_INDEX || q->debug_colors == HD_DEBUG_POSITION ||
+                           q->debug_colors == HD_DEBUG_COLOR_TREE;
+    uint64_t nof = 0;
+    uint32_t debug_index = 0, cn = 0;
+    const or_leaf* leaf = NULL;
+    uint32_t index = t->root;
+    for (uint32_t level = 0; level < leafl;) {
+        level++;
+        const uint32_t* node = sys_ptr(t, index);
+        const uint32_t mask = node[0] & 0xffu;
+        const uint32_t sh = D - level;
+        const uint32_t child = (((p[0] >> sh) & 1) << 2) | (((p[1] >> sh) & 1) << 1) | ((p[2] >> sh) & 1);
+        if (!(mask & (1u << child)))
+            return overlay(q, s, 0xFF00FFu);
+        if (level - 1 < T) {
+            cn = col->nodes[cn + child];
+            if (level == T)
+                leaf = (cn & LEAF_FLAG) ? &col->leaves[cn & ~LEAF_FLAG] : NULL;
+            else if (!cn)
+                return invalid;
+        }
+        if (tree_debug) {
+            if (q->debug_colors == HD_DEBUG_INDEX && q->debug_level == level - 1)
+                debug_index = index;
+            if (level == leafl) {
+                if (q->debug_level == leafl)
+                    debug_index = node[child_offset(mask, child)];
+                if (q->debug_colors == HD_DEBUG_INDEX)
+                    return overlay(q, s, or_murmurhash32(debug_index));
+                if (q->debug_colors == HD_DEBUG_POSITION) {
+                    float c = (float)((p[0] ^ p[1] ^ p[2]) & 0x7FFu) / (float)0x7FF;
+                    c = (float)(((double)c + 0.5) / 2);
+                    return overlay(q, s, (index & LEAF_FLAG) ? or_f3_to_rgb888(c, 0, 0) : or_f3_to_rgb888(c, c, c));
+                }
+                const uint32_t off = D - T;
+                const float c = (float)(((p[0] >> off) ^ (p[1] >> off) ^ (p[2] >> off)) & 1u);
+                return overlay(q, s, or_f3_to_rgb888(c, c, c));
+            }
+            index = node[child_offset(mask, child)];
+            continue;
+        }
+        if (level == leafl) {
+            for (uint32_t cb = 0; cb < child; cb++)
+                if (mask & (1u << cb)) {
+                    const uint32_t* lp = sys_ptr(t, node[child_offset(mask, cb)]);
+                    nof += popc32(lp[0]) + popc32(lp[1]);
+                }
+            const uint32_t* lp = sys_ptr(t, node[child_offset(mask, child)]);
+            const uint64_t bits = (uint64_t)lp[0] | ((uint64_t)lp[1] << 32);
+            const uint32_t bi = ((p[0] & 1) ? 4 : 0) | ((p[1] & 1) ? 2 : 0) | ((p[2] & 1) ? 1 : 0) |
+                                ((p[0] & 2) ? 32 : 0) | ((p[1] & 2) ? 16 : 0) | ((p[2] & 2) ? 8 : 0);
+            nof += popc64(bits & ((1ull << bi) - 1));
+            break;
+        }
+        if (level > T)
+            for (uint32_t cb = 0; cb < child; cb++)
+                if (mask & (1u << cb))
+                    nof += sys_ptr(t, node[child_offset(mask, cb)])[0] >> 8;
+        index = node[child_offset(mask, child)];
+    }
+    if (!leaf || !leaf_valid_index(leaf, nof))
+        return invalid;
+    const hd_color k = leaf_color(leaf, nof);
+    switch (q->debug_colors) {
+    case HD_DEBUG_COLOR_BITS:
+        return overlay(q, s, 0u); /* get_debug_hash without COLOR_DEBUG */
+    case HD_DEBUG_MIN_COLOR: {
+        const f3 c = rgb565_to_f3((uint16_t)(k.color_bits & 0xFFFF));
+        return overlay(q, s, or_f3_to_rgb888(c.x, c.y, c.z));
+    }
+    case HD_DEBUG_MAX_COLOR: {
+        const f3 c = rgb565_to_f3((uint16_t)((k.color_bits >> 16) & 0xFFFF));
+        return overlay(q, s, or_f3_to_rgb888(c.x, c.y, c.z));
+    }
+    case HD_DEBUG_WEIGHT: {
+        const float w = k.bits_per_weight ? (float)k.weight / (float)((1 << k.bits_per_weight) - 1) : 0.f;
+        return overlay(q, s, or_f3_to_rgb888(w, w, w));
+    }
+    default:
+        return overlay(q, s, or_color_rgb888(k));
+    }
+}
+/* the colours of a paths image (uint4 per pixel) */
+void or_trace_colors(const or_table* t, const or_colors* col, const uint32_t* paths, uint64_t n,
+                     const hd_trace_colors_params* params, uint32_t* rgba)
+{
+    hd_trace_colors_params q;
+    memset(&q, 0, sizeof(q));
+    if (params)
+        q = *params;
+    for (uint64_t i = 0; i < n; i++)
+        rgba[i] = trace_color(t, col, paths + 4 * i, &q);
+}
+
 static void push_frame(struct frame** stack, uint64_t* n, uint64_t* cap, struct frame f)
 {
     if (*n == *cap) {

@@ -103,6 +103,9 @@ int or_edit_colored(or_table* t, or_colors* c, const hd_edit* e, hd_edit_stats* 
 int or_undo(or_table* t, or_colors* c); /* 1 if a frame was applied */
 int or_redo(or_table* t, or_colors* c);
 void or_colors_stats(const or_colors* c, uint64_t* out);
+/* Tracer::trace_colors of a paths image (uint4 per pixel) */
+void or_trace_colors(const or_table* t, const or_colors* c, const uint32_t* paths, uint64_t n,
+                     const hd_trace_colors_params* params, uint32_t* rgba);
 /* FastNoise's GetPerlinFractal (FBM, quintic, lacunarity 2, gain 0.5) */
 float or_perlin_fractal(int seed, float frequency, int octaves, float x, float y, float z);
 /* The BasicDAGCompressedColors shipped beside a BasicDAG (enclosedLeaves and

@@ -137,6 +137,9 @@ def lib():
         L.or_voxel_color.argtypes = [u64, u32, u32, u32]
         L.or_color_rgb888.restype = u32
         L.or_color_rgb888.argtypes = [HdColor]
+        L.or_f3_to_rgb888.restype = u32
+        L.or_f3_to_rgb888.argtypes = [C.c_float, C.c_float, C.c_float]
+        L.or_trace_colors.argtypes = [P, P, pu32, u64, P, np.ctypeslib.ndpointer(np.uint32, flags="C")]
         L.or_perlin_fractal.restype = C.c_float
         L.or_perlin_fractal.argtypes = [C.c_int, C.c_float, C.c_int, C.c_float, C.c_float, C.c_float]
         PP = C.POINTER(C.c_void_p)
@@ -341,6 +344,15 @@ class Colors:
         if r:
             raise RuntimeError(f"edit failed {r}")
         return s
+
+    def trace_colors(self, paths, params=None):
+        """Tracer::trace_colors of a paths image (h x w x 4 uint32);
+        params: a ctypes hd_trace_colors_params (or None: the plain view)."""
+        p = np.ascontiguousarray(paths, np.uint32).reshape(-1, 4)
+        out = np.zeros(len(p), np.uint32)
+        lib().or_trace_colors(self.t.h, self.h, p.reshape(-1), len(p), C.byref(params) if params is not None else None,
+                              out)
+        return out
 
     def undo(self):
         return bool(lib().or_undo(self.t.h, self.h))
