@@ -28,7 +28,9 @@ batched (hd_edit_batch, autotuned): edited voxels/s, find-or-add/s, p50/p99
 per-edit device latency of both forms, and the oracle's single-thread CPU
 editor on a bounded sample of the same edits.
 "colors": the 2^15 shell scene with colours, 512 paints, 32 copies of 256^3
-regions, one GC.  "serving": a Poisson request trace on the 2^16 coloured
+regions, one GC.  "tools_files": noise spheres and flood fills, the colour
+view of a frame, snapshot and BasicDAG file round trips, a replay.
+"serving": a Poisson request trace on the 2^16 coloured
 scene, sequential vs continuous policy (p50/p99 edit and frame latency,
 edited voxels/s).
 """
@@ -374,6 +376,90 @@ def colors_bench(args):
     return out
 
 
+def tools_files_bench(args):
+    """The rest of the edit tools, colour views, files and replays on the 2^15
+    shell scene with colours: 64 noise spheres (radius log-uniform in
+    [8, 64]) and 32 flood fills (radius in [8, 48]) through hd_edit_apply;
+    trace_colors of a 1920x1080 frame; a snapshot and a BasicDAG file
+    written and read back; a 32-frame replay (2 sphere edits a frame)."""
+    import tempfile
+    import hashdag_gb300 as hd
+    from hashdag_gb300 import workloads
+    depth = args.depth
+    d = hd.HashDAG(depth)
+    d.generate_scene(workloads.SEED_SCENE, shell=True)
+    d.colors_from_scene(workloads.SEED_COLORS)
+    out = {"workload": f"noise_fill_files_replay_d{depth}_shell"}
+    lat = {7: [], 8: []}
+    vox = {7: 0, 8: 0}
+    wall = {7: 0.0, 8: 0.0}
+    for e in workloads.noise_fill_edits(depth):
+        t0 = time.perf_counter()
+        s = d.edit_threads(hd.editor_from_tuple(e))
+        wall[e[0]] += time.perf_counter() - t0
+        lat[e[0]].append(s.device_ms)
+        vox[e[0]] += s.num_voxels
+    for tool, name in ((7, "noise"), (8, "fill")):
+        out[name] = {"n": len(lat[tool]), "p50_ms": _pct(lat[tool], 50), "p99_ms": _pct(lat[tool], 99),
+                     "voxels_per_s": vox[tool] / max(1e-9, wall[tool]), "latency": "device time per edit"}
+    # colour views
+    W, H = 1920, 1080
+    tr = hd.DAGTracer(W, H)
+    cam = workloads.orbit_camera(depth, W, H)
+    tr.resolve_paths(cam, d)
+    tr.resolve_colors(d)
+    d.sync()
+    t0 = time.perf_counter()
+    for _ in range(8):
+        tr.resolve_colors(d)
+    d.sync()
+    out["trace_colors_mpixels_per_s"] = 8 * W * H / (time.perf_counter() - t0) / 1e6
+    # files
+    tmp = tempfile.mkdtemp()
+    snap = os.path.join(tmp, "scene.snapshot")
+    t0 = time.perf_counter()
+    d.save_snapshot(snap)
+    t1 = time.perf_counter()
+    size = os.path.getsize(snap)
+    e = hd.HashDAG(depth)
+    t2 = time.perf_counter()
+    e.load_snapshot(snap)
+    e.sync()
+    t3 = time.perf_counter()
+    assert e.firstNodeIndex == d.firstNodeIndex
+    e.free()
+    basic = os.path.join(tmp, "scene.basic_dag.dag.bin")
+    t4 = time.perf_counter()
+    d.save_dag_to_file(basic)
+    t5 = time.perf_counter()
+    f = hd.HashDAG(depth)
+    t6 = time.perf_counter()
+    f.load_dag_from_file(basic)
+    f.sync()
+    t7 = time.perf_counter()
+    f.free()
+    out["snapshot"] = {"bytes": size, "save_s": t1 - t0, "load_s": t3 - t2, "save_gb_per_s": size / (t1 - t0) / 1e9,
+                       "load_gb_per_s": size / (t3 - t2) / 1e9}
+    bsize = os.path.getsize(basic)
+    out["basic_dag_file"] = {"bytes": bsize, "save_s": t5 - t4, "load_and_import_s": t7 - t6}
+    for p in (snap, basic):
+        os.remove(p)
+    os.rmdir(tmp)
+    # replay
+    r = hd.ReplayManager(text=workloads.replay_text(depth, 32))
+    frames, edits = 0, 0
+    t0 = time.perf_counter()
+    while not r.at_end():
+        cam_f, n = r.replay_frame(d, 16, W, H, ((0, 0, 0), (100, 100, 100)))
+        frames += 1
+        edits += n
+    d.sync()
+    dt = time.perf_counter() - t0
+    out["replay"] = {"frames": frames, "edits": edits, "frames_per_s": frames / dt, "edits_per_s": edits / dt}
+    d.free()
+    return out
+
+
 def serving_bench(args):
     """Serving loop: the 2^16 shell scene with colours (2^17 does not fit the
     table's 32-bit virtual addresses), a Poisson trace (70% sphere carve /
@@ -580,9 +666,10 @@ def run_gpu(args, dist):
                 edits["cpu_baseline"] = edit_cpu_baseline(args, tuples)
             except Exception as e:  # reported, never required
                 edits["cpu_baseline"] = {"value": None, "sample": f"failed: {e}"}
-    colors = serving = None
+    colors = serving = tools = None
     if not args.no_colors:
         colors = colors_bench(args)
+        tools = tools_files_bench(args)
     if not args.no_serving:
         serving = serving_bench(args)
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": dist.world, "steps": K,
@@ -598,7 +685,7 @@ def run_gpu(args, dist):
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": V * C.sizeof(_capi.Camera),
                     "d2h_bytes_per_step": V * (W * H * 16 + W * H)},
             "gpu_launches": 2 * K, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "wall_s": wall, "edits": edits, "colors": colors, "serving": serving}
+            "wall_s": wall, "edits": edits, "colors": colors, "tools_files": tools, "serving": serving}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dag.free()

@@ -331,7 +331,7 @@ extern "C" hd_status hd_serve(hd_ctx* c, const hd_request* reqs, uint32_t n, con
             return HD_ERR_INVALID;
         if (reqs[i].kind == HD_REQ_RENDER && (!reqs[i].width || !reqs[i].height))
             return HD_ERR_INVALID;
-        if (reqs[i].kind == HD_REQ_EDIT && (reqs[i].edit.tool > HD_TOOL_COPY || !(reqs[i].edit.radius >= 0.0f)))
+        if (reqs[i].kind == HD_REQ_EDIT && (reqs[i].edit.tool > HD_TOOL_FILL || !(reqs[i].edit.radius >= 0.0f)))
             return HD_ERR_INVALID;
     }
     try {

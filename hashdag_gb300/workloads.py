@@ -158,6 +158,47 @@ def paint_copy_edits(depth, n_paint=512, n_copy=32, paint_r=(8.0, 256.0), copy_r
     return out
 
 
+def noise_fill_edits(depth, n_noise=64, n_fill=32, noise_r=(8.0, 64.0), fill_r=(8.0, 48.0), seed=SEED_EDITS):
+    """Noise spheres (SphereNoiseEditor adding, radius log-uniform in noise_r)
+    centred on surface voxels, then flood fills (radius log-uniform in
+    fill_r) started 3 voxels above surface voxels.  Tuples (tool, centre,
+    radius); tools 7 (noise, adding) and 8 (fill)."""
+    rng = np.random.default_rng(seed + 200)
+    c = _centres(depth, n_noise + n_fill, rng)
+    out = []
+    lr = rng.uniform(math.log(noise_r[0]), math.log(noise_r[1]), n_noise)
+    for i in range(n_noise):
+        out.append((7, tuple(float(np.float32(v)) for v in c[i]), float(np.float32(math.exp(lr[i])))))
+    lf = rng.uniform(math.log(fill_r[0]), math.log(fill_r[1]), n_fill)
+    for i in range(n_fill):
+        p = c[n_noise + i] + np.array([0.0, 3.0, 0.0])
+        out.append((8, tuple(float(np.float32(v)) for v in p), float(np.float32(math.exp(lf[i])))))
+    return out
+
+
+def replay_text(depth, n_frames, edits_per_frame=2, replay_depth=16, seed=SEED_EDITS):
+    """A replay in the reference's CSV format (replay.h): n_frames frames,
+    each a camera pose and edits_per_frame sphere carves / fills, positions
+    and radii recorded at replay_depth (scaled to depth on replay)."""
+    rng = np.random.default_rng(seed + 300)
+    s = float(1 << replay_depth) / float(1 << depth)
+    c = _centres(depth, n_frames * edits_per_frame, rng)
+    lines = []
+    for f in range(n_frames):
+        a = 2 * math.pi * f / max(1, n_frames)
+        lines.append("SetLocation,%f,%f,%f" % (50 + 80 * math.cos(a), 70.0, 50 + 80 * math.sin(a)))
+        fwd = _norm(np.array([50.0, 50.0, 50.0]) - np.array([50 + 80 * math.cos(a), 70.0, 50 + 80 * math.sin(a)]))
+        right = _norm(np.cross(fwd, [0.0, 1.0, 0.0]))
+        up = np.cross(right, fwd)
+        lines.append("SetRotation," + ",".join("%f" % v for v in list(-right) + list(up) + list(fwd)))
+        for k in range(edits_per_frame):
+            p = c[f * edits_per_frame + k] * s
+            r = float(rng.uniform(8, 48)) * s
+            lines.append("EditSphere,%f,%f,%f,%f,%s" % (p[0], p[1], p[2], r, "true" if k % 2 else "false"))
+        lines.append("EndFrame")
+    return "\n".join(lines) + "\n"
+
+
 RESOLUTIONS = ((1280, 720), (1920, 1080), (3840, 2160))
 
 
