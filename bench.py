@@ -13,9 +13,10 @@ one launch.  Metric: Mrays/s (primary + shadow).
 
 value  = device throughput (CUDA events around each step's call; L2
          flushed with a 512 MB write before every timed step).
-e2e    = the same metric through the C ABI with host buffers: camera from
-         host memory, paths + shadow mask copied back to pinned host memory
-         every step.
+e2e    = the same metric through the C ABI with host buffers
+         (hd_trace_views_host): cameras from host memory, every view's paths
+         and shadow mask in pinned host memory every step (the primary
+         kernel writes the paths there over NVLink-C2C; the mask is copied).
 --impl reference times the oracle's CPU restatement of the reference tracer
 (the reference has no CPU tracer) on all host cores, a bounded band of rows
 per step.  Under torchrun every rank renders its own poses on its own GPU
@@ -62,6 +63,8 @@ def parse():
     p.add_argument("--width", type=int, default=1920)
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--poses", type=int, default=64)
+    p.add_argument("--e2e-chunk", type=int, default=0,
+                   help="views per chunk of the end-to-end call (0: paths written straight to host memory)")
     p.add_argument("--views", type=int, default=16, help="poses traced per step (one primary and one shadow launch)")
     p.add_argument("--ref-rows", type=int, default=192, help="rows per step of the CPU reference arm")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the traversal cpu_baseline sample")
@@ -622,17 +625,18 @@ def run_gpu(args, dist):
     t0 = time.perf_counter()
     for k in range(K):
         flush.fill_(k & 0xff)
-        launch(k)
-        h_paths.copy_(paths, non_blocking=True)
-        h_mask.copy_(mask, non_blocking=True)
         torch.cuda.synchronize()
+        # hd_trace_views_host: the views in chunks, each chunk's copies to the
+        # pinned host buffers overlapping the next chunk's traversal
+        dag._check(L.hd_trace_views_host(h, step_arrays[k], V, W, H, h_paths.data_ptr(), light, BIAS,
+                                         h_mask.data_ptr(), args.e2e_chunk, None))
     e2e_s = dist.max(time.perf_counter() - t0)
     # the L2 flush is not part of the traversal: time it alone and take it out
     torch.cuda.synchronize()
     f0 = time.perf_counter()
     for k in range(K):
         flush.fill_(k & 0xff)
-    torch.cuda.synchronize()
+        torch.cuda.synchronize()
     flush_s = time.perf_counter() - f0
     e2e_value = rays_all / max(1e-9, e2e_s - flush_s) / 1e6
 
@@ -683,7 +687,9 @@ def run_gpu(args, dist):
                        "scene_nodes": int(sum(lstats.nodes[:depth - 1])),
                        "parallelism": f"replicas x{dist.world}"},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": V * C.sizeof(_capi.Camera),
-                    "d2h_bytes_per_step": V * (W * H * 16 + W * H)},
+                    "d2h_bytes_per_step": V * (W * H * 16 + W * H), "api": "hd_trace_views_host",
+                    "paths": ("written by the primary kernel into the pinned host buffer (NVLink-C2C)"
+                              if not args.e2e_chunk else f"copied in chunks of {args.e2e_chunk} views")},
             "gpu_launches": 2 * K, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "wall_s": wall, "edits": edits, "colors": colors, "tools_files": tools, "serving": serving}
     if dist.rank == 0:

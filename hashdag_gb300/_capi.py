@@ -167,6 +167,8 @@ SIGNATURES = [
                                  C.POINTER(_f32), C.POINTER(_f32)]),
     ("hd_trace_views", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _u32, _P, C.POINTER(_f32), _f32, _P,
                                  C.POINTER(_f32)]),
+    ("hd_trace_views_host", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, _u32, _P, C.POINTER(_f32), _f32, _P, _u32,
+                                      C.POINTER(_f32)]),
     ("hd_trace_counters", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, C.POINTER(_f32), _f32, _P, _P,
                                     C.POINTER(_u64)]),
     ("hd_trace_counters_noalloc", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, C.POINTER(_f32), _f32, _P, _P,

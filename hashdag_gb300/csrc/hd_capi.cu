@@ -1,6 +1,8 @@
 // The C ABI (include/hashdag_gb300.h): status codes instead of aborts, one
 // context per table, all work on the context's stream.
+#include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <functional>
 #include <cstring>
 #include <new>
@@ -123,6 +125,11 @@ hd_status hd_destroy(hd_ctx* c)
     cudaFree(c->t.level_nodes);
     cudaFree(c->d_root);
     cudaFree(c->d_basic);
+    if (c->copy_stream)
+        cudaStreamDestroy(c->copy_stream);
+    for (cudaEvent_t e : {c->ev_traced[0], c->ev_traced[1], c->ev_copied[0], c->ev_copied[1]})
+        if (e)
+            cudaEventDestroy(e);
     if (c->ev0)
         cudaEventDestroy(c->ev0);
     if (c->ev1)
@@ -254,6 +261,85 @@ hd_status hd_trace_views(hd_ctx* c, const hd_camera* cams, uint32_t n_views, uin
             HD_CUDA(cudaEventElapsedTime(ms, c->ev0, c->ev_mid));
             HD_CUDA(cudaEventElapsedTime(ms + 1, c->ev_mid, c->ev1));
         }
+    });
+}
+
+hd_status hd_trace_views_host(hd_ctx* c, const hd_camera* cams, uint32_t n_views, uint32_t width, uint32_t height,
+                              uint32_t* h_paths, const float* light, float bias, uint8_t* h_mask,
+                              uint32_t chunk_views, float* ms)
+{
+    if (!c || !cams || !n_views || !width || !height || !h_paths || !light || !h_mask)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        const auto t0 = std::chrono::steady_clock::now();
+        const uint64_t frame = uint64_t(width) * height;
+        // Pinned host memory the device can address (Grace's NVLink-C2C):
+        // the primary rays write their paths straight into it, and only the
+        // shadow mask is copied.
+        cudaPointerAttributes attr{};
+        void* direct = nullptr;
+        if (cudaPointerGetAttributes(&attr, h_paths) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+            attr.devicePointer)
+            direct = attr.devicePointer;
+        cudaGetLastError();
+        if (direct && !chunk_views) {
+            if (frame * n_views >= 0xFFFFFFFFull)
+                throw StatusError{HD_ERR_INVALID, "views x width x height must stay below 2^32 pixels"};
+            hd_camera* d_cams = c->scratch.get<hd_camera>("views_cams", n_views);
+            uint8_t* d_mask = c->scratch.get<uint8_t>("vh_mask_direct", frame * n_views);
+            HD_CUDA(cudaMemcpyAsync(d_cams, cams, sizeof(hd_camera) * n_views, cudaMemcpyHostToDevice, c->stream));
+            trace_views(c, d_cams, n_views, width, height, static_cast<uint32_t*>(direct), light, bias, d_mask);
+            HD_CUDA(cudaMemcpyAsync(h_mask, d_mask, frame * n_views, cudaMemcpyDeviceToHost, c->stream));
+            HD_CUDA(cudaStreamSynchronize(c->stream));
+            if (ms)
+                *ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            return;
+        }
+        const uint32_t chunk = std::min(n_views, chunk_views ? chunk_views : std::max(1u, (n_views + 1) / 2));
+        if (frame * chunk >= 0xFFFFFFFFull)
+            throw StatusError{HD_ERR_INVALID, "views x width x height must stay below 2^32 pixels per chunk"};
+        if (!c->copy_stream)
+            HD_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        for (auto* e : {&c->ev_traced[0], &c->ev_traced[1], &c->ev_copied[0], &c->ev_copied[1]})
+            if (!*e)
+                HD_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        // two sets of device buffers: chunk k traces into set k % 2 while the
+        // copy stream brings chunk k - 1 back
+        uint32_t* d_paths[2];
+        uint8_t* d_mask[2];
+        uint32_t* d_list[2];
+        hd_camera* d_cams[2];
+        for (int b = 0; b < 2; b++) {
+            char nm[32];
+            snprintf(nm, sizeof(nm), "vh_paths_%d", b);
+            d_paths[b] = c->scratch.get<uint32_t>(nm, frame * chunk * 4);
+            snprintf(nm, sizeof(nm), "vh_mask_%d", b);
+            d_mask[b] = c->scratch.get<uint8_t>(nm, frame * chunk);
+            snprintf(nm, sizeof(nm), "vh_list_%d", b);
+            d_list[b] = c->scratch.get<uint32_t>(nm, shadow_list_words(frame * chunk));
+            snprintf(nm, sizeof(nm), "vh_cams_%d", b);
+            d_cams[b] = c->scratch.get<hd_camera>(nm, chunk);
+        }
+        uint32_t k = 0;
+        for (uint32_t v0 = 0; v0 < n_views; v0 += chunk, k++) {
+            const uint32_t nv = std::min(chunk, n_views - v0);
+            const int b = int(k & 1);
+            if (k >= 2) // the copies out of this buffer set are done
+                HD_CUDA(cudaStreamWaitEvent(c->stream, c->ev_copied[b], 0));
+            HD_CUDA(cudaMemcpyAsync(d_cams[b], cams + v0, sizeof(hd_camera) * nv, cudaMemcpyHostToDevice, c->stream));
+            trace_views(c, d_cams[b], nv, width, height, d_paths[b], light, bias, d_mask[b], c->stream, d_list[b]);
+            HD_CUDA(cudaEventRecord(c->ev_traced[b], c->stream));
+            HD_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_traced[b], 0));
+            HD_CUDA(cudaMemcpyAsync(h_paths + uint64_t(v0) * frame * 4, d_paths[b], frame * nv * 16,
+                                    cudaMemcpyDeviceToHost, c->copy_stream));
+            HD_CUDA(cudaMemcpyAsync(h_mask + uint64_t(v0) * frame, d_mask[b], frame * nv, cudaMemcpyDeviceToHost,
+                                    c->copy_stream));
+            HD_CUDA(cudaEventRecord(c->ev_copied[b], c->copy_stream));
+        }
+        HD_CUDA(cudaStreamSynchronize(c->copy_stream));
+        HD_CUDA(cudaStreamSynchronize(c->stream));
+        if (ms)
+            *ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     });
 }
 

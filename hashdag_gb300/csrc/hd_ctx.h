@@ -35,6 +35,10 @@ struct hd_ctx {
     uint32_t* d_basic = nullptr;
     uint64_t n_basic = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_mid = nullptr;
+    // hd_trace_views_host: the stream that copies results to the host and
+    // the events that pipeline it with the traversal
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_traced[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
     // bucket list heads of the edit path stay all-empty between calls
     bool edit_head_ready = false;
     uint32_t* edit_head_ptr = nullptr;

@@ -191,6 +191,17 @@ hd_status hd_trace_shadow(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uin
  * floats): device time of the primary launch and of the shadow pass. */
 hd_status hd_trace_views(hd_ctx* ctx, const hd_camera* cams, uint32_t n_views, uint32_t width, uint32_t height,
                          uint32_t* d_paths, const float* light, float bias, uint8_t* d_mask, float* ms);
+/* hd_trace_views with host buffers: cameras read from host memory, every
+ * view's paths (width * height * 4 uint32 each) and shadow mask written to
+ * host memory.  With chunk_views = 0 and h_paths in pinned memory the
+ * device can address, the primary rays write their paths straight into
+ * host memory (over NVLink-C2C on a Grace host) and only the mask is
+ * copied.  Otherwise the views are traced chunk_views at a time (0: half of
+ * them) and each chunk's copies run on a second stream while the next
+ * chunk is traced.  ms: wall time of the call. */
+hd_status hd_trace_views_host(hd_ctx* ctx, const hd_camera* cams, uint32_t n_views, uint32_t width, uint32_t height,
+                              uint32_t* h_paths, const float light[3], float bias, uint8_t* h_mask,
+                              uint32_t chunk_views, float* ms);
 /* Primary + shadow in one call: the per-frame traversal step. */
 hd_status hd_trace_frame(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint32_t height,
                          const float light[3], float bias, uint32_t* d_paths, uint8_t* d_mask,

@@ -170,3 +170,31 @@ def test_trace_views_equals_single_views(gpu):
         assert np.array_equal(got_m, tr.get_shadows()), v
     assert ms[0] > 0 and ms[1] > 0
     d.free()
+
+
+@pytest.mark.parametrize("chunk", [0, 1, 3])
+def test_trace_views_host_equals_device_views(gpu, chunk):
+    """hd_trace_views_host (chunks of views, copies to host memory on a
+    second stream) gives every view's paths and mask exactly as
+    hd_trace_views does on device buffers."""
+    import ctypes as C
+
+    import torch
+    depth, W, H, V = 10, 160, 96, 5
+    dag = hd.HashDAG(depth)
+    dag.generate_scene(workloads.SEED_SCENE)
+    poses = workloads.catmull_rom_path(depth, V, W, H)
+    cams = (hd._capi.Camera * V)(*[hd._capi.Camera.from_params(p) for p in poses])
+    light = (C.c_float * 3)(*LIGHT_BENCH)
+    L = hd._capi.lib()
+    d_paths = torch.zeros(V * W * H * 4, dtype=torch.int32, device="cuda")
+    d_mask = torch.zeros(V * W * H, dtype=torch.uint8, device="cuda")
+    ms = (C.c_float * 2)()
+    dag._check(L.hd_trace_views(dag.handle, cams, V, W, H, d_paths.data_ptr(), light, 1.0, d_mask.data_ptr(), ms))
+    h_paths = torch.full((V * W * H * 4,), -1, dtype=torch.int32, pin_memory=True)
+    h_mask = torch.full((V * W * H,), 7, dtype=torch.uint8, pin_memory=True)
+    dag._check(L.hd_trace_views_host(dag.handle, cams, V, W, H, h_paths.data_ptr(), light, 1.0, h_mask.data_ptr(),
+                                     chunk, None))
+    assert torch.equal(h_paths, d_paths.cpu())
+    assert torch.equal(h_mask, d_mask.cpu())
+    dag.free()
