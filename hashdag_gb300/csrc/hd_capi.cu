@@ -346,10 +346,15 @@ hd_status hd_trace_views_host(hd_ctx* c, const hd_camera* cams, uint32_t n_views
 hd_status hd_trace_frame(hd_ctx* c, const hd_camera* cam, uint32_t w, uint32_t h, const float light[3], float bias,
                          uint32_t* d_paths, uint8_t* d_mask, float* ms_primary, float* ms_shadow)
 {
-    hd_status s = hd_trace_primary(c, cam, w, h, d_paths, ms_primary);
-    if (s != HD_OK)
-        return s;
-    return hd_trace_shadow(c, cam, w, h, d_paths, light, bias, d_mask, ms_shadow);
+    // one view of hd_trace_views; ms_primary covers the primary rays with
+    // the shadow-ray list they build
+    float ms[2] = {0, 0};
+    const hd_status s = hd_trace_views(c, cam, 1, w, h, d_paths, light, bias, d_mask, ms);
+    if (ms_primary)
+        *ms_primary = ms[0];
+    if (ms_shadow)
+        *ms_shadow = ms[1];
+    return s;
 }
 
 hd_status hd_trace_counters(hd_ctx* c, const hd_camera* cam, uint32_t w, uint32_t h, const float light[3],

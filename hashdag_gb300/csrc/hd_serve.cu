@@ -70,7 +70,8 @@ struct Slot {
     uint8_t* mask = nullptr;
     uint32_t* rgba = nullptr;
     uint32_t* root = nullptr;
-    uint32_t* list = nullptr; // hit pixels of the shadow pass
+    uint32_t* list = nullptr; // the shadow-ray list
+    hd_camera* cam = nullptr; // the frame's camera on the device
     unsigned long long* sum = nullptr;
     unsigned long long* h_sum = nullptr; // pinned
     cudaEvent_t colors_done = nullptr, done = nullptr;
@@ -130,6 +131,8 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
         s.root = c->scratch.get<uint32_t>(nm, 1);
         snprintf(nm, sizeof(nm), "serve_list_%u", k);
         s.list = c->scratch.get<uint32_t>(nm, shadow_list_words(max_pixels));
+        snprintf(nm, sizeof(nm), "serve_cam_%u", k);
+        s.cam = c->scratch.get<hd_camera>(nm, 1);
         snprintf(nm, sizeof(nm), "serve_sum_%u", k);
         s.sum = c->scratch.get<unsigned long long>(nm, 1);
         HD_CUDA(cudaMallocHost(&s.h_sum, 8));
@@ -172,9 +175,11 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
             res[i].root = c->root;
             res[i].edits_before = edits_done;
             HD_CUDA(cudaMemcpyAsync(s.root, &c->root, 4, cudaMemcpyHostToDevice, s.stream));
-            trace_primary(c, r.camera, r.width, r.height, s.paths, nullptr, s.stream, s.root);
-            trace_shadow(c, r.camera, r.width, r.height, s.paths, cfg.light, cfg.shadow_bias, s.mask, nullptr,
-                         s.stream, s.root, s.list);
+            HD_CUDA(cudaMemcpyAsync(s.cam, &r.camera, sizeof(hd_camera), cudaMemcpyHostToDevice, s.stream));
+            // the frame as a one-view hd_trace_views: persistent primary
+            // warps building the shadow-ray list, then the shadow walks
+            trace_views(c, s.cam, 1, r.width, r.height, s.paths, cfg.light, cfg.shadow_bias, s.mask, s.stream, s.list,
+                        nullptr, s.root);
             if (c->colors)
                 trace_colors(c, s.paths, r.width, r.height, s.rgba, s.stream, s.root);
             HD_CUDA(cudaEventRecord(s.colors_done, s.stream));

@@ -193,12 +193,17 @@ HD_D uint32_t first_child_mask(uint32_t low, uint32_t high) // Leaf::get_first_c
 
 HD_D uint32_t next_child(uint32_t order, uint32_t mask) // next_child (tracer.cu:7-17)
 {
-    // first set bit of mask in the order child ^ order, child = 0..7
-    uint32_t permuted = 0;
-#pragma unroll
-    for (uint32_t c = 0; c < 8; c++)
-        permuted |= ((mask >> (c ^ order)) & 1u) << c;
-    return (__ffs(permuted) - 1) ^ order;
+    // first set bit of mask in the order child ^ order, child = 0..7: bit k
+    // of the permuted mask is bit k ^ order of mask, an XOR by order built
+    // from swaps of adjacent bits, bit pairs and nibbles
+    uint32_t m = mask;
+    if (order & 1)
+        m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (order & 2)
+        m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (order & 4)
+        m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+    return (__ffs(m) - 1) ^ order;
 }
 
 // The walk's stack: per level the node and its child mask | visit mask << 8.
