@@ -89,6 +89,7 @@ hd_status hd_create(const hd_config* cfg, hd_ctx** out)
         Table& t = c->t;
         t.g = c->g;
         HD_CUDA(cudaMalloc(&t.pool, size_t(conf.pool_pages) * HD_PAGE_SIZE * 4));
+        HD_CUDA(cudaMalloc(&t.bloom, size_t(conf.pool_pages) * kBloomWords * 4));
         HD_CUDA(cudaMalloc(&t.page_table, c->g.total_vpages * 4));
         HD_CUDA(cudaMalloc(&t.bucket_sizes, c->g.total_buckets * 4));
         HD_CUDA(cudaMalloc(&t.full_nodes, HD_MAX_DEPTH * 4));
@@ -117,6 +118,7 @@ hd_status hd_destroy(hd_ctx* c)
     hd::batch_release(c);
     hd::color_release(c);
     cudaFree(c->t.pool);
+    cudaFree(c->t.bloom);
     cudaFree(c->t.page_table);
     cudaFree(c->t.bucket_sizes);
     cudaFree(c->t.full_nodes);
@@ -513,6 +515,7 @@ hd_status hd_import_table(hd_ctx* c, const uint32_t* bs, const uint32_t* pt, con
         const uint32_t top = uint32_t(pool_words / HD_PAGE_SIZE);
         HD_CUDA(cudaMemcpyAsync(c->t.pool_top, &top, 4, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemcpyAsync(c->d_root, &root, 4, cudaMemcpyHostToDevice, st));
+        bloom_rebuild(c);
         HD_CUDA(cudaStreamSynchronize(st));
         c->root = root;
         c->needs_gc = false;

@@ -89,6 +89,7 @@ inline Geom make_geom(const hd_config& c)
 // reference's tracer does, tracer.cu:146).
 struct Table {
     uint32_t* pool;
+    uint32_t* bloom;        // kBloomWords per physical page (see bloom_*)
     uint32_t* page_table;
     uint32_t* bucket_sizes;
     uint32_t* full_nodes;   // [depth]
@@ -198,6 +199,25 @@ HD_HD uint64_t mix64(uint64_t z)
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     return z ^ (z >> 31);
 }
+
+// ---- per-page Bloom filters (hash_table.h:564-659, USE_BLOOM_FILTER) --------
+// Every physical page has a 512-bit filter holding 3 bits of every node
+// ever written into it; a bucket scan skips a page whose filter lacks a bit
+// of the node it looks for.  The filter can only say "maybe": a page that
+// holds the node always passes, so results never change, only the pages
+// read.  Bits come from a hash of the node's words independent of the
+// bucket hash.
+constexpr uint32_t kBloomWords = 16;
+constexpr uint32_t kBloomHashes = 3;
+HD_HD uint32_t bloom_bits(const uint32_t* q, uint32_t n)
+{
+    uint64_t h = 0x51ED2701F3A5C9B7ull ^ n;
+    for (uint32_t k = 0; k < n; k++)
+        h = mix64(h ^ q[k]);
+    // three 9-bit positions, packed
+    return uint32_t(h & 0x7FFFFFFu);
+}
+HD_HD uint32_t bloom_pos(uint32_t bits, uint32_t i) { return (bits >> (9 * i)) & 511u; }
 
 // Leaf bit of voxel (x, y, z) inside its 4x4x4 block (dag_utils.h:160-167).
 HD_HD uint32_t leaf_bit(uint32_t x, uint32_t y, uint32_t z)

@@ -102,6 +102,10 @@ void append_items(hd_ctx* c, uint32_t level, const uint32_t* content, uint64_t n
 // hd_scene.cu
 void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words, uint64_t* n_words);
 
+// hd_table.cu: Bloom filters of imported tables and of GC-rebuilt levels
+void bloom_rebuild(hd_ctx* c);
+void bloom_clear_level(hd_ctx* c, uint32_t level);
+
 // hd_io.cu: keeps a copy of the BasicDAG words (host or device pointer)
 void keep_basic(hd_ctx* c, const uint32_t* words, uint64_t n);
 

@@ -481,7 +481,7 @@ HD_D void stage_page(const uint32_t* src, uint32_t used, uint32_t* page, uint32_
 // last node when it holds q (compared by no scan until something follows).
 template <int PW>
 HD_D uint32_t scan_bucket(const Table& t, uint32_t vbase, uint32_t S, const uint32_t* q, uint32_t n, bool leaf,
-                          uint32_t* page, uint32_t* last_match, unsigned long long& scanned)
+                          uint32_t bloom, uint32_t* page, uint32_t* last_match, unsigned long long& scanned)
 {
     const uint32_t lane = threadIdx.x & 31;
     uint32_t found = kNotFound;
@@ -490,6 +490,8 @@ HD_D uint32_t scan_bucket(const Table& t, uint32_t vbase, uint32_t S, const uint
         const uint32_t page_end = S < pindex + kPage ? S : pindex + kPage;
         if (!leaf && pindex + n >= page_end)
             break; // "return 0xFFFFFFFF" of the reference scan
+        if (!bloom_may(t, vbase + pindex, bloom))
+            continue; // the page cannot hold q
         const uint32_t used = page_end - pindex;
         stage_page<PW>(t.sys_cg(vbase + pindex), used, page, lane);
         __syncwarp();
@@ -529,7 +531,8 @@ HD_D uint32_t scan_bucket(const Table& t, uint32_t vbase, uint32_t S, const uint
         scanned += found == kNotFound ? used : (found - pindex + n);
         __syncwarp();
     }
-    if (!leaf && found == kNotFound && S >= n && ((S - n) & ~(kPage - 1)) == ((S - 1) & ~(kPage - 1))) {
+    if (!leaf && found == kNotFound && S >= n && ((S - n) & ~(kPage - 1)) == ((S - 1) & ~(kPage - 1)) &&
+        bloom_may(t, vbase + ((S - n) & ~(kPage - 1)), bloom)) {
         // the bucket's last node ends at S; it holds q iff it starts at S - n
         // (nodes never straddle a page, so S - n lies in the tail's page)
         const uint32_t p = S - n;
@@ -585,12 +588,13 @@ HD_D bool foa_segment(const Table& t, uint32_t level, const Level& lv, const uin
             for (uint32_t k = 0; k < n; k++)
                 hit &= cache.words[lane][k] == q[k];
         const uint32_t hb = __ballot_sync(0xffffffffu, hit);
+        const uint32_t bloom = bloom_bits(q, n);
         uint32_t e;
         if (hb) {
             e = __ffs(hb) - 1;
         } else {
             uint32_t last_match;
-            const uint32_t f = scan_bucket<PW>(t, vbase, S, q, n, leaf, page, &last_match, scanned);
+            const uint32_t f = scan_bucket<PW>(t, vbase, S, q, n, leaf, bloom, page, &last_match, scanned);
             e = next_slot;
             next_slot = (next_slot + 1) % kCache;
             used_entries = used_entries < kCache ? used_entries + 1 : kCache;
@@ -624,6 +628,7 @@ HD_D bool foa_segment(const Table& t, uint32_t level, const Level& lv, const uin
                     uint32_t* dst = t.sys_rw(vbase + pos);
                     for (uint32_t k = 0; k < n; k++)
                         __stcg(dst + k, q[k]);
+                    bloom_add(t, vbase + pos, bloom);
                     result = pos;
                     S = size;
                     appended = 1;

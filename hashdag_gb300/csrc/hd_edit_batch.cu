@@ -796,6 +796,11 @@ void copy_table(hd_ctx* to, hd_ctx* from)
         HD_CUDA(cudaMemsetAsync(to->t.pool + uint64_t(top_from) * kPage, 0, uint64_t(top_to - top_from) * kPage * 4,
                                 st));
     HD_CUDA(cudaMemcpyAsync(to->t.pool, from->t.pool, uint64_t(top_from) * kPage * 4, cudaMemcpyDeviceToDevice, st));
+    if (top_to > top_from)
+        HD_CUDA(cudaMemsetAsync(to->t.bloom + uint64_t(top_from) * kBloomWords, 0,
+                                uint64_t(top_to - top_from) * kBloomWords * 4, st));
+    HD_CUDA(cudaMemcpyAsync(to->t.bloom, from->t.bloom, uint64_t(top_from) * kBloomWords * 4, cudaMemcpyDeviceToDevice,
+                            st));
     HD_CUDA(cudaMemcpyAsync(to->t.page_table, from->t.page_table, from->g.total_vpages * 4, cudaMemcpyDeviceToDevice,
                             st));
     HD_CUDA(cudaMemcpyAsync(to->t.bucket_sizes, from->t.bucket_sizes, from->g.total_buckets * 4,

@@ -160,9 +160,11 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots)
                                                       L < int32_t(leafl) ? newaddr[L + 1] : nullptr, content, head,
                                                       next, touched, d_n);
         HD_LAUNCH_CHECK();
-        // empty the level's buckets, then the full node first
+        // empty the level's buckets and their pages' filters, then the
+        // full node first
         HD_CUDA(cudaMemsetAsync(c->t.bucket_sizes + g.level_first_bucket(uint32_t(L)), 0,
                                 uint64_t(g.buckets(uint32_t(L))) * 4, st));
+        bloom_clear_level(c, uint32_t(L));
         HD_CUDA(cudaMemsetAsync(c->t.level_nodes + L, 0, 8, st));
         add_full_nodes(c, uint32_t(L), uint32_t(L));
         append_items(c, uint32_t(L), content, n, head, next, touched, d_n, newaddr[L]);

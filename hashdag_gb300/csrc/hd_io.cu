@@ -384,6 +384,7 @@ hd_status hd_load_snapshot(hd_ctx* c, const char* path, hd_dag_info* info)
         HD_CUDA(cudaMemcpyAsync(c->t.level_nodes, level_nodes.data(), HD_MAX_DEPTH * 8, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemcpyAsync(c->t.pool_top, &pool_top, 4, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemcpyAsync(c->d_root, &root, 4, cudaMemcpyHostToDevice, st));
+        bloom_rebuild(c);
         color_release(c);
         if (colors) {
             const uint64_t add[5] = {tops[0], tops[1], tops[2], tops[3], tops[4]};

@@ -49,6 +49,7 @@ __global__ void k_add_full_nodes(Table t, uint32_t first_level, uint32_t last_le
         uint32_t* dst = t.sys_rw(v);
         for (uint32_t i = 0; i < n; i++)
             dst[i] = node[i];
+        bloom_add(t, v, bloom_bits(node, n));
         *size_ptr = size;
         t.level_nodes[level] += 1;
         t.full_nodes[level] = v;
@@ -78,6 +79,7 @@ void table_reset(hd_ctx* c)
 {
     const Geom& g = c->g;
     HD_CUDA(cudaMemsetAsync(c->t.pool, 0, size_t(g.pool_pages) * kPage * 4, c->stream));
+    HD_CUDA(cudaMemsetAsync(c->t.bloom, 0, size_t(g.pool_pages) * kBloomWords * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.page_table, 0, g.total_vpages * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.bucket_sizes, 0, g.total_buckets * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.full_nodes, 0, HD_MAX_DEPTH * 4, c->stream));
@@ -227,6 +229,7 @@ __global__ void __launch_bounds__(32 * kAppendWarps)
             uint32_t* dst = t.sys_rw(v);
             for (uint32_t k = 0; k < n; k++)
                 dst[k] = src[k];
+            bloom_add(t, v, bloom_bits(src, n));
             out_addr[r] = v;
         }
         __syncwarp();
@@ -319,6 +322,66 @@ void import_basic_dag(hd_ctx* c, const uint32_t* d_words, uint64_t n_words)
     if (e)
         throw StatusError{hd_status(e == kErrCapacity ? HD_ERR_INVALID : e), "BasicDAG ingest failed"};
     c->root = read_scalar(c->d_root, st);
+}
+
+// Rebuilds the filters of a table written from outside (imports, snapshots)
+// by walking every bucket the way the scans do: leaves two words apart,
+// interior nodes by their sizes from each page's start.  Words past a page's
+// last node (the gap a node that did not fit leaves) are walked as nodes too,
+// which only adds bits, so a filter never misses a node it holds.
+__global__ void k_bloom_rebuild(Table t, uint32_t level)
+{
+    const Geom& g = t.g;
+    const bool leaf = level == g.leaf_level;
+    HD_GRID_STRIDE(b, uint64_t(g.buckets(level)))
+    {
+        const uint32_t S = t.bucket_sizes[g.bucket_global(level, uint32_t(b))];
+        const uint32_t vbase = g.make_ptr(level, uint32_t(b), 0);
+        for (uint32_t pindex = 0; pindex < S; pindex += kPage) {
+            const uint32_t used = S - pindex < kPage ? S - pindex : kPage;
+            const uint32_t* page = t.sys_cg(vbase + pindex);
+            for (uint32_t w = 0; w < used;) {
+                const uint32_t n = leaf ? 2 : total_size(page[w]);
+                if (w + n > used)
+                    break;
+                bloom_add(t, vbase + pindex + w, bloom_bits(page + w, n));
+                w += n;
+            }
+        }
+    }
+}
+
+void bloom_rebuild(hd_ctx* c)
+{
+    const Geom& g = c->g;
+    HD_CUDA(cudaMemsetAsync(c->t.bloom, 0, size_t(g.pool_pages) * kBloomWords * 4, c->stream));
+    for (uint32_t L = 0; L <= g.leaf_level; L++) {
+        k_bloom_rebuild<<<grid_for(g.buckets(L), 128), 128, 0, c->stream>>>(c->t, L);
+        HD_LAUNCH_CHECK();
+    }
+}
+
+__global__ void k_bloom_clear_level(Table t, uint32_t vp0, uint32_t vp1)
+{
+    HD_GRID_STRIDE(i, uint64_t(vp1 - vp0))
+    {
+        const uint32_t p = t.page_table[vp0 + i];
+        if (p)
+            for (uint32_t k = 0; k < kBloomWords; k++)
+                t.bloom[uint64_t(p) * kBloomWords + k] = 0;
+    }
+}
+
+// Empties the filters of every page of a level (GC rebuilds the level's
+// buckets in the same pages).
+void bloom_clear_level(hd_ctx* c, uint32_t level)
+{
+    const Geom& g = c->g;
+    const uint32_t vp0 = g.make_ptr(level, 0, 0) >> kPageShift;
+    const uint64_t words = uint64_t(g.buckets(level)) * g.capacity(level);
+    const uint32_t vp1 = uint32_t((uint64_t(g.make_ptr(level, 0, 0)) + words) >> kPageShift);
+    k_bloom_clear_level<<<grid_for(vp1 - vp0, 256), 256, 0, c->stream>>>(c->t, vp0, vp1);
+    HD_LAUNCH_CHECK();
 }
 
 } // namespace hd

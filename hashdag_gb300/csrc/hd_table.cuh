@@ -49,6 +49,34 @@ HD_D bool map_pages(const Table& t, uint32_t level, uint32_t bucket, uint32_t fr
     return true;
 }
 
+// The filter of the physical page behind virtual word v
+HD_D uint32_t* bloom_of(const Table& t, uint32_t v)
+{
+    return t.bloom + uint64_t(__ldcg(t.page_table + (v >> kPageShift))) * kBloomWords;
+}
+// Adds a node written at virtual word v to its page's filter
+HD_D void bloom_add(const Table& t, uint32_t v, uint32_t bits)
+{
+    uint32_t* f = bloom_of(t, v);
+#pragma unroll
+    for (uint32_t i = 0; i < kBloomHashes; i++) {
+        const uint32_t b = bloom_pos(bits, i);
+        atomicOr(f + (b >> 5), 1u << (b & 31));
+    }
+}
+// False when the page behind virtual word v cannot hold the node
+HD_D bool bloom_may(const Table& t, uint32_t v, uint32_t bits)
+{
+    const uint32_t* f = bloom_of(t, v);
+    bool may = true;
+#pragma unroll
+    for (uint32_t i = 0; i < kBloomHashes; i++) {
+        const uint32_t b = bloom_pos(bits, i);
+        may &= ((__ldcg(f + (b >> 5)) >> (b & 31)) & 1u) != 0;
+    }
+    return may;
+}
+
 // Pushes item i onto the list of bucket gb; the first item of a bucket also
 // records the bucket in `touched`.
 HD_D void link_item(uint32_t gb, uint32_t i, uint32_t* head, uint32_t* next, uint32_t* touched, uint32_t* n_touched)
