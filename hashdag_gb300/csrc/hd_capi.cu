@@ -90,7 +90,7 @@ hd_status hd_create(const hd_config* cfg, hd_ctx** out)
         t.g = c->g;
         HD_CUDA(cudaMalloc(&t.pool, size_t(conf.pool_pages) * HD_PAGE_SIZE * 4));
         HD_CUDA(cudaMalloc(&t.bloom, size_t(conf.pool_pages) * kBloomWords * 4));
-        HD_CUDA(cudaMalloc(&t.page_table, c->g.total_vpages * 4));
+        HD_CUDA(cudaMalloc(&t.page_table, kPageTableEntries * 4));
         HD_CUDA(cudaMalloc(&t.bucket_sizes, c->g.total_buckets * 4));
         HD_CUDA(cudaMalloc(&t.full_nodes, HD_MAX_DEPTH * 4));
         HD_CUDA(cudaMalloc(&t.pool_top, 4));
@@ -396,6 +396,14 @@ hd_status hd_set_root(hd_ctx* c, uint32_t root)
     if (!c)
         return HD_ERR_INVALID;
     return guarded(c, [&] {
+        uint32_t entry = 0;
+        if ((root >> kPageShift) < c->g.total_vpages) {
+            HD_CUDA(cudaMemcpyAsync(&entry, c->t.page_table + (root >> kPageShift), 4, cudaMemcpyDeviceToHost,
+                                    c->stream));
+            HD_CUDA(cudaStreamSynchronize(c->stream));
+        }
+        if (!valid_root(c->g, root, entry))
+            throw StatusError{HD_ERR_INVALID, "root " + std::to_string(root) + " is not on a mapped page"};
         HD_CUDA(cudaMemcpyAsync(c->d_root, &root, 4, cudaMemcpyHostToDevice, c->stream));
         HD_CUDA(cudaStreamSynchronize(c->stream));
         c->root = root;
@@ -453,7 +461,8 @@ hd_status hd_memory_stats(hd_ctx* c, uint64_t* out)
 {
     if (!c || !out)
         return HD_ERR_INVALID;
-    out[0] = uint64_t(c->cfg.pool_pages) * HD_PAGE_SIZE * 4 + c->g.total_vpages * 4 + c->g.total_buckets * 4;
+    out[0] = uint64_t(c->cfg.pool_pages) * HD_PAGE_SIZE * 4 + kPageTableEntries * 4 + c->g.total_buckets * 4 +
+             uint64_t(c->cfg.pool_pages) * kBloomWords * 4;
     const ColorTable& ct = c->ct;
     out[1] = ct.cap_nodes * 4 + ct.cap_leaves * sizeof(LeafDesc) + ct.cap_blocks * 8 + ct.cap_macros * 8 +
              ct.cap_weights * 4;
@@ -507,6 +516,7 @@ hd_status hd_import_table(hd_ctx* c, const uint32_t* bs, const uint32_t* pt, con
         return HD_ERR_INVALID;
     return guarded(c, [&] {
         cudaStream_t st = c->stream;
+        check_table(c->g, pt, bs, uint32_t(pool_words / HD_PAGE_SIZE), root, "the imported table");
         table_reset(c);
         HD_CUDA(cudaMemcpyAsync(c->t.bucket_sizes, bs, c->g.total_buckets * 4, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemcpyAsync(c->t.page_table, pt, c->g.total_vpages * 4, cudaMemcpyHostToDevice, st));

@@ -20,6 +20,11 @@ namespace hd {
 
 constexpr uint32_t kPage = HD_PAGE_SIZE;
 constexpr uint32_t kPageShift = 9;
+// Page-table entries allocated per context: one for every page of the 32-bit
+// virtual space, so that any node index, even one read from a corrupt or
+// foreign table, translates inside the page table (entries past the
+// geometry's pages stay 0, the never-used physical page 0).
+constexpr uint64_t kPageTableEntries = 1ull << (32 - kPageShift);
 constexpr uint32_t kInvalid = HD_INVALID_NODE;
 constexpr uint32_t kNotFound = 0xFFFFFFFFu;
 constexpr uint32_t kEmptyId = 0xFFFFFFFFu; // "no node" in scratch id arrays

@@ -104,6 +104,15 @@ void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words
 
 // hd_table.cu: Bloom filters of imported tables and of GC-rebuilt levels
 void bloom_rebuild(hd_ctx* c);
+
+// hd_table.cu: checks of a table written from outside (host arrays): every
+// mapped page lies below `top`, no bucket holds more than its capacity (bs
+// may be null) and the root is a node of a mapped page.  Throws
+// HD_ERR_INVALID naming `what`.
+void check_table(const Geom& g, const uint32_t* pt, const uint32_t* bs, uint32_t top, uint32_t root,
+                 const std::string& what);
+// The root is an address of a mapped page (pt_entry: its page-table entry)
+bool valid_root(const Geom& g, uint32_t root, uint32_t pt_entry);
 void bloom_clear_level(hd_ctx* c, uint32_t level);
 
 // hd_io.cu: keeps a copy of the BasicDAG words (host or device pointer)

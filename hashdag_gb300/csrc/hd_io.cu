@@ -330,9 +330,6 @@ hd_status hd_load_snapshot(hd_ctx* c, const char* path, hd_dag_info* info)
         std::vector<uint32_t> pool(uint64_t(pool_top) * kPage), pt(pt_size);
         in.read(pool.data(), pool.size() * 4);
         in.read(pt.data(), pt.size() * 4);
-        for (uint32_t p : pt)
-            if (p >= pool_top)
-                throw StatusError{HD_ERR_INVALID, in.path + " maps a page past its pool"};
         std::vector<uint32_t> bs(g.total_buckets, 0), full(c->cfg.depth, 0);
         std::vector<uint64_t> level_nodes(HD_MAX_DEPTH, 0);
         bool extension = false, colors = false;
@@ -376,6 +373,7 @@ hd_status hd_load_snapshot(hd_ctx* c, const char* path, hd_dag_info* info)
             }
             extension = true;
         }
+        check_table(g, pt.data(), extension ? bs.data() : nullptr, pool_top, root, in.path);
         table_reset(c);
         HD_CUDA(cudaMemcpyAsync(c->t.pool, pool.data(), pool.size() * 4, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemcpyAsync(c->t.page_table, pt.data(), pt.size() * 4, cudaMemcpyHostToDevice, st));

@@ -80,7 +80,7 @@ void table_reset(hd_ctx* c)
     const Geom& g = c->g;
     HD_CUDA(cudaMemsetAsync(c->t.pool, 0, size_t(g.pool_pages) * kPage * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.bloom, 0, size_t(g.pool_pages) * kBloomWords * 4, c->stream));
-    HD_CUDA(cudaMemsetAsync(c->t.page_table, 0, g.total_vpages * 4, c->stream));
+    HD_CUDA(cudaMemsetAsync(c->t.page_table, 0, kPageTableEntries * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.bucket_sizes, 0, g.total_buckets * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.full_nodes, 0, HD_MAX_DEPTH * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.level_nodes, 0, HD_MAX_DEPTH * 8, c->stream));
@@ -349,6 +349,29 @@ __global__ void k_bloom_rebuild(Table t, uint32_t level)
             }
         }
     }
+}
+
+bool valid_root(const Geom& g, uint32_t root, uint32_t pt_entry)
+{
+    return (root >> kPageShift) < g.total_vpages && pt_entry != 0;
+}
+
+void check_table(const Geom& g, const uint32_t* pt, const uint32_t* bs, uint32_t top, uint32_t root,
+                 const std::string& what)
+{
+    for (uint64_t p = 0; p < g.total_vpages; p++)
+        if (pt[p] >= top)
+            throw StatusError{HD_ERR_INVALID, what + " maps virtual page " + std::to_string(p) + " to page " +
+                                                  std::to_string(pt[p]) + ", past its " + std::to_string(top) +
+                                                  " pool pages"};
+    if (bs)
+        for (uint32_t L = 0; L < g.depth; L++)
+            for (uint32_t b = 0; b < g.buckets(L); b++)
+                if (bs[g.bucket_global(L, b)] > g.capacity(L))
+                    throw StatusError{HD_ERR_INVALID, what + ": bucket " + std::to_string(b) + " of level " +
+                                                          std::to_string(L) + " holds more than its capacity"};
+    if (!valid_root(g, root, (root >> kPageShift) < g.total_vpages ? pt[root >> kPageShift] : 0))
+        throw StatusError{HD_ERR_INVALID, what + ": the root " + std::to_string(root) + " is not on a mapped page"};
 }
 
 void bloom_rebuild(hd_ctx* c)

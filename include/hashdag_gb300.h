@@ -517,10 +517,12 @@ hd_status hd_replay_frame(hd_ctx* ctx, hd_replay* replay, const hd_replay_config
 /* ---- state and statistics ---------------------------------------------- */
 
 hd_status hd_get_root(hd_ctx* ctx, uint32_t* root);
+/* HD_ERR_INVALID unless root is an address on a mapped page of the table. */
 hd_status hd_set_root(hd_ctx* ctx, uint32_t root);
 hd_status hd_get_config(hd_ctx* ctx, hd_config* cfg);
 hd_status hd_get_level_stats(hd_ctx* ctx, hd_level_stats* out);
-/* Device bytes held: [0] table (pool, page table, bucket sizes), [1] colour
+/* Device bytes held: [0] table (pool, page table for the whole 32-bit
+ * virtual space, bucket sizes, per-page Bloom filters), [1] colour
  * table, [2] scratch buffers, [3] the peak scratch of the last scene
  * generation. */
 hd_status hd_memory_stats(hd_ctx* ctx, uint64_t* out4);
@@ -533,7 +535,12 @@ hd_status hd_table_sizes(hd_ctx* ctx, uint64_t* n_buckets, uint64_t* n_virtual_p
 hd_status hd_export_table(hd_ctx* ctx, uint32_t* h_bucket_sizes, uint32_t* h_page_table,
                           uint32_t* h_pool, uint64_t pool_words_capacity,
                           uint32_t* h_full_nodes);
-/* Replaces the table with host copies (pool_words = pages * 512). */
+/* Replaces the table with host copies (pool_words = pages * 512).
+ * HD_ERR_INVALID (context unchanged) when a page-table entry points past
+ * the given pool, a bucket size exceeds its bucket's capacity or the root is
+ * not on a mapped page; node contents are not checked, but every address
+ * they hold translates inside the page table, so a corrupt table gives wrong
+ * pictures, never out-of-bounds reads of the table. */
 hd_status hd_import_table(hd_ctx* ctx, const uint32_t* h_bucket_sizes, const uint32_t* h_page_table,
                           const uint32_t* h_pool, uint64_t pool_words,
                           const uint32_t* h_full_nodes, uint32_t root);
