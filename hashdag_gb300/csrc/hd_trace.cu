@@ -221,7 +221,7 @@ struct SharedStack {
     uint32_t* idx;
     uint16_t* msk;
     uint32_t stride;
-    HD_D void set(uint32_t l, uint32_t index, uint32_t masks)
+    HD_D void set(uint32_t l, uint32_t index, uint32_t masks) const
     {
         idx[l * stride] = index;
         msk[l * stride] = uint16_t(masks);
@@ -305,6 +305,74 @@ HD_D bool walk(const Table& t, uint32_t root, const F3& o, const F3& d, const F3
 // The child order of a ray: children visited as child ^ octant, 0..7, run
 // front to back along d (rayChildOrder, tracer.cu:161-164).
 HD_D uint32_t octant(const F3& d) { return (d.x < 0.f ? 4u : 0u) + (d.y < 0.f ? 2u : 0u) + (d.z < 0.f ? 1u : 0u); }
+
+// walk() as a resumable state machine, for kernels whose lanes take a new
+// ray as soon as theirs ends: start() enters the root, each step() runs one
+// iteration of walk()'s loop and returns 0 (going on), 1 (reached a voxel)
+// or 2 (left the root).  Same visit order, same result as walk().
+template <int FMA, bool OCTANT>
+struct Walker {
+    uint32_t level, px, py, pz, index, child_mask, visit, leaf_lo, leaf_hi;
+    F3 o;
+
+    HD_D void start(const Table& t, uint32_t root, const F3& origin, const F3& d, const F3& inv)
+    {
+        o = origin;
+        level = px = py = pz = 0;
+        leaf_lo = leaf_hi = 0;
+        index = root;
+        child_mask = *(t.sys_ld(root)) & 0xffu;
+        visit = child_mask & intersection_mask<FMA>(t.g.depth, true, 0, 0, 0, 0, o, d, inv);
+    }
+
+    template <typename Stack>
+    HD_D uint32_t step(const Table& t, const F3& d, const F3& inv, uint32_t order, const Stack& stack,
+                       uint32_t& descents, uint32_t& leaves)
+    {
+        const uint32_t D = t.g.depth, leafl = t.g.leaf_level;
+        uint32_t nl = level;
+        while (nl > 0 && !visit) {
+            nl--;
+            index = stack.index(nl);
+            const uint32_t m = stack.masks(nl);
+            child_mask = m & 0xffu;
+            visit = m >> 8;
+        }
+        if (nl == 0 && !visit)
+            return 2;
+        const uint32_t up = level - nl;
+        px >>= up;
+        py >>= up;
+        pz >>= up;
+        level = nl;
+        const uint32_t nc = OCTANT ? next_child(order, visit) : 31u - __clz(visit);
+        visit &= ~(1u << nc);
+        px = (px << 1) | ((nc >> 2) & 1);
+        py = (py << 1) | ((nc >> 1) & 1);
+        pz = (pz << 1) | (nc & 1);
+        stack.set(level, index, child_mask | (visit << 8));
+        level++;
+        if (level == D)
+            return 1;
+        if (level < leafl) {
+            index = *(t.sys_ld(index + child_offset(child_mask, nc)));
+            child_mask = *(t.sys_ld(index)) & 0xffu;
+            descents++;
+        } else if (level == leafl) {
+            const uint32_t addr = *(t.sys_ld(index + child_offset(child_mask, nc)));
+            const uint2 lf = *(reinterpret_cast<const uint2*>(t.sys_ld(addr)));
+            leaf_lo = lf.x;
+            leaf_hi = lf.y;
+            child_mask = first_child_mask(leaf_lo, leaf_hi);
+            leaves++;
+        } else {
+            child_mask = ((nc & 4) ? leaf_hi : leaf_lo) >> ((nc & 3) * 8) & 0xffu;
+        }
+        visit = child_mask & intersection_mask<FMA>(D, false, level, px, py, pz, o, d, inv);
+        return 0;
+    }
+};
+
 
 // The reference takes float(1.0 / double(x)) (tracer.cu:160): the double
 // quotient rounded again to float.  Rounding a quotient first to a p'-bit
@@ -515,8 +583,13 @@ __global__ void __launch_bounds__(64) k_shadow_list(hd_camera cam, uint32_t W, u
 }
 
 // The any-hit walk of every ray of the list toward the light
-// (intersect_ray_node_out_of_order, tracer.cu:453-543), as persistent warps
-// taking 32 rays at a time from a counter.
+// (intersect_ray_node_out_of_order, tracer.cu:453-543) as persistent warps
+// whose lanes refill independently: a lane whose ray has ended takes the next
+// ray of the list as soon as kShadowRefill lanes of its warp are idle, so the
+// warp does not wait for its longest walk (the walks differ by orders of
+// magnitude).  Each ray's result depends on that ray only.
+constexpr uint32_t kShadowRefill = 8;  // idle lanes that trigger a fetch
+constexpr uint32_t kShadowSteps = 16; // walk steps between fetches
 template <int FMA, bool COUNT>
 __global__ void __launch_bounds__(128) k_trace_shadow(Table t, const uint32_t* __restrict__ d_root, F3 light,
                                                       uint8_t* __restrict__ mask, const ShadowRay* __restrict__ list,
@@ -530,22 +603,41 @@ __global__ void __launch_bounds__(128) k_trace_shadow(Table t, const uint32_t* _
     const uint32_t order = octant(dir);
     extern __shared__ uint32_t smem[];
     const SharedStack stack = shared_stack(smem, t.g.depth);
-    uint32_t base = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(head + 2, 32u) : 0u, 0);
-    while (base < n) {
-        const uint32_t next = lane == 0 ? atomicAdd(head + 2, 32u) : 0u;
-        const uint32_t j = base + lane;
-        if (j < n) {
-            const ShadowRay ray = list[j];
-            uint32_t hit[3], descents = 0, leaves = 0;
-            mask[ray.idx] =
-                walk<FMA, true, true>(t, root, F3{ray.ox, ray.oy, ray.oz}, dir, inv, order, hit, descents, leaves,
-                                      stack)
-                    ? 1
-                    : 0;
-            if (COUNT)
-                add_counts(counters, 1, descents, leaves);
+    Walker<FMA, true> w;
+    uint32_t idx = 0, descents = 0, leaves = 0;
+    bool active = false, more = true;
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (more && __popc(idle) >= kShadowRefill) {
+            const uint32_t k = __popc(idle);
+            const uint32_t base = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(head + 2, k) : 0u, 0);
+            more = base + k < n;
+            if (!active) {
+                const uint32_t j = base + __popc(idle & ((1u << lane) - 1u));
+                if (j < n) {
+                    const ShadowRay ray = list[j];
+                    idx = ray.idx;
+                    w.start(t, root, F3{ray.ox, ray.oy, ray.oz}, dir, inv);
+                    active = true;
+                }
+            }
         }
-        base = __shfl_sync(0xffffffffu, next, 0);
+        if (!__any_sync(0xffffffffu, active)) {
+            if (more)
+                continue; // every lane idle: the next pass fetches
+            break;
+        }
+        for (uint32_t s = 0; s < kShadowSteps && active; s++) {
+            const uint32_t r = w.step(t, dir, inv, order, stack, descents, leaves);
+            if (r) {
+                mask[idx] = r == 1 ? 1 : 0;
+                active = false;
+                if (COUNT) {
+                    add_counts(counters, 1, descents, leaves);
+                    descents = leaves = 0;
+                }
+            }
+        }
     }
 }
 
