@@ -88,7 +88,9 @@ hd_status hd_create(const hd_config* cfg, hd_ctx** out)
     hd_status st = guarded(c, [&] {
         Table& t = c->t;
         t.g = c->g;
-        HD_CUDA(cudaMalloc(&t.pool, size_t(conf.pool_pages) * HD_PAGE_SIZE * 4));
+        // 64 bytes past the last page: a node read at its physical offset
+        // stays inside the allocation even in a corrupt table
+        HD_CUDA(cudaMalloc(&t.pool, size_t(conf.pool_pages) * HD_PAGE_SIZE * 4 + 64));
         HD_CUDA(cudaMalloc(&t.bloom, size_t(conf.pool_pages) * kBloomWords * 4));
         HD_CUDA(cudaMalloc(&t.page_table, kPageTableEntries * 4));
         HD_CUDA(cudaMalloc(&t.bucket_sizes, c->g.total_buckets * 4));

@@ -106,6 +106,13 @@ struct Table {
     // Translation through the read-only data path: for kernels during which
     // neither the page table nor the pool changes (traversal, the edit
     // descent, GC gathers).
+    // Physical word offset of virtual word v in the pool: a node never
+    // straddles a page, so the words after a node's first word are at the
+    // following physical offsets (fits 32 bits: at most 2^23 pages).
+    HD_D uint32_t phys(uint32_t v) const
+    {
+        return (page_table[v >> kPageShift] << kPageShift) | (v & (kPage - 1));
+    }
     HD_D const uint32_t* sys(uint32_t v) const
     {
         return pool + (uint64_t(__ldg(page_table + (v >> kPageShift))) << kPageShift) + (v & (kPage - 1));

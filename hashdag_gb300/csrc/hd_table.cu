@@ -78,7 +78,7 @@ uint32_t check_error(hd_ctx* c)
 void table_reset(hd_ctx* c)
 {
     const Geom& g = c->g;
-    HD_CUDA(cudaMemsetAsync(c->t.pool, 0, size_t(g.pool_pages) * kPage * 4, c->stream));
+    HD_CUDA(cudaMemsetAsync(c->t.pool, 0, size_t(g.pool_pages) * kPage * 4 + 64, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.bloom, 0, size_t(g.pool_pages) * kBloomWords * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.page_table, 0, kPageTableEntries * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.bucket_sizes, 0, g.total_buckets * 4, c->stream));

@@ -249,8 +249,10 @@ HD_D bool walk(const Table& t, uint32_t root, const F3& o, const F3& d, const F3
 {
     const uint32_t D = t.g.depth, leafl = t.g.leaf_level;
     uint32_t level = 0, px = 0, py = 0, pz = 0;
-    uint32_t index = root;
-    uint32_t child_mask = *(t.sys_ld(root)) & 0xffu;
+    // the current node by its physical pool offset: its child pointers are
+    // read with one load, and only the pointer read from it is translated
+    uint32_t index = t.phys(root);
+    uint32_t child_mask = t.pool[index] & 0xffu;
     uint32_t visit = child_mask & intersection_mask<FMA>(D, true, 0, 0, 0, 0, o, d, inv);
     uint32_t leaf_lo = 0, leaf_hi = 0;
     for (;;) {
@@ -285,12 +287,12 @@ HD_D bool walk(const Table& t, uint32_t root, const F3& o, const F3& d, const F3
             return true;
         }
         if (level < leafl) {
-            index = *(t.sys_ld(index + child_offset(child_mask, nc)));
-            child_mask = *(t.sys_ld(index)) & 0xffu;
+            index = t.phys(t.pool[index + child_offset(child_mask, nc)]);
+            child_mask = t.pool[index] & 0xffu;
             descents++;
         } else if (level == leafl) {
-            const uint32_t addr = *(t.sys_ld(index + child_offset(child_mask, nc)));
-            const uint2 lf = *(reinterpret_cast<const uint2*>(t.sys_ld(addr)));
+            const uint32_t addr = t.phys(t.pool[index + child_offset(child_mask, nc)]);
+            const uint2 lf = *(reinterpret_cast<const uint2*>(t.pool + addr));
             leaf_lo = lf.x;
             leaf_hi = lf.y;
             child_mask = first_child_mask(leaf_lo, leaf_hi);
@@ -320,8 +322,8 @@ struct Walker {
         o = origin;
         level = px = py = pz = 0;
         leaf_lo = leaf_hi = 0;
-        index = root;
-        child_mask = *(t.sys_ld(root)) & 0xffu;
+        index = t.phys(root);
+        child_mask = t.pool[index] & 0xffu;
         visit = child_mask & intersection_mask<FMA>(t.g.depth, true, 0, 0, 0, 0, o, d, inv);
     }
 
@@ -355,12 +357,12 @@ struct Walker {
         if (level == D)
             return 1;
         if (level < leafl) {
-            index = *(t.sys_ld(index + child_offset(child_mask, nc)));
-            child_mask = *(t.sys_ld(index)) & 0xffu;
+            index = t.phys(t.pool[index + child_offset(child_mask, nc)]);
+            child_mask = t.pool[index] & 0xffu;
             descents++;
         } else if (level == leafl) {
-            const uint32_t addr = *(t.sys_ld(index + child_offset(child_mask, nc)));
-            const uint2 lf = *(reinterpret_cast<const uint2*>(t.sys_ld(addr)));
+            const uint32_t addr = t.phys(t.pool[index + child_offset(child_mask, nc)]);
+            const uint2 lf = *(reinterpret_cast<const uint2*>(t.pool + addr));
             leaf_lo = lf.x;
             leaf_hi = lf.y;
             child_mask = first_child_mask(leaf_lo, leaf_hi);
