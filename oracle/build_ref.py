@@ -19,18 +19,21 @@ REF = "/root/reference"
 OUT = os.path.join(HERE, "_ref")
 
 
-def lib_path(depth, ctl, top_bits, colors=False):
-    return os.path.join(OUT, f"libhdref_d{depth}_t{ctl}_b{top_bits}{'_c' if colors else ''}.so")
+def lib_path(depth, ctl, top_bits, colors=False, tracer=False):
+    return os.path.join(OUT, f"libhdref_d{depth}_t{ctl}_b{top_bits}{'_c' if colors else ''}"
+                             f"{'_trace' if tracer else ''}.so")
 
 
 def available():
     return os.path.isdir(os.path.join(REF, "src"))
 
 
-def build(depth, ctl, top_bits, force=False, colors=False):
+def build(depth, ctl, top_bits, force=False, colors=False, tracer=False):
     """colors=True: EDITS_ENABLE_COLORS=1 and the colour entry points, linked
-    with the oracle library for the scene's colour field."""
-    out = lib_path(depth, ctl, top_bits, colors)
+    with the oracle library for the scene's colour field.  tracer=True: the
+    reference's traversal code (tracer.cu) compiled for the host on top of the
+    harness (oracle/refharness/ref_tracer.cpp)."""
+    out = lib_path(depth, ctl, top_bits, colors, tracer)
     if os.path.exists(out) and not force:
         return out
     if not available():
@@ -46,7 +49,9 @@ def build(depth, ctl, top_bits, force=False, colors=False):
            "-I", os.path.join(HERE, "refharness", "shim"),
            "-I", src, "-I", os.path.join(src, "dags"), "-I", os.path.join(src, "dags", "hash_dag"),
            "-I", os.path.join(src, "gmath"), "-I", "/usr/local/cuda/include",
-           os.path.join(HERE, "refharness", "ref_host.cpp"), "-o", out + ".tmp"]
+           os.path.join(HERE, "refharness", "ref_tracer.cpp" if tracer else "ref_host.cpp"), "-o", out + ".tmp"]
+    if tracer:
+        cmd += ["-I", os.path.join(HERE, "refharness"), "-pthread"]
     if colors:
         from oracle import build_oracle
         lib = build_oracle.build()

@@ -198,3 +198,54 @@ def test_trace_views_host_equals_device_views(gpu, chunk):
     assert torch.equal(h_paths, d_paths.cpu())
     assert torch.equal(h_mask, d_mask.cpu())
     dag.free()
+
+
+_REF_TRACE = json.load(open(os.path.join(GOLDEN, "ref_trace.json")))
+_REF_CASES = [(s["depth"], f["name"]) for s in _REF_TRACE["scenes"] for f in s["frames"]]
+
+
+@pytest.mark.parametrize("depth,name", _REF_CASES)
+def test_trace_equals_reference_tracer(gpu, depth, name):
+    """Paths and shadow masks of whole 1920 x 1080 frames equal the
+    reference's own trace_paths / trace_shadows hit test (fp_mode 0)."""
+    s = next(s for s in _REF_TRACE["scenes"] if s["depth"] == depth)
+    f = next(f for f in s["frames"] if f["name"] == name)
+    W, H = s["width"], s["height"]
+    d = gpu_dag(depth)
+    d.set_fp_mode(0)
+    try:
+        tr = hd.DAGTracer(W, H)
+        tr.resolve_paths(f["camera"], d)
+        tr.resolve_shadows(f["camera"], d, f["bias"], tuple(f["light"]))
+        paths, mask = np.ascontiguousarray(tr.get_paths()), np.ascontiguousarray(tr.get_shadows())
+    finally:
+        d.set_fp_mode(1)
+    assert int((paths[..., :3] != 0).any(-1).sum()) == f["hits"]
+    assert hashlib.sha256(paths.tobytes()).hexdigest() == f["paths_sha256"]
+    assert hashlib.sha256(mask.tobytes()).hexdigest() == f["mask_sha256"]
+
+
+def test_trace_views_equal_reference_tracer(gpu):
+    """Every frame of a scene in one hd_trace_views launch (fp_mode 0), per
+    view equal to the reference's frames."""
+    import ctypes as C
+    import torch
+    from hashdag_gb300 import _capi
+    s = next(s for s in _REF_TRACE["scenes"] if s["depth"] == 10)
+    frames = [f for f in s["frames"] if f["light"] == s["frames"][0]["light"]]
+    W, H, V = s["width"], s["height"], len(frames)
+    d = gpu_dag(10)
+    d.set_fp_mode(0)
+    try:
+        cams = (_capi.Camera * V)(*[_capi.Camera.from_params(f["camera"]) for f in frames])
+        paths = torch.zeros(V * W * H * 4, dtype=torch.int32, device="cuda")
+        mask = torch.zeros(V * W * H, dtype=torch.uint8, device="cuda")
+        light = (C.c_float * 3)(*frames[0]["light"])
+        d._check(_capi.lib().hd_trace_views(d.handle, cams, V, W, H, paths.data_ptr(), light, 1.0, mask.data_ptr(),
+                                            None))
+        paths, mask = paths.cpu().numpy().view(np.uint32), mask.cpu().numpy()
+    finally:
+        d.set_fp_mode(1)
+    for v, f in enumerate(frames):
+        assert hashlib.sha256(paths[v * W * H * 4:(v + 1) * W * H * 4].tobytes()).hexdigest() == f["paths_sha256"]
+        assert hashlib.sha256(mask[v * W * H:(v + 1) * W * H].tobytes()).hexdigest() == f["mask_sha256"], f["name"]
