@@ -51,7 +51,7 @@ def build(depth, ctl, top_bits, force=False, colors=False, tracer=False):
            "-I", os.path.join(src, "gmath"), "-I", "/usr/local/cuda/include",
            os.path.join(HERE, "refharness", "ref_tracer.cpp" if tracer else "ref_host.cpp"), "-o", out + ".tmp"]
     if tracer:
-        cmd += ["-I", os.path.join(HERE, "refharness"), "-pthread"]
+        cmd += ["-I", os.path.join(HERE, "refharness"), "-pthread", "-DTOOL_OVERLAY=1"]
     if colors:
         from oracle import build_oracle
         lib = build_oracle.build()

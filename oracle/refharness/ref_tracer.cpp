@@ -140,3 +140,36 @@ extern "C" void ref_trace_shadows(const double* cam, const uint32* paths, const 
         mask[size_t(y) * imageWidth + x] = m;
     });
 }
+
+#if EDITS_ENABLE_COLORS
+// Tracer::trace_colors (tracer.cu:254-451) over a paths image made by
+// ref_trace_paths, on the harness's colours; colors: imageHeight x
+// imageWidth uint32 (rgb888).  tool: ETool, or a negative value for no
+// overlay (the overlay needs TOOL_OVERLAY=1, which build_ref.py sets for the
+// tracer build).  pos / src / dst: the ToolInfo paths.
+extern "C" void ref_trace_colors(const uint32* paths, uint32 debug, uint32 debug_level, int tool, const uint32* pos,
+                                 float radius, const uint32* src, const uint32* dst, uint32* colors, int threads)
+{
+    RefSurface ps{const_cast<uint8_t*>(reinterpret_cast<const uint8_t*>(paths)), size_t(imageWidth) * sizeof(uint4)};
+    RefSurface cs{reinterpret_cast<uint8_t*>(colors), size_t(imageWidth) * sizeof(uint32)};
+    Tracer::TraceColorsParams params;
+    params.debugColors = EDebugColors(debug);
+    params.debugColorsIndexLevel = debug_level;
+    // no overlay: a sphere of radius 1e-30 at the null path, whose strength
+    // 1 - distance / radius is negative at every voxel path
+    params.toolInfo = tool < 0 ? ToolInfo(ETool::Sphere, make_uint3(0u, 0u, 0u), 1e-30f, make_uint3(0u, 0u, 0u),
+                                          make_uint3(0u, 0u, 0u))
+                               : ToolInfo(ETool(tool), make_uint3(pos[0], pos[1], pos[2]), radius,
+                                          make_uint3(src[0], src[1], src[2]), make_uint3(dst[0], dst[1], dst[2]));
+    params.pathsSurface = reinterpret_cast<cudaSurfaceObject_t>(&ps);
+    params.colorsSurface = reinterpret_cast<cudaSurfaceObject_t>(&cs);
+    const HashDAG dag = g_dag;
+    const HashDAGColors cols = g_colors;
+    for_pixels(threads, [&](uint32 x, uint32 y) {
+        ref_block_dim = dim3(1, 1, 1);
+        ref_thread_idx = make_uint3(0, 0, 0);
+        ref_block_idx = make_uint3(x, y, 0);
+        Tracer::trace_colors<HashDAG, HashDAGColors>(params, dag, cols);
+    });
+}
+#endif

@@ -69,3 +69,50 @@ def test_trace_colors_views_match_oracle(gpu):
     sky = np.all(paths.reshape(-1, 4)[:, :3] == 0, axis=1)
     assert sky.any() and np.all(got.reshape(-1)[sky] == po.lib().or_f3_to_rgb888(187 / 255, 242 / 255, 250 / 255))
     dag.free()
+
+
+def test_trace_colors_equal_reference(gpu, tmp_path):
+    """Every colour view of a 1920 x 1080 frame equals the reference's own
+    Tracer::trace_colors (tests/golden/ref_trace_colors_d10.json): the scene
+    read from the reference's BasicDAG and compressed-colour files (one
+    shared main colour leaf, the files rebuilt here and checked against the
+    reference's bytes), a paint, a fill and a carve, paths at fp_mode 0."""
+    import hashlib
+    import json
+    fx = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                     "ref_trace_colors_d10.json")))
+    D, T = fx["depth"], fx["color_tree_levels"]
+    words = po.generate_basic_dag(fx["seed"], D, T, flags=po.SCENE_SHELL)
+    e = float(1 << D)
+    data = {"scene.basic_dag.dag.bin": po.basic_dag_file(words, D, ((0.0, 0.0, 0.0), (e, e, e))),
+            "scene.basic_dag.compressed_colors.variable.bin": po.compressed_colors_file(words, D, T,
+                                                                                      fx["color_seed"])}
+    paths_on_disk = {}
+    for name, raw in data.items():
+        assert hashlib.sha256(raw).hexdigest() == fx["files"][name]["sha256"], name
+        p = tmp_path / name
+        p.write_bytes(raw)
+        paths_on_disk[name] = str(p)
+    dag = hd.HashDAG(D)
+    dag.load_dag_from_file(paths_on_disk["scene.basic_dag.dag.bin"])
+    dag.load_compressed_colors_from_file(paths_on_disk["scene.basic_dag.compressed_colors.variable.bin"])
+    for ed in fx["edits"]:
+        if ed["tool"] == hd.TOOL_SPHERE_PAINT:
+            dag.edit_threads(hd.SpherePaintEditor(ed["center"], ed["radius"]))
+        else:
+            dag.edit_threads(hd.editor_from_tuple((ed["tool"], ed["center"], ed["radius"])))
+    assert dag.firstNodeIndex == fx["root"]
+    W, H = fx["width"], fx["height"]
+    dag.set_fp_mode(0)
+    tr = hd.DAGTracer(W, H)
+    tr.resolve_paths(fx["camera"], dag)
+    dag.set_fp_mode(1)
+    assert hashlib.sha256(np.ascontiguousarray(tr.get_paths()).tobytes()).hexdigest() == fx["paths_sha256"]
+    for v in fx["views"]:
+        t = v["tool"]
+        tool = None if t is None else (t["kind"], t["pos"], t["radius"], t["src"], t["dst"])
+        got = np.ascontiguousarray(tr.resolve_colors(dag, v["debug"], v["level"], tool))
+        row = got.reshape(H, W)[fx["sample_row"], ::64].tolist()
+        assert row == v["row"], (v["debug"], v["level"], t)
+        assert hashlib.sha256(got.tobytes()).hexdigest() == v["sha256"], (v["debug"], v["level"], t)
+    dag.free()
