@@ -1,11 +1,12 @@
 // ORACLE — test infrastructure only.
 //
-// The reference's own traversal code (tracer.cu: Tracer::trace_paths,
-// intersect_ray_node_out_of_order, ray_box_intersection, sun_direction),
-// compiled for the host from its unmodified sources on top of the host
-// harness (ref_host.cpp), so that the golden traversal fixtures come from the
-// reference itself rather than from a restatement.  Built by
-// oracle/build_ref.py (tracer=True) into oracle/_ref; never shipped.
+// The reference's own traversal and shading code (tracer.cu:
+// Tracer::trace_paths, intersect_ray_node_out_of_order, ray_box_intersection,
+// Tracer::trace_colors), compiled for the host from its unmodified sources
+// on top of the host harness (ref_host.cpp), so that the golden traversal
+// and colour-view fixtures come from the reference itself rather than from a
+// restatement.  Built by oracle/build_ref.py (tracer=True, with colors=True
+// for trace_colors) into oracle/_ref; never shipped.
 //
 // Host stand-ins, each for a CUDA construct the kernels use:
 //  * blockIdx / blockDim / threadIdx: thread-local values set per pixel;
