@@ -206,7 +206,8 @@ HD_D uint32_t next_child(uint32_t order, uint32_t mask) // next_child (tracer.cu
     return (__ffs(m) - 1) ^ order;
 }
 
-// The walk's stack: per level the node and its child mask | visit mask << 8.
+// The walk's stack: per level the node (its physical pool offset) and its
+// child mask | visit mask << 8.
 struct LocalStack {
     struct {
         uint32_t index, masks;
