@@ -104,25 +104,20 @@ struct Table {
     Geom g;
 
     // Translation through the read-only data path: for kernels during which
-    // neither the page table nor the pool changes (traversal, the edit
-    // descent, GC gathers).
-    // Physical word offset of virtual word v in the pool: a node never
-    // straddles a page, so the words after a node's first word are at the
-    // following physical offsets (fits 32 bits: at most 2^23 pages).
-    HD_D uint32_t phys(uint32_t v) const
-    {
-        return (page_table[v >> kPageShift] << kPageShift) | (v & (kPage - 1));
-    }
+    // neither the page table nor the pool changes (the edit descent, GC
+    // gathers, point queries).
     HD_D const uint32_t* sys(uint32_t v) const
     {
         return pool + (uint64_t(__ldg(page_table + (v >> kPageShift))) << kPageShift) + (v & (kPage - 1));
     }
-    // Translation and node reads as plain global loads, for the traversal
-    // walks: there the read-only path queued on the texture pipe
-    // (tex_throttle stalls) and plain loads measured 3 % faster.
-    HD_D const uint32_t* sys_ld(uint32_t v) const
+    // Physical word offset of virtual word v in the pool, for the traversal
+    // walks, which keep their node by this offset: a node never straddles a
+    // page, so the words after a node's first word are at the following
+    // physical offsets (32 bits: at most 2^23 pages).  Plain global loads:
+    // the read-only path queued on the texture pipe there (tex_throttle).
+    HD_D uint32_t phys(uint32_t v) const
     {
-        return pool + (uint64_t(page_table[v >> kPageShift]) << kPageShift) + (v & (kPage - 1));
+        return (page_table[v >> kPageShift] << kPageShift) | (v & (kPage - 1));
     }
     // Translation with an L2-coherent read of the page table, for kernels
     // that map pages while they scan.
