@@ -789,12 +789,15 @@ __global__ void k_get_values(Table t, const uint32_t* __restrict__ d_root, const
         uint8_t v = 0;
         for (uint32_t level = 0; level < t.g.depth; level++) {
             if (level < t.g.leaf_level) {
-                const uint32_t mask = __ldg(t.sys(index)) & 0xffu;
+                // one translation per node: its child pointers follow the
+                // header in the same page
+                const uint32_t* p = t.sys(index);
+                const uint32_t mask = __ldg(p) & 0xffu;
                 const uint32_t s = t.g.depth - (level + 1);
                 const uint32_t child = (((x >> s) & 1) << 2) | (((y >> s) & 1) << 1) | ((z >> s) & 1);
                 if (!(mask & (1u << child)))
                     break;
-                index = __ldg(t.sys(index + child_offset(mask, child)));
+                index = __ldg(p + child_offset(mask, child));
             } else {
                 const uint32_t* p = t.sys(index);
                 const uint64_t leaf = uint64_t(__ldg(p)) | (uint64_t(__ldg(p + 1)) << 32);
