@@ -26,6 +26,30 @@ namespace hd {
 HD_D float fmax_r(float a, float b) { return a > b ? a : b; } // constexpr_max (cuda_math.h:13)
 HD_D float fmin_r(float a, float b) { return a < b ? a : b; }
 
+// The camera read where it is used, with loads the compiler may neither
+// merge with other reads of it nor move: the camera is then dead during a
+// walk instead of held (and spilled) across it.  Generic addressing (the
+// camera may be a kernel parameter's copy or global memory), default
+// caching.
+HD_D double reload_f64(const double* p)
+{
+    double r;
+    asm volatile("ld.f64 %0, [%1];" : "=d"(r) : "l"(p));
+    return r;
+}
+HD_D hd_camera reload_camera(const hd_camera* c)
+{
+    hd_camera r;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        r.position[a] = reload_f64(c->position + a);
+        r.ray_min[a] = reload_f64(c->ray_min + a);
+        r.ray_ddx[a] = reload_f64(c->ray_ddx + a);
+        r.ray_ddy[a] = reload_f64(c->ray_ddy + a);
+    }
+    return r;
+}
+
 // ray_min + px * ddx + py * ddy - position and its squared length, double
 template <int FMA>
 HD_D double camera_vec(const hd_camera& cam, double px, double py, double v[3])
@@ -104,7 +128,7 @@ template <int FMA>
 HD_D bool camera_dir_float(const hd_camera& cam, uint32_t x, uint32_t y, F3& d)
 {
     double v[3];
-    const double dot = camera_vec<FMA>(cam, u32_to_double(x), u32_to_double(y), v);
+    const double dot = camera_vec<FMA>(reload_camera(&cam), u32_to_double(x), u32_to_double(y), v);
     if (!(dot >= 0x1p-100 && dot <= 0x1p100))
         return false;
     // dot rounded to float by its bits (the carry of the rounding bit
@@ -216,27 +240,28 @@ struct LocalStack {
     HD_D uint32_t index(uint32_t l) const { return e[l].index; }
     HD_D uint32_t masks(uint32_t l) const { return e[l].masks; }
 };
-// The same stack in shared memory: level l of thread k at [l * stride + k],
-// node indices and 16-bit masks in two arrays (6 bytes a level).
+// The same stack in the kernel's dynamic shared memory: level l of thread k
+// at [l * blockDim.x + k], node indices and 16-bit masks in two arrays (6
+// bytes a level).  Addresses come from the thread index and the array
+// itself, so a walk holds no pointer registers for its stack.
+extern __shared__ uint32_t hd_walk_stack[];
 struct SharedStack {
-    uint32_t* idx;
-    uint16_t* msk;
-    uint32_t stride;
+    uint32_t msk_words; // start of the mask array: blockDim.x * depth words
     HD_D void set(uint32_t l, uint32_t index, uint32_t masks) const
     {
-        idx[l * stride] = index;
-        msk[l * stride] = uint16_t(masks);
+        const uint32_t k = l * blockDim.x + threadIdx.x;
+        hd_walk_stack[k] = index;
+        reinterpret_cast<uint16_t*>(hd_walk_stack + msk_words)[k] = uint16_t(masks);
     }
-    HD_D uint32_t index(uint32_t l) const { return idx[l * stride]; }
-    HD_D uint32_t masks(uint32_t l) const { return msk[l * stride]; }
+    HD_D uint32_t index(uint32_t l) const { return hd_walk_stack[l * blockDim.x + threadIdx.x]; }
+    HD_D uint32_t masks(uint32_t l) const
+    {
+        return reinterpret_cast<const uint16_t*>(hd_walk_stack + msk_words)[l * blockDim.x + threadIdx.x];
+    }
 };
 // Shared bytes of a SharedStack for `threads` threads and depth D.
 HD_HD uint32_t shared_stack_bytes(uint32_t threads, uint32_t D) { return threads * D * 6; }
-HD_D SharedStack shared_stack(uint32_t* smem, uint32_t D)
-{
-    return SharedStack{smem + threadIdx.x, reinterpret_cast<uint16_t*>(smem + blockDim.x * D) + threadIdx.x,
-                       blockDim.x};
-}
+HD_D SharedStack shared_stack(uint32_t D) { return SharedStack{blockDim.x * D}; }
 
 // The stack walk shared by the primary ray (nearest hit, children in the
 // ray's octant order) and the shadow ray (any hit).  The reference's shadow
@@ -511,8 +536,7 @@ __global__ void __launch_bounds__(128, 16)
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t tx = (W + 7) / 8, ty = (H + 3) / 4;
     const uint32_t per_view = tx * ty, n_tiles = per_view * n_views;
-    extern __shared__ uint32_t smem[];
-    const SharedStack stack = shared_stack(smem, t.g.depth);
+    const SharedStack stack = shared_stack(t.g.depth);
     const uint32_t root = *d_root;
     uint32_t* next_tile = head + 1;
     uint32_t tile = __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(next_tile, 1u) : 0u, 0);
@@ -534,7 +558,8 @@ __global__ void __launch_bounds__(128, 16)
             const uint32_t base =
                 __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(head, uint32_t(__popc(b))) : 0u, 0);
             if (hit) {
-                const F3 o = shadow_origin<FMA>(cams[v], H, x, H - 1 - y, p, light_dir<FMA>(light), bias);
+                const F3 o = shadow_origin<FMA>(reload_camera(cams + v), H, x, H - 1 - y, p, light_dir<FMA>(light),
+                                                bias);
                 list[base + __popc(b & ((1u << lane) - 1u))] = ShadowRay{uint32_t(i), o.x, o.y, o.z};
             }
         }
@@ -604,8 +629,7 @@ __global__ void __launch_bounds__(128) k_trace_shadow(Table t, const uint32_t* _
     const F3 dir = light_dir<FMA>(light);
     const F3 inv = inverse_dir(dir);
     const uint32_t order = octant(dir);
-    extern __shared__ uint32_t smem[];
-    const SharedStack stack = shared_stack(smem, t.g.depth);
+    const SharedStack stack = shared_stack(t.g.depth);
     Walker<FMA, true> w;
     uint32_t idx = 0, descents = 0, leaves = 0;
     bool active = false, more = true;
