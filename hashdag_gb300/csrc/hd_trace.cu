@@ -146,6 +146,17 @@ HD_D bool camera_dir_float(const hd_camera& cam, uint32_t x, uint32_t y, F3& d)
            round_to_float(y1 * v[2], 8192, d.z);
 }
 
+// The exact path of camera_dir_float, out of line: it runs for about one ray
+// in ten thousand, and inlined its double-precision temporaries would
+// raise the register pressure of every ray.
+template <int FMA>
+__device__ __noinline__ F3 camera_dir_exact(const hd_camera* cam, uint32_t x, uint32_t y)
+{
+    double dd[3];
+    camera_dir<FMA>(*cam, double(x), double(y), dd);
+    return {float(dd[0]), float(dd[1]), float(dd[2])};
+}
+
 // compute_intersection_mask: children of node `path` at `level` crossed by
 // the ray, as an 8-bit mask.
 template <int FMA>
@@ -427,11 +438,8 @@ HD_D uint4 primary_ray(const Table& t, uint32_t root, const hd_camera& cam, uint
                        uint32_t y, uint4* __restrict__ out, unsigned long long* counters, Stack stack = Stack{})
 {
     F3 d;
-    if (!camera_dir_float<FMA>(cam, x, y, d)) {
-        double dd[3];
-        camera_dir<FMA>(cam, double(x), double(y), dd);
-        d = {float(dd[0]), float(dd[1]), float(dd[2])};
-    }
+    if (!camera_dir_float<FMA>(cam, x, y, d))
+        d = camera_dir_exact<FMA>(&cam, x, y);
     const F3 inv = inverse_dir(d);
     F3 o;
     if (!(round_to_float(cam.position[0], 0, o.x) && round_to_float(cam.position[1], 0, o.y) &&
@@ -481,7 +489,8 @@ HD_D F3 light_dir(F3 light)
 // the hit voxel's box (ray_box_intersection, :574-587, in double) plus
 // bias * light.
 template <int FMA>
-HD_D F3 shadow_origin(const hd_camera& cam, uint32_t H, uint32_t x, uint32_t r, uint4 p, F3 dir, float bias)
+__device__ __noinline__ F3 shadow_origin(const hd_camera& cam, uint32_t H, uint32_t x, uint32_t r, uint4 p, F3 dir,
+                                      float bias)
 {
     double cd[3];
     camera_dir<FMA>(cam, double(x), double(H - 1 - r), cd);
@@ -558,8 +567,7 @@ __global__ void __launch_bounds__(128, 16)
             const uint32_t base =
                 __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(head, uint32_t(__popc(b))) : 0u, 0);
             if (hit) {
-                const F3 o = shadow_origin<FMA>(reload_camera(cams + v), H, x, H - 1 - y, p, light_dir<FMA>(light),
-                                                bias);
+                const F3 o = shadow_origin<FMA>(cams[v], H, x, H - 1 - y, p, light_dir<FMA>(light), bias);
                 list[base + __popc(b & ((1u << lane) - 1u))] = ShadowRay{uint32_t(i), o.x, o.y, o.z};
             }
         }
