@@ -488,6 +488,8 @@ HD_D F3 light_dir(F3 light)
 // voxel p (tracer.cu:589-697 reduced to the hit test): the exact hit point on
 // the hit voxel's box (ray_box_intersection, :574-587, in double) plus
 // bias * light.
+// Out of line: its double-precision temporaries stay out of the register
+// allocation of the walk that precedes it.
 template <int FMA>
 __device__ __noinline__ F3 shadow_origin(const hd_camera& cam, uint32_t H, uint32_t x, uint32_t r, uint4 p, F3 dir,
                                       float bias)
