@@ -27,6 +27,9 @@ constexpr uint32_t kPageShift = 9;
 constexpr uint64_t kPageTableEntries = 1ull << (32 - kPageShift);
 constexpr uint32_t kInvalid = HD_INVALID_NODE;
 constexpr uint32_t kNotFound = 0xFFFFFFFFu;
+// Largest grid.y of a launch: 8x8-pixel tile grids hold at most this many
+// rows of tiles (images up to 524,280 pixels high).
+constexpr uint32_t kMaxGridRows = 65535;
 constexpr uint32_t kEmptyId = 0xFFFFFFFFu; // "no node" in scratch id arrays
 
 // Device-side error word values (first error wins).

@@ -704,6 +704,9 @@ void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint
 {
     cudaStream_t st = stream ? stream : c->stream;
     const uint32_t* rt = d_root ? d_root : c->d_root;
+    if ((h + 7) / 8 > kMaxGridRows)
+        throw StatusError{HD_ERR_INVALID, "image height " + std::to_string(h) + " exceeds " +
+                                              std::to_string(8 * kMaxGridRows) + " rows"};
     dim3 grid((w + 7) / 8, (h + 7) / 8);
     uint4* out = reinterpret_cast<uint4*>(d_paths);
     if (d_counters) {
@@ -754,6 +757,9 @@ static void shadow_pass(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h,
                         cudaStream_t st, const uint32_t* rt, uint32_t* d_list)
 {
     const uint64_t px = uint64_t(w) * h;
+    if ((h + 7) / 8 > kMaxGridRows)
+        throw StatusError{HD_ERR_INVALID, "image height " + std::to_string(h) + " exceeds " +
+                                              std::to_string(8 * kMaxGridRows) + " rows"};
     uint32_t* buf = d_list ? d_list : c->scratch.get<uint32_t>("shadow_list", shadow_list_words(px));
     ShadowRay* list = reinterpret_cast<ShadowRay*>(buf);
     uint32_t* head = buf + 4 * px;
@@ -856,14 +862,16 @@ void get_values(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out)
 // ---------------------------------------------------------------------------
 // Traversal counters without any device allocation.
 //
-// Some callers cannot allocate device memory at the time they trace: a
-// render loop running inside a CUDA stream capture (cudaMalloc is not
-// capturable), or an embedding application that hands the library a fixed
-// memory budget and forbids allocations after start-up.  This variant of
+// Some callers cannot call cudaMalloc at the time they trace: an embedding
+// application (a game engine, a plugin host) that reserves the device
+// memory budget at start-up and forbids allocations afterwards, or a
+// real-time loop in which cudaMalloc / cudaFree, which may synchronise the
+// whole device, would stall the other streams' work.  This variant of
 // hd_trace_counters keeps its scratch (one partial sum per 8x8-pixel block
 // and the six totals) in a file-scope device array instead of the context's
 // scratch buffers.  The array holds kNoAllocMaxBlocks blocks, i.e. images of
-// up to 16,777,216 pixels (4096 x 4096); larger images are rejected.  The
+// up to 16,777,216 pixels (4096 x 4096); larger images, and images taller
+// than 65535 rows of blocks (524,280 pixels), are rejected.  The
 // array lives on every GPU that loads the library until the process exits.
 // All calls share it: each call writes every slot it later reads, so
 // nothing needs clearing, but calls that overlap on the GPU (other streams,
@@ -999,6 +1007,11 @@ extern "C" hd_status hd_trace_counters_noalloc(hd_ctx* c, const hd_camera* cam, 
     if (bx * by > kNoAllocMaxBlocks) {
         c->err = "hd_trace_counters_noalloc: image of " + std::to_string(uint64_t(w) * h) +
                  " pixels exceeds the fixed scratch (at most 262144 blocks of 8x8 pixels, 16777216 pixels)";
+        return HD_ERR_INVALID;
+    }
+    if (by > kMaxGridRows) {
+        c->err = "hd_trace_counters_noalloc: image height " + std::to_string(h) + " exceeds " +
+                 std::to_string(8 * kMaxGridRows) + " rows";
         return HD_ERR_INVALID;
     }
     try {

@@ -213,15 +213,20 @@ hd_status hd_trace_frame(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint
 hd_status hd_trace_counters(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint32_t height,
                             const float light[3], float bias, uint32_t* d_paths, uint8_t* d_mask,
                             uint64_t out[6]);
-/* hd_trace_counters for callers that cannot allocate device memory when
- * they trace (a render loop inside a CUDA stream capture, an application
- * that forbids allocations after start-up).  No counterpart in the
- * reference.  Same outputs as hd_trace_counters; its scratch is a fixed
- * device array inside the library, so it allocates nothing.  Images are
- * limited to 262144 blocks of 8x8 pixels (16777216 pixels, e.g. 4096x4096);
- * larger ones return HD_ERR_INVALID.  The first call on each device looks up
- * the array's address (make it before any stream capture).  Calls share the
- * array: calls that overlap on the GPU race. */
+/* hd_trace_counters for callers that cannot call cudaMalloc when they
+ * trace: an embedding application (a game engine, a plugin host) that
+ * reserves the device memory budget at start-up and forbids allocations
+ * afterwards, or a real-time loop in which an allocation, which may
+ * synchronise the whole device, would stall other streams.  No counterpart
+ * in the reference.  Same outputs as hd_trace_counters; its scratch is a
+ * fixed 6 MB device array inside the library (held on every device that
+ * loads the library until the process exits), so it allocates nothing.
+ * Images are limited to 262144 blocks of 8x8 pixels (16777216 pixels, e.g.
+ * 4096x4096) and to 524280 rows; larger ones return HD_ERR_INVALID.  The
+ * first call on each device looks up the array's address with that device
+ * current.  The call copies the six totals to `out` and waits for the
+ * context's stream.  Calls share the array: calls that overlap on the GPU
+ * (other streams, other threads) race. */
 hd_status hd_trace_counters_noalloc(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint32_t height,
                                     const float light[3], float bias, uint32_t* d_paths, uint8_t* d_mask,
                                     uint64_t out[6]);

@@ -5,7 +5,8 @@ infrastructure only).
 
 Compiles oracle/refharness/ref_host.cpp, which #includes the reference's
 unmodified host sources (hash_table.cpp, stats.cpp, hash_dag_factory.cpp and
-the headers of the edit path) from /root/reference/src, into
+the headers of the edit path) from the reference checkout's src/ (see REF
+below), into
 oracle/_ref/libhdref_d<D>_t<T>_b<B>.so.  No reference file is copied; the
 output directory is git-ignored.  Build flags follow the reference's
 parity build: -O2 -ffp-contract=off, no fast-math.
@@ -15,7 +16,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+# The reference checkout: HD_REFERENCE_DIR, else a "reference" directory
+# beside the repository.
+REF = os.environ.get("HD_REFERENCE_DIR") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 OUT = os.path.join(HERE, "_ref")
 
 
