@@ -18,9 +18,12 @@ e2e    = the same metric through the C ABI with host buffers
          and shadow mask in pinned host memory every step (the primary
          kernel writes the paths there over NVLink-C2C; the mask is copied).
 --impl reference times the oracle's CPU restatement of the reference tracer
-(the reference has no CPU tracer) on all host cores, a bounded band of rows
-per step.  Under torchrun every rank renders its own poses on its own GPU
-(replicas, no collective on the data path).
+(the reference has no CPU tracer) on all host cores, on the scene the
+oracle's own generator builds, whole frames (a sample of each step's views).
+ref_gpu (in the GPU arm's line): the reference's own CUDA tracer (tracer.cu
+compiled unmodified for sm_103a) on the same GPU, scene and poses.  Under
+torchrun every rank renders its own poses on its own GPU (replicas, no
+collective on the data path).
 
 "edits" (the same JSON line): the batched-edit workload on the 2^15 scene,
 --edits edits (default 256; 50% sphere carve, 30% sphere fill, 20% box fill,
@@ -66,7 +69,9 @@ def parse():
     p.add_argument("--e2e-chunk", type=int, default=0,
                    help="views per chunk of the end-to-end call (0: paths written straight to host memory)")
     p.add_argument("--views", type=int, default=16, help="poses traced per step (one primary and one shadow launch)")
-    p.add_argument("--ref-rows", type=int, default=192, help="rows per step of the CPU reference arm")
+    p.add_argument("--ref-views", type=int, default=2,
+                   help="whole frames per step of the CPU reference arm (a sample of the step's views)")
+    p.add_argument("--no-ref-gpu", action="store_true", help="skip timing the reference's GPU tracer")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the traversal cpu_baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--pool-pages", type=int, default=0, help="physical pool pages (0 = library default)")
@@ -204,6 +209,27 @@ def replica_poses(step, views, rank, n_poses):
     """Poses of one step on one rank: replicas render their own poses (rank r
     starts 7 r poses further along the path); no data crosses ranks."""
     return [(step * views + j + rank * 7) % n_poses for j in range(views)]
+
+
+def workload_config(args, world):
+    """The workload the headline line is quoted on: the same dict in the GPU
+    arm and the reference arm."""
+    return {"workload": f"catmull_rom_d{args.depth}_{args.width}x{args.height}", "depth": args.depth,
+            "width": args.width, "height": args.height, "poses": args.poses, "views_per_step": args.views,
+            "light": list(LIGHT), "shadow_bias": BIAS, "scene_seed": 1,
+            "l2": "flushed (512 MB write) before every step", "parallelism": f"replicas x{world}"}
+
+
+def oracle_scene(depth):
+    """The seeded scene built by the oracle alone (its threaded C generator
+    and load_from_DAG), no library code."""
+    from oracle import pyoracle as po
+    from hashdag_gb300 import workloads
+    t0 = time.perf_counter()
+    words = po.generate_basic_dag(1, depth, workloads.color_tree_levels(depth), threads=0)
+    ot = po.Table(po.default_config(depth))
+    ot.load_basic_dag(words)
+    return ot, time.perf_counter() - t0
 
 
 def load_scene(depth, pool_pages=0):
@@ -503,34 +529,28 @@ def serving_bench(args):
 
 
 def run_reference(args, dist):
-    """The CPU arm: the oracle's restatement of the reference tracer."""
+    """The reference arm: the oracle's restatement of the reference tracer
+    (the reference has no CPU tracer; the restatement equals its tracer.cu
+    compiled for the host on every golden frame) on all host cores.  The
+    scene comes from the oracle's own generator; each step traces whole
+    frames, a sample of --ref-views of the step's views (the same poses the
+    GPU arm's step renders)."""
     if dist.rank != 0:
         return
-    import torch
-    torch.cuda.set_device(dist.local)
     from hashdag_gb300 import workloads
     W, H, depth = args.width, args.height, args.depth
-    dag, _ = load_scene(depth, args.pool_pages)
-    ot = oracle_from(dag, depth)
-    dag.free()
+    ot, gen_s = oracle_scene(depth)
     poses = workloads.catmull_rom_path(depth, args.poses, W, H)
     threads = os.cpu_count() or 1
-    rows = args.ref_rows
-
-    # each step: 8 bands of rows/8 rows spread evenly over the frame (ray
-    # cost depends strongly on the row: sky, near ground, grazing horizon)
-    bands = 8
-    band = max(1, rows // bands)
-    span = max(1, H // bands)
+    nv = max(1, min(args.ref_views, args.views))
 
     def step(k):
-        cam = poses[k % len(poses)]
+        views = replica_poses(k, args.views, 0, len(poses))
         n = 0
-        for b in range(bands):
-            r0 = min(H - band, b * span + (k * 37) % max(1, span - band))
-            paths, mask = ot.trace_frame(cam, W, H, LIGHT, BIAS, fp_mode=1, threads=threads, rows=(r0, r0 + band))
-            out_rows = slice(H - (r0 + band), H - r0)
-            n += band * W + int((mask[out_rows] != 2).sum())
+        for j in range(nv):
+            cam = poses[views[j * args.views // nv]]
+            paths, mask = ot.trace_frame(cam, W, H, LIGHT, BIAS, fp_mode=1, threads=threads)
+            n += W * H + int((mask != 2).sum())
         return n
 
     for k in range(args.warmup):
@@ -541,18 +561,83 @@ def run_reference(args, dist):
         rays += step(args.warmup + k)
     dt = time.perf_counter() - t0
     value = rays / dt / 1e6
+    sample = (f"{nv} whole {W}x{H} frames per step (of the step's {args.views} views, evenly spaced), "
+              f"oracle C restatement of the reference tracer (the reference has no CPU tracer), {threads} threads; "
+              f"scene from the oracle's generator ({gen_s:.0f} s)")
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": f"catmull_rom_d{depth}_{W}x{H}", "depth": depth, "poses": args.poses,
-                       "rows_per_step": bands * band, "l2": "host CPU run"},
-            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
-                             "sample": f"{bands} bands of {band} rows x {W} px per step, spread over the frame, "
-                                       f"oracle C restatement of the reference tracer (the reference has no CPU "
-                                       f"tracer)"},
-            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": workload_config(args, dist.world),
+            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "rays_per_step": rays / args.steps, "gpu_launches": 0}
     print(json.dumps(line), flush=True)
+
+
+def ref_gpu_baseline(dag, args, poses, flush, ours_value):
+    """The reference's own CUDA tracer (tracer.cu compiled unmodified for
+    sm_103a, oracle/refgpu.py) on the same GPU, scene and poses: one
+    trace_paths launch per view as its DAGTracer makes them, then the
+    shadow hit test, L2 flushed before every step of --views views.  Also
+    checks the first view's paths and mask against the library's."""
+    import numpy as np
+    import torch
+    import hashdag_gb300 as hd
+    from hashdag_gb300 import workloads
+    from oracle import refgpu
+    depth, W, H, V, K = args.depth, args.width, args.height, args.views, args.steps
+    ctl, bits = workloads.color_tree_levels(depth), workloads.top_bucket_bits(depth)
+    if not refgpu.available(depth, ctl, bits):
+        return {"value": None, "unavailable": "reference tracer cubin not built (needs the reference sources)"}
+    ref = refgpu.RefGpuTracer(depth, ctl, bits)
+    try:
+        if (ref.width, ref.height) != (W, H):
+            return {"value": None, "unavailable": f"the reference tracer is compiled for {ref.width}x{ref.height}"}
+        ref.set_table(dag.export_table())
+        # parity on the first view (fp_mode 1 = the reference build's arithmetic)
+        cam0 = poses[replica_poses(0, V, 0, len(poses))[0]]
+        rp, rm, _ = ref.trace_view(cam0, LIGHT, BIAS)
+        tr = hd.DAGTracer(W, H)
+        tr.resolve_paths(cam0, dag)
+        tr.resolve_shadows(cam0, dag, BIAS, LIGHT)
+        diff_paths = int((np.ascontiguousarray(tr.get_paths()).reshape(H, W, 4) != rp).any(-1).sum())
+        diff_mask = int((np.ascontiguousarray(tr.get_shadows()).reshape(H, W) != rm).sum())
+        for k in range(args.warmup):
+            for i in replica_poses(k, V, 0, len(poses)):
+                ref.trace_view(poses[i], LIGHT, BIAS, read=False)
+        clocks = ClockSampler(torch.cuda.current_device())
+        torch.cuda.synchronize()
+        clocks.start()
+        time.sleep(0.3)
+        ms_p = ms_s = 0.0
+        rays = 0
+        for k in range(K):
+            flush.fill_(k & 0xff)
+            torch.cuda.synchronize()
+            for i in replica_poses(k, V, 0, len(poses)):
+                _, mask, ms = ref.trace_view(poses[i], LIGHT, BIAS, read=True)
+                ms_p += ms[0]
+                ms_s += ms[1]
+                rays += W * H + int((mask != 2).sum())
+        clk = clocks.stop()
+        # the reference's unmodified trace_shadows (its own sun, shading) on a few views
+        own = []
+        for i in replica_poses(0, V, 0, len(poses))[:4]:
+            own.append(ref.trace_view(poses[i], LIGHT, BIAS, own_shadows=True, read=False)[2][2])
+        value = rays / ((ms_p + ms_s) * 1e-3) / 1e6
+        return {"value": value, "unit": "Mrays/s", "kind": "reference CUDA kernel",
+                "kernels": "Tracer::trace_paths<HashDAG> (tracer.cu:145-252) + the trace_shadows hit test "
+                           "(ray_box_intersection, intersect_ray_node_out_of_order) with this light",
+                "build": "tracer.cu unmodified, nvcc -O3 --expt-relaxed-constexpr, sm_103a cubin",
+                "launch": "one view per launch, block (4, 64), grid (W/4+1, H/64+1), as DAGTracer::resolve_paths",
+                "paths_ms_per_view": ms_p / (K * V), "shadow_ms_per_view": ms_s / (K * V),
+                "trace_shadows_ms_per_view": sum(own) / max(1, len(own)),
+                "steps": K, "views_per_step": V, "rays": rays,
+                "ours_over_reference": ours_value / value if value else None,
+                "first_view_parity": {"paths_pixels_differing": diff_paths, "mask_pixels_differing": diff_mask},
+                "clocks": clk}
+    finally:
+        ref.close()
 
 
 def run_gpu(args, dist):
@@ -671,6 +756,12 @@ def run_gpu(args, dist):
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}
+    ref_gpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_ref_gpu:
+        try:
+            ref_gpu = ref_gpu_baseline(dag, args, poses, flush, value)
+        except Exception as e:  # reported, never required
+            ref_gpu = {"value": None, "unavailable": f"failed: {e}"}
     edits = None
     if args.edits:
         dag.free()
@@ -689,18 +780,14 @@ def run_gpu(args, dist):
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": dist.world, "steps": K,
             "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload, "depth": depth, "width": W, "height": H, "poses": args.poses,
-                       "views_per_step": V, "light": list(LIGHT), "shadow_bias": BIAS,
-                       "l2": "flushed (512 MB write) before every step",
-                       "scene_gen_s": round(gen_s, 2), "rays_per_step": rays_total / K,
-                       "scene_pages_used": int(lstats.pages_used),
-                       "scene_nodes": int(sum(lstats.nodes[:depth - 1])),
-                       "parallelism": f"replicas x{dist.world}"},
+            "config": workload_config(args, dist.world),
+            "scene": {"gen_s": round(gen_s, 2), "rays_per_step": rays_total / K,
+                      "pages_used": int(lstats.pages_used), "nodes": int(sum(lstats.nodes[:depth - 1]))},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": V * C.sizeof(_capi.Camera),
                     "d2h_bytes_per_step": V * (W * H * 16 + W * H), "api": "hd_trace_views_host",
                     "paths": ("written by the primary kernel into the pinned host buffer (NVLink-C2C)"
                               if not args.e2e_chunk else f"copied in chunks of {args.e2e_chunk} views")},
-            "gpu_launches": 2 * K, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": 2 * K, "roofline": roofline, "cpu_baseline": cpu, "ref_gpu": ref_gpu, "clocks": clk,
             "wall_s": wall, "edits": edits, "colors": colors, "tools_files": tools, "serving": serving}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)

@@ -36,6 +36,10 @@ __global__ void k_edit_spawn(Table t, uint32_t n, Level lv, Level next)
 __global__ void k_edit_candidates(Table t, uint32_t level, uint32_t n, Level lv, Level child, uint32_t* keys,
                                   uint32_t* vals, uint32_t* n_cand)
 {
+    // after a failed append below, the levels above are not rebuilt: their
+    // children would be unresolved
+    if (__ldcg(t.error) != 0)
+        return;
     HD_GRID_STRIDE(i, n)
     {
         const uint32_t b = candidate_entry(t, level, lv, child, uint32_t(i));
@@ -73,6 +77,8 @@ __global__ void __launch_bounds__(32 * kFoaWarps)
     __shared__ uint32_t page_s[kFoaWarps][kPage];
     __shared__ uint32_t q_s[kFoaWarps][9];
     __shared__ FoaCache cache_s[kFoaWarps];
+    if (__ldcg(t.error) != 0)
+        return; // a level below failed (see k_edit_candidates)
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t nseg = *n_seg, ncand = *n_cand;
     const uint32_t first = t.g.level_first_bucket(level);
@@ -92,6 +98,8 @@ __global__ void __launch_bounds__(32 * kFoaWarps)
 
 __global__ void k_edit_finish(const Level lv0, uint32_t* d_root, uint32_t* err)
 {
+    if (err[0] != 0)
+        return; // the edit failed: the root stays
     const uint32_t r = lv0.res[0];
     if (r == kInvalid || r == kNotFound)
         set_error(err, kErrCapacity);

@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kLevelThreads)
 __global__ void k_b_candidates(Table t, const BatchState* bs, uint32_t level, Level lv, Level child, uint32_t* keys,
                                uint32_t* vals)
 {
-    if (bs->skip)
+    if (bs->skip || __ldcg(t.error) != 0) // after a failed append, levels above are not rebuilt
         return;
     const uint32_t n = bs->count[level];
     const uint32_t empty = t.g.buckets(level);
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(32 * WARPS)
     k_b_find_or_add(Table t, const BatchState* bs, uint32_t level, Level lv, const uint32_t* __restrict__ keys,
                     const uint32_t* __restrict__ vals, EditCounters* ctr)
 {
-    if (bs->skip)
+    if (bs->skip || __ldcg(t.error) != 0)
         return;
     __shared__ uint32_t page_s[WARPS][kPage];
     __shared__ uint32_t q_s[WARPS][9];

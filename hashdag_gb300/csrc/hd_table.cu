@@ -62,6 +62,32 @@ void add_full_nodes(hd_ctx* c, uint32_t first_level, uint32_t last_level)
     HD_LAUNCH_CHECK();
 }
 
+// The device error word in words: e = {code, detail words} as set_error
+// writes them.
+static std::string describe_error(const Geom& g, const uint32_t* e)
+{
+    const std::string level = std::to_string(e[1]), bucket = std::to_string(e[2]);
+    switch (e[0]) {
+    case kErrPoolFull:
+        return "the pool is full: all " + std::to_string(g.pool_pages) +
+               " pages are in use and an append to level " + level + ", bucket " + bucket + " needed one more";
+    case kErrBucketFull:
+        if (e[1] == 0xFFFFFFFFu)
+            return "global bucket " + bucket + " received more than " + std::to_string(kMaxBucketItems) +
+                   " nodes in one pass";
+        if (!e[1] && !e[2] && !e[3])
+            return "a bucket is full";
+        return "bucket " + bucket + " of level " + level + " is full: an append would grow it to " +
+               std::to_string(e[3]) + " words, past its capacity of " +
+               std::to_string(e[1] < g.depth ? g.capacity(e[1]) : 0) + " words";
+    case kErrTimeout:
+        return "a bounded device wait gave up";
+    default:
+        return "error " + std::to_string(e[0]) + ": level " + std::to_string(int32_t(e[1])) + ", bucket " + bucket +
+               ", value " + std::to_string(e[3]);
+    }
+}
+
 uint32_t check_error(hd_ctx* c)
 {
     uint32_t e[4];
@@ -69,8 +95,7 @@ uint32_t check_error(hd_ctx* c)
     HD_CUDA(cudaStreamSynchronize(c->stream));
     if (e[0]) {
         HD_CUDA(cudaMemsetAsync(c->t.error, 0, 16, c->stream));
-        c->err_detail = "level " + std::to_string(int32_t(e[1])) + ", bucket " + std::to_string(e[2]) + ", value " +
-                        std::to_string(e[3]);
+        c->err_detail = describe_error(c->g, e);
     }
     return e[0];
 }

@@ -29,7 +29,9 @@ HD_HD uint32_t append_position(uint32_t& size, uint32_t n, bool leaf)
 
 // Maps every unmapped virtual page that [from, to) of the bucket touches
 // (allocate_page, hash_table.h:794-809: poolTop++).  Pages are never
-// unmapped, so a bucket rebuilt by GC reuses its pages.
+// unmapped, so a bucket rebuilt by GC reuses its pages.  A claim past the
+// pool's end is given back at once, so poolTop never exceeds the pool (the
+// reference, unchecked in release builds, would write past its pool).
 HD_D bool map_pages(const Table& t, uint32_t level, uint32_t bucket, uint32_t from, uint32_t to)
 {
     if (to <= from)
@@ -40,6 +42,7 @@ HD_D bool map_pages(const Table& t, uint32_t level, uint32_t bucket, uint32_t fr
         if (__ldcg(t.page_table + vp) == 0) {
             const uint32_t p = atomicAdd(t.pool_top, 1u);
             if (p >= t.g.pool_pages) {
+                atomicSub(t.pool_top, 1u);
                 set_error(t.error, kErrPoolFull, level, bucket, p);
                 return false;
             }

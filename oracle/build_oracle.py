@@ -32,5 +32,34 @@ def build(force=False, verbose=False):
     return LIB
 
 
+LOADER = os.path.join(OUT_DIR, "libhdrefgpu.so")
+
+
+def _cuda_home():
+    for cand in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if cand and os.path.isdir(os.path.join(cand, "include")):
+            return cand
+    raise FileNotFoundError("CUDA toolkit not found")
+
+
+def build_loader(force=False):
+    """oracle/refgpu_loader.cpp (own code, no reference header) into
+    oracle/_build/libhdrefgpu.so: the loader of the reference GPU tracer's
+    cubin.  Built on every machine; the cubin itself is made where the
+    reference sources are (oracle/build_ref.py build_gpu_tracer)."""
+    src = os.path.join(HERE, "refgpu_loader.cpp")
+    os.makedirs(OUT_DIR, exist_ok=True)
+    if not force and os.path.exists(LOADER) and os.path.getmtime(LOADER) >= os.path.getmtime(src):
+        return LOADER
+    cuda = _cuda_home()
+    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-Wall", "-I", os.path.join(cuda, "include"), src,
+           "-o", LOADER + ".tmp", "-L", os.path.join(cuda, "lib64"), "-lcudart",
+           "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+    subprocess.check_call(cmd)
+    os.replace(LOADER + ".tmp", LOADER)
+    return LOADER
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))
+    print(build_loader(force="--force" in sys.argv))

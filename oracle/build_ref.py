@@ -64,6 +64,37 @@ def build(depth, ctl, top_bits, force=False, colors=False, tracer=False):
     return out
 
 
+def cubin_path(depth, ctl, top_bits):
+    return os.path.join(OUT, f"ref_tracer_d{depth}_t{ctl}_b{top_bits}.cubin")
+
+
+def build_gpu_tracer(depth, ctl, top_bits, force=False):
+    """The reference's tracer.cu, unmodified, compiled for sm_103a into a
+    cubin with the harness kernels of oracle/refharness/ref_tracer_gpu.cu,
+    with the reference's CUDA flags (CMakeLists.txt:21-28: nvcc defaults,
+    --expt-relaxed-constexpr).  A device binary: it travels to the GPU
+    machine with oracle/_ref and is loaded there by oracle/refgpu_loader.cpp."""
+    out = cubin_path(depth, ctl, top_bits)
+    if os.path.exists(out) and not force:
+        return out
+    if not available():
+        raise FileNotFoundError("reference sources are not present on this machine")
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(REF, "src")
+    nvcc = os.environ.get("NVCC") or "nvcc"
+    cmd = [nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++17", "--expt-relaxed-constexpr",
+           "-O3", "-w", "-DBENCHMARK=1", "-DUSE_BLOOM_FILTER=0", "-DEDITS_ENABLE_COLORS=0", "-DEDITS_COUNTERS=1",
+           "-DENABLE_CHECKS=0", "-DTRACK_GLOBAL_NEWDELETE=0", f"-DHARNESS_DEPTH={depth}",
+           f"-DBUCKETS_BITS_FOR_TOP_LEVELS={top_bits}", f"-DHARNESS_CTL={ctl}",
+           "-I", os.path.join(HERE, "refharness", "shim"),
+           "-I", src, "-I", os.path.join(src, "dags"), "-I", os.path.join(src, "dags", "hash_dag"),
+           "-I", os.path.join(src, "gmath"),
+           os.path.join(HERE, "refharness", "ref_tracer_gpu.cu"), "-o", out + ".tmp"]
+    subprocess.check_call(cmd)
+    os.replace(out + ".tmp", out)
+    return out
+
+
 if __name__ == "__main__":
     d = int(sys.argv[1]) if len(sys.argv) > 1 else 10
     t = int(sys.argv[2]) if len(sys.argv) > 2 else min(10, d - 5)

@@ -11,6 +11,7 @@
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #define PAGE HD_PAGE_SIZE
 #define NOT_FOUND 0xFFFFFFFFu
@@ -549,6 +550,12 @@ typedef struct {
     int64_t spheres[256];
     gen_level lv[HD_MAX_DEPTH];
     uint32_t full_id[HD_MAX_DEPTH];
+    /* threaded builds: the level whose nodes come from finished subtree
+     * tasks (-1: none), their node ids and counts in visit order */
+    int32_t task_level;
+    const uint32_t* task_id;
+    const uint64_t* task_count;
+    uint64_t task_next;
 } gen_ctx;
 
 #define GEN_EMPTY 0xFFFFFFFFu
@@ -815,6 +822,11 @@ static uint32_t gen_build(gen_ctx* g, uint32_t level, uint32_t x0, uint32_t y0, 
                           const uint8_t* live, uint64_t* count)
 {
     uint8_t live2[64];
+    if ((int32_t)level == g->task_level) {
+        const uint64_t i = g->task_next++;
+        *count = g->task_count[i];
+        return g->task_id[i];
+    }
     int cls = classify(g, level, x0, y0, z0, live, live2);
     if (cls == 0) {
         *count = 0;
@@ -881,64 +893,283 @@ uint32_t* or_generate_basic_dag(uint64_t seed, uint32_t depth, uint32_t T, uint6
     return or_generate_basic_dag_ex(seed, depth, T, 0, n_words);
 }
 
+/* Rows [x0, x1) of the height field, or leaf-level cells [x0, x1) of the
+ * min / max pyramid, on one thread. */
+typedef struct {
+    gen_ctx* g;
+    int32_t* h;
+    uint32_t x0, x1, pass;
+} pyr_job;
+
+static void* pyramid_worker(void* arg)
+{
+    pyr_job* j = (pyr_job*)arg;
+    gen_ctx* g = j->g;
+    const uint32_t E = 1u << g->depth, n = 1u << g->leaf_level;
+    for (uint32_t x = j->x0; x < j->x1; x++) {
+        if (j->pass == 0) {
+            for (uint32_t z = 0; z < E; z++)
+                j->h[(size_t)x * E + z] = or_scene_height(g->seed, g->depth, x, z);
+            continue;
+        }
+        for (uint32_t cz = 0; cz < n; cz++) {
+            int32_t lo = 0x7fffffff, hi = -0x7fffffff;
+            for (uint32_t a = 0; a < 4; a++)
+                for (uint32_t b = 0; b < 4; b++) {
+                    int32_t v = j->h[(size_t)(4 * x + a) * E + 4 * cz + b];
+                    lo = v < lo ? v : lo;
+                    hi = v > hi ? v : hi;
+                }
+            g->hmin[g->leaf_level][(size_t)x * n + cz] = lo;
+            g->hmax[g->leaf_level][(size_t)x * n + cz] = hi;
+        }
+    }
+    return NULL;
+}
+
+/* The height min / max pyramid over node footprints, levels leaf..0. */
+static void gen_pyramid(gen_ctx* g, uint32_t threads)
+{
+    const uint32_t E = 1u << g->depth;
+    int32_t* h = (int32_t*)malloc((size_t)E * E * 4);
+    const uint32_t n = 1u << g->leaf_level; /* 4x4 footprints */
+    g->hmin[g->leaf_level] = (int32_t*)malloc((size_t)n * n * 4);
+    g->hmax[g->leaf_level] = (int32_t*)malloc((size_t)n * n * 4);
+    if (threads < 1)
+        threads = 1;
+    if (threads > 256)
+        threads = 256;
+    pthread_t th[256];
+    pyr_job jobs[256];
+    for (uint32_t pass = 0; pass < 2; pass++) {
+        const uint32_t rows = pass == 0 ? E : n;
+        for (uint32_t i = 0; i < threads; i++) {
+            jobs[i] = (pyr_job){g, h, (uint32_t)((uint64_t)rows * i / threads),
+                                (uint32_t)((uint64_t)rows * (i + 1) / threads), pass};
+            if (threads == 1)
+                pyramid_worker(&jobs[i]);
+            else
+                pthread_create(&th[i], NULL, pyramid_worker, &jobs[i]);
+        }
+        if (threads > 1)
+            for (uint32_t i = 0; i < threads; i++)
+                pthread_join(th[i], NULL);
+    }
+    free(h);
+    for (int32_t l = (int32_t)g->leaf_level - 1; l >= 0; l--) {
+        const uint32_t m = 1u << l, m2 = 2 * m;
+        g->hmin[l] = (int32_t*)malloc((size_t)m * m * 4);
+        g->hmax[l] = (int32_t*)malloc((size_t)m * m * 4);
+        for (uint32_t cx = 0; cx < m; cx++)
+            for (uint32_t cz = 0; cz < m; cz++) {
+                int32_t lo = 0x7fffffff, hi = -0x7fffffff;
+                for (uint32_t a = 0; a < 2; a++)
+                    for (uint32_t b = 0; b < 2; b++) {
+                        size_t i = (size_t)(2 * cx + a) * m2 + 2 * cz + b;
+                        lo = g->hmin[l + 1][i] < lo ? g->hmin[l + 1][i] : lo;
+                        hi = g->hmax[l + 1][i] > hi ? g->hmax[l + 1][i] : hi;
+                    }
+                g->hmin[l][(size_t)cx * m + cz] = lo;
+                g->hmax[l][(size_t)cx * m + cz] = hi;
+            }
+    }
+}
+
+static void gen_levels_free(gen_ctx* g)
+{
+    for (uint32_t l = 0; l <= g->leaf_level; l++) {
+        gen_level* L = &g->lv[l];
+        free(L->mask); free(L->count); free(L->leaf); free(L->kid0); free(L->kids);
+        free(L->map.keys); free(L->map.ids);
+        memset(L, 0, sizeof(*L));
+    }
+}
+
+/* ---- threaded build ----------------------------------------------------
+ * The subtrees below the nodes of one level (kTaskLevel) are independent:
+ * each worker builds its share of them into levels of its own, deduplicated
+ * within the worker; the workers' nodes are then merged level by level,
+ * leaves first, into the shared levels (content-deduplicated, so the merged
+ * DAG is the one a single-threaded build makes), and the levels above are
+ * built with the subtrees' results in the same visit order.  The BasicDAG
+ * words depend only on the DAG (depth-first ranks), not on node ids, so the
+ * output is identical to the single-threaded build's. */
+#define GEN_TASK_LEVEL 4
+
+typedef struct {
+    uint32_t x, y, z;
+    uint8_t live[64];
+} gen_task;
+
+typedef struct {
+    gen_task* v;
+    uint64_t n, cap;
+} gen_tasks;
+
+static void tasks_push(gen_tasks* t, uint32_t x, uint32_t y, uint32_t z, const uint8_t* live)
+{
+    if (t->n == t->cap) {
+        t->cap = t->cap ? 2 * t->cap : 1024;
+        t->v = (gen_task*)realloc(t->v, t->cap * sizeof(gen_task));
+    }
+    gen_task* k = &t->v[t->n++];
+    k->x = x;
+    k->y = y;
+    k->z = z;
+    memcpy(k->live, live, 64);
+}
+
+/* The subtree roots at level P in the order gen_build visits them: every
+ * child of a level-(P-1) node that gen_build descends into. */
+static void gen_enumerate(const gen_ctx* g, uint32_t level, uint32_t P, uint32_t x0, uint32_t y0, uint32_t z0,
+                          const uint8_t* live, gen_tasks* out)
+{
+    uint8_t live2[64];
+    if (classify(g, level, x0, y0, z0, live, live2) != 2)
+        return;
+    const uint32_t half = 1u << (g->depth - level - 1);
+    for (uint32_t c = 0; c < 8; c++) {
+        const uint32_t x = x0 + ((c >> 2) & 1) * half, y = y0 + ((c >> 1) & 1) * half, z = z0 + (c & 1) * half;
+        if (level + 1 == P)
+            tasks_push(out, x, y, z, live2);
+        else
+            gen_enumerate(g, level + 1, P, x, y, z, live2, out);
+    }
+}
+
+typedef struct {
+    gen_ctx local;
+    const gen_tasks* tasks;
+    uint64_t* next; /* shared task counter */
+    uint32_t* owner;
+    uint32_t* id;
+    uint64_t* count;
+    uint32_t index;
+} gen_worker;
+
+static void* build_worker(void* arg)
+{
+    gen_worker* w = (gen_worker*)arg;
+    for (;;) {
+        const uint64_t i = __atomic_fetch_add(w->next, 1, __ATOMIC_RELAXED);
+        if (i >= w->tasks->n)
+            break;
+        const gen_task* k = &w->tasks->v[i];
+        uint64_t cnt;
+        w->id[i] = gen_build(&w->local, GEN_TASK_LEVEL, k->x, k->y, k->z, k->live, &cnt);
+        w->count[i] = cnt;
+        w->owner[i] = w->index;
+    }
+    return NULL;
+}
+
+/* Inserts a worker's nodes of levels P..leaf into the shared levels;
+ * map[l][local id] = shared id. */
+static void merge_worker(gen_ctx* g, gen_ctx* w, uint32_t P, uint32_t** map)
+{
+    for (int32_t l = (int32_t)g->leaf_level; l >= (int32_t)P; l--) {
+        gen_level* L = &w->lv[l];
+        map[l] = (uint32_t*)malloc((L->n + 1) * 4);
+        const int is_leaf = (uint32_t)l == g->leaf_level;
+        for (uint64_t id = 0; id < L->n; id++) {
+            uint32_t kids[8];
+            const uint32_t nk = is_leaf ? 0 : popc32(L->mask[id]);
+            for (uint32_t k = 0; k < nk; k++)
+                kids[k] = map[l + 1][L->kids[L->kid0[id] + k]];
+            map[l][id] = level_insert(&g->lv[l], is_leaf, L->mask[id], L->count[id], L->leaf[id], kids);
+        }
+    }
+}
+
+static uint32_t gen_build_threaded(gen_ctx* g, uint32_t threads, uint64_t* total)
+{
+    const uint32_t P = GEN_TASK_LEVEL;
+    uint8_t live[64];
+    memset(live, 1, 64);
+    gen_tasks tasks = {0};
+    gen_enumerate(g, 0, P, 0, 0, 0, live, &tasks);
+    uint32_t* owner = (uint32_t*)calloc(tasks.n + 1, 4);
+    uint32_t* id = (uint32_t*)calloc(tasks.n + 1, 4);
+    uint64_t* count = (uint64_t*)calloc(tasks.n + 1, 8);
+    if (threads > 256)
+        threads = 256;
+    gen_worker* w = (gen_worker*)calloc(threads, sizeof(gen_worker));
+    pthread_t th[256];
+    uint64_t next = 0;
+    for (uint32_t i = 0; i < threads; i++) {
+        w[i].local = *g;
+        memset(w[i].local.lv, 0, sizeof(w[i].local.lv));
+        for (uint32_t l = 0; l < HD_MAX_DEPTH; l++)
+            w[i].local.full_id[l] = GEN_EMPTY;
+        w[i].local.task_level = -1;
+        w[i].tasks = &tasks;
+        w[i].next = &next;
+        w[i].owner = owner;
+        w[i].id = id;
+        w[i].count = count;
+        w[i].index = i;
+        pthread_create(&th[i], NULL, build_worker, &w[i]);
+    }
+    for (uint32_t i = 0; i < threads; i++)
+        pthread_join(th[i], NULL);
+    /* merge, worker by worker; task ids become shared ids */
+    uint32_t* shared = (uint32_t*)malloc((tasks.n + 1) * 4);
+    for (uint32_t i = 0; i < threads; i++) {
+        uint32_t* map[HD_MAX_DEPTH + 1] = {0};
+        merge_worker(g, &w[i].local, P, map);
+        for (uint64_t k = 0; k < tasks.n; k++)
+            if (owner[k] == i)
+                shared[k] = id[k] == GEN_EMPTY ? GEN_EMPTY : map[P][id[k]];
+        for (uint32_t l = 0; l <= HD_MAX_DEPTH; l++)
+            free(map[l]);
+        gen_levels_free(&w[i].local);
+    }
+    /* the levels above, taking the subtrees' results in visit order */
+    g->task_level = (int32_t)P;
+    g->task_id = shared;
+    g->task_count = count;
+    g->task_next = 0;
+    const uint32_t root = gen_build(g, 0, 0, 0, 0, live, total);
+    g->task_level = -1;
+    free(shared);
+    free(owner);
+    free(id);
+    free(count);
+    free(tasks.v);
+    free(w);
+    return root;
+}
+
 uint32_t* or_generate_basic_dag_ex(uint64_t seed, uint32_t depth, uint32_t T, uint32_t flags, uint64_t* n_words)
+{
+    return or_generate_basic_dag_mt(seed, depth, T, flags, 1, n_words);
+}
+
+uint32_t* or_generate_basic_dag_mt(uint64_t seed, uint32_t depth, uint32_t T, uint32_t flags, uint32_t threads,
+                                   uint64_t* n_words)
 {
     if (depth < 6 || depth > 16 || T > depth - 2)
         return NULL;
+    if (threads == 0) {
+        const long n = sysconf(_SC_NPROCESSORS_ONLN);
+        threads = n > 0 ? (uint32_t)n : 1;
+    }
     gen_ctx* g = (gen_ctx*)calloc(1, sizeof(gen_ctx));
     g->seed = seed;
     g->shell = (flags & HD_SCENE_SHELL) != 0;
     g->depth = depth;
     g->leaf_level = depth - 2;
     g->T = T;
+    g->task_level = -1;
     for (uint32_t l = 0; l < HD_MAX_DEPTH; l++)
         g->full_id[l] = GEN_EMPTY;
     or_scene_spheres(seed, depth, g->spheres);
-    /* height min/max pyramid over node footprints, levels leaf..0 */
-    {
-        const uint32_t E = 1u << depth;
-        int32_t* h = (int32_t*)malloc((size_t)E * E * 4);
-        for (uint32_t x = 0; x < E; x++)
-            for (uint32_t z = 0; z < E; z++)
-                h[(size_t)x * E + z] = or_scene_height(seed, depth, x, z);
-        const uint32_t n = 1u << g->leaf_level; /* 4x4 footprints */
-        g->hmin[g->leaf_level] = (int32_t*)malloc((size_t)n * n * 4);
-        g->hmax[g->leaf_level] = (int32_t*)malloc((size_t)n * n * 4);
-        for (uint32_t cx = 0; cx < n; cx++)
-            for (uint32_t cz = 0; cz < n; cz++) {
-                int32_t lo = 0x7fffffff, hi = -0x7fffffff;
-                for (uint32_t a = 0; a < 4; a++)
-                    for (uint32_t b = 0; b < 4; b++) {
-                        int32_t v = h[(size_t)(4 * cx + a) * E + 4 * cz + b];
-                        lo = v < lo ? v : lo;
-                        hi = v > hi ? v : hi;
-                    }
-                g->hmin[g->leaf_level][(size_t)cx * n + cz] = lo;
-                g->hmax[g->leaf_level][(size_t)cx * n + cz] = hi;
-            }
-        free(h);
-        for (int32_t l = (int32_t)g->leaf_level - 1; l >= 0; l--) {
-            const uint32_t m = 1u << l, m2 = 2 * m;
-            g->hmin[l] = (int32_t*)malloc((size_t)m * m * 4);
-            g->hmax[l] = (int32_t*)malloc((size_t)m * m * 4);
-            for (uint32_t cx = 0; cx < m; cx++)
-                for (uint32_t cz = 0; cz < m; cz++) {
-                    int32_t lo = 0x7fffffff, hi = -0x7fffffff;
-                    for (uint32_t a = 0; a < 2; a++)
-                        for (uint32_t b = 0; b < 2; b++) {
-                            size_t i = (size_t)(2 * cx + a) * m2 + 2 * cz + b;
-                            lo = g->hmin[l + 1][i] < lo ? g->hmin[l + 1][i] : lo;
-                            hi = g->hmax[l + 1][i] > hi ? g->hmax[l + 1][i] : hi;
-                        }
-                    g->hmin[l][(size_t)cx * m + cz] = lo;
-                    g->hmax[l][(size_t)cx * m + cz] = hi;
-                }
-        }
-    }
+    gen_pyramid(g, threads);
     uint8_t live[64];
     memset(live, 1, 64);
     uint64_t total;
-    uint32_t root = gen_build(g, 0, 0, 0, 0, live, &total);
+    uint32_t root = threads > 1 && GEN_TASK_LEVEL <= g->leaf_level ? gen_build_threaded(g, threads, &total)
+                                                                   : gen_build(g, 0, 0, 0, 0, live, &total);
     uint32_t* words = NULL;
     if (root != GEN_EMPTY) {
         /* depth-first first-visit rank per level (create_hash_dag order) */
@@ -1027,11 +1258,10 @@ uint32_t* or_generate_basic_dag_ex(uint64_t seed, uint32_t depth, uint32_t T, ui
             words = NULL;
         }
     }
+    gen_levels_free(g);
     for (uint32_t l = 0; l <= g->leaf_level; l++) {
-        gen_level* L = &g->lv[l];
-        free(L->mask); free(L->count); free(L->leaf); free(L->kid0); free(L->kids);
-        free(L->map.keys); free(L->map.ids);
-        free(g->hmin[l]); free(g->hmax[l]);
+        free(g->hmin[l]);
+        free(g->hmax[l]);
     }
     free(g);
     return words;

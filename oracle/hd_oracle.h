@@ -62,6 +62,9 @@ uint32_t* or_generate_basic_dag(uint64_t seed, uint32_t depth, uint32_t color_tr
 /* flags: HD_SCENE_SHELL keeps only the surface shell of the solid scene */
 uint32_t* or_generate_basic_dag_ex(uint64_t seed, uint32_t depth, uint32_t color_tree_levels, uint32_t flags,
                                    uint64_t* n_words);
+/* the same words, built by `threads` threads (0: every online core) */
+uint32_t* or_generate_basic_dag_mt(uint64_t seed, uint32_t depth, uint32_t color_tree_levels, uint32_t flags,
+                                   uint32_t threads, uint64_t* n_words);
 void or_free(void* p);
 
 /* ---- ingest: HashDAGFactory::load_from_DAG ---------------------------- */

@@ -105,6 +105,8 @@ def lib():
         L.or_generate_basic_dag.argtypes = [u64, u32, u32, C.POINTER(u64)]
         L.or_generate_basic_dag_ex.restype = C.POINTER(u32)
         L.or_generate_basic_dag_ex.argtypes = [u64, u32, u32, u32, C.POINTER(u64)]
+        L.or_generate_basic_dag_mt.restype = C.POINTER(u32)
+        L.or_generate_basic_dag_mt.argtypes = [u64, u32, u32, u32, u32, C.POINTER(u64)]
         L.or_scene_shell.restype = C.c_int
         L.or_scene_shell.argtypes = [u64, u32, u32, u32, u32]
         L.or_free.argtypes = [P]
@@ -174,9 +176,11 @@ def camera(cam):
 SCENE_SHELL = 1
 
 
-def generate_basic_dag(seed, depth, color_tree_levels, flags=0):
+def generate_basic_dag(seed, depth, color_tree_levels, flags=0, threads=1):
+    """BasicDAG words of the seeded scene; threads > 1 (0: every core)
+    builds subtrees in parallel, with the same words."""
     n = C.c_uint64(0)
-    p = lib().or_generate_basic_dag_ex(seed, depth, color_tree_levels, flags, C.byref(n))
+    p = lib().or_generate_basic_dag_mt(seed, depth, color_tree_levels, flags, threads, C.byref(n))
     if not p:
         raise RuntimeError("scene generation failed")
     words = np.ctypeslib.as_array(p, shape=(n.value,)).copy()

@@ -1,0 +1,53 @@
+"""Traversal against the reference's own CUDA tracer on the same GPU.
+
+The reference's tracer.cu, compiled unmodified for sm_103a with its own
+build's flags (fused multiply-adds contracted, as nvcc does by default), is
+loaded from oracle/_ref and launched as its headless DAGTracer launches it
+(oracle/refgpu.py).  Whole 1920 x 1080 frames of the 2^10, 2^12 and 2^15
+scenes: the library's paths (fp_mode 1, the arithmetic of that build) and
+shadow masks must equal the reference kernel's bit for bit.
+"""
+import numpy as np
+import pytest
+
+import hashdag_gb300 as hd
+from hashdag_gb300 import workloads
+from oracle import refgpu
+
+pytestmark = pytest.mark.gpu
+LIGHT = (0.3, 1.0, 0.2)
+W, H = 1920, 1080
+
+
+def _poses(depth, n):
+    return [workloads.orbit_camera(depth, W, H)] + workloads.catmull_rom_path(depth, 64, W, H)[::64 // n][:n]
+
+
+@pytest.mark.parametrize("depth,n_path", [(10, 6), (12, 4), (15, 3)])
+def test_frames_equal_reference_gpu_tracer(gpu, depth, n_path):
+    ctl, bits = workloads.color_tree_levels(depth), workloads.top_bucket_bits(depth)
+    if not refgpu.available(depth, ctl, bits):
+        pytest.skip("the reference tracer's cubin is built only where the reference sources are")
+    d = hd.HashDAG(depth)
+    d.generate_scene(workloads.SEED_SCENE)
+    ref = refgpu.RefGpuTracer(depth, ctl, bits)
+    try:
+        assert (ref.width, ref.height) == (W, H)
+        ref.set_table(d.export_table())
+        tr = hd.DAGTracer(W, H)
+        d.set_fp_mode(1)
+        for k, cam in enumerate(_poses(depth, n_path)):
+            want_paths, want_mask, ms = ref.trace_view(cam, LIGHT, 1.0)
+            tr.resolve_paths(cam, d)
+            tr.resolve_shadows(cam, d, 1.0, LIGHT)
+            paths = np.ascontiguousarray(tr.get_paths()).reshape(H, W, 4)
+            mask = np.ascontiguousarray(tr.get_shadows()).reshape(H, W)
+            hits = int((want_paths[..., :3] != 0).any(-1).sum())
+            assert hits > W * H // 100, (depth, k)
+            diff = int((paths != want_paths).any(-1).sum())
+            assert diff == 0, f"depth {depth} pose {k}: {diff} pixels differ from the reference kernel"
+            assert np.array_equal(mask, want_mask), (depth, k)
+            assert ms[0] > 0 and ms[1] > 0
+    finally:
+        ref.close()
+        d.free()
