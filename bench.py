@@ -258,7 +258,7 @@ def cpu_baseline(ot, cams_params, W, H, seconds):
     t0 = time.perf_counter()
     rays = frames = 0
     while frames < len(cams_params) and time.perf_counter() - t0 < seconds:
-        paths, mask = ot.trace_frame(cams_params[frames], W, H, LIGHT, BIAS, fp_mode=1, threads=threads)
+        paths, mask = ot.trace_frame(cams_params[frames], W, H, LIGHT, BIAS, fp_mode=0, threads=threads)
         rays += W * H + int((mask != 2).sum())
         frames += 1
     dt = time.perf_counter() - t0
@@ -549,7 +549,7 @@ def run_reference(args, dist):
         n = 0
         for j in range(nv):
             cam = poses[views[j * args.views // nv]]
-            paths, mask = ot.trace_frame(cam, W, H, LIGHT, BIAS, fp_mode=1, threads=threads)
+            paths, mask = ot.trace_frame(cam, W, H, LIGHT, BIAS, fp_mode=0, threads=threads)
             n += W * H + int((mask != 2).sum())
         return n
 
@@ -594,7 +594,7 @@ def ref_gpu_baseline(dag, args, poses, flush, ours_value):
         if (ref.width, ref.height) != (W, H):
             return {"value": None, "unavailable": f"the reference tracer is compiled for {ref.width}x{ref.height}"}
         ref.set_table(dag.export_table())
-        # parity on the first view (fp_mode 1 = the reference build's arithmetic)
+        # parity on the first view (the library's default arithmetic, fp_mode 0)
         cam0 = poses[replica_poses(0, V, 0, len(poses))[0]]
         rp, rm, _ = ref.trace_view(cam0, LIGHT, BIAS)
         tr = hd.DAGTracer(W, H)

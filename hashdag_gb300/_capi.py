@@ -151,6 +151,8 @@ SIGNATURES = [
     ("hd_save_basic_dag_file", C.c_int, [_P, C.c_char_p, C.POINTER(DagInfo)]),
     ("hd_load_colors_file", C.c_int, [_P, C.c_char_p, _u32]),
     ("hd_save_snapshot", C.c_int, [_P, C.c_char_p, C.POINTER(DagInfo)]),
+    ("hd_camera_from_view", C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double, _u32,
+                                      C.POINTER(DagInfo), _u32, _u32, C.POINTER(Camera)]),
     ("hd_replay_load", C.c_int, [C.c_char_p, C.POINTER(_P)]),
     ("hd_replay_load_text", C.c_int, [C.c_char_p, _u64, C.POINTER(_P)]),
     ("hd_replay_free", C.c_int, [_P]),

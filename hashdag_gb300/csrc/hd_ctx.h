@@ -27,7 +27,7 @@ struct hd_ctx {
     cudaStream_t stream = nullptr;
     uint32_t* d_root = nullptr;        // firstNodeIndex on the device
     uint32_t root = 0;                 // host copy, refreshed after each call
-    uint32_t fp_mode = 1;
+    uint32_t fp_mode = 0; // every operation rounded on its own: the reference kernel's arithmetic
     std::string err;
     std::string err_detail;           // detail words of the last device error
     hd::Scratch scratch;               // grow-only working buffers

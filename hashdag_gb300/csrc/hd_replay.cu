@@ -206,14 +206,18 @@ void write(const hd_replay& r, std::ostream& os)
     }
 }
 
-// get_trace_params (dag_tracer.cu:71-113) of the replay's view
-hd_camera camera_of(const hd_replay& r, uint32_t levels, const hd_replay_config& cfg)
+// get_trace_params (dag_tracer.cu:71-113): the camera frame (right = -row
+// 0, up = row 1, forward = row 2 of the rotation, camera_view.h:13-27) at
+// fov_degrees, mapped into the voxel space of a 2^levels scene whose
+// bounding box is info.
+hd_camera camera_from_view(const double position[3], const double rotation[9], double fov_degrees, uint32_t levels,
+                           const hd_dag_info& info, uint32_t width, uint32_t height)
 {
-    const double* p = r.position;
-    const double* m = r.rotation;
+    const double* p = position;
+    const double* m = rotation;
     const double right[3] = {-m[0], -m[1], -m[2]}, up[3] = {m[3], m[4], m[5]}, fwd[3] = {m[6], m[7], m[8]};
-    const double fov = double(60.f) / 2.0 * (double(M_PI) / 180.);
-    const double aspect = double(cfg.width) / double(cfg.height);
+    const double fov = fov_degrees / 2.0 * (double(M_PI) / 180.);
+    const double aspect = double(width) / double(height);
     hd_camera cam{};
     double bl[3], br[3], tl[3];
     for (int a = 0; a < 3; a++) {
@@ -223,16 +227,22 @@ hd_camera camera_of(const hd_replay& r, uint32_t levels, const hd_replay_config&
         tl[a] = p[a] + Z + Y - X;
     }
     for (int a = 0; a < 3; a++) {
-        const double translation = -cfg.info.aabb_min[a];
-        const double scale = double(1u << levels) / (cfg.info.aabb_max[a] - cfg.info.aabb_min[a]);
+        const double translation = -info.aabb_min[a];
+        const double scale = double(1u << levels) / (info.aabb_max[a] - info.aabb_min[a]);
         const double fp = (p[a] + translation) * scale, fbl = (bl[a] + translation) * scale,
                      ftl = (tl[a] + translation) * scale, fbr = (br[a] + translation) * scale;
         cam.position[a] = fp;
         cam.ray_min[a] = fbl;
-        cam.ray_ddx[a] = (fbr - fbl) * (1.0 / cfg.width);
-        cam.ray_ddy[a] = (ftl - fbl) * (1.0 / cfg.height);
+        cam.ray_ddx[a] = (fbr - fbl) * (1.0 / width);
+        cam.ray_ddy[a] = (ftl - fbl) * (1.0 / height);
     }
     return cam;
+}
+
+// the replay's view, with CameraView::fov (60 degrees, camera_view.h:9)
+hd_camera camera_of(const hd_replay& r, uint32_t levels, const hd_replay_config& cfg)
+{
+    return camera_from_view(r.position, r.rotation, double(60.f), levels, cfg.info, cfg.width, cfg.height);
 }
 
 // IReplayAction::apply (replay.cpp:5-100) on the context
@@ -312,6 +322,19 @@ void apply(hd_ctx* c, hd_replay& r, const hd_replay::Action& a, float scale, uin
 using namespace hd;
 
 extern "C" {
+
+hd_status hd_camera_from_view(const double position[3], const double rotation[9], double fov_degrees, uint32_t levels,
+                              const hd_dag_info* info, uint32_t width, uint32_t height, hd_camera* out)
+{
+    if (!position || !rotation || !info || !out || !width || !height || levels > 31 || !(fov_degrees > 0.0) ||
+        !(fov_degrees < 180.0))
+        return HD_ERR_INVALID;
+    for (int a = 0; a < 3; a++)
+        if (!(info->aabb_max[a] > info->aabb_min[a]))
+            return HD_ERR_INVALID;
+    *out = camera_from_view(position, rotation, fov_degrees, levels, *info, width, height);
+    return HD_OK;
+}
 
 hd_status hd_replay_load(const char* path, hd_replay** out)
 {

@@ -230,9 +230,12 @@ hd_status hd_trace_counters(hd_ctx* ctx, const hd_camera* cam, uint32_t width, u
 hd_status hd_trace_counters_noalloc(hd_ctx* ctx, const hd_camera* cam, uint32_t width, uint32_t height,
                                     const float light[3], float bias, uint32_t* d_paths, uint8_t* d_mask,
                                     uint64_t out[6]);
-/* Selects the arithmetic of the ray set-up: 0 = every float/double op
- * rounded on its own, 1 = the fused multiply-adds nvcc contracts in the
- * reference's default build.  Default 1. */
+/* Selects the arithmetic of the ray set-up: 0 = every float/double
+ * operation rounded on its own, which is what the reference's tracer.cu
+ * computes when nvcc compiles it for sm_103a with its build's flags (the
+ * library equals that kernel bit for bit on the same GPU, and equals the
+ * reference compiled for the host); 1 = fused multiply-adds at the places a
+ * contracting build would put them.  Default 0. */
 hd_status hd_set_fp_mode(hd_ctx* ctx, uint32_t mode);
 
 /* ---- point queries (DAGUtils::get_value, dag_utils.h:138-172) ---------- */
@@ -428,6 +431,13 @@ typedef struct hd_dag_info {
     double aabb_min[3];
     double aabb_max[3];
 } hd_dag_info;
+
+/* get_trace_params (dag_tracer.cu:71-113): the camera of a CameraView
+ * (camera_view.h:7-28: position, rotation rows right = -row 0, up = row 1,
+ * forward = row 2, fov 60 degrees in the reference) for a width x height
+ * image of a 2^levels scene whose bounding box is info, in voxel space. */
+hd_status hd_camera_from_view(const double position[3], const double rotation[9], double fov_degrees, uint32_t levels,
+                              const hd_dag_info* info, uint32_t width, uint32_t height, hd_camera* out);
 
 /* BasicDAGFactory::load_dag_from_file (basic_dag.cpp:105-117) followed by
  * load_from_DAG (as hd_load_basic_dag).  The file's level count must equal

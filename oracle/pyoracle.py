@@ -280,13 +280,13 @@ class Table:
         lib().or_reachable_counts(self.h, self.root if root is None else root, out)
         return out[:self.cfg.depth - 1]
 
-    def trace_primary(self, cam, w, h, fp_mode=1, rows=None):
+    def trace_primary(self, cam, w, h, fp_mode=0, rows=None):
         paths = np.zeros(w * h * 4, np.uint32)
         r0, r1 = (0, h) if rows is None else rows
         lib().or_trace_primary(self.h, C.byref(camera(cam)), w, h, fp_mode, paths, r0, r1, None)
         return paths.reshape(h, w, 4)
 
-    def trace_shadow(self, cam, w, h, paths, light, bias, fp_mode=1, rows=None):
+    def trace_shadow(self, cam, w, h, paths, light, bias, fp_mode=0, rows=None):
         mask = np.zeros(w * h, np.uint8)
         r0, r1 = (0, h) if rows is None else rows
         lib().or_trace_shadow(self.h, C.byref(camera(cam)), w, h, fp_mode,
@@ -294,7 +294,7 @@ class Table:
                               np.asarray(light, np.float32), bias, mask, r0, r1, None)
         return mask.reshape(h, w)
 
-    def trace_frame(self, cam, w, h, light, bias, fp_mode=1, threads=1, rows=None):
+    def trace_frame(self, cam, w, h, light, bias, fp_mode=0, threads=1, rows=None):
         paths = np.zeros(w * h * 4, np.uint32)
         mask = np.zeros(w * h, np.uint8)
         r0, r1 = (0, h) if rows is None else rows

@@ -96,7 +96,7 @@ def test_pool_full_edit_is_refused_and_table_stays_usable(gpu):
 def _bucket_case():
     """2^9 top-level buckets: the scene fits (largest bucket 744 of 1024
     words) and the sixth of these edits overflows a level-7 bucket."""
-    return {"top_bucket_bits": 9}, workloads.mixed_edits(DEPTH, 6, (64.0, 400.0), seed=7)
+    return {"top_bucket_bits": 9}, workloads.mixed_edits(DEPTH, 40, (64.0, 400.0), seed=7)[:6]
 
 
 @pytest.mark.parametrize("batched", [False, True])
@@ -132,7 +132,7 @@ def test_bucket_full_edit_is_refused(gpu, batched):
     ot2 = _oracle(kw, words)
     for e in edits[:5]:
         ot2.edit(*e)
-    op, om = ot2.trace_frame(workloads.orbit_camera(DEPTH, W, H), W, H, (0.3, 1.0, 0.2), 1.0, fp_mode=1, threads=4)
+    op, om = ot2.trace_frame(workloads.orbit_camera(DEPTH, W, H), W, H, (0.3, 1.0, 0.2), 1.0, fp_mode=0, threads=4)
     assert np.array_equal(frame[0], op) and np.array_equal(frame[1], om)
     # after a GC both tables hold the same nodes at the same virtual addresses
     d.remove_stale_nodes()

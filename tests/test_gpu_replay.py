@@ -98,6 +98,6 @@ def test_replay_matches_oracle(gpu):
     # the last frame, traced from its camera
     tr = hd.DAGTracer(W, H)
     tr.resolve_paths(last_cam, dag)
-    opaths, _ = ot.trace_frame(last_cam, W, H, (0.3, 1.0, 0.2), 1.0, fp_mode=1, threads=os.cpu_count() or 4)
+    opaths, _ = ot.trace_frame(last_cam, W, H, (0.3, 1.0, 0.2), 1.0, fp_mode=0, threads=os.cpu_count() or 4)
     assert np.array_equal(tr.get_paths(), opaths)
     dag.free()

@@ -93,7 +93,7 @@ def test_primary_and_shadow_match_oracle_1080p(gpu, fp_mode):
     assert hits > W * H // 50
     assert np.array_equal(paths, opaths)
     assert np.array_equal(shadows, omask)
-    d.set_fp_mode(1)
+    d.set_fp_mode(0)
 
 
 def test_get_values_match_scene_function(gpu):
@@ -137,7 +137,7 @@ def test_trace_depth15_rows_match_oracle(gpu):
     ot = po.Table(cfg)
     ot.import_(t)
     rows = (1000, 1064)  # pixel rows; output rows H-1-y
-    opaths, omask = ot.trace_frame(cam, W, H, LIGHT_BENCH, 1.0, fp_mode=1, threads=os.cpu_count() or 4,
+    opaths, omask = ot.trace_frame(cam, W, H, LIGHT_BENCH, 1.0, fp_mode=0, threads=os.cpu_count() or 4,
                                    rows=rows)
     out_rows = slice(H - rows[1], H - rows[0])
     assert np.array_equal(paths[out_rows], opaths[out_rows])
@@ -219,7 +219,7 @@ def test_trace_equals_reference_tracer(gpu, depth, name):
         tr.resolve_shadows(f["camera"], d, f["bias"], tuple(f["light"]))
         paths, mask = np.ascontiguousarray(tr.get_paths()), np.ascontiguousarray(tr.get_shadows())
     finally:
-        d.set_fp_mode(1)
+        d.set_fp_mode(0)
     assert int((paths[..., :3] != 0).any(-1).sum()) == f["hits"]
     assert hashlib.sha256(paths.tobytes()).hexdigest() == f["paths_sha256"]
     assert hashlib.sha256(mask.tobytes()).hexdigest() == f["mask_sha256"]
@@ -245,7 +245,7 @@ def test_trace_views_equal_reference_tracer(gpu):
                                             None))
         paths, mask = paths.cpu().numpy().view(np.uint32), mask.cpu().numpy()
     finally:
-        d.set_fp_mode(1)
+        d.set_fp_mode(0)
     for v, f in enumerate(frames):
         assert hashlib.sha256(paths[v * W * H * 4:(v + 1) * W * H * 4].tobytes()).hexdigest() == f["paths_sha256"]
         assert hashlib.sha256(mask[v * W * H:(v + 1) * W * H].tobytes()).hexdigest() == f["mask_sha256"], f["name"]

@@ -106,7 +106,7 @@ def test_trace_colors_equal_reference(gpu, tmp_path):
     dag.set_fp_mode(0)
     tr = hd.DAGTracer(W, H)
     tr.resolve_paths(fx["camera"], dag)
-    dag.set_fp_mode(1)
+    dag.set_fp_mode(0)
     assert hashlib.sha256(np.ascontiguousarray(tr.get_paths()).tobytes()).hexdigest() == fx["paths_sha256"]
     for v in fx["views"]:
         t = v["tool"]
