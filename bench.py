@@ -339,7 +339,8 @@ def edit_bench(args, dist):
                                           "p99_completion_ms": _pct([s.host_ms for s in per], 99),
                                           "tuning": {"foa_warps": tuning.foa_warps,
                                                      "probe_words": tuning.probe_words,
-                                                     "grid_blocks": tuning.grid_blocks},
+                                                     "grid_blocks": tuning.grid_blocks,
+                                                     "mode": ["graph per edit", "persistent"][tuning.mode]},
                                           "fallbacks": fallbacks}),
            "same_root": bool(plain_root == batch_root)}
     res["batched_over_plain_voxels_per_s"] = res["batched"]["voxels_per_s"] / res["plain"]["voxels_per_s"]

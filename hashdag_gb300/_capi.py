@@ -76,10 +76,12 @@ class EditStats(C.Structure):
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("foa_warps", C.c_uint32), ("probe_words", C.c_uint32), ("grid_blocks", C.c_uint32)]
+    _fields_ = [("foa_warps", C.c_uint32), ("probe_words", C.c_uint32), ("grid_blocks", C.c_uint32),
+                ("mode", C.c_uint32)]
 
     def __repr__(self):
-        return f"BatchTuning(foa_warps={self.foa_warps}, probe_words={self.probe_words}, grid_blocks={self.grid_blocks})"
+        return (f"BatchTuning(foa_warps={self.foa_warps}, probe_words={self.probe_words}, "
+                f"grid_blocks={self.grid_blocks}, mode={self.mode})")
 
 
 class Request(C.Structure):

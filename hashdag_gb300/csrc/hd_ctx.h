@@ -44,7 +44,7 @@ struct hd_ctx {
     uint32_t* edit_head_ptr = nullptr;
     // batched edits: tuning, the captured graph, edits that took the
     // one-edit path because a level outgrew its bound
-    hd_batch_tuning tuning{4, 4, 304};
+    hd_batch_tuning tuning{4, 4, 304, HD_BATCH_PERSISTENT};
     hd::BatchGraph* batch = nullptr;
     uint64_t batch_fallbacks = 0;
     // colours: the table, host mirror of its counters

@@ -240,8 +240,21 @@ HD_D void warp_add(unsigned long long* p, unsigned long long v)
         atomicAdd(p, v);
 }
 
+// Reads of a node's words.  CG = false: through the read-only path, for
+// kernels during which the table does not change; CG = true: L2-coherent
+// loads, for a launch that also appends to the table (the persistent batched
+// edits read in one edit the nodes and pages an earlier edit of the same
+// launch wrote).
+template <bool CG>
+struct NodeRead {
+    const uint32_t* p;
+    HD_D NodeRead(const Table& t, uint32_t v) : p(CG ? t.sys_cg(v) : t.sys(v)) {}
+    HD_D uint32_t operator[](uint32_t k) const { return CG ? __ldcg(p + k) : p[k]; }
+};
+
 // Top-down classification of entry i of level `level` (edit_threaded /
 // edit_leaf early exits); nodes / voxels: its share of the edit counters.
+template <bool CG = false>
 HD_D void classify_entry(const Table& t, const Editor& ed, uint32_t level, const Level& lv, uint32_t i,
                          unsigned long long& nodes, unsigned long long& voxels)
 {
@@ -268,7 +281,7 @@ HD_D void classify_entry(const Table& t, const Editor& ed, uint32_t level, const
             if (!se) {
                 state = kKeep;
                 if (old != kInvalid) {
-                    const uint32_t* p = t.sys(old);
+                    const NodeRead<CG> p(t, old);
                     cnt = level < leafl ? (p[0] >> 8) : popc32(p[0]) + popc32(p[1]);
                 }
             } else if (ed.shortcuts() && inside_tool(ed, mnx, mny, mnz, mxx, mxy, mxz)) {
@@ -286,7 +299,7 @@ HD_D void classify_entry(const Table& t, const Editor& ed, uint32_t level, const
                 state = kLeafEval;
                 uint64_t leaf = 0;
                 if (old != kInvalid) {
-                    const uint32_t* p = t.sys(old);
+                    const NodeRead<CG> p(t, old);
                     leaf = uint64_t(p[0]) | (uint64_t(p[1]) << 32);
                 }
                 const uint32_t x0 = lv.x[i] << 2, y0 = lv.y[i] << 2, z0 = lv.z[i] << 2;
@@ -316,7 +329,7 @@ HD_D void classify_entry(const Table& t, const Editor& ed, uint32_t level, const
     if (lv.ocnt && level >= T) {
         uint32_t oc = 0;
         if (old != kInvalid) {
-            const uint32_t* p = t.sys(old);
+            const NodeRead<CG> p(t, old);
             oc = level < leafl ? (p[0] >> 8) : popc32(p[0]) + popc32(p[1]);
         }
         lv.ocnt[i] = oc;
@@ -346,9 +359,28 @@ HD_D void spawn_entry(const Table& t, const Level& lv, const Level& next, uint32
     }
 }
 
+// Child c of descended entry i, written at slot `at` of the next level
+// (spawn_entry for one child, with L2-coherent table reads).
+HD_D void spawn_child(const Table& t, const Level& lv, const Level& next, uint32_t i, uint32_t c, uint32_t at)
+{
+    const uint32_t old = lv.old[i];
+    uint32_t child = kInvalid;
+    if (old != kInvalid) {
+        const NodeRead<true> p(t, old);
+        const uint32_t mask = p[0] & 0xffu;
+        if (mask & (1u << c))
+            child = p[child_offset(mask, c)];
+    }
+    next.x[at] = (lv.x[i] << 1) | ((c >> 2) & 1);
+    next.y[at] = (lv.y[i] << 1) | ((c >> 1) & 1);
+    next.z[at] = (lv.z[i] << 1) | (c & 1);
+    next.old[at] = child;
+}
+
 // Bottom-up: the rebuilt content of entry i (kLeafEval / kDescend).  Unchanged
 // and emptied nodes resolve at once (kNoBucket); otherwise the content goes
 // to lv.cand and the function returns its bucket for find-or-add.
+template <bool CG = false>
 HD_D uint32_t candidate_entry(const Table& t, uint32_t level, const Level& lv, const Level& child, uint32_t i)
 {
     const uint32_t T = t.g.T;
@@ -360,7 +392,7 @@ HD_D uint32_t candidate_entry(const Table& t, uint32_t level, const Level& lv, c
         const uint32_t old = lv.old[i];
         uint64_t initial = 0;
         if (old != kInvalid) {
-            const uint32_t* p = t.sys(old);
+            const NodeRead<CG> p(t, old);
             initial = uint64_t(p[0]) | (uint64_t(p[1]) << 32);
         }
         lv.cnt[i] = popc64(leaf);
@@ -382,11 +414,9 @@ HD_D uint32_t candidate_entry(const Table& t, uint32_t level, const Level& lv, c
         uint32_t mask = 0, k = 1, total = 0;
         bool changed = false;
         uint32_t omask = 0;
-        const uint32_t* p = nullptr;
-        if (old != kInvalid) {
-            p = t.sys(old);
+        const NodeRead<CG> p(t, old != kInvalid ? old : 0u);
+        if (old != kInvalid)
             omask = p[0] & 0xffu;
-        }
         uint32_t ok = 1;
         for (uint32_t s = 0; s < 8; s++) {
             const uint32_t oc = (omask & (1u << s)) ? p[ok++] : kInvalid;

@@ -26,6 +26,12 @@
 namespace hd {
 
 void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats); // hd_edit.cu
+// hd_edit_persist.cu
+void edit_batch_persistent(hd_ctx* c, const hd_edit* edits, uint32_t n, const std::vector<Level>& lv,
+                           const std::vector<uint32_t>& caps, uint32_t* keys, uint32_t* vals, uint32_t* keys2,
+                           uint32_t* vals2, hd_edit* d_edits, EditCounters* d_ctr, uint32_t* d_roots,
+                           std::vector<EditCounters>& ctr, std::vector<float>& dur_ms, std::vector<float>& end_ms,
+                           float& device_ms, uint64_t& fallbacks);
 
 enum : uint32_t { kStopNone = 0, kStopCapacity = 1, kStopTableError = 2, kStopEmptyScene = 3 };
 
@@ -644,6 +650,41 @@ void edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* per_
         cap[L] = std::max<uint64_t>(v, L < bg.caps.size() ? bg.caps[L] : 0);
     }
     const BatchBuffers b = batch_buffers(c, cap, std::max<uint32_t>(n, bg.edit_cap));
+    if (c->tuning.mode == HD_BATCH_PERSISTENT) {
+        std::vector<EditCounters> ctr(n);
+        std::vector<float> end_ms(n, 0.0f), dur_ms(n, 0.0f);
+        float device_ms = 0.0f;
+        try {
+            edit_batch_persistent(c, edits, n, b.lv, b.caps, b.keys, b.vals, b.keys2, b.vals2, b.edits, b.ctr,
+                                  b.roots, ctr, dur_ms, end_ms, device_ms, c->batch_fallbacks);
+        } catch (...) {
+            c->root = read_scalar(c->d_root, st);
+            throw;
+        }
+        c->root = read_scalar(c->d_root, st);
+        for (uint32_t i = 0; i < n; i++) {
+            hd_edit_stats s{};
+            s.num_voxels = ctr[i].num_voxels;
+            s.num_nodes = ctr[i].num_nodes;
+            s.find_or_add_calls = ctr[i].foa;
+            s.nodes_added = ctr[i].added;
+            s.words_scanned = ctr[i].scanned;
+            s.device_ms = dur_ms[i];
+            s.host_ms = end_ms[i];
+            if (per_edit)
+                per_edit[i] = s;
+            sum.num_voxels += s.num_voxels;
+            sum.num_nodes += s.num_nodes;
+            sum.find_or_add_calls += s.find_or_add_calls;
+            sum.nodes_added += s.nodes_added;
+            sum.words_scanned += s.words_scanned;
+        }
+        sum.device_ms = device_ms;
+        sum.host_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (total)
+            *total = sum;
+        return;
+    }
     if (!bg.exec || bg.ptrs != b.ptrs() || bg.caps != b.caps || bg.tuning.foa_warps != c->tuning.foa_warps ||
         bg.tuning.probe_words != c->tuning.probe_words || bg.tuning.grid_blocks != c->tuning.grid_blocks)
         capture(c, bg, b, b.edit_cap);
@@ -781,7 +822,7 @@ bool valid_tuning(const hd_batch_tuning& t)
 {
     return (t.foa_warps == 2 || t.foa_warps == 4 || t.foa_warps == 8) &&
            (t.probe_words == 1 || t.probe_words == 2 || t.probe_words == 4) && t.grid_blocks >= 64 &&
-           t.grid_blocks <= 2048 && t.grid_blocks % 8 == 0;
+           t.grid_blocks <= 2048 && t.grid_blocks % 8 == 0 && (t.mode == HD_BATCH_GRAPH || t.mode == HD_BATCH_PERSISTENT);
 }
 
 // Copies the table of `from` into `to` (same configuration); pages that `to`
@@ -874,10 +915,23 @@ hd_status hd_autotune_batch(hd_ctx* c, const hd_edit* sample, uint32_t n, hd_bat
         const uint32_t grids[3] = {sms * 2, sms * 4, sms * 8};
         const uint32_t warps[3] = {2, 4, 8};
         const uint32_t probes[3] = {1, 2, 4};
+        for (uint32_t P : probes) {
+            // the persistent form (its launch shape is fixed: one CTA per SM)
+            k->tuning = hd_batch_tuning{4, P, 304, HD_BATCH_PERSISTENT};
+            hd_edit_stats tot{};
+            copy_table(k, c);
+            edit_batch(k, sample, n, nullptr, &tot);
+            copy_table(k, c);
+            edit_batch(k, sample, n, nullptr, &tot);
+            if (chosen_ms < 0.0f || tot.device_ms < chosen_ms) {
+                chosen_ms = tot.device_ms;
+                chosen = k->tuning;
+            }
+        }
         for (uint32_t G : grids)
             for (uint32_t W : warps)
                 for (uint32_t P : probes) {
-                    k->tuning = hd_batch_tuning{W, P, G};
+                    k->tuning = hd_batch_tuning{W, P, G, HD_BATCH_GRAPH};
                     hd_edit_stats tot{};
                     // first run captures the graph; the second is timed
                     copy_table(k, c);

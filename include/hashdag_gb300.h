@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define HD_ABI_VERSION 6u
+#define HD_ABI_VERSION 7u
 #define HD_PAGE_SIZE 512u
 #define HD_MAX_DEPTH 20u
 /* Sentinel of the edit recursion (hash_dag_edits.h:17). */
@@ -262,11 +262,17 @@ hd_status hd_edit_batch(hd_ctx* ctx, const hd_edit* edits, uint32_t n, hd_edit_s
 hd_status hd_edit_batch_ex(hd_ctx* ctx, const hd_edit* edits, uint32_t n, hd_edit_stats* per_edit,
                            hd_edit_stats* total);
 
-/* Launch shape of the batched edit kernels (results never depend on it). */
+/* Launch shape of the batched edit kernels (results never depend on it).
+ * mode HD_BATCH_GRAPH: one captured CUDA graph of level kernels per edit;
+ * mode HD_BATCH_PERSISTENT: the whole batch in one cooperative launch of one
+ * CTA per SM (foa_warps and grid_blocks unused). */
+#define HD_BATCH_GRAPH 0u
+#define HD_BATCH_PERSISTENT 1u
 typedef struct hd_batch_tuning {
     uint32_t foa_warps;   /* warps per find-or-add block: 2, 4 or 8            */
     uint32_t probe_words; /* words per lane per bucket-page load: 1, 2 or 4    */
     uint32_t grid_blocks; /* blocks of the level kernels: 64 .. 2048           */
+    uint32_t mode;        /* HD_BATCH_GRAPH or HD_BATCH_PERSISTENT             */
 } hd_batch_tuning;
 hd_status hd_set_batch_tuning(hd_ctx* ctx, const hd_batch_tuning* tuning);
 hd_status hd_get_batch_tuning(hd_ctx* ctx, hd_batch_tuning* tuning);

@@ -141,10 +141,12 @@ def _stats_tuple(s):
     return (s.num_voxels, s.num_nodes, s.find_or_add_calls, s.nodes_added, s.words_scanned)
 
 
-@pytest.mark.parametrize("tuning", [(4, 4, 304), (2, 1, 1216), (8, 2, 608)])
+@pytest.mark.parametrize("tuning", [(4, 4, 304, 0), (2, 1, 1216, 0), (8, 2, 608, 0), (4, 4, 304, 1), (4, 1, 304, 1),
+                                    (4, 2, 304, 1)])
 def test_batch_launch_shapes_agree(gpu, tuning):
-    """Every launch shape of the batched path gives the plain path's table
-    and per-edit counters (depth 12, uneven radii)."""
+    """Every launch shape of the batched path, graph per edit (mode 0) or one
+    persistent launch (mode 1), gives the plain path's table and per-edit
+    counters (depth 12, uneven radii)."""
     depth = 12
     edits = workloads.mixed_edits(depth, 24, (2.0, 200.0), seed=37)
     a = hd.HashDAG(depth)
@@ -164,10 +166,11 @@ def test_batch_launch_shapes_agree(gpu, tuning):
     b.free()
 
 
-def test_batch_depth15_matches_plain(gpu):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_batch_depth15_matches_plain(gpu, mode):
     """A batch of 64 edits of radius 4..512 on the 2^15 scene: same roots,
     per-level words and nodes, counters and sampled occupancy as the
-    one-edit path."""
+    one-edit path, in both batch modes."""
     depth = 15
     edits = workloads.mixed_edits(depth, 64, (4.0, 512.0), seed=3)
     a = hd.HashDAG(depth)
@@ -175,6 +178,7 @@ def test_batch_depth15_matches_plain(gpu):
     plain = [a.edit_threads(hd.editor_from_tuple(e)) for e in edits]
     b = hd.HashDAG(depth)
     b.generate_scene(1)
+    b.batch_tuning = (4, 4, 304, mode)
     total, per = b.edit_batch([hd.editor_from_tuple(e) for e in edits], per_edit=True)
     assert [_stats_tuple(s) for s in per] == [_stats_tuple(s) for s in plain]
     assert a.firstNodeIndex == b.firstNodeIndex
@@ -202,5 +206,6 @@ def test_autotune_leaves_table_unchanged(gpu):
     assert d.firstNodeIndex == r0
     assert table_digest(d.export_table(), depth) == before
     cur = d.batch_tuning
-    assert (cur.foa_warps, cur.probe_words, cur.grid_blocks) == (t.foa_warps, t.probe_words, t.grid_blocks)
+    assert (cur.foa_warps, cur.probe_words, cur.grid_blocks, cur.mode) == \
+        (t.foa_warps, t.probe_words, t.grid_blocks, t.mode)
     d.free()

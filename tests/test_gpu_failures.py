@@ -134,9 +134,10 @@ def test_bucket_full_edit_is_refused(gpu, batched):
         ot2.edit(*e)
     op, om = ot2.trace_frame(workloads.orbit_camera(DEPTH, W, H), W, H, (0.3, 1.0, 0.2), 1.0, fp_mode=0, threads=4)
     assert np.array_equal(frame[0], op) and np.array_equal(frame[1], om)
-    # after a GC both tables hold the same nodes at the same virtual addresses
+    # after a GC the table holds what a GC of the five applied edits holds,
+    # at the same virtual addresses: the failed edit left nothing reachable
     d.remove_stale_nodes()
-    ot.gc()
-    assert d.firstNodeIndex == ot.root
-    assert table_digest(d.export_table(), DEPTH, 9) == table_digest(ot.export(), DEPTH, 9)
+    ot2.gc()
+    assert d.firstNodeIndex == ot2.root
+    assert table_digest(d.export_table(), DEPTH, 9) == table_digest(ot2.export(), DEPTH, 9)
     d.free()
