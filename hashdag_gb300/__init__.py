@@ -32,6 +32,7 @@ TOOL_SPHERE_REMOVE, TOOL_SPHERE_ADD, TOOL_BOX_REMOVE, TOOL_BOX_ADD, TOOL_SPHERE_
     TOOL_NOISE_REMOVE, TOOL_NOISE_ADD, TOOL_FILL = range(9)
 SCENE_SHELL = 1
 GC_KEEP_HISTORY = 1
+GC_RELEASE_PAGES = 2
 # EDebugColors (tracer.h:7-17) and the overlay's ETool (tracer.h:21-29)
 DEBUG_NONE, DEBUG_INDEX, DEBUG_POSITION, DEBUG_COLOR_TREE, DEBUG_COLOR_BITS, DEBUG_MIN_COLOR, DEBUG_MAX_COLOR, \
     DEBUG_WEIGHT = range(8)
@@ -478,24 +479,25 @@ class HashDAG:
         self._check(lib().hd_batch_fallbacks(self._h, C.byref(v)))
         return v.value
 
-    def remove_stale_nodes(self, extra_roots=(), keep_history=False):
+    def remove_stale_nodes(self, extra_roots=(), keep_history=False, release_pages=False):
         """HashDAG::remove_stale_nodes(levels - 2), marking from the root and
         from extra_roots; returns the remapped extra roots.  The undo / redo
         history is dropped (as the reference's engine does) unless
-        keep_history, which keeps its states alive."""
+        keep_history, which keeps its states alive.  release_pages: pages
+        past every bucket's new size go back to a free list."""
         arr = np.array(list(extra_roots) + [0], np.uint32)
-        self._check(lib().hd_gc_ex(self._h, arr.ctypes.data, len(extra_roots),
-                                   GC_KEEP_HISTORY if keep_history else 0))
+        flags = (GC_KEEP_HISTORY if keep_history else 0) | (GC_RELEASE_PAGES if release_pages else 0)
+        self._check(lib().hd_gc_ex(self._h, arr.ctypes.data, len(extra_roots), flags))
         return [int(v) for v in arr[:len(extra_roots)]]
 
     # -- serving loop ----------------------------------------------------------
     def serve(self, requests, continuous=True, max_renders=3, realtime=True, gc_free_fraction=0.1,
-              light=(0.3, 1.0, 0.2), shadow_bias=1.0):
+              light=(0.3, 1.0, 0.2), shadow_bias=1.0, release_pages=True, batch_edits=True):
         """Runs a request trace (a list of Request, arrival times
         non-decreasing); returns (list of RequestResult, ServeStats)."""
         arr = (Request * max(1, len(requests)))(*requests)
         cfg = ServeConfig(int(continuous), int(max_renders), int(realtime), float(gc_free_fraction),
-                          (C.c_float * 3)(*light), float(shadow_bias))
+                          (C.c_float * 3)(*light), float(shadow_bias), int(release_pages), int(batch_edits))
         res = (RequestResult * max(1, len(requests)))()
         st = ServeStats()
         self._check(lib().hd_serve(self._h, arr, len(requests), C.byref(cfg), res, C.byref(st)))

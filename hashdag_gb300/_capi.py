@@ -91,7 +91,8 @@ class Request(C.Structure):
 
 class ServeConfig(C.Structure):
     _fields_ = [("continuous", C.c_uint32), ("max_renders", C.c_uint32), ("realtime", C.c_uint32),
-                ("gc_free_fraction", C.c_float), ("light", C.c_float * 3), ("shadow_bias", C.c_float)]
+                ("gc_free_fraction", C.c_float), ("light", C.c_float * 3), ("shadow_bias", C.c_float),
+                ("release_pages", C.c_uint32), ("batch_edits", C.c_uint32)]
 
 
 class RequestResult(C.Structure):
@@ -102,7 +103,7 @@ class RequestResult(C.Structure):
 
 class ServeStats(C.Structure):
     _fields_ = [("wall_ms", C.c_double), ("edits", C.c_uint32), ("renders", C.c_uint32), ("gcs", C.c_uint32),
-                ("reserved", C.c_uint32), ("edit_p50_ms", C.c_double), ("edit_p99_ms", C.c_double),
+                ("refused", C.c_uint32), ("edit_p50_ms", C.c_double), ("edit_p99_ms", C.c_double),
                 ("frame_p50_ms", C.c_double), ("frame_p99_ms", C.c_double), ("voxels_per_s", C.c_double),
                 ("num_voxels", C.c_uint64)]
 

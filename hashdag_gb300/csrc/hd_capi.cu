@@ -95,7 +95,8 @@ hd_status hd_create(const hd_config* cfg, hd_ctx** out)
         HD_CUDA(cudaMalloc(&t.page_table, kPageTableEntries * 4));
         HD_CUDA(cudaMalloc(&t.bucket_sizes, c->g.total_buckets * 4));
         HD_CUDA(cudaMalloc(&t.full_nodes, HD_MAX_DEPTH * 4));
-        HD_CUDA(cudaMalloc(&t.pool_top, 4));
+        HD_CUDA(cudaMalloc(&t.pool_top, 8));
+        HD_CUDA(cudaMalloc(&t.free_pages, size_t(conf.pool_pages) * 4));
         HD_CUDA(cudaMalloc(&t.error, 16));
         HD_CUDA(cudaMalloc(&t.level_nodes, HD_MAX_DEPTH * 8));
         HD_CUDA(cudaMalloc(&c->d_root, 4));
@@ -125,6 +126,7 @@ hd_status hd_destroy(hd_ctx* c)
     cudaFree(c->t.bucket_sizes);
     cudaFree(c->t.full_nodes);
     cudaFree(c->t.pool_top);
+    cudaFree(c->t.free_pages);
     cudaFree(c->t.error);
     cudaFree(c->t.level_nodes);
     cudaFree(c->d_root);
@@ -449,11 +451,11 @@ hd_status hd_get_level_stats(hd_ctx* c, hd_level_stats* out)
         HD_LAUNCH_CHECK();
         HD_CUDA(cudaMemcpyAsync(out->words, d, levels * 8, cudaMemcpyDeviceToHost, c->stream));
         HD_CUDA(cudaMemcpyAsync(out->nodes, c->t.level_nodes, levels * 8, cudaMemcpyDeviceToHost, c->stream));
-        uint32_t top = 0;
-        HD_CUDA(cudaMemcpyAsync(&top, c->t.pool_top, 4, cudaMemcpyDeviceToHost, c->stream));
+        uint32_t top[2] = {0, 0};
+        HD_CUDA(cudaMemcpyAsync(top, c->t.pool_top, 8, cudaMemcpyDeviceToHost, c->stream));
         HD_CUDA(cudaMemcpyAsync(&c->root, c->d_root, 4, cudaMemcpyDeviceToHost, c->stream));
         HD_CUDA(cudaStreamSynchronize(c->stream));
-        out->pages_used = top - 1;
+        out->pages_used = top[0] - 1 - top[1]; // pages a GC released are not in use
         out->root = c->root;
         out->levels = c->cfg.depth;
     });
@@ -524,8 +526,8 @@ hd_status hd_import_table(hd_ctx* c, const uint32_t* bs, const uint32_t* pt, con
         HD_CUDA(cudaMemcpyAsync(c->t.page_table, pt, c->g.total_vpages * 4, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemcpyAsync(c->t.pool, pool, pool_words * 4, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemcpyAsync(c->t.full_nodes, full, c->cfg.depth * 4, cudaMemcpyHostToDevice, st));
-        const uint32_t top = uint32_t(pool_words / HD_PAGE_SIZE);
-        HD_CUDA(cudaMemcpyAsync(c->t.pool_top, &top, 4, cudaMemcpyHostToDevice, st));
+        const uint32_t top[2] = {uint32_t(pool_words / HD_PAGE_SIZE), 0};
+        HD_CUDA(cudaMemcpyAsync(c->t.pool_top, top, 8, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemcpyAsync(c->d_root, &root, 4, cudaMemcpyHostToDevice, st));
         bloom_rebuild(c);
         HD_CUDA(cudaStreamSynchronize(st));

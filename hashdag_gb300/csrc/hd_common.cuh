@@ -101,7 +101,8 @@ struct Table {
     uint32_t* page_table;
     uint32_t* bucket_sizes;
     uint32_t* full_nodes;   // [depth]
-    uint32_t* pool_top;     // device counter (poolTop)
+    uint32_t* pool_top;     // device counters: [0] poolTop, [1] pages in the free list
+    uint32_t* free_pages;   // pages a page-releasing GC gave back (pool_pages entries)
     uint32_t* error;        // device error word
     uint64_t* level_nodes;  // stored node count per level
     Geom g;

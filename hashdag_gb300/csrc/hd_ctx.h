@@ -47,6 +47,7 @@ struct hd_ctx {
     hd_batch_tuning tuning{4, 4, 304, HD_BATCH_PERSISTENT};
     hd::BatchGraph* batch = nullptr;
     uint64_t batch_fallbacks = 0;
+    uint32_t batch_applied = 0; // edits of the last batch call that were applied (also when it failed)
     // colours: the table, host mirror of its counters
     bool colors = false;
     uint64_t color_seed = 0;

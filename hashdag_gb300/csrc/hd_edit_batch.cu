@@ -654,15 +654,19 @@ void edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* per_
         std::vector<EditCounters> ctr(n);
         std::vector<float> end_ms(n, 0.0f), dur_ms(n, 0.0f);
         float device_ms = 0.0f;
+        bool failed = false;
+        StatusError failure{HD_OK, ""};
         try {
             edit_batch_persistent(c, edits, n, b.lv, b.caps, b.keys, b.vals, b.keys2, b.vals2, b.edits, b.ctr,
                                   b.roots, ctr, dur_ms, end_ms, device_ms, c->batch_fallbacks);
-        } catch (...) {
-            c->root = read_scalar(c->d_root, st);
-            throw;
+        } catch (const StatusError& e) {
+            failed = true;
+            failure = e;
         }
         c->root = read_scalar(c->d_root, st);
-        for (uint32_t i = 0; i < n; i++) {
+        // the applied edits' counters and times, also when a later one failed
+        const uint32_t applied = failed ? c->batch_applied : n;
+        for (uint32_t i = 0; i < applied; i++) {
             hd_edit_stats s{};
             s.num_voxels = ctr[i].num_voxels;
             s.num_nodes = ctr[i].num_nodes;
@@ -679,6 +683,8 @@ void edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* per_
             sum.nodes_added += s.nodes_added;
             sum.words_scanned += s.words_scanned;
         }
+        if (failed)
+            throw failure;
         sum.device_ms = device_ms;
         sum.host_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
         if (total)
@@ -848,7 +854,13 @@ void copy_table(hd_ctx* to, hd_ctx* from)
                             cudaMemcpyDeviceToDevice, st));
     HD_CUDA(cudaMemcpyAsync(to->t.full_nodes, from->t.full_nodes, HD_MAX_DEPTH * 4, cudaMemcpyDeviceToDevice, st));
     HD_CUDA(cudaMemcpyAsync(to->t.level_nodes, from->t.level_nodes, HD_MAX_DEPTH * 8, cudaMemcpyDeviceToDevice, st));
-    HD_CUDA(cudaMemcpyAsync(to->t.pool_top, from->t.pool_top, 4, cudaMemcpyDeviceToDevice, st));
+    HD_CUDA(cudaMemcpyAsync(to->t.pool_top, from->t.pool_top, 8, cudaMemcpyDeviceToDevice, st));
+    uint32_t counters[2];
+    HD_CUDA(cudaMemcpyAsync(counters, from->t.pool_top, 8, cudaMemcpyDeviceToHost, st));
+    HD_CUDA(cudaStreamSynchronize(st));
+    if (counters[1])
+        HD_CUDA(cudaMemcpyAsync(to->t.free_pages, from->t.free_pages, uint64_t(counters[1]) * 4,
+                                cudaMemcpyDeviceToDevice, st));
     HD_CUDA(cudaMemcpyAsync(to->d_root, from->d_root, 4, cudaMemcpyDeviceToDevice, st));
     HD_CUDA(cudaStreamSynchronize(st));
     to->root = from->root;

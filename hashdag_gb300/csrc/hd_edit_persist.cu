@@ -44,14 +44,30 @@ constexpr unsigned long long kWaitNs = 2000000000ull;
 
 enum : uint32_t { kRun = 0, kDone = 1, kCapacity = 2, kTableError = 3, kEmptyScene = 4, kAborted = 5 };
 
+// What CTA 0 asks of the grid at a barrier.
+struct Cmd {
+    uint32_t stop, phase, level, deepest, idx, pad[3];
+};
+
 // Control block in global memory, reset by the host before a launch.
+// stop / idx / phase / level / deepest are CTA 0's own state (stop and idx
+// also read by the host after the launch); the other CTAs read the copy CTA 0
+// publishes in cmd[k & 1] before barrier k.  CTA 0 runs ahead as soon as it
+// leaves a barrier, so it must not change what the others are still about to
+// read: it writes the slot of the next barrier, which no CTA reads until
+// every CTA has left this one.
 struct Ctl {
     uint32_t arrived, gen, abort, stop;
     uint32_t idx;       // edit being applied
     uint32_t phase;     // the grid step CTA 0 asks for (kPh*)
     uint32_t level;     // its level
     uint32_t deepest;   // deepest level of the current edit
+    Cmd cmd[2];
     uint32_t count[HD_MAX_DEPTH];
+    // where a wait ran out: the CTA, its barrier count, the arrivals and the
+    // generation then, CTA 0's barrier count, phase, level and edit
+    uint32_t diag[8];
+    uint32_t bars0; // barriers CTA 0 has passed
     Editor ed;
 };
 
@@ -90,12 +106,15 @@ HD_D void st_release(uint32_t* p, uint32_t v)
 
 // Grid barrier of the cooperative launch with a bounded wait; false when a
 // wait ran out or another CTA gave up (the caller returns).
-HD_D bool grid_sync(Ctl* ctl, uint32_t* err)
+HD_D bool grid_sync(Ctl* ctl, uint32_t* err, uint32_t& nbar)
 {
     __shared__ uint32_t ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         ok = 1;
+        nbar++;
+        if (blockIdx.x == 0)
+            atomicExch(&ctl->bars0, nbar);
         const uint32_t g = ld_acquire(&ctl->gen);
         __threadfence();
         if (atomicAdd(&ctl->arrived, 1u) == gridDim.x - 1) {
@@ -111,7 +130,16 @@ HD_D bool grid_sync(Ctl* ctl, uint32_t* err)
                     break;
                 }
                 if ((++spins & 255u) == 0 && now_ns() - t0 > kWaitNs) {
-                    atomicExch(&ctl->abort, 1u);
+                    if (atomicExch(&ctl->abort, 1u) == 0) {
+                        ctl->diag[0] = blockIdx.x;
+                        ctl->diag[1] = nbar;
+                        ctl->diag[2] = ld_acquire(&ctl->arrived);
+                        ctl->diag[3] = g;
+                        ctl->diag[4] = ld_acquire(&ctl->bars0);
+                        ctl->diag[5] = ld_acquire(&ctl->phase);
+                        ctl->diag[6] = ld_acquire(&ctl->level);
+                        ctl->diag[7] = ld_acquire(&ctl->idx);
+                    }
                     set_error(err, kErrTimeout, 0xFFFFFFFEu, blockIdx.x, 0);
                     ok = 0;
                     break;
@@ -598,22 +626,37 @@ __global__ void __launch_bounds__(kPT, 1) k_edit_persistent(Table t, PArgs a)
     const uint32_t warp = threadIdx.x >> 5;
     const uint32_t leafl = t.g.leaf_level;
     uint32_t ls = kLsBegin, L = 0;
+    __shared__ uint32_t nbar; // barriers this CTA has passed (thread 0)
+    if (threadIdx.x == 0)
+        nbar = 0;
+    __syncthreads();
     for (;;) {
-        if (cta == 0)
+        if (cta == 0) {
             local_advance<PW>(t, a, ls, L, sm);
-        if (!grid_sync(ctl, t.error))
-            return;
-        if (__ldcg(&ctl->stop) != kRun)
+            if (threadIdx.x == 0) // the command of the coming barrier
+                ctl->cmd[(nbar + 1) & 1] = Cmd{ctl->stop, ctl->phase, ctl->level, ctl->deepest, ctl->idx, {0, 0, 0}};
+        }
+        if (!grid_sync(ctl, t.error, nbar))
             return;
         // the grid step CTA 0 asked for, decided the same way by every CTA
-        uint32_t phase = __ldcg(&ctl->phase);
+        __shared__ Cmd cmd;
+        if (threadIdx.x == 0) {
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(&ctl->cmd[nbar & 1]);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&cmd);
+            for (uint32_t k = 0; k < sizeof(Cmd) / 4; k++)
+                dst[k] = __ldcg(src + k);
+        }
+        __syncthreads();
+        if (cmd.stop != kRun)
+            return;
+        uint32_t phase = cmd.phase;
         if (phase == kPhNone) {
             ls = kLsBegin; // an edit ended: CTA 0 starts the next
             continue;
         }
-        L = __ldcg(&ctl->level);
-        uint32_t deepest = __ldcg(&ctl->deepest);
-        const uint32_t idx = __ldcg(&ctl->idx);
+        L = cmd.level;
+        uint32_t deepest = cmd.deepest;
+        const uint32_t idx = cmd.idx;
         EditCounters* ctr = a.ctr + idx;
         if (threadIdx.x == 0) {
             const uint32_t* src = reinterpret_cast<const uint32_t*>(&ctl->ed);
@@ -652,7 +695,7 @@ __global__ void __launch_bounds__(kPT, 1) k_edit_persistent(Table t, PArgs a)
                          sm.list);
                 if (cta == 0 && threadIdx.x == 0)
                     ctl->count[L + 1] = uint32_t(n_next);
-                if (!grid_sync(ctl, t.error))
+                if (!grid_sync(ctl, t.error, nbar))
                     return;
                 L++;
                 if (L == leafl)
@@ -668,7 +711,7 @@ __global__ void __launch_bounds__(kPT, 1) k_edit_persistent(Table t, PArgs a)
             const uint32_t n = __ldcg(&ctl->count[L]);
             foa_sorted<PW>(t, L, a.lv[L], a.keys, a.vals, n, cta * kPWarps + warp, G * kPWarps,
                            sm.page + warp * kPage, sm.q + warp * 12, sm.cache[warp], ctr);
-            if (!grid_sync(ctl, t.error))
+            if (!grid_sync(ctl, t.error, nbar))
                 return;
             if (L == 0) {
                 ls = kLsFinish;
@@ -701,32 +744,32 @@ __global__ void __launch_bounds__(kPT, 1) k_edit_persistent(Table t, PArgs a)
                 for (uint32_t d = threadIdx.x; d < nd; d += kPT)
                     a.hist[d * nb + cta] = cnt[d];
             }
-            if (!grid_sync(ctl, t.error))
+            if (!grid_sync(ctl, t.error, nbar))
                 return;
             // 2. pass-1 rows
             scan_rows(a.hist, nb, nd, a.rows);
-            if (!grid_sync(ctl, t.error))
+            if (!grid_sync(ctl, t.error, nbar))
                 return;
             // 3. pass-1 scatter, pass-2 counts
             if (cta < nb)
                 scatter_chunk(a.keys, a.vals, n, nb, cta, 0, nd, a.hist, a.rows, a.keys2, a.vals2, a.hist2, dbits,
                               run, sm32);
-            if (!grid_sync(ctl, t.error))
+            if (!grid_sync(ctl, t.error, nbar))
                 return;
             // 4. pass-2 rows
             scan_rows(a.hist2, nb, nd, a.rows2);
-            if (!grid_sync(ctl, t.error))
+            if (!grid_sync(ctl, t.error, nbar))
                 return;
             // 5. pass-2 scatter
             if (cta < nb)
                 scatter_chunk(a.keys2, a.vals2, n, nb, cta, dbits, nd, a.hist2, a.rows2, a.keys, a.vals, nullptr, 0,
                               run, sm32);
-            if (!grid_sync(ctl, t.error))
+            if (!grid_sync(ctl, t.error, nbar))
                 return;
             // 6. find-or-add, one warp per bucket run
             foa_sorted<PW>(t, L, a.lv[L], a.keys, a.vals, n, cta * kPWarps + warp, G * kPWarps,
                            sm.page + warp * kPage, sm.q + warp * 12, sm.cache[warp], ctr);
-            if (!grid_sync(ctl, t.error))
+            if (!grid_sync(ctl, t.error, nbar))
                 return;
             if (L == 0)
                 break; // (level 0 holds one entry: never big)
@@ -809,6 +852,7 @@ void edit_batch_persistent(hd_ctx* c, const hd_edit* edits, uint32_t n, const st
     a.d_root = c->d_root;
     std::vector<unsigned long long> tb(n), te(n);
     uint32_t done = 0;
+    c->batch_applied = 0;
     float elapsed_before = 0.0f;
     unsigned long long first_ns = 0;
     while (done < n) {
@@ -846,11 +890,17 @@ void edit_batch_persistent(hd_ctx* c, const hd_edit* edits, uint32_t n, const st
         }
         elapsed_before += launch_ms;
         done += ok;
+        c->batch_applied = done;
         if (fin.abort) {
             check_error(c);
             c->root = read_scalar(c->d_root, st);
+            std::string where;
+            for (uint32_t k = 0; k < 8; k++)
+                where += (k ? " " : "") + std::to_string(fin.diag[k]);
             throw StatusError{HD_ERR_TIMEOUT, "edit " + std::to_string(done) +
-                                                  ": a grid barrier of the persistent edit kernel ran out of time"};
+                                                  ": a grid barrier of the persistent edit kernel ran out of time "
+                                                  "(cta, barriers, arrived, gen, cta0 barriers, phase, level, edit: " +
+                                                  where + ")"};
         }
         if (fin.stop == kDone)
             break;
@@ -875,6 +925,7 @@ void edit_batch_persistent(hd_ctx* c, const hd_edit* edits, uint32_t n, const st
         elapsed_before += es.device_ms;
         end_ms[done] = elapsed_before;
         done++;
+        c->batch_applied = done;
         fallbacks++;
     }
     device_ms = elapsed_before;

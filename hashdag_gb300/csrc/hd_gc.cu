@@ -8,7 +8,11 @@
 // (add_full_node) and the live nodes are re-appended without a find, in
 // increasing old-address order (the reference uses its hash-set order), so a
 // reachable full node is kept twice as in the reference.  Pages stay mapped;
-// the words past a bucket's new size keep their old contents.
+// the words past a bucket's new size keep their old contents.  With
+// HD_GC_RELEASE_PAGES (no reference counterpart: its poolTop only grows,
+// hash_table.h:794-809), the pages wholly past each bucket's new size are
+// unmapped, zeroed and put on the table's free list, from which the next
+// page claims draw first.
 #include <algorithm>
 #include <vector>
 
@@ -94,6 +98,49 @@ __global__ void k_gc_gather(Table t, uint32_t level, const uint32_t* __restrict_
     }
 }
 
+// Pages wholly past a bucket's new size go to the free list (one thread per
+// bucket, at most capacity / 512 pages each).
+__global__ void k_gc_release(Table t)
+{
+    const Geom& g = t.g;
+    uint32_t* free_count = t.pool_top + 1;
+    const uint32_t top = g.ntop << g.top_bits;
+    HD_GRID_STRIDE(i, g.total_buckets)
+    {
+        const uint32_t gb = uint32_t(i);
+        uint32_t level, bucket;
+        if (gb < top) {
+            level = gb >> g.top_bits;
+            bucket = gb & ((1u << g.top_bits) - 1);
+        } else {
+            level = g.top_levels + ((gb - top) >> g.low_bits);
+            bucket = (gb - top) & ((1u << g.low_bits) - 1);
+        }
+        const uint32_t size = t.bucket_sizes[gb], cap = g.capacity(level);
+        for (uint32_t off = (size + kPage - 1) & ~(kPage - 1); off < cap; off += kPage) {
+            const uint32_t vp = g.make_ptr(level, bucket, off) >> kPageShift;
+            const uint32_t p = t.page_table[vp];
+            if (p) {
+                t.page_table[vp] = 0;
+                t.free_pages[atomicAdd(free_count, 1u)] = p;
+            }
+        }
+    }
+}
+
+// Zeroes the pages free_pages[from, to) and their Bloom filters.
+__global__ void k_zero_pages(Table t, uint32_t from, uint32_t to)
+{
+    const uint64_t n = uint64_t(to - from) * kPage;
+    HD_GRID_STRIDE(i, n)
+    {
+        const uint32_t p = t.free_pages[from + uint32_t(i / kPage)];
+        t.pool[uint64_t(p) * kPage + (i % kPage)] = 0;
+        if (i % kPage < kBloomWords)
+            t.bloom[uint64_t(p) * kBloomWords + (i % kPage)] = 0;
+    }
+}
+
 __global__ void k_gc_remap_roots(const uint32_t* __restrict__ live, uint32_t n, const uint32_t* __restrict__ newaddr,
                                  uint32_t* roots, uint32_t n_roots, uint32_t* d_root)
 {
@@ -102,7 +149,7 @@ __global__ void k_gc_remap_roots(const uint32_t* __restrict__ live, uint32_t n, 
     *d_root = roots[0];
 }
 
-void gc(hd_ctx* c, std::vector<uint32_t>& roots)
+void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
 {
     cudaStream_t st = c->stream;
     Scratch& s = c->scratch;
@@ -174,6 +221,20 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots)
     k_gc_remap_roots<<<1, 1, 0, st>>>(live[0], nlive[0], newaddr[0], d_roots, uint32_t(roots.size()), c->d_root);
     HD_LAUNCH_CHECK();
     HD_CUDA(cudaMemcpyAsync(roots.data(), d_roots, roots.size() * 4, cudaMemcpyDeviceToHost, st));
+    if (release_pages) {
+        uint32_t before[2], after[2];
+        HD_CUDA(cudaMemcpyAsync(before, c->t.pool_top, 8, cudaMemcpyDeviceToHost, st));
+        HD_CUDA(cudaStreamSynchronize(st));
+        k_gc_release<<<grid_for(g.total_buckets, 256), 256, 0, st>>>(c->t);
+        HD_LAUNCH_CHECK();
+        HD_CUDA(cudaMemcpyAsync(after, c->t.pool_top, 8, cudaMemcpyDeviceToHost, st));
+        HD_CUDA(cudaStreamSynchronize(st));
+        if (after[1] > before[1]) {
+            k_zero_pages<<<grid_for(uint64_t(after[1] - before[1]) * kPage, 256), 256, 0, st>>>(c->t, before[1],
+                                                                                               after[1]);
+            HD_LAUNCH_CHECK();
+        }
+    }
     HD_CUDA(cudaStreamSynchronize(st));
     const uint32_t e = check_error(c);
     if (e)
@@ -186,7 +247,7 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots)
 
 extern "C" hd_status hd_gc_ex(hd_ctx* c, uint32_t* extra, uint32_t n, uint32_t flags)
 {
-    if (!c || (n && !extra) || (flags & ~uint32_t(HD_GC_KEEP_HISTORY)))
+    if (!c || (n && !extra) || (flags & ~uint32_t(HD_GC_KEEP_HISTORY | HD_GC_RELEASE_PAGES)))
         return HD_ERR_INVALID;
     try {
         std::vector<uint32_t> roots(1 + n);
@@ -204,7 +265,7 @@ extern "C" hd_status hd_gc_ex(hd_ctx* c, uint32_t* extra, uint32_t n, uint32_t f
             c->undo.clear();
             c->redo.clear();
         }
-        hd::gc(c, roots);
+        hd::gc(c, roots, (flags & HD_GC_RELEASE_PAGES) != 0);
         c->needs_gc = false; // the buckets are rebuilt
         // the remapped extra roots go back to the caller
         for (uint32_t i = 0; i < n; i++)

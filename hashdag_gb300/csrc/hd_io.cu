@@ -380,7 +380,8 @@ hd_status hd_load_snapshot(hd_ctx* c, const char* path, hd_dag_info* info)
         HD_CUDA(cudaMemcpyAsync(c->t.bucket_sizes, bs.data(), bs.size() * 4, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemcpyAsync(c->t.full_nodes, full.data(), full.size() * 4, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemcpyAsync(c->t.level_nodes, level_nodes.data(), HD_MAX_DEPTH * 8, cudaMemcpyHostToDevice, st));
-        HD_CUDA(cudaMemcpyAsync(c->t.pool_top, &pool_top, 4, cudaMemcpyHostToDevice, st));
+        const uint32_t top[2] = {pool_top, 0};
+        HD_CUDA(cudaMemcpyAsync(c->t.pool_top, top, 8, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemcpyAsync(c->d_root, &root, 4, cudaMemcpyHostToDevice, st));
         bloom_rebuild(c);
         color_release(c);

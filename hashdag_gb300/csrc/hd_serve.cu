@@ -10,9 +10,15 @@
 //    its own stream, reading the root of the moment they are admitted;
 //    edits run in arrival order on the context stream while renders are in
 //    flight (a render's colour pass completes before a later edit replaces
-//    colour leaves); when free pool words fall below gc_free_fraction the
-//    renders drain and a GC runs that keeps the undo history.  Without
-//    colours, queued geometry edits go through the batched graph path.
+//    colour leaves).  Without colours and with batch_edits, the edits queued
+//    at that moment run as one batch: one persistent launch (hd_edit_batch)
+//    while the renders in flight go on on their own streams.
+// Both policies gate edits on free physical pages (never-claimed pages plus
+// pages on the free list): below gc_free_fraction of the pool, the renders
+// drain and a GC runs that keeps the undo history and, with release_pages,
+// gives emptied pages back.  An edit that still finds the pool full is
+// retried once after a GC, then refused (status HD_ERR_POOL_FULL; the
+// table's root is unchanged).
 // Every render produces paths, a shadow mask and (with colours) RGBA, and a
 // checksum of them that does not depend on node addresses, so a render can
 // be compared with the same render made alone on the same state.
@@ -28,6 +34,7 @@
 namespace hd {
 
 void edit_one(hd_ctx* c, const hd_edit& e, hd_edit_stats* stats);
+void edit_batch(hd_ctx* c, const hd_edit* edits, uint32_t n, hd_edit_stats* per_edit, hd_edit_stats* total);
 
 // order-independent checksum of a rendered frame: sum over pixels of a mix of
 // (pixel, path, shadow, colour)
@@ -46,20 +53,6 @@ __global__ void k_frame_checksum(const uint4* __restrict__ paths, const uint8_t*
         acc += __shfl_down_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31) == 0)
         atomicAdd(out, acc);
-}
-
-__global__ void k_words_total(Table t, uint32_t levels, unsigned long long* out)
-{
-    unsigned long long sum = 0;
-    for (uint32_t level = 0; level < levels; level++) {
-        const uint32_t nb = t.g.buckets(level), first = t.g.level_first_bucket(level);
-        for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x)
-            sum += t.bucket_sizes[first + b];
-    }
-    for (int o = 16; o; o >>= 1)
-        sum += __shfl_down_sync(0xffffffffu, sum, o);
-    if ((threadIdx.x & 31) == 0)
-        atomicAdd(out, sum);
 }
 
 namespace {
@@ -91,15 +84,14 @@ struct Clock {
     }
 };
 
-uint64_t free_words(hd_ctx* c)
+// Physical pages an edit can still claim: never-claimed pages of the pool
+// plus the pages a releasing GC put on the free list.
+uint64_t free_pages(hd_ctx* c)
 {
-    unsigned long long* d = c->scratch.get<unsigned long long>("serve_words", 1);
-    HD_CUDA(cudaMemsetAsync(d, 0, 8, c->stream));
-    k_words_total<<<152, 256, 0, c->stream>>>(c->t, c->g.leaf_level + 1, d);
-    HD_LAUNCH_CHECK();
-    const unsigned long long used = read_scalar(d, c->stream);
-    const uint64_t cap = uint64_t(c->cfg.pool_pages) * kPage;
-    return used >= cap ? 0 : cap - used;
+    uint32_t top[2];
+    HD_CUDA(cudaMemcpyAsync(top, c->t.pool_top, 8, cudaMemcpyDeviceToHost, c->stream));
+    HD_CUDA(cudaStreamSynchronize(c->stream));
+    return uint64_t(c->cfg.pool_pages) - top[0] + top[1];
 }
 
 } // namespace
@@ -161,8 +153,8 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
         HD_CUDA(cudaEventRecord(clk.ev0, st));
         HD_CUDA(cudaEventSynchronize(clk.ev0));
         clk.t0 = std::chrono::steady_clock::now();
-        const uint64_t cap_words = uint64_t(c->cfg.pool_pages) * kPage;
-        uint32_t edits_done = 0, gcs = 0, completed = 0;
+        uint32_t edits_done = 0, gcs = 0, completed = 0, refused = 0;
+        uint64_t free_after_gc = ~0ull; // free pages right after the last GC
         uint64_t voxels = 0;
         std::deque<uint32_t> edits, renders;
         uint32_t next = 0;
@@ -208,34 +200,105 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
                     finish_render(s);
                 }
         };
-        auto run_edit = [&](uint32_t i) {
-            if (cfg.gc_free_fraction > 0 && double(free_words(c)) < cfg.gc_free_fraction * double(cap_words)) {
-                drain();
-                uint32_t dummy = 0;
-                const hd_status g = hd_gc_ex(c, &dummy, 0, HD_GC_KEEP_HISTORY);
-                if (g != HD_OK)
-                    throw StatusError{g, "GC inside the serving loop failed: " + c->err};
-                gcs++;
-            }
+        auto run_gc = [&] {
+            drain();
+            uint32_t dummy = 0;
+            const uint32_t flags = HD_GC_KEEP_HISTORY | (cfg.release_pages ? HD_GC_RELEASE_PAGES : 0u);
+            const hd_status g = hd_gc_ex(c, &dummy, 0, flags);
+            if (g != HD_OK)
+                throw StatusError{g, "GC inside the serving loop failed: " + c->err};
+            gcs++;
+            free_after_gc = free_pages(c);
+        };
+        // admission: free pages above the threshold, or a GC first (again
+        // only once something was claimed since the last one)
+        auto admit = [&] {
+            if (cfg.gc_free_fraction <= 0)
+                return;
+            const uint64_t f = free_pages(c);
+            if (double(f) < cfg.gc_free_fraction * double(c->cfg.pool_pages) && f < free_after_gc)
+                run_gc();
+        };
+        auto fence_renders = [&] {
             c->color_fences.clear();
             for (Slot& s : slots)
                 if (s.req >= 0)
                     c->color_fences.push_back(s.colors_done);
+        };
+        auto commit = [&](uint32_t i, double end_ms, uint64_t vox) {
+            res[i].end_ms = end_ms;
+            res[i].root = c->root;
+            res[i].num_voxels = vox;
+            res[i].checksum = vox;
+            res[i].edits_before = edits_done;
+            res[i].status = HD_OK;
+            voxels += vox;
+            edits_done++;
+            completed++;
+        };
+        auto run_edit = [&](uint32_t i) {
+            admit();
             res[i].start_ms = clk.now();
             hd_edit_stats es{};
-            edit_one(c, reqs[i].edit, &es);
+            for (int attempt = 0;; attempt++) {
+                fence_renders();
+                try {
+                    edit_one(c, reqs[i].edit, &es);
+                    break;
+                } catch (const StatusError& e) {
+                    c->color_fences.clear();
+                    if (e.status != HD_ERR_POOL_FULL)
+                        throw;
+                    if (attempt == 1 || cfg.gc_free_fraction <= 0) {
+                        // refused: the pool stays full; the root is unchanged
+                        res[i].end_ms = clk.now();
+                        res[i].root = c->root;
+                        res[i].status = HD_ERR_POOL_FULL;
+                        res[i].edits_before = edits_done;
+                        refused++;
+                        completed++;
+                        return;
+                    }
+                    run_gc();
+                }
+            }
             HD_CUDA(cudaEventRecord(edit_ev, st));
             HD_CUDA(cudaEventSynchronize(edit_ev));
             c->color_fences.clear();
-            res[i].end_ms = clk.at(edit_ev);
-            res[i].root = c->root;
-            res[i].num_voxels = es.num_voxels;
-            res[i].checksum = es.num_voxels;
-            res[i].edits_before = edits_done;
-            res[i].status = HD_OK;
-            voxels += es.num_voxels;
-            edits_done++;
-            completed++;
+            commit(i, clk.at(edit_ev), es.num_voxels);
+        };
+        // the queued edits as one batch (no colours): one persistent launch
+        auto run_batch = [&](std::deque<uint32_t>& q) {
+            admit();
+            std::vector<uint32_t> idx(q.begin(), q.end());
+            q.clear();
+            std::vector<hd_edit> eds(idx.size());
+            std::vector<hd_edit_stats> per(idx.size());
+            for (size_t k = 0; k < idx.size(); k++) {
+                eds[k] = reqs[idx[k]].edit;
+                res[idx[k]].start_ms = clk.now();
+            }
+            const hd_batch_tuning saved = c->tuning;
+            c->tuning.mode = HD_BATCH_PERSISTENT;
+            HD_CUDA(cudaEventRecord(edit_ev, st));
+            uint32_t applied = uint32_t(idx.size());
+            bool full = false;
+            try {
+                edit_batch(c, eds.data(), uint32_t(idx.size()), per.data(), nullptr);
+            } catch (const StatusError& e) {
+                c->tuning = saved;
+                if (e.status != HD_ERR_POOL_FULL)
+                    throw;
+                applied = c->batch_applied;
+                full = true;
+            }
+            c->tuning = saved;
+            const double base = clk.at(edit_ev);
+            for (uint32_t k = 0; k < applied; k++)
+                commit(idx[k], base + per[k].host_ms, per[k].num_voxels);
+            if (full) // the rest one by one, with a GC first
+                for (size_t k = applied; k < idx.size(); k++)
+                    run_edit(idx[k]);
         };
 
         while (completed < n) {
@@ -276,9 +339,13 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
                         progress = true;
                     }
                 if (!edits.empty()) {
-                    const uint32_t i = edits.front();
-                    edits.pop_front();
-                    run_edit(i);
+                    if (cfg.batch_edits && !c->colors && edits.size() > 1) {
+                        run_batch(edits);
+                    } else {
+                        const uint32_t i = edits.front();
+                        edits.pop_front();
+                        run_edit(i);
+                    }
                     progress = true;
                 }
                 if (progress)
@@ -292,7 +359,8 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
         const double wall = clk.now();
         std::vector<double> el, fr;
         for (uint32_t i = 0; i < n; i++)
-            (reqs[i].kind == HD_REQ_RENDER ? fr : el).push_back(res[i].end_ms - reqs[i].arrival_ms);
+            if (res[i].status == HD_OK)
+                (reqs[i].kind == HD_REQ_RENDER ? fr : el).push_back(res[i].end_ms - reqs[i].arrival_ms);
         auto pct = [](std::vector<double> v, double q) {
             if (v.empty())
                 return 0.0;
@@ -308,6 +376,7 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
             stats->edits = uint32_t(el.size());
             stats->renders = uint32_t(fr.size());
             stats->gcs = gcs;
+            stats->refused = refused;
             stats->edit_p50_ms = pct(el, 50);
             stats->edit_p99_ms = pct(el, 99);
             stats->frame_p50_ms = pct(fr, 50);

@@ -110,8 +110,8 @@ void table_reset(hd_ctx* c)
     HD_CUDA(cudaMemsetAsync(c->t.full_nodes, 0, HD_MAX_DEPTH * 4, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.level_nodes, 0, HD_MAX_DEPTH * 8, c->stream));
     HD_CUDA(cudaMemsetAsync(c->t.error, 0, 16, c->stream));
-    const uint32_t one = 1;
-    HD_CUDA(cudaMemcpyAsync(c->t.pool_top, &one, 4, cudaMemcpyHostToDevice, c->stream));
+    const uint32_t top[2] = {1, 0}; // page 0 is the null page; no free pages
+    HD_CUDA(cudaMemcpyAsync(c->t.pool_top, top, 8, cudaMemcpyHostToDevice, c->stream));
     HD_CUDA(cudaMemsetAsync(c->d_root, 0, 4, c->stream));
 }
 

@@ -27,11 +27,32 @@ HD_HD uint32_t append_position(uint32_t& size, uint32_t n, bool leaf)
     return pos;
 }
 
-// Maps every unmapped virtual page that [from, to) of the bucket touches
-// (allocate_page, hash_table.h:794-809: poolTop++).  Pages are never
-// unmapped, so a bucket rebuilt by GC reuses its pages.  A claim past the
-// pool's end is given back at once, so poolTop never exceeds the pool (the
+// A physical page for a new virtual page: one a page-releasing GC gave back
+// (zeroed, like a never-used page), else poolTop++ (allocate_page,
+// hash_table.h:794-809).  0 when the pool is full: a claim past the pool's
+// end is given back at once, so poolTop never exceeds the pool (the
 // reference, unchecked in release builds, would write past its pool).
+// Free-list pops may run concurrently; pushes happen only inside a GC.
+HD_D uint32_t claim_page(const Table& t)
+{
+    uint32_t* free_count = t.pool_top + 1;
+    if (__ldcg(free_count) != 0) {
+        const uint32_t k = atomicSub(free_count, 1u);
+        if (int32_t(k) > 0)
+            return __ldcg(t.free_pages + (k - 1));
+        atomicAdd(free_count, 1u); // none left: undo
+    }
+    const uint32_t p = atomicAdd(t.pool_top, 1u);
+    if (p >= t.g.pool_pages) {
+        atomicSub(t.pool_top, 1u);
+        return 0;
+    }
+    return p;
+}
+
+// Maps every unmapped virtual page that [from, to) of the bucket touches.
+// A bucket rebuilt by the default GC keeps its pages; the page-releasing GC
+// unmaps those wholly past the bucket's new size.
 HD_D bool map_pages(const Table& t, uint32_t level, uint32_t bucket, uint32_t from, uint32_t to)
 {
     if (to <= from)
@@ -40,10 +61,9 @@ HD_D bool map_pages(const Table& t, uint32_t level, uint32_t bucket, uint32_t fr
     const uint32_t v1 = t.g.make_ptr(level, bucket, to - 1) >> kPageShift;
     for (uint32_t vp = v0; vp <= v1; vp++) {
         if (__ldcg(t.page_table + vp) == 0) {
-            const uint32_t p = atomicAdd(t.pool_top, 1u);
-            if (p >= t.g.pool_pages) {
-                atomicSub(t.pool_top, 1u);
-                set_error(t.error, kErrPoolFull, level, bucket, p);
+            const uint32_t p = claim_page(t);
+            if (!p) {
+                set_error(t.error, kErrPoolFull, level, bucket, t.g.pool_pages);
                 return false;
             }
             __stcg(t.page_table + vp, p);

@@ -385,9 +385,13 @@ typedef struct hd_serve_config {
     uint32_t max_renders;    /* render slots (continuous)                      */
     uint32_t realtime;       /* 1: a request is available at its arrival time  */
     float gc_free_fraction;  /* GC (keeping the undo history) when the free
-                                pool words fall below this fraction; 0 = never */
+                                pool pages fall below this fraction of the
+                                pool; 0 = never                                */
     float light[3];
     float shadow_bias;
+    uint32_t release_pages;  /* the serving GC releases pages (HD_GC_RELEASE_PAGES) */
+    uint32_t batch_edits;    /* continuous, no colours: the queued edits run as
+                                one batch (hd_edit_batch, persistent launch)   */
 } hd_serve_config;
 
 typedef struct hd_request_result {
@@ -403,7 +407,9 @@ typedef struct hd_request_result {
 
 typedef struct hd_serve_stats {
     double wall_ms;
-    uint32_t edits, renders, gcs, reserved;
+    uint32_t edits, renders, gcs;
+    uint32_t refused;                   /* edits refused: the pool stayed full
+                                           after a GC (status HD_ERR_POOL_FULL) */
     double edit_p50_ms, edit_p99_ms;    /* completion - arrival                */
     double frame_p50_ms, frame_p99_ms;
     double voxels_per_s;                /* edited voxels over the wall time    */
@@ -428,6 +434,13 @@ hd_status hd_gc(hd_ctx* ctx, uint32_t* h_extra_roots, uint32_t n_extra);
  * the reference's engine frees its HashDAGUndoRedo after a GC
  * (engine.cpp:178-185). */
 #define HD_GC_KEEP_HISTORY 1u
+/* HD_GC_RELEASE_PAGES (no reference counterpart: the reference's poolTop only
+ * grows, hash_table.h:794-809): the pages wholly past each bucket's new size
+ * are unmapped, zeroed and kept on a free list that later page claims draw
+ * from first, so a GC raises the free page count (hd_level_stats.pages_used
+ * counts the pages in use).  Bucket contents and addresses are the same as
+ * without the flag. */
+#define HD_GC_RELEASE_PAGES 2u
 hd_status hd_gc_ex(hd_ctx* ctx, uint32_t* h_extra_roots, uint32_t n_extra, uint32_t flags);
 
 /* ---- files (serializer.h:11-121) ---------------------------------------- */

@@ -99,3 +99,71 @@ def test_realtime_trace_reports_latencies(gpu):
     assert st.edits + st.renders == 30 and st.edit_p99_ms >= st.edit_p50_ms >= 0
     assert all(r.end_ms >= t - 1e-3 for r, (_, t, _) in zip(res, trace))
     d.free()
+
+
+def _geometry_requests(depth, n, rate, seed=5, r_range=(4.0, 64.0)):
+    trace = workloads.serving_trace(depth, n, rate, seed=seed, r_range=r_range,
+                                    resolutions=((320, 180), (640, 360)))
+    # no colours: paints become fills
+    return [(k, t, ((1 if p[0] == 4 else p[0]),) + tuple(p[1:])) if k == "edit" else (k, t, p)
+            for k, t, p in trace]
+
+
+def test_batched_mix_equals_alone(gpu):
+    """Continuous policy on a scene without colours: the edits queued at a
+    moment run as one persistent batch while renders are in flight; every
+    render equals the same render alone on the state it saw, the scene
+    equals one-by-one application."""
+    depth = 10
+    trace = _geometry_requests(depth, 64, 4000.0)
+    d = hd.HashDAG(depth)
+    d.generate_scene(1)
+    reqs = _requests(trace)
+    res, st = d.serve(reqs, continuous=True, max_renders=2, realtime=False, gc_free_fraction=0.0, batch_edits=True)
+    assert st.edits + st.renders == len(reqs) and st.refused == 0
+    edits = [i for i, r in enumerate(reqs) if r.kind == 0]
+    renders = sorted((i for i, r in enumerate(reqs) if r.kind == 1), key=lambda i: (res[i].edits_before, i))
+    order, k = [], 0
+    for n_done in range(len(edits) + 1):
+        while k < len(renders) and res[renders[k]].edits_before == n_done:
+            order.append(renders[k])
+            k += 1
+        if n_done < len(edits):
+            order.append(edits[n_done])
+    alone = _requests([trace[i] for i in order], zero_time=True)
+    d2 = hd.HashDAG(depth)
+    d2.generate_scene(1)
+    res2, _ = d2.serve(alone, continuous=False, realtime=False, gc_free_fraction=0.0)
+    for pos, i in enumerate(order):
+        assert res2[pos].checksum == res[i].checksum, (pos, i)
+    assert d.firstNodeIndex == d2.firstNodeIndex
+    d.free()
+    d2.free()
+
+
+def test_pool_gated_admission_with_page_release(gpu):
+    """A pool too small for the trace without page reuse: edits are refused
+    once it fills; with the page-releasing GC the loop collects and takes
+    every edit."""
+    depth = 10
+    trace = [x for x in _geometry_requests(depth, 120, 4000.0, seed=9, r_range=(16.0, 96.0)) if x[0] == "edit"]
+    probe = hd.HashDAG(depth)
+    probe.generate_scene(1)
+    res0, _ = probe.serve(_requests(trace), continuous=False, realtime=False, gc_free_fraction=0.0)
+    total = probe.level_stats().pages_used
+    probe.remove_stale_nodes(release_pages=True)
+    live = probe.level_stats().pages_used
+    probe.free()
+    pool = live + 1 + (total - live) // 3
+    outcomes = {}
+    for release in (False, True):
+        d = hd.HashDAG(config=hd.default_config(depth, pool_pages=pool))
+        d.generate_scene(1)
+        res, st = d.serve(_requests(trace), continuous=True, realtime=False, gc_free_fraction=0.25,
+                          release_pages=release, batch_edits=False)
+        outcomes[release] = (st.refused, st.gcs, d.firstNodeIndex)
+        if release:
+            assert [r.num_voxels for r in res] == [r.num_voxels for r in res0]
+        d.free()
+    assert outcomes[False][0] > 0          # the pool ran out without page reuse
+    assert outcomes[True][0] == 0 and outcomes[True][1] > 0
