@@ -82,6 +82,10 @@ def parse():
     p.add_argument("--serving-depth", type=int, default=16)
     p.add_argument("--serving-requests", type=int, default=300)
     p.add_argument("--serving-rate", type=float, default=400.0, help="requests per second")
+    p.add_argument("--serving-rates", default="100,200,400",
+                   help="rate sweep of the 2^15 geometry serving section (requests per second)")
+    p.add_argument("--serving-sweep-requests", type=int, default=200)
+    p.add_argument("--views-4k", type=int, default=4, help="poses per step of the 3840x2160 line (0 = skip)")
     return p.parse_args()
 
 
@@ -301,23 +305,33 @@ def edit_bench(args, dist):
     plain_s = time.perf_counter() - t0
     plain_root = d.firstNodeIndex
     d.free()
-    # batched: tune on a copy, capture once, then the timed batch
+    # batched: tune on a copy (graph shapes and the persistent form), warm
+    # up, then the timed batch; the other mode timed alike for the A/B
     d = fresh()
     tuning, _ = d.autotune_batch(eds[:32])
     d.edit_batch(eds[:2])
     d.free()
-    d = fresh()
-    d.batch_tuning = tuning
-    d.edit_batch(eds[:1])  # capture on this context
-    d.free()
-    d = fresh()
-    d.batch_tuning = tuning
-    t0 = time.perf_counter()
-    total, per = d.edit_batch(eds, per_edit=True)
-    batch_s = time.perf_counter() - t0
-    batch_root = d.firstNodeIndex
-    fallbacks = d.batch_fallbacks()
-    d.free()
+    other = hd.BatchTuning(4, 4, 304, 1 - tuning.mode)
+
+    def timed_batch(tu):
+        d = fresh()
+        d.batch_tuning = tu
+        d.edit_batch(eds[:1])  # capture / module load on this context
+        d.free()
+        d = fresh()
+        d.batch_tuning = tu
+        before = d.level_stats()
+        t0 = time.perf_counter()
+        total, per = d.edit_batch(eds, per_edit=True)
+        seconds = time.perf_counter() - t0
+        after = d.level_stats()
+        out = (total, per, seconds, d.firstNodeIndex, d.batch_fallbacks(),
+               int(sum(after.words[:depth]) - sum(before.words[:depth])))
+        d.free()
+        return out
+
+    total, per, batch_s, batch_root, fallbacks, growth = timed_batch(tuning)
+    o_total, o_per, o_s, o_root, o_fb, _ = timed_batch(other)
     plain_s = dist.max(plain_s)
     batch_s = dist.max(batch_s)
     vox = sum(s.num_voxels for s in plain)
@@ -334,7 +348,8 @@ def edit_bench(args, dist):
     res = {"workload": f"mixed_edits_d{depth}_{n}_r4-512", "edits": n, "num_voxels": vox, "find_or_add_calls": foa,
            "nodes_added": sum(s.nodes_added for s in plain),
            "plain": form(plain_s, plain, {"api": "hd_edit_apply per edit", "latency": "device time per edit"}),
-           "batched": form(batch_s, per, {"api": "hd_edit_batch (one CUDA graph launch per edit)",
+           "batched": form(batch_s, per, {"api": "hd_edit_batch (" + ["one CUDA graph launch per edit",
+                                                                      "one persistent launch"][tuning.mode] + ")",
                                           "latency": "device time per edit inside the batch",
                                           "p99_completion_ms": _pct([s.host_ms for s in per], 99),
                                           "tuning": {"foa_warps": tuning.foa_warps,
@@ -344,6 +359,23 @@ def edit_bench(args, dist):
                                           "fallbacks": fallbacks}),
            "same_root": bool(plain_root == batch_root)}
     res["batched_over_plain_voxels_per_s"] = res["batched"]["voxels_per_s"] / res["plain"]["voxels_per_s"]
+    res["other_mode"] = form(dist.max(o_s), o_per, {"mode": ["graph per edit", "persistent"][other.mode],
+                                                   "same_root": bool(o_root == plain_root), "fallbacks": o_fb})
+    # roofline of the edit path: the algorithmic bytes of find-or-add (bucket
+    # words scanned, words appended, bucket-size read + write per call) over
+    # the batch's device time, against the measured HBM copy bandwidth
+    peaks, peak_kind = measured_peaks()
+    scanned = sum(s.words_scanned for s in per)
+    alg = 4 * scanned + 4 * growth + 8 * foa
+    achieved = alg / (total.device_ms * 1e-3) / 1e9
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    res["roofline"] = {"bound": "hbm", "scope": "whole batch (every phase of every edit)", "achieved": achieved,
+                       "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                       "algorithmic_bytes": alg, "words_scanned": scanned, "words_appended": growth,
+                       "find_or_add_calls": foa, "device_ms": total.device_ms,
+                       "bytes_note": "4 B x bucket words scanned + 4 B x words appended + 8 B bucket size per "
+                                     "find-or-add; page-table reads (one per scanned page) and the descent's node "
+                                     "reads are not counted"}
     return res, tuples
 
 
@@ -526,6 +558,62 @@ def serving_bench(args):
         d.free()
     out["continuous_over_sequential_voxels_per_s"] = (out["continuous"]["voxels_per_s"] /
                                                       max(1e-9, out["sequential"]["voxels_per_s"]))
+    return out
+
+
+def _serve_requests(hd, trace, colors):
+    out = []
+    for kind, t, p in trace:
+        if kind == "edit":
+            tool, centre, radius, rgb = p
+            if tool == 4 and not colors:
+                tool = 1  # no colours: paints become fills
+            ed = hd.SpherePaintEditor(centre, radius, rgb) if tool == 4 else hd.editor_from_tuple((tool, centre, radius))
+            out.append(hd.edit_request(t, ed))
+        else:
+            out.append(hd.render_request(t, p[0], p[1], p[2]))
+    return out
+
+
+def serving_sweep_bench(args):
+    """Serving at 2^15 without colours, a rate sweep below and up to
+    saturation: Poisson traces (70% sphere carve / fill, radius log-uniform
+    in [4, 512]; 30% renders at 720p, 1080p or 4K) replayed in real time by
+    the sequential policy (one request at a time, one edit per launch) and
+    the continuous one (renders in up to 3 slots on their own streams, the
+    queued edits as one persistent batch, GC with page release under 10%
+    free pages).  Then the same trace at 400/s on a pool 12% larger than the
+    scene, with and without page release."""
+    import hashdag_gb300 as hd
+    from hashdag_gb300 import workloads
+    depth, n = args.depth, args.serving_sweep_requests
+    out = {"workload": f"serving_d{depth}_{n}req_r4-512", "rates": []}
+    for rate in [float(r) for r in args.serving_rates.split(",") if r]:
+        trace = workloads.serving_trace(depth, n, rate, r_range=(4.0, 512.0))
+        row = {"rate_per_s": rate}
+        for name, continuous in (("sequential", False), ("continuous", True)):
+            d, _ = load_scene(depth)
+            res, st = d.serve(_serve_requests(hd, trace, False), continuous=continuous, max_renders=3, realtime=True,
+                              gc_free_fraction=0.1, release_pages=True, batch_edits=continuous)
+            row[name] = st.as_dict()
+            d.free()
+        row["edit_p99_continuous_over_sequential"] = (row["continuous"]["edit_p99_ms"] /
+                                                     max(1e-9, row["sequential"]["edit_p99_ms"]))
+        out["rates"].append(row)
+    # a pool 12% larger than the scene
+    probe, _ = load_scene(depth)
+    scene_pages = probe.level_stats().pages_used
+    probe.free()
+    pool = int(scene_pages * 1.12) + 1
+    trace = workloads.serving_trace(depth, 300, 400.0, r_range=(4.0, 512.0))
+    pool_rows = {"pool_pages": pool, "scene_pages": scene_pages}
+    for name, release in (("no_page_release", False), ("page_release", True)):
+        d, _ = load_scene(depth, pool)
+        res, st = d.serve(_serve_requests(hd, trace, False), continuous=True, max_renders=3, realtime=True,
+                          gc_free_fraction=0.1, release_pages=release, batch_edits=True)
+        pool_rows[name] = dict(st.as_dict(), pages_used_after=int(d.level_stats().pages_used))
+        d.free()
+    out["small_pool"] = pool_rows
     return out
 
 
@@ -736,6 +824,42 @@ def run_gpu(args, dist):
     flush_s = time.perf_counter() - f0
     e2e_value = rays_all / max(1e-9, e2e_s - flush_s) / 1e6
 
+    # the same poses at 3840 x 2160, fewer views per step
+    trace_4k = None
+    if args.views_4k:
+        W4, H4, V4 = 3840, 2160, args.views_4k
+        poses4 = workloads.catmull_rom_path(depth, args.poses, W4, H4)
+        cams4 = [_capi.Camera.from_params(p) for p in poses4]
+        p4 = torch.zeros(V4 * W4 * H4 * 4, dtype=torch.int32, device="cuda")
+        m4 = torch.zeros(V4 * W4 * H4, dtype=torch.uint8, device="cuda")
+        rays4 = 0
+        arrays4 = []
+        for k in range(max(K, args.warmup)):
+            idx4 = replica_poses(k, V4, dist.rank, len(cams4))
+            arrays4.append((_capi.Camera * V4)(*[cams4[i] for i in idx4]))
+        for k in range(K):
+            for i in replica_poses(k, V4, dist.rank, len(cams4)):
+                o4 = (C.c_uint64 * 6)()
+                dag._check(L.hd_trace_counters(h, C.byref(cams4[i]), W4, H4, light, BIAS, p4.data_ptr(),
+                                               m4.data_ptr(), o4))
+                rays4 += o4[0] + o4[3]
+        for k in range(args.warmup):
+            dag._check(L.hd_trace_views(h, arrays4[k], V4, W4, H4, p4.data_ptr(), light, BIAS, m4.data_ptr(), None))
+        torch.cuda.synchronize()
+        ms4 = 0.0
+        for k in range(K):
+            flush.fill_(k & 0xff)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dag._check(L.hd_trace_views(h, arrays4[k], V4, W4, H4, p4.data_ptr(), light, BIAS, m4.data_ptr(), None))
+            e1.record()
+            torch.cuda.synchronize()
+            ms4 += e0.elapsed_time(e1)
+        ms4 = dist.max(ms4)
+        trace_4k = {"width": W4, "height": H4, "views_per_step": V4, "steps": K,
+                    "value": dist.sum(rays4) / (ms4 * 1e-3) / 1e6, "unit": "Mrays/s", "ms_per_step": ms4 / K,
+                    "rays_per_step": rays4 / K, "l2": "flushed (512 MB write) before every step"}
+        del p4, m4
     peaks, peak_kind = measured_peaks()
     dominant = "trace_primary" if ms_p >= ms_s else "trace_shadow"
     dom_ms = (ms_p if ms_p >= ms_s else ms_s) / K
@@ -776,8 +900,10 @@ def run_gpu(args, dist):
     if not args.no_colors:
         colors = colors_bench(args)
         tools = tools_files_bench(args)
+    sweep = None
     if not args.no_serving:
         serving = serving_bench(args)
+        sweep = serving_sweep_bench(args)
     line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": dist.world, "steps": K,
             "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -789,7 +915,8 @@ def run_gpu(args, dist):
                     "paths": ("written by the primary kernel into the pinned host buffer (NVLink-C2C)"
                               if not args.e2e_chunk else f"copied in chunks of {args.e2e_chunk} views")},
             "gpu_launches": 2 * K, "roofline": roofline, "cpu_baseline": cpu, "ref_gpu": ref_gpu, "clocks": clk,
-            "wall_s": wall, "edits": edits, "colors": colors, "tools_files": tools, "serving": serving}
+            "wall_s": wall, "trace_4k": trace_4k, "edits": edits, "colors": colors, "tools_files": tools,
+            "serving": serving, "serving_d15": sweep}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dag.free()

@@ -98,25 +98,17 @@ __global__ void k_gc_gather(Table t, uint32_t level, const uint32_t* __restrict_
     }
 }
 
-// Pages wholly past a bucket's new size go to the free list (one thread per
-// bucket, at most capacity / 512 pages each).
-__global__ void k_gc_release(Table t)
+// Pages wholly past the new size of a bucket of `level` go to the free list
+// (one thread per bucket, at most capacity / 512 pages each).
+__global__ void k_gc_release(Table t, uint32_t level)
 {
     const Geom& g = t.g;
     uint32_t* free_count = t.pool_top + 1;
-    const uint32_t top = g.ntop << g.top_bits;
-    HD_GRID_STRIDE(i, g.total_buckets)
+    const uint32_t first = g.level_first_bucket(level);
+    HD_GRID_STRIDE(i, g.buckets(level))
     {
-        const uint32_t gb = uint32_t(i);
-        uint32_t level, bucket;
-        if (gb < top) {
-            level = gb >> g.top_bits;
-            bucket = gb & ((1u << g.top_bits) - 1);
-        } else {
-            level = g.top_levels + ((gb - top) >> g.low_bits);
-            bucket = (gb - top) & ((1u << g.low_bits) - 1);
-        }
-        const uint32_t size = t.bucket_sizes[gb], cap = g.capacity(level);
+        const uint32_t bucket = uint32_t(i);
+        const uint32_t size = t.bucket_sizes[first + bucket], cap = g.capacity(level);
         for (uint32_t off = (size + kPage - 1) & ~(kPage - 1); off < cap; off += kPage) {
             const uint32_t vp = g.make_ptr(level, bucket, off) >> kPageShift;
             const uint32_t p = t.page_table[vp];
@@ -215,26 +207,26 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
         HD_CUDA(cudaMemsetAsync(c->t.level_nodes + L, 0, 8, st));
         add_full_nodes(c, uint32_t(L), uint32_t(L));
         append_items(c, uint32_t(L), content, n, head, next, touched, d_n, newaddr[L]);
+        if (release_pages) {
+            // this level's emptied pages, zeroed, serve the levels above
+            uint32_t before[2], after[2];
+            HD_CUDA(cudaMemcpyAsync(before, c->t.pool_top, 8, cudaMemcpyDeviceToHost, st));
+            k_gc_release<<<grid_for(g.buckets(uint32_t(L)), 256), 256, 0, st>>>(c->t, uint32_t(L));
+            HD_LAUNCH_CHECK();
+            HD_CUDA(cudaMemcpyAsync(after, c->t.pool_top, 8, cudaMemcpyDeviceToHost, st));
+            HD_CUDA(cudaStreamSynchronize(st));
+            if (after[1] > before[1]) {
+                k_zero_pages<<<grid_for(uint64_t(after[1] - before[1]) * kPage, 256), 256, 0, st>>>(c->t, before[1],
+                                                                                                   after[1]);
+                HD_LAUNCH_CHECK();
+            }
+        }
     }
     uint32_t* d_roots = s.get<uint32_t>("gc_roots", roots.size());
     HD_CUDA(cudaMemcpyAsync(d_roots, roots.data(), roots.size() * 4, cudaMemcpyHostToDevice, st));
     k_gc_remap_roots<<<1, 1, 0, st>>>(live[0], nlive[0], newaddr[0], d_roots, uint32_t(roots.size()), c->d_root);
     HD_LAUNCH_CHECK();
     HD_CUDA(cudaMemcpyAsync(roots.data(), d_roots, roots.size() * 4, cudaMemcpyDeviceToHost, st));
-    if (release_pages) {
-        uint32_t before[2], after[2];
-        HD_CUDA(cudaMemcpyAsync(before, c->t.pool_top, 8, cudaMemcpyDeviceToHost, st));
-        HD_CUDA(cudaStreamSynchronize(st));
-        k_gc_release<<<grid_for(g.total_buckets, 256), 256, 0, st>>>(c->t);
-        HD_LAUNCH_CHECK();
-        HD_CUDA(cudaMemcpyAsync(after, c->t.pool_top, 8, cudaMemcpyDeviceToHost, st));
-        HD_CUDA(cudaStreamSynchronize(st));
-        if (after[1] > before[1]) {
-            k_zero_pages<<<grid_for(uint64_t(after[1] - before[1]) * kPage, 256), 256, 0, st>>>(c->t, before[1],
-                                                                                               after[1]);
-            HD_LAUNCH_CHECK();
-        }
-    }
     HD_CUDA(cudaStreamSynchronize(st));
     const uint32_t e = check_error(c);
     if (e)
@@ -250,6 +242,19 @@ extern "C" hd_status hd_gc_ex(hd_ctx* c, uint32_t* extra, uint32_t n, uint32_t f
     if (!c || (n && !extra) || (flags & ~uint32_t(HD_GC_KEEP_HISTORY | HD_GC_RELEASE_PAGES)))
         return HD_ERR_INVALID;
     try {
+        // the rebuild re-appends every live node; a different order can pad
+        // pages differently and claim a few new pages, and a rebuild that
+        // runs out of pages half way cannot be undone: refuse before any
+        // change when fewer than the reserve are free
+        uint32_t top[2];
+        HD_CUDA(cudaMemcpyAsync(top, c->t.pool_top, 8, cudaMemcpyDeviceToHost, c->stream));
+        HD_CUDA(cudaStreamSynchronize(c->stream));
+        const uint64_t used = uint64_t(top[0]) - 1 - top[1], free = uint64_t(c->cfg.pool_pages) - top[0] + top[1];
+        if (free < hd::gc_page_reserve(used)) {
+            c->err = "GC needs " + std::to_string(hd::gc_page_reserve(used)) + " free pages to rebuild the table, " +
+                     std::to_string(free) + " are free; the table is unchanged";
+            return HD_ERR_POOL_FULL;
+        }
         std::vector<uint32_t> roots(1 + n);
         roots[0] = hd::read_scalar(c->d_root, c->stream);
         for (uint32_t i = 0; i < n; i++)

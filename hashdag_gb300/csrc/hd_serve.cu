@@ -86,11 +86,13 @@ struct Clock {
 
 // Physical pages an edit can still claim: never-claimed pages of the pool
 // plus the pages a releasing GC put on the free list.
-uint64_t free_pages(hd_ctx* c)
+uint64_t free_pages(hd_ctx* c, uint64_t* used = nullptr)
 {
     uint32_t top[2];
     HD_CUDA(cudaMemcpyAsync(top, c->t.pool_top, 8, cudaMemcpyDeviceToHost, c->stream));
     HD_CUDA(cudaStreamSynchronize(c->stream));
+    if (used)
+        *used = uint64_t(top[0]) - 1 - top[1];
     return uint64_t(c->cfg.pool_pages) - top[0] + top[1];
 }
 
@@ -200,6 +202,11 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
                     finish_render(s);
                 }
         };
+        // a GC runs only when it has the pages its rebuild may claim
+        auto gc_possible = [&] {
+            uint64_t used = 0;
+            return free_pages(c, &used) >= gc_page_reserve(used);
+        };
         auto run_gc = [&] {
             drain();
             uint32_t dummy = 0;
@@ -216,7 +223,7 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
             if (cfg.gc_free_fraction <= 0)
                 return;
             const uint64_t f = free_pages(c);
-            if (double(f) < cfg.gc_free_fraction * double(c->cfg.pool_pages) && f < free_after_gc)
+            if (double(f) < cfg.gc_free_fraction * double(c->cfg.pool_pages) && f < free_after_gc && gc_possible())
                 run_gc();
         };
         auto fence_renders = [&] {
@@ -249,7 +256,7 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
                     c->color_fences.clear();
                     if (e.status != HD_ERR_POOL_FULL)
                         throw;
-                    if (attempt == 1 || cfg.gc_free_fraction <= 0) {
+                    if (attempt == 1 || cfg.gc_free_fraction <= 0 || !gc_possible()) {
                         // refused: the pool stays full; the root is unchanged
                         res[i].end_ms = clk.now();
                         res[i].root = c->root;

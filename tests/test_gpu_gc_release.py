@@ -18,8 +18,8 @@ pytestmark = pytest.mark.gpu
 DEPTH = 12
 
 
-def _edited(edits, **cfg):
-    d = hd.HashDAG(config=hd.default_config(DEPTH, **cfg))
+def _edited(edits, depth=DEPTH, **cfg):
+    d = hd.HashDAG(config=hd.default_config(depth, **cfg))
     d.generate_scene(workloads.SEED_SCENE)
     for e in edits:
         d.edit_threads(hd.editor_from_tuple(e))
@@ -37,7 +37,8 @@ def test_release_gc_keeps_buckets_and_frees_pages(gpu):
     assert list(sa.words[:DEPTH]) == list(sb.words[:DEPTH])
     ta, tb = a.export_table(), b.export_table()
     assert table_digest(ta, DEPTH, 12) == table_digest(tb, DEPTH, 12)
-    assert sb.pages_used < sa.pages_used <= before
+    # (the default GC can claim a few pages: its order pads pages differently)
+    assert sb.pages_used < sa.pages_used and sb.pages_used < before
     # later edits draw on the freed pages and land where they land after the
     # default GC
     more = workloads.mixed_edits(DEPTH, 16, (8.0, 200.0), seed=18)
@@ -53,9 +54,10 @@ def test_release_gc_keeps_buckets_and_frees_pages(gpu):
 
 
 def test_release_gc_lets_a_small_pool_take_an_edit_stream(gpu):
-    edits = workloads.mixed_edits(DEPTH, 48, (16.0, 160.0), seed=23)
+    depth = 10
+    edits = workloads.mixed_edits(depth, 64, (16.0, 160.0), seed=23)
     # the stream without a GC: pages each edit claims, pages at the end
-    ref = _edited([])
+    ref = _edited([], depth)
     scene_pages = ref.level_stats().pages_used
     step = []
     for e in edits:
@@ -63,16 +65,18 @@ def test_release_gc_lets_a_small_pool_take_an_edit_stream(gpu):
         ref.edit_threads(hd.editor_from_tuple(e))
         step.append(ref.level_stats().pages_used - before)
     total = ref.level_stats().pages_used
-    live = hd.HashDAG(DEPTH)
+    live = hd.HashDAG(depth)
     live.import_table(ref.export_table())
     live.remove_stale_nodes(release_pages=True)
     live_pages = live.level_stats().pages_used
     live.free()
-    need = 2 * max(step)
-    pool = live_pages + 1 + 3 * need
+    # free pages to keep: an edit's worth twice over, and the GC's reserve
+    # (1/32 of the pages in use + 64)
+    need = max(2 * max(step), total // 32 + 64)
+    pool = live_pages + 1 + 2 * need
     assert pool - 1 < total, "the stream must not fit the pool without page reuse"
     # without page reuse the pool runs out partway through the stream
-    plain = hd.HashDAG(config=hd.default_config(DEPTH, pool_pages=pool))
+    plain = hd.HashDAG(config=hd.default_config(depth, pool_pages=pool))
     plain.generate_scene(workloads.SEED_SCENE)
     refused = 0
     for e in edits:
@@ -85,7 +89,7 @@ def test_release_gc_lets_a_small_pool_take_an_edit_stream(gpu):
     plain.free()
     # with a releasing GC whenever fewer than `need` pages are free, every
     # edit lands and the scene equals the unconstrained one
-    d = hd.HashDAG(config=hd.default_config(DEPTH, pool_pages=pool))
+    d = hd.HashDAG(config=hd.default_config(depth, pool_pages=pool))
     d.generate_scene(workloads.SEED_SCENE)
     gcs = 0
     for e in edits:
@@ -94,7 +98,25 @@ def test_release_gc_lets_a_small_pool_take_an_edit_stream(gpu):
             gcs += 1
         d.edit_threads(hd.editor_from_tuple(e))
     assert gcs > 0 and scene_pages < pool
-    q = np.random.default_rng(7).integers(0, 1 << DEPTH, (40000, 3)).astype(np.uint32)
+    q = np.random.default_rng(7).integers(0, 1 << depth, (40000, 3)).astype(np.uint32)
     assert np.array_equal(d.get_values(q), ref.get_values(q))
     d.free()
     ref.free()
+
+
+def test_gc_refuses_without_its_page_reserve(gpu):
+    """A GC that may need pages it does not have refuses before it changes
+    anything (HD_ERR_POOL_FULL), and the table stays as it was."""
+    depth = 10
+    probe = _edited([], depth)
+    scene_pages = probe.level_stats().pages_used
+    probe.free()
+    d = hd.HashDAG(config=hd.default_config(depth, pool_pages=scene_pages + 1 + 8))
+    d.generate_scene(workloads.SEED_SCENE)
+    root = d.firstNodeIndex
+    before = table_digest(d.export_table(), depth, 10)
+    with pytest.raises(hd.HashDagError) as ei:
+        d.remove_stale_nodes(release_pages=True)
+    assert ei.value.status == _capi.HD_ERR_POOL_FULL and "unchanged" in str(ei.value)
+    assert d.firstNodeIndex == root and table_digest(d.export_table(), depth, 10) == before
+    d.free()
