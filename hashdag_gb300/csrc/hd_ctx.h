@@ -103,10 +103,6 @@ void append_items(hd_ctx* c, uint32_t level, const uint32_t* content, uint64_t n
 // hd_scene.cu
 void generate_scene(hd_ctx* c, uint64_t seed, uint32_t flags, uint32_t** d_words, uint64_t* n_words);
 
-// hd_gc.cu: free pages a GC wants before it starts (the rebuild's padding can
-// claim a few pages): 1/32 of the pages in use, plus 64
-inline uint64_t gc_page_reserve(uint64_t used_pages) { return used_pages / 32 + 64; }
-
 // hd_table.cu: Bloom filters of imported tables and of GC-rebuilt levels
 void bloom_rebuild(hd_ctx* c);
 

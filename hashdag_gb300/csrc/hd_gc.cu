@@ -133,6 +133,101 @@ __global__ void k_zero_pages(Table t, uint32_t from, uint32_t to)
     }
 }
 
+// ---- dry run: the rebuild's page needs, computed before anything changes ----
+// The rebuild of a level re-appends its live nodes with a different order
+// and so a different padding: a bucket can need a page it never had.  A
+// rebuild that runs out of pages half way cannot be undone, so the GC first
+// runs every level's rebuild on scratch bucket sizes (the same full node
+// first, the same items in the same order, hence the same addresses) and
+// counts the pages it would map, and the pages a releasing GC would free.
+
+// The level's full node at the head of its (empty) bucket, on dry sizes.
+__global__ void k_gc_dry_full(Table t, uint32_t level, uint32_t* dry_sizes, uint32_t* full_dry)
+{
+    uint32_t node[9];
+    uint32_t n, hash;
+    const bool leaf = level == t.g.leaf_level;
+    if (leaf) {
+        node[0] = node[1] = 0xFFFFFFFFu;
+        n = 2;
+        hash = hash_leaf(~0ull);
+    } else {
+        const uint32_t depth = t.g.depth - level;
+        const uint32_t voxels = level < t.g.T ? 0u : (1u << (3 * depth));
+        node[0] = (voxels << 8) | 0xffu;
+        for (int c = 0; c < 8; c++)
+            node[1 + c] = full_dry[level + 1];
+        n = 9;
+        hash = hash_interior(9, node);
+    }
+    const uint32_t bucket = hash & (t.g.buckets(level) - 1);
+    dry_sizes[bucket] = n;
+    full_dry[level] = t.g.make_ptr(level, bucket, 0);
+}
+
+// The items' addresses and the buckets' final sizes, as k_append_items
+// places them, without writing the table.
+__global__ void __launch_bounds__(64)
+    k_gc_dry_append(Table t, uint32_t level, const uint32_t* __restrict__ content, uint32_t* __restrict__ head,
+                    const uint32_t* __restrict__ next, const uint32_t* __restrict__ touched,
+                    const uint32_t* __restrict__ n_touched, uint32_t* __restrict__ dry_sizes,
+                    uint32_t* __restrict__ out_addr, uint32_t* __restrict__ overflow)
+{
+    __shared__ uint32_t items_s[2][kMaxBucketItems];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t* items = items_s[warp];
+    const bool leaf = level == t.g.leaf_level;
+    const uint32_t nt = *n_touched;
+    const uint32_t first = t.g.level_first_bucket(level);
+    for (uint32_t ti = blockIdx.x * 2 + warp; ti < nt; ti += gridDim.x * 2) {
+        const uint32_t gb = touched[ti];
+        const uint32_t cnt = collect_sorted(gb, head, next, items, t.error);
+        if (cnt == 0)
+            continue;
+        const uint32_t bucket = gb - first;
+        if (lane == 0) {
+            uint32_t size = dry_sizes[bucket];
+            for (uint32_t i = 0; i < cnt; i++) {
+                const uint32_t r = items[i];
+                const uint32_t n = leaf ? 2 : total_size(content[9 * uint64_t(r)]);
+                out_addr[r] = t.g.make_ptr(level, bucket, append_position(size, n, leaf));
+            }
+            if (size > t.g.capacity(level))
+                atomicExch(overflow, 1u);
+            dry_sizes[bucket] = size;
+        }
+        __syncwarp();
+    }
+}
+
+// Pages the level's rebuild maps (unmapped pages below a bucket's final
+// size) and, releasing, frees (mapped pages wholly past it).
+__global__ void k_gc_dry_pages(Table t, uint32_t level, const uint32_t* __restrict__ dry_sizes, uint32_t release,
+                               unsigned long long* need, unsigned long long* freed)
+{
+    const uint32_t cap = t.g.capacity(level);
+    unsigned long long a = 0, f = 0;
+    HD_GRID_STRIDE(i, t.g.buckets(level))
+    {
+        const uint32_t bucket = uint32_t(i), size = dry_sizes[bucket];
+        for (uint32_t off = 0; off < cap; off += kPage) {
+            const bool mapped = t.page_table[t.g.make_ptr(level, bucket, off) >> kPageShift] != 0;
+            if (off < size)
+                a += !mapped;
+            else if (release)
+                f += mapped;
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        f += __shfl_down_sync(0xffffffffu, f, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(need, a);
+        atomicAdd(freed, f);
+    }
+}
+
 __global__ void k_gc_remap_roots(const uint32_t* __restrict__ live, uint32_t n, const uint32_t* __restrict__ newaddr,
                                  uint32_t* roots, uint32_t n_roots, uint32_t* d_root)
 {
@@ -178,7 +273,6 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
         k_bitmap_to_list<<<grid_for(nwords, 256), 256, 0, st>>>(bitmap, pos, nwords, base, live[L + 1]);
         HD_LAUNCH_CHECK();
     }
-    // rebuild bottom-up
     uint32_t maxn = 1;
     for (uint32_t L = 0; L <= leafl; L++)
         maxn = std::max(maxn, nlive[L]);
@@ -187,6 +281,62 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
     uint32_t* head = s.get<uint32_t>("gc_head", g.total_buckets);
     uint32_t* touched = s.get<uint32_t>("gc_touched", g.total_buckets);
     fill<uint32_t>(head, kEmpty, g.total_buckets, st);
+    // dry run, bottom-up: the pages every level's rebuild needs against the
+    // free pages (and those the levels below free when releasing)
+    {
+        uint32_t top[2];
+        HD_CUDA(cudaMemcpyAsync(top, c->t.pool_top, 8, cudaMemcpyDeviceToHost, st));
+        uint32_t* dry_sizes = s.get<uint32_t>("gc_dry_sizes", uint64_t(1) << std::max(g.top_bits, g.low_bits));
+        uint32_t* full_dry = s.get<uint32_t>("gc_full_dry", HD_MAX_DEPTH);
+        uint32_t* dry_addr[2] = {s.get<uint32_t>("gc_dry_addr_a", uint64_t(maxn) + 1),
+                                 s.get<uint32_t>("gc_dry_addr_b", uint64_t(maxn) + 1)};
+        unsigned long long* cnt = s.get<unsigned long long>("gc_dry_cnt", 2);
+        uint32_t* overflow = s.get<uint32_t>("gc_dry_overflow", 1);
+        HD_CUDA(cudaMemsetAsync(overflow, 0, 4, st));
+        HD_CUDA(cudaStreamSynchronize(st));
+        int64_t avail = int64_t(g.pool_pages) - top[0] + top[1];
+        for (int32_t L = int32_t(leafl); L >= 0; L--) {
+            const uint32_t n = nlive[L];
+            uint32_t* addr = dry_addr[L & 1];
+            const uint32_t* child_addr = dry_addr[(L + 1) & 1];
+            HD_CUDA(cudaMemsetAsync(dry_sizes, 0, uint64_t(g.buckets(uint32_t(L))) * 4, st));
+            HD_CUDA(cudaMemsetAsync(d_n, 0, 4, st));
+            k_gc_dry_full<<<1, 1, 0, st>>>(c->t, uint32_t(L), dry_sizes, full_dry);
+            HD_LAUNCH_CHECK();
+            k_gc_gather<<<grid_for(n, 256), 256, 0, st>>>(c->t, uint32_t(L), live[L], n,
+                                                          L < int32_t(leafl) ? live[L + 1] : nullptr,
+                                                          L < int32_t(leafl) ? nlive[L + 1] : 0,
+                                                          L < int32_t(leafl) ? child_addr : nullptr, content, head,
+                                                          next, touched, d_n);
+            HD_LAUNCH_CHECK();
+            k_gc_dry_append<<<grid_for(uint64_t(n) * 32, 64, 152 * 16), 64, 0, st>>>(
+                c->t, uint32_t(L), content, head, next, touched, d_n, dry_sizes, addr, overflow);
+            HD_LAUNCH_CHECK();
+            HD_CUDA(cudaMemsetAsync(cnt, 0, 16, st));
+            k_gc_dry_pages<<<grid_for(g.buckets(uint32_t(L)), 256), 256, 0, st>>>(
+                c->t, uint32_t(L), dry_sizes, release_pages ? 1u : 0u, cnt, cnt + 1);
+            HD_LAUNCH_CHECK();
+            unsigned long long h[2];
+            uint32_t ovf = 0;
+            HD_CUDA(cudaMemcpyAsync(h, cnt, 16, cudaMemcpyDeviceToHost, st));
+            HD_CUDA(cudaMemcpyAsync(&ovf, overflow, 4, cudaMemcpyDeviceToHost, st));
+            HD_CUDA(cudaStreamSynchronize(st));
+            if (ovf)
+                throw StatusError{HD_ERR_BUCKET_FULL, "GC: a rebuilt bucket of level " + std::to_string(L) +
+                                                          " would exceed its capacity; the table is unchanged"};
+            if (int64_t(h[0]) > avail)
+                throw StatusError{HD_ERR_POOL_FULL, "GC: rebuilding level " + std::to_string(L) + " needs " +
+                                                        std::to_string(h[0]) + " new pages, " +
+                                                        std::to_string(std::max<int64_t>(avail, 0)) +
+                                                        " are free; the table is unchanged"};
+            avail -= int64_t(h[0]);
+            avail += int64_t(h[1]);
+        }
+        const uint32_t e = check_error(c); // a bucket list over kMaxBucketItems in the dry run
+        if (e)
+            throw StatusError{hd_status(e), "GC: " + c->err_detail + "; the table is unchanged"};
+    }
+    // rebuild bottom-up
     for (int32_t L = int32_t(leafl); L >= 0; L--) {
         const uint32_t n = nlive[L];
         char nm[32];
@@ -242,19 +392,6 @@ extern "C" hd_status hd_gc_ex(hd_ctx* c, uint32_t* extra, uint32_t n, uint32_t f
     if (!c || (n && !extra) || (flags & ~uint32_t(HD_GC_KEEP_HISTORY | HD_GC_RELEASE_PAGES)))
         return HD_ERR_INVALID;
     try {
-        // the rebuild re-appends every live node; a different order can pad
-        // pages differently and claim a few new pages, and a rebuild that
-        // runs out of pages half way cannot be undone: refuse before any
-        // change when fewer than the reserve are free
-        uint32_t top[2];
-        HD_CUDA(cudaMemcpyAsync(top, c->t.pool_top, 8, cudaMemcpyDeviceToHost, c->stream));
-        HD_CUDA(cudaStreamSynchronize(c->stream));
-        const uint64_t used = uint64_t(top[0]) - 1 - top[1], free = uint64_t(c->cfg.pool_pages) - top[0] + top[1];
-        if (free < hd::gc_page_reserve(used)) {
-            c->err = "GC needs " + std::to_string(hd::gc_page_reserve(used)) + " free pages to rebuild the table, " +
-                     std::to_string(free) + " are free; the table is unchanged";
-            return HD_ERR_POOL_FULL;
-        }
         std::vector<uint32_t> roots(1 + n);
         roots[0] = hd::read_scalar(c->d_root, c->stream);
         for (uint32_t i = 0; i < n; i++)

@@ -86,13 +86,11 @@ struct Clock {
 
 // Physical pages an edit can still claim: never-claimed pages of the pool
 // plus the pages a releasing GC put on the free list.
-uint64_t free_pages(hd_ctx* c, uint64_t* used = nullptr)
+uint64_t free_pages(hd_ctx* c)
 {
     uint32_t top[2];
     HD_CUDA(cudaMemcpyAsync(top, c->t.pool_top, 8, cudaMemcpyDeviceToHost, c->stream));
     HD_CUDA(cudaStreamSynchronize(c->stream));
-    if (used)
-        *used = uint64_t(top[0]) - 1 - top[1];
     return uint64_t(c->cfg.pool_pages) - top[0] + top[1];
 }
 
@@ -202,20 +200,20 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
                     finish_render(s);
                 }
         };
-        // a GC runs only when it has the pages its rebuild may claim
-        auto gc_possible = [&] {
-            uint64_t used = 0;
-            return free_pages(c, &used) >= gc_page_reserve(used);
-        };
+        // a GC; false when it refused to start (its rebuild would not fit the
+        // free pages; the table is unchanged)
         auto run_gc = [&] {
             drain();
             uint32_t dummy = 0;
             const uint32_t flags = HD_GC_KEEP_HISTORY | (cfg.release_pages ? HD_GC_RELEASE_PAGES : 0u);
             const hd_status g = hd_gc_ex(c, &dummy, 0, flags);
+            free_after_gc = free_pages(c);
+            if (g == HD_ERR_POOL_FULL || g == HD_ERR_BUCKET_FULL)
+                return false;
             if (g != HD_OK)
                 throw StatusError{g, "GC inside the serving loop failed: " + c->err};
             gcs++;
-            free_after_gc = free_pages(c);
+            return true;
         };
         // admission: free pages above the threshold, or a GC first (again
         // only once something was claimed since the last one)
@@ -223,7 +221,7 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
             if (cfg.gc_free_fraction <= 0)
                 return;
             const uint64_t f = free_pages(c);
-            if (double(f) < cfg.gc_free_fraction * double(c->cfg.pool_pages) && f < free_after_gc && gc_possible())
+            if (double(f) < cfg.gc_free_fraction * double(c->cfg.pool_pages) && f < free_after_gc)
                 run_gc();
         };
         auto fence_renders = [&] {
@@ -256,7 +254,7 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
                     c->color_fences.clear();
                     if (e.status != HD_ERR_POOL_FULL)
                         throw;
-                    if (attempt == 1 || cfg.gc_free_fraction <= 0 || !gc_possible()) {
+                    if (attempt == 1 || cfg.gc_free_fraction <= 0 || !run_gc()) {
                         // refused: the pool stays full; the root is unchanged
                         res[i].end_ms = clk.now();
                         res[i].root = c->root;
@@ -266,7 +264,6 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
                         completed++;
                         return;
                     }
-                    run_gc();
                 }
             }
             HD_CUDA(cudaEventRecord(edit_ev, st));

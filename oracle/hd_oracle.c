@@ -2716,6 +2716,96 @@ int or_colors_from_scene(or_colors* col, const or_table* t, uint64_t color_seed)
     return HD_OK;
 }
 
+/* The same tree built by `threads` threads: the node and leaf slots are laid
+ * out first in colors_tree's depth-first order (same indices), then the
+ * leaves, independent of one another, are built in parallel. */
+typedef struct {
+    uint32_t slot, child, path[3];
+} leaf_task;
+typedef struct {
+    leaf_task* v;
+    uint64_t n, cap;
+} leaf_tasks;
+
+static uint32_t colors_tree_plan(const or_table* t, or_colors* col, uint32_t level, uint32_t index,
+                                 const uint32_t path[3], leaf_tasks* tasks)
+{
+    const uint32_t T = t->cfg.color_tree_levels;
+    const uint32_t cn = colors_alloc_node(col);
+    const uint32_t* p = sys_ptr(t, index);
+    const uint32_t mask = p[0] & 0xffu;
+    uint32_t off = 1;
+    for (uint32_t c = 0; c < 8; c++) {
+        if (!(mask & (1u << c)))
+            continue;
+        const uint32_t child = sys_ptr(t, index)[off++];
+        uint32_t np[3];
+        descend(path, c, np);
+        if (level == T - 1) {
+            const uint32_t ref = colors_alloc_leaf(col);
+            GROW(tasks->v, tasks->n, tasks->cap, leaf_task);
+            tasks->v[tasks->n++] = (leaf_task){ref & ~LEAF_FLAG, child, {np[0], np[1], np[2]}};
+            col->nodes[cn + c] = ref;
+        } else {
+            /* the call may grow (move) col->nodes: store after it */
+            const uint32_t sub = colors_tree_plan(t, col, level + 1, child, np, tasks);
+            col->nodes[cn + c] = sub;
+        }
+    }
+    return cn;
+}
+
+typedef struct {
+    const or_table* t;
+    or_colors* col;
+    const leaf_tasks* tasks;
+    uint64_t seed;
+    uint64_t* next;
+} leaf_worker;
+
+static void* leaf_worker_run(void* arg)
+{
+    leaf_worker* w = (leaf_worker*)arg;
+    const uint32_t T = w->t->cfg.color_tree_levels;
+    for (;;) {
+        const uint64_t i = __atomic_fetch_add(w->next, 1, __ATOMIC_RELAXED);
+        if (i >= w->tasks->n)
+            break;
+        const leaf_task* k = &w->tasks->v[i];
+        or_builder b;
+        memset(&b, 0, sizeof(b));
+        leaf_voxels(w->t, T, k->child, k->path, w->seed, &b);
+        builder_build(&b, &w->col->leaves[k->slot]);
+        builder_free(&b);
+    }
+    return NULL;
+}
+
+int or_colors_from_scene_mt(or_colors* col, const or_table* t, uint64_t color_seed, uint32_t threads)
+{
+    const uint32_t T = t->cfg.color_tree_levels;
+    if (!col || col->n_nodes || T == 0 || T >= t->leaf_level || t->root == INVALID)
+        return HD_ERR_INVALID;
+    if (threads == 0) {
+        const long n = sysconf(_SC_NPROCESSORS_ONLN);
+        threads = n > 0 ? (uint32_t)n : 1;
+    }
+    if (threads > 256)
+        threads = 256;
+    const uint32_t path[3] = {0, 0, 0};
+    leaf_tasks tasks = {0};
+    colors_tree_plan(t, col, 0, t->root, path, &tasks);
+    uint64_t next = 0;
+    pthread_t th[256];
+    leaf_worker w = {t, col, &tasks, color_seed, &next};
+    for (uint32_t i = 0; i < threads; i++)
+        pthread_create(&th[i], NULL, leaf_worker_run, &w);
+    for (uint32_t i = 0; i < threads; i++)
+        pthread_join(th[i], NULL);
+    free(tasks.v);
+    return HD_OK;
+}
+
 /* ---- the compressed colours that ship beside a BasicDAG ------------------ */
 
 typedef struct {

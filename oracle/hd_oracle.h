@@ -100,6 +100,8 @@ or_colors* or_colors_create(void);
 void or_colors_destroy(or_colors* c);
 /* colour tree + one leaf per level-T slot from the scene's colour field */
 int or_colors_from_scene(or_colors* c, const or_table* t, uint64_t color_seed);
+/* the same colours, leaves built by `threads` threads (0: every core) */
+int or_colors_from_scene_mt(or_colors* col, const or_table* t, uint64_t color_seed, uint32_t threads);
 hd_color or_get_color(const or_table* t, const or_colors* c, uint32_t x, uint32_t y, uint32_t z);
 /* every tool incl. paint and copy; records an undo frame */
 int or_edit_colored(or_table* t, or_colors* c, const hd_edit* e, hd_edit_stats* stats);

@@ -127,6 +127,7 @@ def lib():
         L.or_colors_create.restype = P
         L.or_colors_destroy.argtypes = [P]
         L.or_colors_from_scene.argtypes = [P, P, u64]
+        L.or_colors_from_scene_mt.argtypes = [P, P, u64, u32]
         L.or_get_color.restype = HdColor
         L.or_get_color.argtypes = [P, P, u32, u32, u32]
         L.or_edit_colored.argtypes = [P, P, C.POINTER(HdEdit), C.POINTER(HdEditStats)]
@@ -334,8 +335,12 @@ class Colors:
             lib().or_colors_destroy(self.h)
             self.h = None
 
-    def from_scene(self, color_seed):
-        if lib().or_colors_from_scene(self.h, self.t.h, color_seed):
+    def from_scene(self, color_seed, threads=1):
+        """threads > 1 (0: every core) builds the leaves in parallel, with the
+        same result."""
+        r = (lib().or_colors_from_scene(self.h, self.t.h, color_seed) if threads == 1 else
+             lib().or_colors_from_scene_mt(self.h, self.t.h, color_seed, threads))
+        if r:
             raise RuntimeError("colour import failed")
 
     def get_color(self, x, y, z):

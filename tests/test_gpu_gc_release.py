@@ -70,9 +70,9 @@ def test_release_gc_lets_a_small_pool_take_an_edit_stream(gpu):
     live.remove_stale_nodes(release_pages=True)
     live_pages = live.level_stats().pages_used
     live.free()
-    # free pages to keep: an edit's worth twice over, and the GC's reserve
-    # (1/32 of the pages in use + 64)
-    need = max(2 * max(step), total // 32 + 64)
+    # free pages to keep: an edit's worth twice over, and room for the GC's
+    # rebuild (its order pads pages differently from the edits')
+    need = 2 * max(step) + total // 16 + 64
     pool = live_pages + 1 + 2 * need
     assert pool - 1 < total, "the stream must not fit the pool without page reuse"
     # without page reuse the pool runs out partway through the stream
@@ -104,19 +104,22 @@ def test_release_gc_lets_a_small_pool_take_an_edit_stream(gpu):
     ref.free()
 
 
-def test_gc_refuses_without_its_page_reserve(gpu):
-    """A GC that may need pages it does not have refuses before it changes
-    anything (HD_ERR_POOL_FULL), and the table stays as it was."""
+def test_gc_refuses_when_its_rebuild_does_not_fit(gpu):
+    """The GC first runs its rebuild dry (same order, same addresses) and
+    counts the pages it would map; when they are not free it refuses before
+    it changes anything (HD_ERR_POOL_FULL) and the table stays as it was.
+    Here: an edited table imported into a pool with no free page."""
     depth = 10
-    probe = _edited([], depth)
-    scene_pages = probe.level_stats().pages_used
-    probe.free()
-    d = hd.HashDAG(config=hd.default_config(depth, pool_pages=scene_pages + 1 + 8))
-    d.generate_scene(workloads.SEED_SCENE)
+    edits = workloads.mixed_edits(depth, 16, (16.0, 96.0), seed=29)
+    src = _edited(edits, depth)
+    t = src.export_table()
+    src.free()
+    d = hd.HashDAG(config=hd.default_config(depth, pool_pages=int(t["pool"].size // 512)))
+    d.import_table(t)
     root = d.firstNodeIndex
     before = table_digest(d.export_table(), depth, 10)
     with pytest.raises(hd.HashDagError) as ei:
-        d.remove_stale_nodes(release_pages=True)
-    assert ei.value.status == _capi.HD_ERR_POOL_FULL and "unchanged" in str(ei.value)
+        d.remove_stale_nodes()
+    assert ei.value.status == _capi.HD_ERR_POOL_FULL and "unchanged" in str(ei.value), str(ei.value)
     assert d.firstNodeIndex == root and table_digest(d.export_table(), depth, 10) == before
     d.free()
