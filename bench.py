@@ -77,6 +77,8 @@ def parse():
     p.add_argument("--pool-pages", type=int, default=0, help="physical pool pages (0 = library default)")
     p.add_argument("--edits", type=int, default=256, help="edits of the edit benchmark (0 = skip it)")
     p.add_argument("--edit-cpu-seconds", type=float, default=12.0, help="budget of the CPU edit sample")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="batched edits with the library's default launch shape (no hd_autotune_batch)")
     p.add_argument("--no-colors", action="store_true", help="skip the colours / copy / GC workload")
     p.add_argument("--no-serving", action="store_true", help="skip the serving-loop workload")
     p.add_argument("--serving-depth", type=int, default=16)
@@ -281,9 +283,11 @@ def edit_bench(args, dist):
     sphere fill, 20% box fill, radius log-uniform in [4, 512], centred on
     surface voxels (seed 3).  The plain form applies them one call per edit
     (hd_edit_apply: host-driven levels, a sync per level); the batched form
-    runs them through hd_edit_batch (one captured graph per edit, launch
-    shape from hd_autotune_batch on the first 32 edits).  Both start from
-    the same freshly generated scene and must end on the same root."""
+    runs them through hd_edit_batch: the whole batch in one persistent
+    launch, or one captured graph per edit, the mode and launch shape from
+    hd_autotune_batch on the first 32 edits (the library's default with
+    --no-autotune), and the other mode timed alike.  All start from the
+    same freshly generated scene and must end on the same root."""
     import hashdag_gb300 as hd
     from hashdag_gb300 import workloads
     depth, n = args.depth, args.edits
@@ -308,7 +312,7 @@ def edit_bench(args, dist):
     # batched: tune on a copy (graph shapes and the persistent form), warm
     # up, then the timed batch; the other mode timed alike for the A/B
     d = fresh()
-    tuning, _ = d.autotune_batch(eds[:32])
+    tuning = d.batch_tuning if args.no_autotune else d.autotune_batch(eds[:32])[0]
     d.edit_batch(eds[:2])
     d.free()
     other = hd.BatchTuning(4, 4, 304, 1 - tuning.mode)
@@ -380,22 +384,37 @@ def edit_bench(args, dist):
 
 
 def edit_cpu_baseline(args, tuples):
-    """The oracle's C restatement of the reference editor (single thread) on
-    the same scene and edits, as many edits as fit the time budget."""
-    import hashdag_gb300 as hd
+    """The oracle's C restatement of the reference editor on the same scene
+    and edits: the reference's threaded edit_threads (level-T tasks on every
+    host core, per-bucket locks) on the first edits for half the time
+    budget, then the single-threaded editor on the edits after them for the
+    other half."""
     d, _ = load_scene(args.depth, args.pool_pages)
     ot = oracle_from(d, args.depth, spare_pages=1 << 18)
     d.free()
-    t0 = time.perf_counter()
-    vox = foa = k = 0
-    while k < len(tuples) and time.perf_counter() - t0 < args.edit_cpu_seconds:
-        s = ot.edit(*tuples[k])
-        vox += s.num_voxels
-        foa += s.find_or_add_calls
-        k += 1
-    dt = time.perf_counter() - t0
-    return {"voxels_per_s": vox / dt, "find_or_add_per_s": foa / dt, "edits_per_s": k / dt, "cores": 1,
-            "kind": "port", "sample": f"first {k} of the {len(tuples)} edits, oracle C editor, 1 thread, {dt:.1f} s"}
+    cores = os.cpu_count() or 1
+
+    def sample(first, threads, budget):
+        t0 = time.perf_counter()
+        vox = foa = 0
+        k = first
+        while k < len(tuples) and time.perf_counter() - t0 < budget:
+            s = ot.edit(*tuples[k], threads=threads)
+            vox += s.num_voxels
+            foa += s.find_or_add_calls
+            k += 1
+        return k, vox, foa, time.perf_counter() - t0
+
+    k1, vox, foa, dt = sample(0, cores, args.edit_cpu_seconds / 2)
+    k2, vox1, foa1, dt1 = sample(k1, 1, args.edit_cpu_seconds / 2)
+    return {"voxels_per_s": vox / dt, "find_or_add_per_s": foa / dt, "edits_per_s": k1 / dt, "cores": cores,
+            "kind": "port",
+            "sample": f"edits 0-{k1 - 1} of {len(tuples)}, oracle C editor with the reference's threaded "
+                      f"edit_threads on {cores} threads, {dt:.1f} s",
+            "one_thread": {"voxels_per_s": vox1 / dt1 if dt1 else None,
+                           "find_or_add_per_s": foa1 / dt1 if dt1 else None,
+                           "edits_per_s": (k2 - k1) / dt1 if dt1 else None, "cores": 1,
+                           "sample": f"edits {k1}-{k2 - 1}, 1 thread, {dt1:.1f} s"}}
 
 
 def colors_bench(args):

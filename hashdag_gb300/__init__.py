@@ -506,6 +506,11 @@ class HashDAG:
     def set_fp_mode(self, mode):
         self._check(lib().hd_set_fp_mode(self._h, int(mode)))
 
+    def set_page_reserve(self, pages):
+        """Keeps `pages` pool pages back from edits for the GC's rebuild
+        (hd_set_page_reserve)."""
+        self._check(lib().hd_set_page_reserve(self._h, int(pages)))
+
 
 class DAGTracer:
     """Headless DAGTracer: results in device buffers (torch tensors)."""

@@ -179,6 +179,7 @@ SIGNATURES = [
     ("hd_trace_counters_noalloc", C.c_int, [_P, C.POINTER(Camera), _u32, _u32, C.POINTER(_f32), _f32, _P, _P,
                                             C.POINTER(_u64)]),
     ("hd_set_fp_mode", C.c_int, [_P, _u32]),
+    ("hd_set_page_reserve", C.c_int, [_P, _u32]),
     ("hd_get_values", C.c_int, [_P, _P, _u64, _P]),
     ("hd_edit_apply", C.c_int, [_P, C.POINTER(Edit), C.POINTER(EditStats)]),
     ("hd_edit_batch", C.c_int, [_P, C.POINTER(Edit), _u32, C.POINTER(EditStats)]),

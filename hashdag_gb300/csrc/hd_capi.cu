@@ -95,7 +95,8 @@ hd_status hd_create(const hd_config* cfg, hd_ctx** out)
         HD_CUDA(cudaMalloc(&t.page_table, kPageTableEntries * 4));
         HD_CUDA(cudaMalloc(&t.bucket_sizes, c->g.total_buckets * 4));
         HD_CUDA(cudaMalloc(&t.full_nodes, HD_MAX_DEPTH * 4));
-        HD_CUDA(cudaMalloc(&t.pool_top, 8));
+        // poolTop, free-list count, claim limit
+        HD_CUDA(cudaMalloc(&t.pool_top, 16));
         HD_CUDA(cudaMalloc(&t.free_pages, size_t(conf.pool_pages) * 4));
         HD_CUDA(cudaMalloc(&t.error, 16));
         HD_CUDA(cudaMalloc(&t.level_nodes, HD_MAX_DEPTH * 8));
@@ -210,6 +211,16 @@ hd_status hd_export_basic_dag(hd_ctx* c, uint32_t* h_words, uint64_t capacity, u
     return guarded(c, [&] {
         HD_CUDA(cudaMemcpyAsync(h_words, c->d_basic, c->n_basic * 4, cudaMemcpyDeviceToHost, c->stream));
         HD_CUDA(cudaStreamSynchronize(c->stream));
+    });
+}
+
+hd_status hd_set_page_reserve(hd_ctx* c, uint32_t pages)
+{
+    if (!c || pages >= c->cfg.pool_pages)
+        return HD_ERR_INVALID;
+    return guarded(c, [&] {
+        c->page_reserve = pages;
+        set_claim_limit(c, false);
     });
 }
 

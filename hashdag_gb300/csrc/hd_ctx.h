@@ -63,6 +63,9 @@ struct hd_ctx {
     // a table loaded from a hash-DAG file without bucket sizes: traversal
     // works, edits wait for a GC to rebuild the buckets
     bool needs_gc = false;
+    // pages page claims outside a GC leave untouched (hd_set_page_reserve):
+    // the GC's rebuild draws on them
+    uint32_t page_reserve = 0;
 };
 
 namespace hd {
@@ -155,13 +158,22 @@ void trace_primary(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, uint
 // 32-bit words of a shadow-ray list buffer for px pixels: 16 bytes per ray
 // and a 4-word head (ray count, two work counters).
 inline uint64_t shadow_list_words(uint64_t px) { return 4 * px + 4; }
+// Doubles of one view's camera tables (trace_views): a column entry per
+// column and a row entry per row, 3 doubles each.
+__host__ __device__ inline uint64_t camera_table_words(uint32_t w, uint32_t h) { return 3ull * (uint64_t(w) + h); }
 void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const uint32_t* d_paths,
                   const float light[3], float bias, uint8_t* d_mask, unsigned long long* d_counters = nullptr,
                   cudaStream_t stream = nullptr, const uint32_t* d_root = nullptr, uint32_t* d_list = nullptr);
 void get_values(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out);
-// mid (optional): recorded between the primary and the shadow launches
+// The page claims' limit on poolTop (the table's third pool_top word):
+// pool_pages less the reserve, or (gc = true) the whole pool.
+void set_claim_limit(hd_ctx* c, bool gc);
+// mid (optional): recorded between the primary and the shadow launches;
+// d_tables (optional): camera_table_words(w, h) * n_views doubles of
+// scratch for the per-view camera tables (default: the context's)
 void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t w, uint32_t h, uint32_t* d_paths,
                  const float light[3], float bias, uint8_t* d_mask, cudaStream_t stream = nullptr,
-                 uint32_t* d_list = nullptr, cudaEvent_t mid = nullptr, const uint32_t* d_root = nullptr);
+                 uint32_t* d_list = nullptr, cudaEvent_t mid = nullptr, const uint32_t* d_root = nullptr,
+                 double* d_tables = nullptr);
 
 } // namespace hd

@@ -98,17 +98,17 @@ __global__ void k_gc_gather(Table t, uint32_t level, const uint32_t* __restrict_
     }
 }
 
-// Pages wholly past the new size of a bucket of `level` go to the free list
-// (one thread per bucket, at most capacity / 512 pages each).
-__global__ void k_gc_release(Table t, uint32_t level)
+// Pages wholly past a bucket's final size (`sizes`, the level's buckets)
+// go to the free list (one thread per bucket, at most capacity / 512 pages
+// each).
+__global__ void k_gc_release(Table t, uint32_t level, const uint32_t* __restrict__ sizes)
 {
     const Geom& g = t.g;
     uint32_t* free_count = t.pool_top + 1;
-    const uint32_t first = g.level_first_bucket(level);
     HD_GRID_STRIDE(i, g.buckets(level))
     {
         const uint32_t bucket = uint32_t(i);
-        const uint32_t size = t.bucket_sizes[first + bucket], cap = g.capacity(level);
+        const uint32_t size = sizes[bucket], cap = g.capacity(level);
         for (uint32_t off = (size + kPage - 1) & ~(kPage - 1); off < cap; off += kPage) {
             const uint32_t vp = g.make_ptr(level, bucket, off) >> kPageShift;
             const uint32_t p = t.page_table[vp];
@@ -140,6 +140,11 @@ __global__ void k_zero_pages(Table t, uint32_t from, uint32_t to)
 // runs every level's rebuild on scratch bucket sizes (the same full node
 // first, the same items in the same order, hence the same addresses) and
 // counts the pages it would map, and the pages a releasing GC would free.
+// A releasing GC frees a level's pages that lie wholly past their bucket's
+// final size (kept from the dry run) before it re-appends the level, so the
+// appends of the same level can take them: re-hashed parents (children
+// remapped) move between buckets, and one bucket's growth is met by
+// another's shrinkage.
 
 // The level's full node at the head of its (empty) bucket, on dry sizes.
 __global__ void k_gc_dry_full(Table t, uint32_t level, uint32_t* dry_sizes, uint32_t* full_dry)
@@ -236,12 +241,29 @@ __global__ void k_gc_remap_roots(const uint32_t* __restrict__ live, uint32_t n, 
     *d_root = roots[0];
 }
 
+namespace {
+// The rebuild may claim the pages other claims leave as the GC's reserve
+// (hd_set_page_reserve); the limit comes back however the GC ends.
+struct ReserveOpen {
+    hd_ctx* c;
+    explicit ReserveOpen(hd_ctx* ctx) : c(ctx) { set_claim_limit(c, true); }
+    ~ReserveOpen()
+    {
+        try {
+            set_claim_limit(c, false);
+        } catch (...) {
+        }
+    }
+};
+} // namespace
+
 void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
 {
     cudaStream_t st = c->stream;
     Scratch& s = c->scratch;
     const Geom& g = c->g;
     const uint32_t leafl = g.leaf_level;
+    ReserveOpen reserve_open(c);
     uint32_t* d_n = s.get<uint32_t>("gc_n", 4);
     // level 0: the roots, sorted unique
     std::vector<uint32_t> r0(roots.begin(), roots.end());
@@ -286,7 +308,7 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
     {
         uint32_t top[2];
         HD_CUDA(cudaMemcpyAsync(top, c->t.pool_top, 8, cudaMemcpyDeviceToHost, st));
-        uint32_t* dry_sizes = s.get<uint32_t>("gc_dry_sizes", uint64_t(1) << std::max(g.top_bits, g.low_bits));
+        uint32_t* dry_all = s.get<uint32_t>("gc_dry_sizes", g.total_buckets);
         uint32_t* full_dry = s.get<uint32_t>("gc_full_dry", HD_MAX_DEPTH);
         uint32_t* dry_addr[2] = {s.get<uint32_t>("gc_dry_addr_a", uint64_t(maxn) + 1),
                                  s.get<uint32_t>("gc_dry_addr_b", uint64_t(maxn) + 1)};
@@ -299,6 +321,7 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
             const uint32_t n = nlive[L];
             uint32_t* addr = dry_addr[L & 1];
             const uint32_t* child_addr = dry_addr[(L + 1) & 1];
+            uint32_t* dry_sizes = dry_all + g.level_first_bucket(uint32_t(L));
             HD_CUDA(cudaMemsetAsync(dry_sizes, 0, uint64_t(g.buckets(uint32_t(L))) * 4, st));
             HD_CUDA(cudaMemsetAsync(d_n, 0, 4, st));
             k_gc_dry_full<<<1, 1, 0, st>>>(c->t, uint32_t(L), dry_sizes, full_dry);
@@ -324,19 +347,22 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
             if (ovf)
                 throw StatusError{HD_ERR_BUCKET_FULL, "GC: a rebuilt bucket of level " + std::to_string(L) +
                                                           " would exceed its capacity; the table is unchanged"};
+            // releasing: the level's pages past the final sizes are freed
+            // before its appends claim
+            avail += int64_t(h[1]);
             if (int64_t(h[0]) > avail)
                 throw StatusError{HD_ERR_POOL_FULL, "GC: rebuilding level " + std::to_string(L) + " needs " +
                                                         std::to_string(h[0]) + " new pages, " +
                                                         std::to_string(std::max<int64_t>(avail, 0)) +
                                                         " are free; the table is unchanged"};
             avail -= int64_t(h[0]);
-            avail += int64_t(h[1]);
         }
         const uint32_t e = check_error(c); // a bucket list over kMaxBucketItems in the dry run
         if (e)
             throw StatusError{hd_status(e), "GC: " + c->err_detail + "; the table is unchanged"};
     }
     // rebuild bottom-up
+    const uint32_t* dry_all = s.get<uint32_t>("gc_dry_sizes", g.total_buckets);
     for (int32_t L = int32_t(leafl); L >= 0; L--) {
         const uint32_t n = nlive[L];
         char nm[32];
@@ -355,13 +381,13 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
                                 uint64_t(g.buckets(uint32_t(L))) * 4, st));
         bloom_clear_level(c, uint32_t(L));
         HD_CUDA(cudaMemsetAsync(c->t.level_nodes + L, 0, 8, st));
-        add_full_nodes(c, uint32_t(L), uint32_t(L));
-        append_items(c, uint32_t(L), content, n, head, next, touched, d_n, newaddr[L]);
         if (release_pages) {
-            // this level's emptied pages, zeroed, serve the levels above
+            // the level's pages past its final bucket sizes (the dry run's),
+            // zeroed, serve this level's appends and the levels above
             uint32_t before[2], after[2];
             HD_CUDA(cudaMemcpyAsync(before, c->t.pool_top, 8, cudaMemcpyDeviceToHost, st));
-            k_gc_release<<<grid_for(g.buckets(uint32_t(L)), 256), 256, 0, st>>>(c->t, uint32_t(L));
+            k_gc_release<<<grid_for(g.buckets(uint32_t(L)), 256), 256, 0, st>>>(
+                c->t, uint32_t(L), dry_all + g.level_first_bucket(uint32_t(L)));
             HD_LAUNCH_CHECK();
             HD_CUDA(cudaMemcpyAsync(after, c->t.pool_top, 8, cudaMemcpyDeviceToHost, st));
             HD_CUDA(cudaStreamSynchronize(st));
@@ -371,6 +397,8 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
                 HD_LAUNCH_CHECK();
             }
         }
+        add_full_nodes(c, uint32_t(L), uint32_t(L));
+        append_items(c, uint32_t(L), content, n, head, next, touched, d_n, newaddr[L]);
     }
     uint32_t* d_roots = s.get<uint32_t>("gc_roots", roots.size());
     HD_CUDA(cudaMemcpyAsync(d_roots, roots.data(), roots.size() * 4, cudaMemcpyHostToDevice, st));

@@ -65,6 +65,7 @@ struct Slot {
     uint32_t* root = nullptr;
     uint32_t* list = nullptr; // the shadow-ray list
     hd_camera* cam = nullptr; // the frame's camera on the device
+    double* tables = nullptr; // its camera tables
     unsigned long long* sum = nullptr;
     unsigned long long* h_sum = nullptr; // pinned
     cudaEvent_t colors_done = nullptr, done = nullptr;
@@ -101,10 +102,12 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
 {
     cudaStream_t st = c->stream;
     const uint32_t R = cfg.continuous ? (cfg.max_renders ? cfg.max_renders : 1) : 1;
-    uint64_t max_pixels = 1;
+    uint64_t max_pixels = 1, max_table = 1;
     for (uint32_t i = 0; i < n; i++)
-        if (reqs[i].kind == HD_REQ_RENDER)
+        if (reqs[i].kind == HD_REQ_RENDER) {
             max_pixels = std::max<uint64_t>(max_pixels, uint64_t(reqs[i].width) * reqs[i].height);
+            max_table = std::max<uint64_t>(max_table, camera_table_words(reqs[i].width, reqs[i].height));
+        }
     std::vector<Slot> slots(R);
     for (uint32_t k = 0; k < R; k++) {
         Slot& s = slots[k];
@@ -125,12 +128,15 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
         s.list = c->scratch.get<uint32_t>(nm, shadow_list_words(max_pixels));
         snprintf(nm, sizeof(nm), "serve_cam_%u", k);
         s.cam = c->scratch.get<hd_camera>(nm, 1);
+        snprintf(nm, sizeof(nm), "serve_tables_%u", k);
+        s.tables = c->scratch.get<double>(nm, max_table);
         snprintf(nm, sizeof(nm), "serve_sum_%u", k);
         s.sum = c->scratch.get<unsigned long long>(nm, 1);
         HD_CUDA(cudaMallocHost(&s.h_sum, 8));
         HD_CUDA(cudaEventCreateWithFlags(&s.colors_done, cudaEventDisableTiming));
         HD_CUDA(cudaEventCreate(&s.done));
     }
+    const uint32_t saved_reserve = c->page_reserve;
     auto cleanup = [&] {
         for (Slot& s : slots) {
             if (s.stream && s.stream != st) {
@@ -145,8 +151,22 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
                 cudaEventDestroy(s.done);
         }
         c->color_fences.clear();
+        if (c->page_reserve != saved_reserve) {
+            c->page_reserve = saved_reserve;
+            try {
+                set_claim_limit(c, false);
+            } catch (...) {
+            }
+        }
     };
     try {
+        // with GCs in the loop, pages kept back from edits for the GC's
+        // rebuild (an edit that fills the pool would otherwise leave the GC
+        // none)
+        if (cfg.gc_free_fraction > 0 && c->page_reserve < c->cfg.pool_pages / 64) {
+            c->page_reserve = c->cfg.pool_pages / 64;
+            set_claim_limit(c, false);
+        }
         Clock clk;
         HD_CUDA(cudaEventCreate(&clk.ev0));
         HD_CUDA(cudaStreamSynchronize(st));
@@ -171,7 +191,7 @@ void serve(hd_ctx* c, const hd_request* reqs, uint32_t n, const hd_serve_config&
             // the frame as a one-view hd_trace_views: persistent primary
             // warps building the shadow-ray list, then the shadow walks
             trace_views(c, s.cam, 1, r.width, r.height, s.paths, cfg.light, cfg.shadow_bias, s.mask, s.stream, s.list,
-                        nullptr, s.root);
+                        nullptr, s.root, s.tables);
             if (c->colors)
                 trace_colors(c, s.paths, r.width, r.height, s.rgba, s.stream, s.root);
             HD_CUDA(cudaEventRecord(s.colors_done, s.stream));

@@ -5,6 +5,7 @@
 // (hash_table.h:359-468), allocate_page (:794-809), add_full_node
 // (:749-789); HashDAGFactory::load_from_DAG and create_hash_dag
 // (hash_dag_factory.cpp:5-99, :152-184).
+#include <algorithm>
 #include <vector>
 
 #include "hd_ctx.h"
@@ -69,6 +70,10 @@ static std::string describe_error(const Geom& g, const uint32_t* e)
     const std::string level = std::to_string(e[1]), bucket = std::to_string(e[2]);
     switch (e[0]) {
     case kErrPoolFull:
+        if (e[3] && e[3] < g.pool_pages)
+            return "the pool is full: the " + std::to_string(e[3]) + " pages edits may claim (of " +
+                   std::to_string(g.pool_pages) + "; the rest are the GC's reserve) are in use and an append to "
+                   "level " + level + ", bucket " + bucket + " needed one more";
         return "the pool is full: all " + std::to_string(g.pool_pages) +
                " pages are in use and an append to level " + level + ", bucket " + bucket + " needed one more";
     case kErrBucketFull:
@@ -112,7 +117,16 @@ void table_reset(hd_ctx* c)
     HD_CUDA(cudaMemsetAsync(c->t.error, 0, 16, c->stream));
     const uint32_t top[2] = {1, 0}; // page 0 is the null page; no free pages
     HD_CUDA(cudaMemcpyAsync(c->t.pool_top, top, 8, cudaMemcpyHostToDevice, c->stream));
+    set_claim_limit(c, false);
     HD_CUDA(cudaMemsetAsync(c->d_root, 0, 4, c->stream));
+}
+
+void set_claim_limit(hd_ctx* c, bool gc)
+{
+    // the copy reads a local: wait for it
+    const uint32_t limit = gc ? c->g.pool_pages : c->g.pool_pages - std::min(c->page_reserve, c->g.pool_pages);
+    HD_CUDA(cudaMemcpyAsync(c->t.pool_top + 2, &limit, 4, cudaMemcpyHostToDevice, c->stream));
+    HD_CUDA(cudaStreamSynchronize(c->stream));
 }
 
 // ---------------------------------------------------------------------------

@@ -43,7 +43,7 @@ HD_D uint32_t claim_page(const Table& t)
         atomicAdd(free_count, 1u); // none left: undo
     }
     const uint32_t p = atomicAdd(t.pool_top, 1u);
-    if (p >= t.g.pool_pages) {
+    if (p >= __ldcg(t.pool_top + 2)) { // the claim limit: the pool less the GC's reserve
         atomicSub(t.pool_top, 1u);
         return 0;
     }
@@ -63,7 +63,7 @@ HD_D bool map_pages(const Table& t, uint32_t level, uint32_t bucket, uint32_t fr
         if (__ldcg(t.page_table + vp) == 0) {
             const uint32_t p = claim_page(t);
             if (!p) {
-                set_error(t.error, kErrPoolFull, level, bucket, t.g.pool_pages);
+                set_error(t.error, kErrPoolFull, level, bucket, __ldcg(t.pool_top + 2));
                 return false;
             }
             __stcg(t.page_table + vp, p);

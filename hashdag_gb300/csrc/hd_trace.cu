@@ -113,6 +113,38 @@ HD_D bool round_to_float(double v, uint32_t margin, float& out)
     return true;
 }
 
+// A positive normal float as a double, from its bits.
+HD_D double float_to_double_bits(uint32_t fb)
+{
+    return __longlong_as_double(
+        (long long)((uint64_t(((fb >> 23) & 0xFF) - 127 + 1023) << 52) | (uint64_t(fb & 0x7FFFFFu) << 29)));
+}
+
+// 1 / sqrt(dot) for dot in [2^-100, 2^100]: an rsqrtf seed (its argument
+// dot rounded to float by its bits; the carry of the rounding bit reaches
+// the exponent when it must) and one Newton-Raphson step in double,
+// y1 = y0 + y0 (1 - dot y0^2) / 2: relative error below 2^-43.
+HD_D double rsqrt_newton(double dot)
+{
+    const uint64_t db = (uint64_t)__double_as_longlong(dot);
+    const uint32_t fb = ((uint32_t(db >> 52) - 1023 + 127) << 23) + ((uint32_t(db >> 29) & 0x7FFFFFu)) +
+                        uint32_t((db >> 28) & 1);
+    const double y0 = float_to_double_bits(__float_as_uint(rsqrtf(__uint_as_float(fb))));
+    const double h = dot * y0;
+    const double e = __fma_rn(-h, y0, 1.0);
+    return __fma_rn(y0 * e, 0.5, y0);
+}
+
+// float(normalize(v)) from v and its squared length (see camera_dir_float).
+HD_D bool dir_from_vec(const double v[3], double dot, F3& d)
+{
+    if (!(dot >= 0x1p-100 && dot <= 0x1p100))
+        return false;
+    const double y1 = rsqrt_newton(dot);
+    return round_to_float(y1 * v[0], 8192, d.x) && round_to_float(y1 * v[1], 8192, d.y) &&
+           round_to_float(y1 * v[2], 8192, d.z);
+}
+
 // float(normalize(...)) of camera_dir with a third of its double-precision
 // work (the GB300's FP64 pipe is narrow, and every primary ray pays for
 // this).  The reference rounds 1 / sqrt(dot) twice and the product once more
@@ -129,21 +161,55 @@ HD_D bool camera_dir_float(const hd_camera& cam, uint32_t x, uint32_t y, F3& d)
 {
     double v[3];
     const double dot = camera_vec<FMA>(reload_camera(&cam), u32_to_double(x), u32_to_double(y), v);
-    if (!(dot >= 0x1p-100 && dot <= 0x1p100))
-        return false;
-    // dot rounded to float by its bits (the carry of the rounding bit
-    // reaches the exponent when it must)
-    const uint64_t db = (uint64_t)__double_as_longlong(dot);
-    const uint32_t fb = ((uint32_t(db >> 52) - 1023 + 127) << 23) + ((uint32_t(db >> 29) & 0x7FFFFFu)) +
-                        uint32_t((db >> 28) & 1);
-    const uint32_t yb = __float_as_uint(rsqrtf(__uint_as_float(fb)));
-    const double y0 = __longlong_as_double(
-        (long long)((uint64_t(((yb >> 23) & 0xFF) - 127 + 1023) << 52) | (uint64_t(yb & 0x7FFFFFu) << 29)));
-    const double h = dot * y0;
-    const double e = __fma_rn(-h, y0, 1.0);
-    const double y1 = __fma_rn(y0 * e, 0.5, y0);
-    return round_to_float(y1 * v[0], 8192, d.x) && round_to_float(y1 * v[1], 8192, d.y) &&
-           round_to_float(y1 * v[2], 8192, d.z);
+    return dir_from_vec(v, dot, d);
+}
+
+// ---- per-view camera tables -------------------------------------------------
+// Of ray_min + px * ddx + py * ddy - position, the part that depends on the
+// column alone, ray_min + px * ddx (rounded as camera_vec rounds it), is the
+// same for every row, and with every operation rounded on its own (FMA = 0)
+// py * ddy is the same for every column: tables of both per view leave a
+// pixel two additions (or one fused multiply-add and a subtraction) per axis
+// instead of four or five operations on the GB300's narrow FP64 pipe.  Per
+// view: W column entries, then H row entries, 3 doubles each
+// (camera_table_words).
+
+template <int FMA>
+__global__ void k_camera_tables(const hd_camera* __restrict__ cams, uint32_t n_views, uint32_t W, uint32_t H,
+                                double* __restrict__ tables)
+{
+    const uint64_t per = uint64_t(W) + H;
+    HD_GRID_STRIDE(i, per * n_views)
+    {
+        const uint32_t v = uint32_t(i / per), k = uint32_t(i % per);
+        const hd_camera& cam = cams[v];
+        double* out = tables + camera_table_words(W, H) * v + 3ull * k;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (k < W) {
+                const double px = u32_to_double(k);
+                out[a] = FMA ? __fma_rn(px, cam.ray_ddx[a], cam.ray_min[a]) : cam.ray_min[a] + px * cam.ray_ddx[a];
+            } else {
+                out[a] = u32_to_double(k - W) * cam.ray_ddy[a];
+            }
+        }
+    }
+}
+
+// camera_vec of pixel (x, y) from its view's tables: the same doubles.
+template <int FMA>
+HD_D double camera_vec_tab(const hd_camera* cam, const double* __restrict__ tab, uint32_t W, uint32_t x, uint32_t y,
+                           double v[3])
+{
+    const double* col = tab + 3ull * x;
+    const double* row = tab + 3ull * (uint64_t(W) + y);
+    const double py = u32_to_double(y);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const double t = FMA ? __fma_rn(py, reload_f64(cam->ray_ddy + a), col[a]) : col[a] + row[a];
+        v[a] = t - reload_f64(cam->position + a);
+    }
+    return FMA ? __fma_rn(v[2], v[2], __fma_rn(v[1], v[1], v[0] * v[0])) : (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
 }
 
 // The exact path of camera_dir_float, out of line: it runs for about one ray
@@ -433,12 +499,22 @@ HD_D void add_counts(unsigned long long* counters, uint32_t rays, uint32_t desce
     atomicAdd(counters + 2, leaves);
 }
 
-template <int FMA, bool COUNT, typename Stack = LocalStack>
+// tab (TAB): the view's camera tables (k_camera_tables)
+template <int FMA, bool COUNT, typename Stack = LocalStack, bool TAB = false>
 HD_D uint4 primary_ray(const Table& t, uint32_t root, const hd_camera& cam, uint32_t W, uint32_t H, uint32_t x,
-                       uint32_t y, uint4* __restrict__ out, unsigned long long* counters, Stack stack = Stack{})
+                       uint32_t y, uint4* __restrict__ out, unsigned long long* counters, Stack stack = Stack{},
+                       const double* __restrict__ tab = nullptr)
 {
     F3 d;
-    if (!camera_dir_float<FMA>(cam, x, y, d))
+    bool fast;
+    if (TAB) {
+        double v[3];
+        const double dot = camera_vec_tab<FMA>(&cam, tab, W, x, y, v);
+        fast = dir_from_vec(v, dot, d);
+    } else {
+        fast = camera_dir_float<FMA>(cam, x, y, d);
+    }
+    if (!fast)
         d = camera_dir_exact<FMA>(&cam, x, y);
     const F3 inv = inverse_dir(d);
     F3 o;
@@ -530,6 +606,80 @@ __device__ __noinline__ F3 shadow_origin(const hd_camera& cam, uint32_t H, uint3
     return o;
 }
 
+// shadow_origin of pixel (x, y) without its double square root and
+// divisions, for the many-view kernel (the GB300's FP64 pipe is narrow and
+// most pixels hit):
+//  * the camera direction cd = y1 * v, y1 from rsqrt_newton: less than
+//    2^-42.9 relative from the reference's double (camera_dir_float);
+//  * each 1 / cd from a float reciprocal seed (2^-22.4 from a truncated
+//    argument) and one Newton step in double, below 2^-44.5, so that each
+//    candidate t = numerator / cd (the numerators are the reference's
+//    doubles) lies within 2^-42.4 of the reference's quotient, and so does
+//    their maximum, maxmin;
+//  * x = cd * maxmin then lies within 2^-41.6 of the reference's product,
+//    and hp = position + x within |x| 2^-41.6 + 1 ulp(hp) of the
+//    reference's sum: at most (|x| / |hp|) 2^11.4 + 1 double ulps of hp.
+// Each float(hp) is taken from hp's bits when hp lies more than
+// 2^(12 + k) + 16 double ulps from a float rounding midpoint, with
+// |x| / |hp| < 2^k from the exponents; there the reference's double rounds
+// to the same float.  Otherwise (or for a zero or tiny direction component)
+// false: the caller takes the exact path.
+template <int FMA>
+__device__ __noinline__ bool shadow_origin_fast(const hd_camera* cam, const double* __restrict__ tab, uint32_t W,
+                                                uint32_t x, uint32_t y, uint4 p, F3 dir, float bias, F3* out)
+{
+    double v[3];
+    const double dot = camera_vec_tab<FMA>(cam, tab, W, x, y, v);
+    if (!(dot >= 0x1p-100 && dot <= 0x1p100))
+        return false;
+    const double y1 = rsqrt_newton(dot);
+    const uint32_t pv[3] = {p.x, p.y, p.z};
+    double cd[3], pos[3], maxmin = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        cd[a] = y1 * v[a];
+        pos[a] = reload_f64(cam->position + a);
+        const uint64_t cb = (uint64_t)__double_as_longlong(cd[a]);
+        const int32_t ce = int32_t((cb >> 52) & 0x7FF) - 1023;
+        if (ce < -60 || ce > 60)
+            return false; // zero or tiny (the exact path handles cd = 0)
+        // a float seed of |cd| from its bits (truncated), its reciprocal, one
+        // Newton step, the sign put back (negation is exact)
+        const uint32_t sb = (uint32_t(ce + 127) << 23) | (uint32_t(cb >> 29) & 0x7FFFFFu);
+        const double r0 = float_to_double_bits(__float_as_uint(__frcp_rn(__uint_as_float(sb))));
+        const double mag = fabs(cd[a]);
+        const double ra = __fma_rn(r0, __fma_rn(-mag, r0, 1.0), r0);
+        const double r1 = cd[a] < 0.0 ? -ra : ra;
+        // the voxel's box: min(t0, t1) is t0 for cd > 0, t1 for cd < 0 (the
+        // numerators are ordered)
+        const double bmin = double(float(pv[a]));
+        const double num = cd[a] > 0.0 ? bmin - pos[a] : (bmin + 1.0) - pos[a];
+        const double t = num * r1;
+        maxmin = a == 0 ? t : fmax(maxmin, t);
+    }
+    float start[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const double xa = cd[a] * maxmin;
+        const double hp = FMA ? __fma_rn(cd[a], maxmin, pos[a]) : pos[a] + xa;
+        const int32_t ex = int32_t((uint64_t(__double_as_longlong(xa)) >> 52) & 0x7FF);
+        const int32_t eh = int32_t((uint64_t(__double_as_longlong(hp)) >> 52) & 0x7FF);
+        if (eh == 0)
+            return false;
+        const int32_t k = ex - eh + 1; // |x| / |hp| < 2^k
+        if (k > 14)
+            return false;
+        const uint32_t margin = k < -12 ? 17u : (1u << (12 + k)) + 16u;
+        if (!round_to_float(hp, margin, start[a]))
+            return false;
+    }
+    if (FMA)
+        *out = {__fmaf_rn(bias, dir.x, start[0]), __fmaf_rn(bias, dir.y, start[1]), __fmaf_rn(bias, dir.z, start[2])};
+    else
+        *out = {start[0] + bias * dir.x, start[1] + bias * dir.y, start[2] + bias * dir.z};
+    return true;
+}
+
 // Several views in one launch, as persistent warps: each warp takes 8x4
 // pixel tiles from a counter (view-major, then tile rows), so warps whose
 // rays end early take more tiles and every resident warp stays busy to the
@@ -542,7 +692,8 @@ template <int FMA>
 __global__ void __launch_bounds__(128, 16)
     k_trace_views(Table t, const uint32_t* __restrict__ d_root, const hd_camera* __restrict__ cams, uint32_t W,
                   uint32_t H, uint32_t n_views, uint4* __restrict__ out, F3 light, float bias,
-                  uint8_t* __restrict__ mask, ShadowRay* __restrict__ list, uint32_t* __restrict__ head)
+                  uint8_t* __restrict__ mask, ShadowRay* __restrict__ list, uint32_t* __restrict__ head,
+                  const double* __restrict__ tables)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t tx = (W + 7) / 8, ty = (H + 3) / 4;
@@ -559,7 +710,8 @@ __global__ void __launch_bounds__(128, 16)
         bool hit = false;
         uint4 p = make_uint4(0, 0, 0, 0);
         if (x < W && y < H) {
-            p = primary_ray<FMA, false>(t, root, cams[v], W, H, x, y, out + uint64_t(v) * W * H, nullptr, stack);
+            p = primary_ray<FMA, false, SharedStack, true>(t, root, cams[v], W, H, x, y, out + uint64_t(v) * W * H,
+                                                           nullptr, stack, tables + camera_table_words(W, H) * v);
             hit = (p.x | p.y | p.z) != 0;
             if (!hit)
                 mask[i] = 2;
@@ -569,7 +721,11 @@ __global__ void __launch_bounds__(128, 16)
             const uint32_t base =
                 __shfl_sync(0xffffffffu, lane == 0 ? atomicAdd(head, uint32_t(__popc(b))) : 0u, 0);
             if (hit) {
-                const F3 o = shadow_origin<FMA>(cams[v], H, x, H - 1 - y, p, light_dir<FMA>(light), bias);
+                const F3 ld = light_dir<FMA>(light);
+                F3 o;
+                if (!shadow_origin_fast<FMA>(cams + v, tables + camera_table_words(W, H) * v, W, x, y, p, ld, bias,
+                                             &o))
+                    o = shadow_origin<FMA>(cams[v], H, x, H - 1 - y, p, ld, bias);
                 list[base + __popc(b & ((1u << lane) - 1u))] = ShadowRay{uint32_t(i), o.x, o.y, o.z};
             }
         }
@@ -787,7 +943,7 @@ void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const
 // shadow-ray list, then the shadow rays of every hit pixel of every view.
 void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t w, uint32_t h, uint32_t* d_paths,
                  const float light[3], float bias, uint8_t* d_mask, cudaStream_t stream, uint32_t* d_list,
-                 cudaEvent_t mid, const uint32_t* d_root)
+                 cudaEvent_t mid, const uint32_t* d_root, double* d_tables)
 {
     cudaStream_t st = stream ? stream : c->stream;
     const uint32_t* rt = d_root ? d_root : c->d_root;
@@ -801,16 +957,21 @@ void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t 
     uint4* out = reinterpret_cast<uint4*>(d_paths);
     const uint64_t tiles = uint64_t((w + 7) / 8) * ((h + 3) / 4);
     const F3 l = {light[0], light[1], light[2]};
-    auto launch = [&](auto kernel) {
+    const uint64_t tab_words = camera_table_words(w, h) * n_views;
+    double* tables = d_tables ? d_tables : c->scratch.get<double>("cam_tables", tab_words);
+    const uint32_t tab_blocks = grid_for(uint64_t(w + h) * n_views, 256);
+    auto launch = [&](auto tab_kernel, auto kernel) {
+        tab_kernel<<<tab_blocks, 256, 0, st>>>(d_cams, n_views, w, h, tables);
+        HD_LAUNCH_CHECK();
         const uint32_t smem = shared_stack_bytes(128, c->t.g.depth);
         const uint32_t blocks = uint32_t(std::min<uint64_t>(
             (tiles * n_views + 3) / 4, resident_blocks(reinterpret_cast<const void*>(kernel), 128, smem)));
-        kernel<<<blocks, 128, smem, st>>>(c->t, rt, d_cams, w, h, n_views, out, l, bias, d_mask, list, head);
+        kernel<<<blocks, 128, smem, st>>>(c->t, rt, d_cams, w, h, n_views, out, l, bias, d_mask, list, head, tables);
     };
     if (c->fp_mode)
-        launch(k_trace_views<1>);
+        launch(k_camera_tables<1>, k_trace_views<1>);
     else
-        launch(k_trace_views<0>);
+        launch(k_camera_tables<0>, k_trace_views<0>);
     HD_LAUNCH_CHECK();
     if (mid)
         HD_CUDA(cudaEventRecord(mid, st));

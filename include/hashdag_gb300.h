@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define HD_ABI_VERSION 7u
+#define HD_ABI_VERSION 8u
 #define HD_PAGE_SIZE 512u
 #define HD_MAX_DEPTH 20u
 /* Sentinel of the edit recursion (hash_dag_edits.h:17). */
@@ -386,7 +386,11 @@ typedef struct hd_serve_config {
     uint32_t realtime;       /* 1: a request is available at its arrival time  */
     float gc_free_fraction;  /* GC (keeping the undo history) when the free
                                 pool pages fall below this fraction of the
-                                pool; 0 = never                                */
+                                pool, and once more when an edit finds the
+                                pool full (then the edit is retried); 0 =
+                                never.  Above 0 the loop keeps
+                                max(hd_set_page_reserve's pages, pool / 64)
+                                pages back for its GCs                        */
     float light[3];
     float shadow_bias;
     uint32_t release_pages;  /* the serving GC releases pages (HD_GC_RELEASE_PAGES) */
@@ -442,6 +446,16 @@ hd_status hd_gc(hd_ctx* ctx, uint32_t* h_extra_roots, uint32_t n_extra);
  * without the flag. */
 #define HD_GC_RELEASE_PAGES 2u
 hd_status hd_gc_ex(hd_ctx* ctx, uint32_t* h_extra_roots, uint32_t n_extra, uint32_t flags);
+/* Keeps `pages` pool pages back from every page claim outside a GC (no
+ * reference counterpart).  A GC re-appends the live nodes of a level into
+ * buckets chosen by their new hashes (children remapped), so a bucket can
+ * need a page it never had; with no free page the GC refuses
+ * (HD_ERR_POOL_FULL, table unchanged), which is where an edit stream that
+ * fills the pool would leave it.  With a reserve, edits fail at
+ * pool_pages - pages (HD_ERR_POOL_FULL, as on a full pool) and the GC's
+ * rebuild may use the reserve.  Default 0 (the reference: every page is an
+ * edit's). */
+hd_status hd_set_page_reserve(hd_ctx* ctx, uint32_t pages);
 
 /* ---- files (serializer.h:11-121) ---------------------------------------- */
 

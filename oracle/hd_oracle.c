@@ -128,14 +128,21 @@ struct or_table {
     int error;
     /* find-or-add counters of the current edit */
     uint64_t foa_calls, nodes_added, words_scanned;
+    /* or_edit_mt: one lock byte per bucket while edit tasks run on several
+       threads (NULL otherwise) */
+    uint8_t* locks;
 };
+
+/* Counters and poolTop are shared by the threads of or_edit_mt: relaxed
+   atomic adds (uncontended on one thread). */
+static void cnt_add(uint64_t* p, uint64_t v) { __atomic_fetch_add(p, v, __ATOMIC_RELAXED); }
 
 static uint64_t unique_sorted(uint32_t* v, uint64_t n);
 
 static void set_error(or_table* t, int e)
 {
-    if (!t->error)
-        t->error = e;
+    int none = 0;
+    __atomic_compare_exchange_n(&t->error, &none, e, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED);
 }
 
 or_table* or_table_create(const hd_config* cfg)
@@ -183,11 +190,13 @@ uint32_t or_read_word(const or_table* t, uint32_t vptr) { return *sys_ptr(t, vpt
 /* allocate_page (hash_table.h:794-809) */
 static void allocate_page(or_table* t, uint32_t page)
 {
-    if (t->pool_top >= t->cfg.pool_pages) {
+    const uint32_t p = __atomic_fetch_add(&t->pool_top, 1u, __ATOMIC_RELAXED);
+    if (p >= t->cfg.pool_pages) {
+        __atomic_fetch_sub(&t->pool_top, 1u, __ATOMIC_RELAXED);
         set_error(t, HD_ERR_POOL_FULL);
         return;
     }
-    t->page_table[page] = t->pool_top++;
+    t->page_table[page] = p;
 }
 
 /* find_leaf_node_in_bucket (hash_table.h:196-274), Bloom filter off */
@@ -201,12 +210,12 @@ static uint32_t find_leaf(or_table* t, uint32_t bucket_size, uint32_t bucket, ui
         for (uint32_t index = pindex; index < end; index += 2, p += 2) {
             uint64_t bits = (uint64_t)p[0] | ((uint64_t)p[1] << 32);
             if (bits == leaf) {
-                t->words_scanned += index + 2;
+                cnt_add(&t->words_scanned, index + 2);
                 return base + index;
             }
         }
     }
-    t->words_scanned += bucket_size;
+    cnt_add(&t->words_scanned, bucket_size);
     return NOT_FOUND;
 }
 
@@ -223,20 +232,20 @@ static uint32_t find_interior(or_table* t, uint32_t bucket_size, uint32_t level,
         const uint32_t* page = sys_ptr(t, base + pindex);
         uint32_t page_end = bucket_size < pindex + PAGE ? bucket_size : pindex + PAGE;
         if (pindex + n >= page_end) {
-            t->words_scanned += bucket_size;
+            cnt_add(&t->words_scanned, bucket_size);
             return NOT_FOUND;
         }
         page_end -= n;
         for (uint32_t index = pindex; index < page_end;) {
             const uint32_t* p = page + (index - pindex);
             if (memcmp(node, p, n * sizeof(uint32_t)) == 0) {
-                t->words_scanned += index + n;
+                cnt_add(&t->words_scanned, index + n);
                 return base + index;
             }
             index += total_size(*p);
         }
     }
-    t->words_scanned += bucket_size;
+    cnt_add(&t->words_scanned, bucket_size);
     return NOT_FOUND;
 }
 
@@ -261,8 +270,8 @@ static uint32_t add_leaf(or_table* t, uint64_t leaf, uint32_t hash)
     p[0] = (uint32_t)leaf;
     p[1] = (uint32_t)(leaf >> 32);
     *size_ptr = size + 2;
-    t->level_nodes[level]++;
-    t->nodes_added++;
+    cnt_add(&t->level_nodes[level], 1);
+    cnt_add(&t->nodes_added, 1);
     return ptr;
 }
 
@@ -298,8 +307,8 @@ static uint32_t add_interior(or_table* t, uint32_t level, uint32_t n, const uint
     for (uint32_t i = 0; i < n; i++)
         p[i] = node[i];
     *size_ptr = size + n;
-    t->level_nodes[level]++;
-    t->nodes_added++;
+    cnt_add(&t->level_nodes[level], 1);
+    cnt_add(&t->nodes_added, 1);
     return ptr;
 }
 
@@ -324,16 +333,31 @@ static void log_foa(uint32_t level, uint32_t n, const uint32_t* node, uint32_t r
 }
 
 /* find_or_add_leaf_node (hash_table.h:470-514), single writer */
+static void bucket_lock(or_table* t, uint64_t gb)
+{
+    if (t->locks)
+        while (__atomic_test_and_set(t->locks + gb, __ATOMIC_ACQUIRE))
+            ;
+}
+static void bucket_unlock(or_table* t, uint64_t gb)
+{
+    if (t->locks)
+        __atomic_clear(t->locks + gb, __ATOMIC_RELEASE);
+}
+
 uint32_t or_find_or_add_leaf(or_table* t, uint64_t leaf)
 {
     const uint32_t level = t->leaf_level;
     const uint32_t hash = or_hash_leaf(leaf);
     const uint32_t bucket = hash & (bucket_count(&t->cfg, level) - 1);
-    const uint32_t size = t->bucket_sizes[bucket_global(&t->cfg, level, bucket)];
-    t->foa_calls++;
+    const uint64_t gb = bucket_global(&t->cfg, level, bucket);
+    bucket_lock(t, gb);
+    const uint32_t size = t->bucket_sizes[gb];
+    cnt_add(&t->foa_calls, 1);
     uint32_t r = find_leaf(t, size, bucket, leaf);
     if (r == NOT_FOUND)
         r = add_leaf(t, leaf, hash);
+    bucket_unlock(t, gb);
     const uint32_t words[2] = {(uint32_t)leaf, (uint32_t)(leaf >> 32)};
     log_foa(level, 2, words, r);
     return r;
@@ -343,11 +367,14 @@ uint32_t or_find_or_add_interior(or_table* t, uint32_t level, uint32_t n, const 
 {
     const uint32_t hash = or_hash_interior(n, node);
     const uint32_t bucket = hash & (bucket_count(&t->cfg, level) - 1);
-    const uint32_t size = t->bucket_sizes[bucket_global(&t->cfg, level, bucket)];
-    t->foa_calls++;
+    const uint64_t gb = bucket_global(&t->cfg, level, bucket);
+    bucket_lock(t, gb);
+    const uint32_t size = t->bucket_sizes[gb];
+    cnt_add(&t->foa_calls, 1);
     uint32_t r = find_interior(t, size, level, bucket, n, node);
     if (r == NOT_FOUND)
         r = add_interior(t, level, n, node, hash);
+    bucket_unlock(t, gb);
     log_foa(level, n, node, r);
     return r;
 }
@@ -1400,13 +1427,23 @@ static uint64_t fp_node(const or_table* t, fp_map* maps, uint32_t level, uint32_
     return h;
 }
 
-void or_reachable_counts(const or_table* t, uint32_t root, uint64_t* out)
+/* Nodes reachable from root per level (out) and, when words is given, the
+   words they occupy (a leaf 2, an interior node total_size): what the
+   reference's GC re-appends per level besides the full node and the
+   padding at page ends (hash_dag.h:407-547). */
+void or_reachable_words(const or_table* t, uint32_t root, uint64_t* out, uint64_t* words)
 {
     uint32_t* cur = (uint32_t*)malloc(4);
     uint64_t n = 1;
     cur[0] = root;
     for (uint32_t level = 0; level <= t->leaf_level; level++) {
         out[level] = n;
+        if (words) {
+            uint64_t w = 0;
+            for (uint64_t i = 0; i < n; i++)
+                w += level == t->leaf_level ? 2 : total_size(*sys_ptr(t, cur[i]));
+            words[level] = w;
+        }
         if (level == t->leaf_level)
             break;
         uint64_t cap = 0;
@@ -1425,6 +1462,8 @@ void or_reachable_counts(const or_table* t, uint32_t root, uint64_t* out)
     }
     free(cur);
 }
+
+void or_reachable_counts(const or_table* t, uint32_t root, uint64_t* out) { or_reachable_words(t, root, out, NULL); }
 
 uint64_t or_occupancy_fingerprint(const or_table* t, uint32_t root)
 {
@@ -2604,6 +2643,168 @@ int or_edit(or_table* t, const hd_edit* e, hd_edit_stats* stats)
     } else {
         root = edit_top(&j, 0, t->root, path, 0, &cn);
     }
+    free(j.ed.state);
+    free(j.ed.colors);
+    if (!t->error)
+        t->root = root;
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->num_voxels = j.num_voxels;
+        stats->num_nodes = j.num_nodes;
+        stats->find_or_add_calls = t->foa_calls;
+        stats->nodes_added = t->nodes_added;
+        stats->words_scanned = t->words_scanned;
+    }
+    return t->error;
+}
+
+/* ---- threaded edits (hash_dag.h:255-405 with THREADED_EDITS) ------------
+ * The reference's edit_threads, multi-threaded: the first pass of
+ * edit_threaded queues one task per level-T subtree the tool touches, a
+ * pool of threads takes the tasks from an atomic counter (its NUM_THREADS
+ * lambda, hash_dag.h:306-331) and runs edit_leaf on each, the hash table
+ * shared under per-bucket locks (its ENABLE_THREAD_SAFE_HASHTABLE), and the
+ * second pass combines the results into the top levels on one thread.
+ * Which task appends first into a shared bucket depends on the threads, so
+ * the table's node order (not its voxels) can differ from or_edit's; the
+ * CPU timing baseline of the edit path uses it.  Geometry tools without
+ * colours only. */
+typedef struct {
+    uint32_t old, path[3], result;
+    uint64_t num_voxels, num_nodes;
+} edit_task;
+
+typedef struct {
+    edit_task* v;
+    uint64_t n, cap, cursor;
+} edit_tasks;
+
+static uint32_t edit_top_tasks(edit_job* j, uint32_t level, uint32_t index, const uint32_t path[3], edit_tasks* tl,
+                               int build)
+{
+    or_table* t = j->t;
+    const uint32_t D = t->cfg.depth, T = t->cfg.color_tree_levels;
+    if (build)
+        j->num_nodes += 2; /* both passes, as edit_top */
+    f3 mn, mx;
+    node_box(path, D - level, &mn, &mx);
+    if (!should_edit_impl(&j->ed, mn, mx))
+        return index;
+    uint32_t mask = 0;
+    const uint32_t* p = NULL;
+    if (index != INVALID) {
+        p = sys_ptr(t, index);
+        mask = p[0] & 0xffu;
+    }
+    uint32_t off = 1, kids[8];
+    int changed = 0;
+    for (uint32_t c = 0; c < 8; c++) {
+        uint32_t np[3];
+        descend(path, c, np);
+        const uint32_t old = (mask & (1u << c)) ? p[off++] : INVALID;
+        uint32_t nk = old;
+        if (level == T - 1) {
+            f3 cmn, cmx;
+            node_box(np, D - level - 1, &cmn, &cmx);
+            if (should_edit_impl(&j->ed, cmn, cmx)) {
+                if (!build) {
+                    if (tl->n == tl->cap) {
+                        tl->cap = tl->cap ? 2 * tl->cap : 64;
+                        tl->v = (edit_task*)realloc(tl->v, tl->cap * sizeof(edit_task));
+                    }
+                    edit_task* k = &tl->v[tl->n++];
+                    memset(k, 0, sizeof(*k));
+                    k->old = old;
+                    memcpy(k->path, np, sizeof(np));
+                } else {
+                    nk = tl->v[tl->cursor++].result;
+                }
+            }
+        } else {
+            nk = edit_top_tasks(j, level + 1, old, np, tl, build);
+        }
+        if (build && t->error)
+            return INVALID;
+        changed |= old != nk;
+        kids[c] = nk;
+    }
+    if (!build || !changed)
+        return index;
+    uint32_t node[9], n = 0;
+    node[n++] = 0;
+    for (uint32_t c = 0; c < 8; c++)
+        if (kids[c] != INVALID) {
+            node[n++] = kids[c];
+            node[0] |= 1u << c;
+        }
+    if ((node[0] & 0xffu) == 0)
+        return INVALID;
+    return or_find_or_add_interior(t, level, n, node);
+}
+
+typedef struct {
+    const edit_job* proto;
+    edit_tasks* tl;
+    uint64_t* counter;
+} edit_worker;
+
+static void* edit_worker_run(void* arg)
+{
+    edit_worker* w = (edit_worker*)arg;
+    const uint32_t T = w->proto->t->cfg.color_tree_levels;
+    for (;;) {
+        const uint64_t i = __atomic_fetch_add(w->counter, 1, __ATOMIC_RELAXED);
+        if (i >= w->tl->n)
+            return NULL;
+        edit_task* k = &w->tl->v[i];
+        edit_job j = *w->proto;
+        j.num_voxels = j.num_nodes = 0;
+        uint32_t cc;
+        k->result = edit_leaf(&j, T, k->old, k->path, &cc);
+        k->num_voxels = j.num_voxels;
+        k->num_nodes = j.num_nodes;
+    }
+}
+
+int or_edit_mt(or_table* t, const hd_edit* e, hd_edit_stats* stats, uint32_t threads)
+{
+    if (threads == 0)
+        threads = (uint32_t)sysconf(_SC_NPROCESSORS_ONLN);
+    if (threads <= 1 || e->tool > HD_TOOL_BOX_ADD || t->cfg.color_tree_levels == 0)
+        return or_edit(t, e, stats);
+    edit_job j;
+    memset(&j, 0, sizeof(j));
+    j.t = t;
+    j.ed = make_editor(e);
+    t->foa_calls = t->nodes_added = t->words_scanned = 0;
+    if (make_buffers(&j.ed, t, NULL))
+        return HD_ERR_INVALID;
+    const uint32_t path[3] = {0, 0, 0};
+    edit_tasks tl = {0};
+    edit_top_tasks(&j, 0, t->root, path, &tl, 0); /* first pass: the tasks */
+    t->locks = (uint8_t*)calloc(t->n_buckets, 1);
+    uint64_t counter = 0;
+    edit_worker w = {&j, &tl, &counter};
+    pthread_t* th = (pthread_t*)malloc(threads * sizeof(pthread_t));
+    uint32_t started = 0;
+    for (; started < threads; started++)
+        if (pthread_create(&th[started], NULL, edit_worker_run, &w))
+            break;
+    if (started == 0)
+        edit_worker_run(&w);
+    for (uint32_t i = 0; i < started; i++)
+        pthread_join(th[i], NULL);
+    free(th);
+    free(t->locks);
+    t->locks = NULL;
+    for (uint64_t i = 0; i < tl.n; i++) {
+        j.num_voxels += tl.v[i].num_voxels;
+        j.num_nodes += tl.v[i].num_nodes;
+    }
+    uint32_t root = t->root;
+    if (!t->error)
+        root = edit_top_tasks(&j, 0, t->root, path, &tl, 1); /* second pass */
+    free(tl.v);
     free(j.ed.state);
     free(j.ed.colors);
     if (!t->error)

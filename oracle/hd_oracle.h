@@ -78,6 +78,7 @@ int or_get_value(const or_table* t, uint32_t x, uint32_t y, uint32_t z);
 uint64_t or_occupancy_fingerprint(const or_table* t, uint32_t root);
 /* Distinct node addresses reachable from root, per level. */
 void or_reachable_counts(const or_table* t, uint32_t root, uint64_t* out);
+void or_reachable_words(const or_table* t, uint32_t root, uint64_t* out, uint64_t* words);
 
 /* ---- traversal (tracer.cu) -------------------------------------------- */
 void or_trace_primary(const or_table* t, const hd_camera* cam, uint32_t width, uint32_t height,
@@ -93,6 +94,9 @@ void or_trace_frame_mt(const or_table* t, const hd_camera* cam, uint32_t width, 
 
 /* ---- edits (hash_dag_edits.h) and GC (hash_dag.h:407-547) ------------- */
 int or_edit(or_table* t, const hd_edit* edit, hd_edit_stats* stats);
+/* edit_threads with THREADED_EDITS: level-T tasks on `threads` threads (0:
+   every core); same voxels as or_edit, node order may differ */
+int or_edit_mt(or_table* t, const hd_edit* edit, hd_edit_stats* stats, uint32_t threads);
 int or_gc(or_table* t, uint32_t* extra_roots, uint32_t n_extra);
 /* ---- colours (variable_weight_size_colors.h, hash_dag_colors.h) ------- */
 typedef struct or_colors or_colors;

@@ -121,7 +121,10 @@ def lib():
                                         np.ctypeslib.ndpointer(np.float32, flags="C"), f32, pu32, pu8, u32,
                                         u32, u32]
         L.or_reachable_counts.argtypes = [P, u32, np.ctypeslib.ndpointer(np.uint64, flags="C")]
+        L.or_reachable_words.argtypes = [P, u32, np.ctypeslib.ndpointer(np.uint64, flags="C"),
+                                         np.ctypeslib.ndpointer(np.uint64, flags="C")]
         L.or_edit.argtypes = [P, C.POINTER(HdEdit), C.POINTER(HdEditStats)]
+        L.or_edit_mt.argtypes = [P, C.POINTER(HdEdit), C.POINTER(HdEditStats), u32]
         L.or_gc.argtypes = [P, P, u32]
         L.or_set_foa_log.argtypes = [C.c_char_p]
         L.or_colors_create.restype = P
@@ -281,6 +284,12 @@ class Table:
         lib().or_reachable_counts(self.h, self.root if root is None else root, out)
         return out[:self.cfg.depth - 1]
 
+    def reachable_words(self, root=None):
+        """Words of the nodes reachable from root, per level."""
+        out, words = np.zeros(20, np.uint64), np.zeros(20, np.uint64)
+        lib().or_reachable_words(self.h, self.root if root is None else root, out, words)
+        return words[:self.cfg.depth - 1]
+
     def trace_primary(self, cam, w, h, fp_mode=0, rows=None):
         paths = np.zeros(w * h * 4, np.uint32)
         r0, r1 = (0, h) if rows is None else rows
@@ -303,10 +312,15 @@ class Table:
                                 bias, paths, mask, threads, r0, r1)
         return paths.reshape(h, w, 4), mask.reshape(h, w)
 
-    def edit(self, tool, center, radius):
+    def edit(self, tool, center, radius, threads=1):
+        """One edit; threads > 1 (0: every core) runs the level-T tasks on
+        that many threads (same voxels, node order may differ)."""
         e = make_edit(tool, center, radius)
         s = HdEditStats()
-        r = lib().or_edit(self.h, C.byref(e), C.byref(s))
+        if threads == 1:
+            r = lib().or_edit(self.h, C.byref(e), C.byref(s))
+        else:
+            r = lib().or_edit_mt(self.h, C.byref(e), C.byref(s), threads)
         if r:
             raise RuntimeError(f"edit failed {r}")
         return s

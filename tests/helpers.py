@@ -39,8 +39,8 @@ def used_words(table, depth, top_bits=10):
     vpage = (bases[bucket_of_page] + page_in_bucket * PAGE) // PAGE
     used = np.minimum(PAGE, bs[bucket_of_page] - page_in_bucket * PAGE)
     phys = np.asarray(table["page_table"], np.int64)[vpage]
-    pool = np.asarray(table["pool"], np.uint32)
-    pages = pool[(phys[:, None] * PAGE + np.arange(PAGE)[None, :])]
+    pool = np.asarray(table["pool"], np.uint32).reshape(-1, PAGE)
+    pages = pool[phys]  # one row per used page (no per-word index array)
     keep = np.arange(PAGE)[None, :] < used[:, None]
     return pages[keep]
 

@@ -29,7 +29,7 @@ def test_library_exports_every_declared_symbol():
 def test_abi_version_and_default_config():
     build.build()
     L = _capi.lib()
-    assert L.hd_abi_version() == 7
+    assert L.hd_abi_version() == 8
     cfg = _capi.Config()
     L.hd_default_config(15, C.byref(cfg))
     assert (cfg.depth, cfg.color_tree_levels, cfg.top_levels) == (15, 10, 9)

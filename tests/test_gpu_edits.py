@@ -50,6 +50,30 @@ def test_edits_match_reference_fixture(gpu, name):
     assert ot.fingerprint() == g["fingerprint"]
     st = d.level_stats()
     assert [int(v) for v in st.nodes[:depth - 1]] == [r + 1 for r in g["reachable"]]
+    # Post-GC words per level = the full node + the reachable nodes' words +
+    # padding at page ends.  The first two are the same on both sides; the
+    # padding depends on the re-append order (the reference's hash-set
+    # iteration order, here increasing old address), so it is reported
+    # beside the reference's and bounded: a node never straddles a page, so
+    # at most 8 words (the largest node, 9 words, less one) go unused at the
+    # end of each page.  The order also decides each node's new address, so
+    # its parent (whose words hold that address) hashes into another bucket:
+    # the buckets' sizes, and with them the pages the rebuild maps (pool_top),
+    # differ by a few per cent of the pages the GC maps.
+    live = [int(v) for v in ot.reachable_words()]
+    full = [9] * (depth - 2) + [2]
+    ours = [int(v) for v in st.words[:depth - 1]]
+    pad_ref = [w - l - f for w, l, f in zip(g["level_words"], live, full)]
+    pad_ours = [w - l - f for w, l, f in zip(ours, live, full)]
+    sizes = np.asarray(d.export_table()["bucket_sizes"], np.int64)
+    print(f"\n{name} post-GC padding words per level: reference {pad_ref}, ours {pad_ours}; "
+          f"pool_top reference {g['pool_top']}, ours {st.pages_used + 1}")
+    for level in range(depth - 1):
+        pages = int(np.ceil(g["level_words"][level] / 512)) + int((sizes > 0).sum())
+        assert 0 <= pad_ref[level] <= 8 * pages and 0 <= pad_ours[level] <= 8 * pages, level
+    assert [int(v) for v in st.words[:depth - 1]] == g["level_words"]
+    gc_pages = g["pool_top"] - fx["edits"][-1]["pool_top"]
+    assert abs(st.pages_used + 1 - g["pool_top"]) <= max(8, gc_pages // 20)
     d.free()
 
 

@@ -12,6 +12,7 @@ import pytest
 
 import hashdag_gb300 as hd
 from hashdag_gb300 import _capi, workloads
+from oracle import pyoracle as po
 from tests.helpers import table_digest
 
 pytestmark = pytest.mark.gpu
@@ -53,28 +54,41 @@ def test_release_gc_keeps_buckets_and_frees_pages(gpu):
     b.free()
 
 
-def test_release_gc_lets_a_small_pool_take_an_edit_stream(gpu):
-    depth = 10
-    edits = workloads.mixed_edits(depth, 64, (16.0, 160.0), seed=23)
-    # the stream without a GC: pages each edit claims, pages at the end
+def _stream(depth, n):
+    """n edits of a seeded stream, and the pages in use after each of them
+    without a GC (the scene's first)."""
+    edits = workloads.mixed_edits(depth, n, (16.0, 96.0), seed=23)
     ref = _edited([], depth)
-    scene_pages = ref.level_stats().pages_used
-    step = []
+    pages = [ref.level_stats().pages_used]
     for e in edits:
-        before = ref.level_stats().pages_used
         ref.edit_threads(hd.editor_from_tuple(e))
-        step.append(ref.level_stats().pages_used - before)
-    total = ref.level_stats().pages_used
-    live = hd.HashDAG(depth)
-    live.import_table(ref.export_table())
-    live.remove_stale_nodes(release_pages=True)
-    live_pages = live.level_stats().pages_used
-    live.free()
-    # free pages to keep: an edit's worth twice over, and room for the GC's
-    # rebuild (its order pads pages differently from the edits')
-    need = 2 * max(step) + total // 16 + 64
-    pool = live_pages + 1 + 2 * need
-    assert pool - 1 < total, "the stream must not fit the pool without page reuse"
+        pages.append(ref.level_stats().pages_used)
+    return edits, pages, ref
+
+
+def test_release_gc_lets_a_small_pool_take_an_edit_stream(gpu):
+    """A pool too small for an edit stream without page reuse takes the whole
+    stream when every edit that finds it full is retried after a releasing
+    GC.  The GC's rebuild re-hashes the interior levels (children
+    remapped), so a bucket can need a page it never had: a page reserve
+    (hd_set_page_reserve) keeps room for it once edits have filled the
+    pool."""
+    depth, reserve = 10, 64
+    n = 64
+    while True:  # enough edits that the stream's garbage dwarfs one edit
+        edits, pages, ref = _stream(depth, n)
+        live = hd.HashDAG(depth)
+        live.import_table(ref.export_table())
+        live.remove_stale_nodes(release_pages=True)
+        live_pages = live.level_stats().pages_used
+        live.free()
+        step = max(b - a for a, b in zip(pages, pages[1:]))
+        pool = live_pages + 1 + reserve + 4 * step
+        if pool - 1 < pages[-1] - 4 * step or n >= 512:
+            break
+        ref.free()
+        n *= 2
+    assert pool - 1 < pages[-1], "the stream must not fit the pool without page reuse"
     # without page reuse the pool runs out partway through the stream
     plain = hd.HashDAG(config=hd.default_config(depth, pool_pages=pool))
     plain.generate_scene(workloads.SEED_SCENE)
@@ -87,19 +101,33 @@ def test_release_gc_lets_a_small_pool_take_an_edit_stream(gpu):
             refused += 1
     assert refused > 0
     plain.free()
-    # with a releasing GC whenever fewer than `need` pages are free, every
-    # edit lands and the scene equals the unconstrained one
+    # edits stop at the reserve; a releasing GC then frees the garbage and
+    # the edit lands on the retry
     d = hd.HashDAG(config=hd.default_config(depth, pool_pages=pool))
     d.generate_scene(workloads.SEED_SCENE)
+    d.set_page_reserve(reserve)
     gcs = 0
     for e in edits:
-        if pool - 1 - d.level_stats().pages_used < need:
+        try:
+            d.edit_threads(hd.editor_from_tuple(e))
+        except hd.HashDagError as err:
+            assert err.status == _capi.HD_ERR_POOL_FULL and "reserve" in str(err), str(err)
+            assert d.level_stats().pages_used + 1 <= pool - reserve
             d.remove_stale_nodes(release_pages=True)
             gcs += 1
-        d.edit_threads(hd.editor_from_tuple(e))
-    assert gcs > 0 and scene_pages < pool
+            d.edit_threads(hd.editor_from_tuple(e))
+    assert gcs > 0
     q = np.random.default_rng(7).integers(0, 1 << depth, (40000, 3)).astype(np.uint32)
     assert np.array_equal(d.get_values(q), ref.get_values(q))
+    # the same voxels everywhere (the GCs moved nodes, so addresses differ,
+    # and with them which equal nodes the scans' visibility rule duplicates)
+    fp = []
+    for x in (d, ref):
+        t = x.export_table()
+        ot = po.Table(po.default_config(depth, pool_pages=int(t["pool"].size // 512) + 8))
+        ot.import_(t)
+        fp.append(ot.fingerprint())
+    assert fp[0] == fp[1]
     d.free()
     ref.free()
 

@@ -142,9 +142,12 @@ def test_batched_mix_equals_alone(gpu):
 
 
 def test_pool_gated_admission_with_page_release(gpu):
-    """A pool too small for the trace without page reuse: edits are refused
-    once it fills; with the page-releasing GC the loop collects and takes
-    every edit."""
+    """A pool too small for the trace without page reuse: without GCs the
+    loop refuses edits once the pool is full; with the page-releasing GC
+    (below 5 % free pages, and on a full pool before a retry) it takes every
+    edit and ends on the same voxels.  The undo history is kept to 8 frames:
+    the GC keeps every state the history can return to, so a longer history
+    than the pool's slack would keep the garbage alive."""
     depth = 10
     trace = [x for x in _geometry_requests(depth, 120, 4000.0, seed=9, r_range=(16.0, 96.0)) if x[0] == "edit"]
     probe = hd.HashDAG(depth)
@@ -156,14 +159,22 @@ def test_pool_gated_admission_with_page_release(gpu):
     probe.free()
     pool = live + 1 + (total - live) // 3
     outcomes = {}
-    for release in (False, True):
+    for gc_free, release in ((0.0, False), (0.05, True)):
         d = hd.HashDAG(config=hd.default_config(depth, pool_pages=pool))
         d.generate_scene(1)
-        res, st = d.serve(_requests(trace), continuous=True, realtime=False, gc_free_fraction=0.25,
+        d.set_undo_capacity(8)
+        res, st = d.serve(_requests(trace), continuous=True, realtime=False, gc_free_fraction=gc_free,
                           release_pages=release, batch_edits=False)
-        outcomes[release] = (st.refused, st.gcs, d.firstNodeIndex)
+        outcomes[release] = (st.refused, st.gcs)
         if release:
             assert [r.num_voxels for r in res] == [r.num_voxels for r in res0]
+            q = np.random.default_rng(3).integers(0, 1 << depth, (40000, 3)).astype(np.uint32)
+            probe = hd.HashDAG(depth)
+            probe.generate_scene(1)
+            for e in trace:
+                probe.edit_threads(hd.editor_from_tuple(e[2][:3]))
+            assert np.array_equal(d.get_values(q), probe.get_values(q))
+            probe.free()
         d.free()
     assert outcomes[False][0] > 0          # the pool ran out without page reuse
     assert outcomes[True][0] == 0 and outcomes[True][1] > 0
