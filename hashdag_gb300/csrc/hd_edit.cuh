@@ -511,19 +511,27 @@ HD_D void stage_page(const uint32_t* src, uint32_t used, uint32_t* page, uint32_
 // last node when it holds q (compared by no scan until something follows).
 template <int PW>
 HD_D uint32_t scan_bucket(const Table& t, uint32_t vbase, uint32_t S, const uint32_t* q, uint32_t n, bool leaf,
-                          uint32_t bloom, uint32_t* page, uint32_t* last_match, unsigned long long& scanned)
+                          uint32_t bloom, uint32_t pt_lane, uint32_t* page, uint32_t* last_match,
+                          unsigned long long& scanned)
 {
     const uint32_t lane = threadIdx.x & 31;
     uint32_t found = kNotFound;
     *last_match = kNotFound;
+    // the filters of the bucket's first 32 pages at once, a lane per page
+    // (pt_lane: the physical page behind the bucket's page `lane`, read
+    // once per bucket run)
+    const uint32_t npages = (S + kPage - 1) / kPage;
+    const uint32_t may = __ballot_sync(0xffffffffu, lane < npages && bloom_may_phys(t, pt_lane, bloom));
     for (uint32_t pindex = 0; pindex < S && found == kNotFound; pindex += kPage) {
         const uint32_t page_end = S < pindex + kPage ? S : pindex + kPage;
         if (!leaf && pindex + n >= page_end)
             break; // "return 0xFFFFFFFF" of the reference scan
-        if (!bloom_may(t, vbase + pindex, bloom))
+        const uint32_t pi = pindex / kPage;
+        if (pi < 32 ? !((may >> pi) & 1u) : !bloom_may(t, vbase + pindex, bloom))
             continue; // the page cannot hold q
         const uint32_t used = page_end - pindex;
-        stage_page<PW>(t.sys_cg(vbase + pindex), used, page, lane);
+        const uint32_t phys = __shfl_sync(0xffffffffu, pt_lane, pi & 31);
+        stage_page<PW>(pi < 32 ? t.pool + (uint64_t(phys) << kPageShift) : t.sys_cg(vbase + pindex), used, page, lane);
         __syncwarp();
         if (leaf) {
             for (uint32_t w0 = 0; w0 < used && found == kNotFound; w0 += 64) {
@@ -561,13 +569,16 @@ HD_D uint32_t scan_bucket(const Table& t, uint32_t vbase, uint32_t S, const uint
         scanned += found == kNotFound ? used : (found - pindex + n);
         __syncwarp();
     }
+    const uint32_t tail_pi = (S - n) / kPage;
     if (!leaf && found == kNotFound && S >= n && ((S - n) & ~(kPage - 1)) == ((S - 1) & ~(kPage - 1)) &&
-        bloom_may(t, vbase + ((S - n) & ~(kPage - 1)), bloom)) {
+        (tail_pi < 32 ? ((may >> tail_pi) & 1u) != 0 : bloom_may(t, vbase + ((S - n) & ~(kPage - 1)), bloom))) {
         // the bucket's last node ends at S; it holds q iff it starts at S - n
         // (nodes never straddle a page, so S - n lies in the tail's page)
         const uint32_t p = S - n;
         const uint32_t pindex = p & ~(kPage - 1);
-        stage_page<PW>(t.sys_cg(vbase + pindex), S - pindex, page, lane); // S - pindex <= kPage
+        const uint32_t phys = __shfl_sync(0xffffffffu, pt_lane, tail_pi & 31);
+        stage_page<PW>(tail_pi < 32 ? t.pool + (uint64_t(phys) << kPageShift) : t.sys_cg(vbase + pindex), S - pindex,
+                       page, lane); // S - pindex <= kPage
         __syncwarp();
         uint32_t ok = 0;
         if (lane == 0) {
@@ -603,14 +614,39 @@ HD_D bool foa_segment(const Table& t, uint32_t level, const Level& lv, const uin
     const uint32_t gb = t.g.bucket_global(level, bucket);
     const uint32_t vbase = t.g.make_ptr(level, bucket, 0);
     uint32_t S = __ldcg(t.bucket_sizes + gb);
+    // the bucket's page-table entries, lane p holding page p's (the warp owns
+    // the bucket for the run: only its own appends map pages here)
+    const uint32_t vpage0 = vbase >> kPageShift, cap_pages = t.g.capacity(level) >> kPageShift;
+    uint32_t pt_lane = lane < cap_pages ? __ldcg(t.page_table + vpage0 + lane) : 0u;
     uint32_t used_entries = 0, next_slot = 0;
     bool failed = false;
     uint32_t j = j0;
+    // the run's entry indices 32 at a time (lane k: entry of position vb + k)
+    // and the next candidate's words loaded while the current one resolves
+    uint32_t vb = j0, vreg = j0 + lane < j1 ? vals[j0 + lane] : 0u;
+    const uint32_t c0 = __shfl_sync(0xffffffffu, vreg, 0); // every lane: a full-warp shuffle
+    uint32_t qj = j0, qw = lane < 9 ? lv.cand[9 * uint64_t(c0) + lane] : 0u;
     while (j < j1 && !failed) {
-        const uint32_t ci = vals[j];
+        if (j - vb >= 32) {
+            vb = j;
+            vreg = j + lane < j1 ? vals[j + lane] : 0u;
+        }
+        const uint32_t ci = __shfl_sync(0xffffffffu, vreg, j - vb);
+        if (qj != j && lane < 9)
+            qw = lv.cand[9 * uint64_t(ci) + lane];
         if (lane < 9)
-            q[lane] = lv.cand[9 * uint64_t(ci) + lane];
+            q[lane] = qw;
         __syncwarp();
+        // prefetch candidate j + 1 (its entry index is in vreg unless it
+        // starts the next group of 32)
+        qj = j + 1;
+        if (qj < j1 && qj - vb < 32) {
+            const uint32_t cn = __shfl_sync(0xffffffffu, vreg, qj - vb);
+            if (lane < 9)
+                qw = lv.cand[9 * uint64_t(cn) + lane];
+        } else {
+            qj = kNotFound;
+        }
         const uint32_t n = leaf ? 2 : total_size(q[0]);
         // cache lookup: lane e checks entry e
         bool hit = lane < used_entries && cache.n[lane] == n;
@@ -624,7 +660,7 @@ HD_D bool foa_segment(const Table& t, uint32_t level, const Level& lv, const uin
             e = __ffs(hb) - 1;
         } else {
             uint32_t last_match;
-            const uint32_t f = scan_bucket<PW>(t, vbase, S, q, n, leaf, bloom, page, &last_match, scanned);
+            const uint32_t f = scan_bucket<PW>(t, vbase, S, q, n, leaf, bloom, pt_lane, page, &last_match, scanned);
             e = next_slot;
             next_slot = (next_slot + 1) % kCache;
             used_entries = used_entries < kCache ? used_entries + 1 : kCache;
@@ -642,23 +678,34 @@ HD_D bool foa_segment(const Table& t, uint32_t level, const Level& lv, const uin
         }
         // the first visible copy, else append (lane 0)
         uint32_t result = kNotFound, appended = 0, ok = 1;
+        const uint32_t S_scan = S;
+        // where an append would go, on every lane (S and n are the warp's),
+        // and the physical page there when it is already mapped: the pages
+        // below the size are, so an append that stays in the size's last
+        // page reads no page-table entry
+        uint32_t a_size = S;
+        const uint32_t a_pos = append_position(a_size, n, leaf);
+        const bool a_mapped = S > 0 && a_size <= ((S + kPage - 1) & ~(kPage - 1));
+        const uint32_t a_phys = __shfl_sync(0xffffffffu, pt_lane, (a_pos >> kPageShift) & 31);
         if (lane == 0) {
             for (uint32_t k = 0; k < cache.npos[e] && result == kNotFound; k++)
                 if (visible(cache.pos[e][k], n, S, leaf))
                     result = cache.pos[e][k];
             if (result == kNotFound) {
-                uint32_t size = S;
-                const uint32_t pos = append_position(size, n, leaf);
+                uint32_t size = a_size;
+                const uint32_t pos = a_pos;
                 if (size > t.g.capacity(level)) {
                     set_error(t.error, kErrBucketFull, level, bucket, size);
                     ok = 0;
-                } else if (!map_pages(t, level, bucket, pos, size)) {
+                } else if (!a_mapped && !map_pages(t, level, bucket, pos, size)) {
                     ok = 0;
                 } else {
-                    uint32_t* dst = t.sys_rw(vbase + pos);
+                    const uint32_t phys =
+                        a_mapped && (pos >> kPageShift) < 32 ? a_phys : __ldcg(t.page_table + vpage0 + (pos >> kPageShift));
+                    uint32_t* dst = t.pool + (uint64_t(phys) << kPageShift) + (pos & (kPage - 1));
                     for (uint32_t k = 0; k < n; k++)
                         __stcg(dst + k, q[k]);
-                    bloom_add(t, vbase + pos, bloom);
+                    bloom_add_phys(t, phys, bloom);
                     result = pos;
                     S = size;
                     appended = 1;
@@ -675,7 +722,11 @@ HD_D bool foa_segment(const Table& t, uint32_t level, const Level& lv, const uin
         ok = __shfl_sync(0xffffffffu, ok, 0);
         result = __shfl_sync(0xffffffffu, result, 0);
         appended = __shfl_sync(0xffffffffu, appended, 0);
+        const uint32_t S_before = __shfl_sync(0xffffffffu, S_scan, 0);
         S = __shfl_sync(0xffffffffu, S, 0);
+        // an append that reached a new page mapped it: refresh that lane
+        if (appended && lane < cap_pages && lane * kPage < S && lane * kPage + kPage > S_before)
+            pt_lane = __ldcg(t.page_table + vpage0 + lane);
         foa++;
         added += appended;
         if (!ok) {

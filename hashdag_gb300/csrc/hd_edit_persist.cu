@@ -305,6 +305,34 @@ HD_D uint32_t small_sort(const Table& t, uint32_t L, uint32_t n, uint32_t* keys,
                          unsigned long long* s64, uint32_t* sm32)
 {
     const uint32_t empty = t.g.buckets(L);
+    if (n <= 32) {
+        // one warp, in registers: a bitonic network over the lanes on the
+        // (bucket, entry) pairs (entries are distinct: the order is total)
+        if (threadIdx.x < 32) {
+            const uint32_t lane = threadIdx.x;
+            unsigned long long x = lane < n ? (uint64_t(keys[lane]) << 32) | vals[lane] : ~0ull;
+            for (uint32_t k = 2; k <= 32; k <<= 1)
+                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                    const unsigned long long y = __shfl_xor_sync(0xffffffffu, x, j);
+                    const bool up = (lane & k) == 0, low = (lane & j) == 0;
+                    x = (low == up) ? (x < y ? x : y) : (x < y ? y : x);
+                }
+            const uint32_t key = uint32_t(x >> 32);
+            const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+            if (lane < n) {
+                keys[lane] = key;
+                vals[lane] = uint32_t(x);
+            }
+            const uint32_t runs = __popc(__ballot_sync(0xffffffffu, lane < n && key < empty && (lane == 0 || prev != key)));
+            __threadfence();
+            if (lane == 0)
+                sm32[0] = runs;
+        }
+        __syncthreads();
+        const uint32_t runs = sm32[0];
+        __syncthreads();
+        return runs;
+    }
     uint32_t n2 = 1;
     while (n2 < n)
         n2 <<= 1;

@@ -87,6 +87,28 @@ HD_D void bloom_add(const Table& t, uint32_t v, uint32_t bits)
         atomicOr(f + (b >> 5), 1u << (b & 31));
     }
 }
+// Adds a node written into physical page p to the page's filter
+HD_D void bloom_add_phys(const Table& t, uint32_t p, uint32_t bits)
+{
+    uint32_t* f = t.bloom + uint64_t(p) * kBloomWords;
+#pragma unroll
+    for (uint32_t i = 0; i < kBloomHashes; i++) {
+        const uint32_t b = bloom_pos(bits, i);
+        atomicOr(f + (b >> 5), 1u << (b & 31));
+    }
+}
+// False when physical page p's filter rules the node out
+HD_D bool bloom_may_phys(const Table& t, uint32_t p, uint32_t bits)
+{
+    const uint32_t* f = t.bloom + uint64_t(p) * kBloomWords;
+    bool may = true;
+#pragma unroll
+    for (uint32_t i = 0; i < kBloomHashes; i++) {
+        const uint32_t b = bloom_pos(bits, i);
+        may &= ((__ldcg(f + (b >> 5)) >> (b & 31)) & 1u) != 0;
+    }
+    return may;
+}
 // False when the page behind virtual word v cannot hold the node
 HD_D bool bloom_may(const Table& t, uint32_t v, uint32_t bits)
 {
