@@ -28,9 +28,11 @@ collective on the data path).
 "edits" (the same JSON line): the batched-edit workload on the 2^15 scene,
 --edits edits (default 256; 50% sphere carve, 30% sphere fill, 20% box fill,
 radius log-uniform in [4, 512]) applied plainly (hd_edit_apply per edit) and
-batched (hd_edit_batch, autotuned): edited voxels/s, find-or-add/s, p50/p99
-per-edit device latency of both forms, and the oracle's single-thread CPU
-editor on a bounded sample of the same edits.
+batched (hd_edit_batch: one persistent launch or a graph per edit,
+autotuned): edited voxels/s, find-or-add/s, p50/p99
+per-edit device latency of both batch modes, and the oracle's CPU editor
+(the reference's threaded edit_threads on every host core, and one thread)
+on bounded samples of the same edits.
 "colors": the 2^15 shell scene with colours, 512 paints, 32 copies of 256^3
 regions, one GC.  "tools_files": noise spheres and flood fills, the colour
 view of a frame, snapshot and BasicDAG file round trips, a replay.
@@ -196,6 +198,16 @@ def traffic_from_profiles(workload, kernel, views):
             d = json.load(f)
         per_view = d[workload]["per_view"][kernel]
         return per_view * views
+    except (OSError, ValueError, KeyError, TypeError):
+        return None
+
+
+def sectors_from_profiles(workload):
+    """L2 sectors per ray and L2 hit rates of the committed ncu captures for
+    this workload (profiles/traffic.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)[workload]["l2_sectors_per_ray"]
     except (OSError, ValueError, KeyError, TypeError):
         return None
 
@@ -386,27 +398,27 @@ def edit_bench(args, dist):
 def edit_cpu_baseline(args, tuples):
     """The oracle's C restatement of the reference editor on the same scene
     and edits: the reference's threaded edit_threads (level-T tasks on every
-    host core, per-bucket locks) on the first edits for half the time
-    budget, then the single-threaded editor on the edits after them for the
-    other half."""
+    host core, per-bucket locks) on the first half of the edits (at most half
+    the time budget), then the single-threaded editor on the edits after
+    them for the other half of the budget."""
     d, _ = load_scene(args.depth, args.pool_pages)
     ot = oracle_from(d, args.depth, spare_pages=1 << 18)
     d.free()
     cores = os.cpu_count() or 1
 
-    def sample(first, threads, budget):
+    def sample(first, last, threads, budget):
         t0 = time.perf_counter()
         vox = foa = 0
         k = first
-        while k < len(tuples) and time.perf_counter() - t0 < budget:
+        while k < last and time.perf_counter() - t0 < budget:
             s = ot.edit(*tuples[k], threads=threads)
             vox += s.num_voxels
             foa += s.find_or_add_calls
             k += 1
         return k, vox, foa, time.perf_counter() - t0
 
-    k1, vox, foa, dt = sample(0, cores, args.edit_cpu_seconds / 2)
-    k2, vox1, foa1, dt1 = sample(k1, 1, args.edit_cpu_seconds / 2)
+    k1, vox, foa, dt = sample(0, (len(tuples) + 1) // 2, cores, args.edit_cpu_seconds / 2)
+    k2, vox1, foa1, dt1 = sample(k1, len(tuples), 1, args.edit_cpu_seconds / 2)
     return {"voxels_per_s": vox / dt, "find_or_add_per_s": foa / dt, "edits_per_s": k1 / dt, "cores": cores,
             "kind": "port",
             "sample": f"edits 0-{k1 - 1} of {len(tuples)}, oracle C editor with the reference's threaded "
@@ -889,6 +901,7 @@ def run_gpu(args, dist):
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": dom_bytes, "traffic": traffic_from_profiles(workload, dominant, V),
+                "l2_sectors_per_ray": sectors_from_profiles(workload),
                 "primary_ms_per_launch": ms_p / K, "shadow_ms_per_launch": ms_s / K,
                 "primary_bytes_per_launch": prim_bytes / K, "shadow_bytes_per_launch": shad_bytes / K}
     cpu = None

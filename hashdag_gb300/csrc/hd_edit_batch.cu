@@ -298,8 +298,10 @@ __global__ void __launch_bounds__(kSortBlock)
     }
 }
 
-// Find-or-add over the sorted keys: warps take chunks of 32 sorted positions
-// and resolve every bucket run that starts in their chunk.
+// Find-or-add over the sorted keys: the sorted positions are split into one
+// chunk per warp (ceil(n / warps) positions, at least one), and each warp
+// resolves every bucket run that starts in its chunk, so that short runs
+// spread over all the warps.
 template <int PW, uint32_t WARPS>
 __global__ void __launch_bounds__(32 * WARPS)
     k_b_find_or_add(Table t, const BatchState* bs, uint32_t level, Level lv, const uint32_t* __restrict__ keys,
@@ -314,11 +316,16 @@ __global__ void __launch_bounds__(32 * WARPS)
     const uint32_t n = bs->count[level];
     const uint32_t empty = t.g.buckets(level);
     unsigned long long foa = 0, added = 0, scanned = 0;
-    for (uint32_t c0 = (blockIdx.x * WARPS + warp) * 32; c0 < n; c0 += gridDim.x * WARPS * 32) {
+    const uint32_t nw = gridDim.x * WARPS, gw = blockIdx.x * WARPS + warp;
+    const uint32_t chunk = n > nw ? (n + nw - 1) / nw : 1u;
+    const uint64_t cbeg64 = uint64_t(gw) * chunk;
+    const uint32_t cbeg = cbeg64 < n ? uint32_t(cbeg64) : n, cend = n - cbeg < chunk ? n : cbeg + chunk;
+    for (uint32_t c0 = cbeg; c0 < cend; c0 += 32) {
         const uint32_t j = c0 + lane;
-        const uint32_t key = j < n ? keys[j] : empty;
-        const uint32_t prev = (j > 0 && j < n) ? keys[j - 1] : kNoBucket;
-        uint32_t starts = __ballot_sync(0xffffffffu, j < n && key < empty && key != prev);
+        const bool in = j < cend;
+        const uint32_t key = in ? keys[j] : empty;
+        const uint32_t prev = (in && j > 0) ? keys[j - 1] : kNoBucket;
+        uint32_t starts = __ballot_sync(0xffffffffu, in && key < empty && key != prev);
         while (starts) {
             const uint32_t s = __ffs(starts) - 1;
             starts &= starts - 1;

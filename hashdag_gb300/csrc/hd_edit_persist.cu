@@ -159,9 +159,14 @@ HD_D uint32_t chunk_len(uint32_t n, uint32_t parts, uint32_t align)
     return (per + align - 1) / align * align;
 }
 
+// Grid phases split a level into one chunk per CTA, a multiple of the warp
+// width long (so that a warp's 32 consecutive slots fall in at most two
+// chunks): every CTA gets work once a level holds 32 entries per CTA.
+constexpr uint32_t kChunkAlign = 32;
+
 // Chunk of level entries a descend flag is counted in (the grid's top-down
 // chunking of that level).
-HD_D uint32_t td_chunk(uint32_t i, uint32_t n, uint32_t G) { return i / chunk_len(n, G, kPT); }
+HD_D uint32_t td_chunk(uint32_t i, uint32_t n, uint32_t G) { return i / chunk_len(n, G, kChunkAlign); }
 
 // Block-wide exclusive scan (kPT threads) of v; *total = the block's sum.
 HD_D uint32_t cta_scan(uint32_t v, uint32_t* total, uint32_t* sm32)
@@ -223,7 +228,7 @@ HD_D void td_range(const Table& t, const Editor& ed, const Level* lvs, uint32_t 
                 ch = td_chunk(at, n_next, G);
             }
             // the warp's children are 32 consecutive slots (at = 8 run + k),
-            // so they fall in at most two chunks (chunks hold >= kPT slots):
+            // so they fall in at most two chunks (chunks hold >= 32 slots):
             // one atomic per chunk; flags are 0 or 1
             const uint32_t ch0 = __shfl_sync(0xffffffffu, ch, 0);
             const uint32_t b0 = __ballot_sync(0xffffffffu, act && fl && ch == ch0);
@@ -256,8 +261,9 @@ HD_D void candidates_range(const Table& t, const Level* lvs, uint32_t L, uint32_
 }
 
 // Find-or-add over sorted keys [0, n) (runs of one bucket in entry order):
-// warps w of nw take chunks of 32 sorted positions and resolve every run
-// that starts in their chunk.
+// the positions are split into one chunk per warp (ceil(n / nw), at least
+// one) and warp w of nw resolves every run that starts in its chunk, so that
+// short runs spread over all the warps.
 template <int PW>
 HD_D void foa_sorted(const Table& t, uint32_t L, const Level& lv, const uint32_t* keys, const uint32_t* vals,
                      uint32_t n, uint32_t w, uint32_t nw, uint32_t* page, uint32_t* q, FoaCache& cache,
@@ -266,11 +272,15 @@ HD_D void foa_sorted(const Table& t, uint32_t L, const Level& lv, const uint32_t
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t empty = t.g.buckets(L);
     unsigned long long foa = 0, added = 0, scanned = 0;
-    for (uint32_t c0 = w * 32; c0 < n; c0 += nw * 32) {
+    const uint32_t chunk = n > nw ? (n + nw - 1) / nw : 1u;
+    const uint64_t cbeg64 = uint64_t(w) * chunk;
+    const uint32_t cbeg = cbeg64 < n ? uint32_t(cbeg64) : n, cend = n - cbeg < chunk ? n : cbeg + chunk;
+    for (uint32_t c0 = cbeg; c0 < cend; c0 += 32) {
         const uint32_t j = c0 + lane;
-        const uint32_t key = j < n ? __ldcg(keys + j) : empty;
-        const uint32_t prev = (j > 0 && j < n) ? __ldcg(keys + j - 1) : kNoBucket;
-        uint32_t starts = __ballot_sync(0xffffffffu, j < n && key < empty && key != prev);
+        const bool in = j < cend;
+        const uint32_t key = in ? __ldcg(keys + j) : empty;
+        const uint32_t prev = (in && j > 0) ? __ldcg(keys + j - 1) : kNoBucket;
+        uint32_t starts = __ballot_sync(0xffffffffu, in && key < empty && key != prev);
         while (starts) {
             const uint32_t s = __ffs(starts) - 1;
             starts &= starts - 1;
@@ -333,32 +343,28 @@ HD_D uint32_t small_sort(const Table& t, uint32_t L, uint32_t n, uint32_t* keys,
         __syncthreads();
         return runs;
     }
-    uint32_t n2 = 1;
-    while (n2 < n)
-        n2 <<= 1;
-    for (uint32_t i = threadIdx.x; i < n2; i += kPT)
-        s64[i] = i < n ? (uint64_t(keys[i]) << 32) | vals[i] : ~0ull;
+    // n <= kPT: a rank sort, one element per thread: the (bucket, entry)
+    // pairs are distinct, so an element's rank is the count of smaller ones
+    // (every thread reads the same shared word at a time: a broadcast)
+    unsigned long long* in = s64;
+    unsigned long long* out = s64 + kPT;
+    const uint32_t i = threadIdx.x;
+    const unsigned long long x = i < n ? (uint64_t(keys[i]) << 32) | vals[i] : ~0ull;
+    in[i] = x;
     __syncthreads();
-    for (uint32_t k = 2; k <= n2; k <<= 1)
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = threadIdx.x; i < n2; i += kPT) {
-                const uint32_t ixj = i ^ j;
-                if (ixj > i) {
-                    const unsigned long long x = s64[i], y = s64[ixj];
-                    if ((x > y) == ((i & k) == 0)) {
-                        s64[i] = y;
-                        s64[ixj] = x;
-                    }
-                }
-            }
-            __syncthreads();
-        }
+    if (i < n) {
+        uint32_t rank = 0;
+        for (uint32_t k = 0; k < n; k++)
+            rank += in[k] < x;
+        out[rank] = x;
+    }
+    __syncthreads();
     uint32_t runs = 0;
-    for (uint32_t i = threadIdx.x; i < n; i += kPT) {
-        const uint32_t key = uint32_t(s64[i] >> 32);
+    if (i < n) {
+        const uint32_t key = uint32_t(out[i] >> 32);
         keys[i] = key;
-        vals[i] = uint32_t(s64[i]);
-        runs += key < empty && (i == 0 || uint32_t(s64[i - 1] >> 32) != key);
+        vals[i] = uint32_t(out[i]);
+        runs = key < empty && (i == 0 || uint32_t(out[i - 1] >> 32) != key);
     }
     __threadfence();
     uint32_t total;
@@ -398,7 +404,7 @@ HD_D void scatter_chunk(const uint32_t* keys, const uint32_t* vals, uint32_t n, 
 {
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt = (1u << lane) - 1u;
-    const uint32_t chunk = chunk_len(n, nb, kPT);
+    const uint32_t chunk = chunk_len(n, nb, kChunkAlign);
     // digit bases: exclusive scan of the row totals (nd <= kPT)
     {
         const uint32_t d = threadIdx.x;
@@ -717,7 +723,7 @@ __global__ void __launch_bounds__(kPT, 1) k_edit_persistent(Table t, PArgs a)
                 }
                 if (threadIdx.x == 0)
                     a.bsum[((L + 2) % 3) * G + cta] = 0;
-                const uint32_t chunk = chunk_len(n, G, kPT);
+                const uint32_t chunk = chunk_len(n, G, kChunkAlign);
                 const uint32_t i0 = min(n, cta * chunk), i1 = min(n, i0 + chunk);
                 td_range(t, ed_s, a.lv, L, i0, i1, tb, uint32_t(n_next), G, a.bsum + ((L + 1) % 3) * G, ctr, sm32,
                          sm.list);
@@ -751,8 +757,8 @@ __global__ void __launch_bounds__(kPT, 1) k_edit_persistent(Table t, PArgs a)
         // bottom-up, big levels: six phases each; small ones go back to CTA 0
         while (__ldcg(&ctl->count[L]) > kSmall && __ldcg(t.error) == 0) {
             const uint32_t n = __ldcg(&ctl->count[L]);
-            const uint32_t nb = min(G, (n + kPT - 1) / kPT);
-            const uint32_t chunk = chunk_len(n, nb, kPT);
+            const uint32_t nb = min(G, (n + kChunkAlign - 1) / kChunkAlign);
+            const uint32_t chunk = chunk_len(n, nb, kChunkAlign);
             uint32_t key_bits = 1;
             while ((1u << key_bits) <= t.g.buckets(L))
                 key_bits++;
@@ -821,7 +827,7 @@ struct PersistBuffers {
 static size_t persist_smem()
 {
     const size_t foa = size_t(kPWarps) * kPage * 4 + size_t(kPWarps) * 12 * 4 + size_t(kPWarps) * sizeof(FoaCache);
-    const size_t sort = size_t(kPT) * 8;
+    const size_t sort = size_t(kPT) * 8 * 2; // the small sort's two arrays
     return foa > sort ? foa : sort;
 }
 
