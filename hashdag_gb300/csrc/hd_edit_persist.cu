@@ -245,6 +245,76 @@ HD_D void td_range(const Table& t, const Editor& ed, const Level* lvs, uint32_t 
     warp_add(&ctr->num_voxels, voxels);
 }
 
+// Top-down, one warp of CTA 0 alone: consecutive levels of at most 32
+// entries (the levels near the root), as td_range does them for a whole
+// level (positions, children spawned and classified, the next level's
+// per-chunk descend counts) but with warp votes in place of CTA scans and
+// barriers.  Returns the first level it did not descend from; status 0: that
+// level holds more than 32 entries (or is the leaf level), 1: it had no
+// descended entry (it is the deepest), 2: its children would exceed their
+// level's capacity.
+HD_D uint32_t td_tiny(const Table& t, const Editor& ed, const PArgs& a, uint32_t L, uint32_t n, EditCounters* ctr,
+                      uint32_t* list, uint32_t& status)
+{
+    const uint32_t lane = threadIdx.x & 31, G = gridDim.x, leafl = t.g.leaf_level;
+    unsigned long long nodes = 0, voxels = 0;
+    status = 0;
+    while (L < leafl && n <= 32) {
+        const Level lv = a.lv[L], nx = a.lv[L + 1];
+        const uint32_t f = lane < n ? lv.flag[lane] : 0u;
+        const uint32_t fb = __ballot_sync(0xffffffffu, f != 0);
+        const uint32_t total = __popc(fb);
+        if (total == 0) {
+            status = 1;
+            break;
+        }
+        const uint32_t n_next = 8 * total;
+        if (n_next > a.cap[L + 1]) {
+            status = 2;
+            break;
+        }
+        uint32_t* zero = a.bsum + ((L + 2) % 3) * G;
+        for (uint32_t k = lane; k < G; k += 32)
+            zero[k] = 0;
+        uint32_t* cnt_next = a.bsum + ((L + 1) % 3) * G;
+        if (f) {
+            const uint32_t off = __popc(fb & ((1u << lane) - 1u));
+            lv.exp[lane] = off;
+            list[off] = lane;
+        }
+        __syncwarp();
+        for (uint32_t k0 = 0; k0 < n_next; k0 += 32) {
+            const uint32_t k = k0 + lane;
+            const bool act = k < n_next;
+            uint32_t fl = 0, ch = 0xFFFFFFFFu;
+            if (act) {
+                spawn_child(t, lv, nx, list[k >> 3], k & 7, k);
+                unsigned long long nn, vv;
+                classify_entry<true>(t, ed, L + 1, nx, k, nn, vv);
+                nodes += nn;
+                voxels += vv;
+                fl = nx.flag[k];
+                ch = td_chunk(k, n_next, G);
+            }
+            const uint32_t ch0 = __shfl_sync(0xffffffffu, ch, 0);
+            const uint32_t b0 = __ballot_sync(0xffffffffu, act && fl && ch == ch0);
+            const uint32_t b1 = __ballot_sync(0xffffffffu, act && fl && ch != ch0);
+            if (lane == 0 && b0)
+                atomicAdd(cnt_next + ch0, uint32_t(__popc(b0)));
+            if (b1 && lane == uint32_t(__ffs(b1) - 1))
+                atomicAdd(cnt_next + ch, uint32_t(__popc(b1)));
+        }
+        if (lane == 0)
+            a.ctl->count[L + 1] = n_next;
+        __syncwarp(); // the next level reads the flags other lanes wrote
+        n = n_next;
+        L++;
+    }
+    warp_add(&ctr->num_nodes, nodes);
+    warp_add(&ctr->num_voxels, voxels);
+    return L;
+}
+
 // Bottom-up candidates of entries [i0, i1) of level L: key = level-local
 // bucket, or buckets(L) (sorts last) for entries resolved at once.
 HD_D void candidates_range(const Table& t, const Level* lvs, uint32_t L, uint32_t deepest, uint32_t i0, uint32_t i1,
@@ -558,8 +628,33 @@ HD_D void local_advance(const Table& t, const PArgs& a, uint32_t ls, uint32_t L,
         const uint32_t idx = ctl->idx;
         EditCounters* ctr = a.ctr + idx;
         if (ls == kLsTopDown) {
+            __shared__ uint32_t tiny[2];
             while (L < leafl) {
-                const uint32_t n = ctl->count[L];
+                uint32_t n = ctl->count[L];
+                if (n <= 32) {
+                    // the levels of at most 32 entries: warp 0 alone
+                    if (warp == 0) {
+                        uint32_t st;
+                        const uint32_t L2 = td_tiny(t, *sm.ed, a, L, n, ctr, sm.list, st);
+                        if ((threadIdx.x & 31) == 0) {
+                            tiny[0] = L2;
+                            tiny[1] = st;
+                        }
+                    }
+                    __syncthreads();
+                    L = tiny[0];
+                    const uint32_t st = tiny[1];
+                    __syncthreads();
+                    if (st == 2) {
+                        if (threadIdx.x == 0)
+                            ctl->stop = kCapacity;
+                        __syncthreads();
+                        return;
+                    }
+                    if (st == 1 || L >= leafl)
+                        break;
+                    n = ctl->count[L];
+                }
                 if (n > kSmall) {
                     if (threadIdx.x == 0) {
                         ctl->phase = kPhTopDown;
