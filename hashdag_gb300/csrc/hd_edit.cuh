@@ -254,16 +254,17 @@ struct NodeRead {
 
 // Top-down classification of entry i of level `level` (edit_threaded /
 // edit_leaf early exits); nodes / voxels: its share of the edit counters.
+// The entry's path (x, y, z) and old node are given (a caller that has just
+// spawned it holds them in registers); classify_entry reads them.
 template <bool CG = false>
-HD_D void classify_entry(const Table& t, const Editor& ed, uint32_t level, const Level& lv, uint32_t i,
-                         unsigned long long& nodes, unsigned long long& voxels)
+HD_D void classify_values(const Table& t, const Editor& ed, uint32_t level, const Level& lv, uint32_t i, uint32_t x,
+                          uint32_t y, uint32_t z, uint32_t old, unsigned long long& nodes, unsigned long long& voxels)
 {
     const uint32_t D = t.g.depth, T = t.g.T, leafl = t.g.leaf_level;
     const uint32_t depth = D - level;
     const float s = float(1u << depth);
-    const float mnx = float(lv.x[i] << depth), mny = float(lv.y[i] << depth), mnz = float(lv.z[i] << depth);
+    const float mnx = float(x << depth), mny = float(y << depth), mnz = float(z << depth);
     const float mxx = mnx + s, mxy = mny + s, mxz = mnz + s;
-    const uint32_t old = lv.old[i];
     const bool se = should_edit_impl(ed, mnx, mny, mnz, mxx, mxy, mxz);
     uint8_t state;
     uint32_t res = old, cnt = 0;
@@ -302,7 +303,7 @@ HD_D void classify_entry(const Table& t, const Editor& ed, uint32_t level, const
                     const NodeRead<CG> p(t, old);
                     leaf = uint64_t(p[0]) | (uint64_t(p[1]) << 32);
                 }
-                const uint32_t x0 = lv.x[i] << 2, y0 = lv.y[i] << 2, z0 = lv.z[i] << 2;
+                const uint32_t x0 = x << 2, y0 = y << 2, z0 = z << 2;
                 uint32_t edited = 0;
                 for (uint32_t c1 = 0; c1 < 8; c1++)
                     for (uint32_t c2 = 0; c2 < 8; c2++) {
@@ -336,6 +337,13 @@ HD_D void classify_entry(const Table& t, const Editor& ed, uint32_t level, const
     }
 }
 
+template <bool CG = false>
+HD_D void classify_entry(const Table& t, const Editor& ed, uint32_t level, const Level& lv, uint32_t i,
+                         unsigned long long& nodes, unsigned long long& voxels)
+{
+    classify_values<CG>(t, ed, level, lv, i, lv.x[i], lv.y[i], lv.z[i], lv.old[i], nodes, voxels);
+}
+
 // A descended entry spawns its 8 children (child order) at 8 * exp[i] on the
 // next level.
 HD_D void spawn_entry(const Table& t, const Level& lv, const Level& next, uint32_t i)
@@ -360,20 +368,25 @@ HD_D void spawn_entry(const Table& t, const Level& lv, const Level& next, uint32
 }
 
 // Child c of descended entry i, written at slot `at` of the next level
-// (spawn_entry for one child, with L2-coherent table reads).
-HD_D void spawn_child(const Table& t, const Level& lv, const Level& next, uint32_t i, uint32_t c, uint32_t at)
+// (spawn_entry for one child, with L2-coherent table reads); its path and
+// old node are also returned (for classify_values).
+HD_D void spawn_child(const Table& t, const Level& lv, const Level& next, uint32_t i, uint32_t c, uint32_t at,
+                      uint32_t& x, uint32_t& y, uint32_t& z, uint32_t& child)
 {
     const uint32_t old = lv.old[i];
-    uint32_t child = kInvalid;
+    child = kInvalid;
     if (old != kInvalid) {
         const NodeRead<true> p(t, old);
         const uint32_t mask = p[0] & 0xffu;
         if (mask & (1u << c))
             child = p[child_offset(mask, c)];
     }
-    next.x[at] = (lv.x[i] << 1) | ((c >> 2) & 1);
-    next.y[at] = (lv.y[i] << 1) | ((c >> 1) & 1);
-    next.z[at] = (lv.z[i] << 1) | (c & 1);
+    x = (lv.x[i] << 1) | ((c >> 2) & 1);
+    y = (lv.y[i] << 1) | ((c >> 1) & 1);
+    z = (lv.z[i] << 1) | (c & 1);
+    next.x[at] = x;
+    next.y[at] = y;
+    next.z[at] = z;
     next.old[at] = child;
 }
 

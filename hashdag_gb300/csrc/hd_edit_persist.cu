@@ -219,9 +219,10 @@ HD_D void td_range(const Table& t, const Editor& ed, const Level* lvs, uint32_t 
             if (act) {
                 const uint32_t parent = list[k >> 3], c = k & 7;
                 const uint32_t at = 8 * (run + (k >> 3)) + c;
-                spawn_child(t, lv, nx, parent, c, at);
+                uint32_t x, y, z, old;
+                spawn_child(t, lv, nx, parent, c, at, x, y, z, old);
                 unsigned long long nn, vv;
-                classify_entry<true>(t, ed, L + 1, nx, at, nn, vv);
+                classify_values<true>(t, ed, L + 1, nx, at, x, y, z, old, nn, vv);
                 nodes += nn;
                 voxels += vv;
                 fl = nx.flag[at];
@@ -288,9 +289,10 @@ HD_D uint32_t td_tiny(const Table& t, const Editor& ed, const PArgs& a, uint32_t
             const bool act = k < n_next;
             uint32_t fl = 0, ch = 0xFFFFFFFFu;
             if (act) {
-                spawn_child(t, lv, nx, list[k >> 3], k & 7, k);
+                uint32_t x, y, z, old;
+                spawn_child(t, lv, nx, list[k >> 3], k & 7, k, x, y, z, old);
                 unsigned long long nn, vv;
-                classify_entry<true>(t, ed, L + 1, nx, k, nn, vv);
+                classify_values<true>(t, ed, L + 1, nx, k, x, y, z, old, nn, vv);
                 nodes += nn;
                 voxels += vv;
                 fl = nx.flag[k];
@@ -380,7 +382,8 @@ HD_D void foa_sorted(const Table& t, uint32_t L, const Level& lv, const uint32_t
 
 // CTA 0 alone: stable sort of the n (<= kPT) candidates of a small level by
 // (bucket, entry) in shared memory, written back to keys / vals (visible to
-// the whole grid); returns the number of bucket runs.
+// the CTA after its barriers, to the grid after the next grid barrier);
+// returns the number of bucket runs.
 HD_D uint32_t small_sort(const Table& t, uint32_t L, uint32_t n, uint32_t* keys, uint32_t* vals,
                          unsigned long long* s64, uint32_t* sm32)
 {
@@ -404,7 +407,6 @@ HD_D uint32_t small_sort(const Table& t, uint32_t L, uint32_t n, uint32_t* keys,
                 vals[lane] = uint32_t(x);
             }
             const uint32_t runs = __popc(__ballot_sync(0xffffffffu, lane < n && key < empty && (lane == 0 || prev != key)));
-            __threadfence();
             if (lane == 0)
                 sm32[0] = runs;
         }
@@ -436,7 +438,6 @@ HD_D uint32_t small_sort(const Table& t, uint32_t L, uint32_t n, uint32_t* keys,
         vals[i] = uint32_t(out[i]);
         runs = key < empty && (i == 0 || uint32_t(out[i - 1] >> 32) != key);
     }
-    __threadfence();
     uint32_t total;
     cta_scan(runs, &total, sm32);
     return total;
@@ -721,7 +722,9 @@ HD_D void local_advance(const Table& t, const PArgs& a, uint32_t ls, uint32_t L,
                 }
                 foa_sorted<PW>(t, L, a.lv[L], a.keys, a.vals, n, warp, kPWarps, sm.page + warp * kPage,
                                sm.q + warp * 12, sm.cache[warp], ctr);
-                __threadfence();
+                // the CTA barrier makes this level's results (lv.res, appended
+                // nodes) visible to CTA 0's next level; the grid barrier
+                // (a CTA barrier, then a fence by its thread 0) to the grid
                 __syncthreads();
                 if (L == 0)
                     break;
