@@ -506,6 +506,12 @@ class HashDAG:
     def set_fp_mode(self, mode):
         self._check(lib().hd_set_fp_mode(self._h, int(mode)))
 
+    def set_test_barrier_skip(self, cta_plus_one, wait_ms=50):
+        """Test hook (hd_set_test_barrier_skip): the next persistent batch
+        launch leaves one CTA out of its grid barriers, so the others' waits
+        run out after wait_ms and the call fails with HD_ERR_TIMEOUT."""
+        self._check(lib().hd_set_test_barrier_skip(self._h, int(cta_plus_one), int(wait_ms)))
+
     def set_page_reserve(self, pages):
         """Keeps `pages` pool pages back from edits for the GC's rebuild
         (hd_set_page_reserve)."""

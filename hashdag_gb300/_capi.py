@@ -180,6 +180,7 @@ SIGNATURES = [
                                             C.POINTER(_u64)]),
     ("hd_set_fp_mode", C.c_int, [_P, _u32]),
     ("hd_set_page_reserve", C.c_int, [_P, _u32]),
+    ("hd_set_test_barrier_skip", C.c_int, [_P, _u32, _u32]),
     ("hd_get_values", C.c_int, [_P, _P, _u64, _P]),
     ("hd_edit_apply", C.c_int, [_P, C.POINTER(Edit), C.POINTER(EditStats)]),
     ("hd_edit_batch", C.c_int, [_P, C.POINTER(Edit), _u32, C.POINTER(EditStats)]),

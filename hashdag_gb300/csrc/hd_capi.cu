@@ -224,6 +224,15 @@ hd_status hd_set_page_reserve(hd_ctx* c, uint32_t pages)
     });
 }
 
+hd_status hd_set_test_barrier_skip(hd_ctx* c, uint32_t cta_plus_one, uint32_t wait_ms)
+{
+    if (!c)
+        return HD_ERR_INVALID;
+    c->test_skip_cta = cta_plus_one;
+    c->test_wait_ns = uint64_t(wait_ms) * 1000000ull;
+    return HD_OK;
+}
+
 hd_status hd_set_fp_mode(hd_ctx* c, uint32_t mode)
 {
     if (!c || mode > 1)

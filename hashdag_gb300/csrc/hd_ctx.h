@@ -66,6 +66,9 @@ struct hd_ctx {
     // pages page claims outside a GC leave untouched (hd_set_page_reserve):
     // the GC's rebuild draws on them
     uint32_t page_reserve = 0;
+    // hd_set_test_barrier_skip: for the next persistent batch launch only
+    uint32_t test_skip_cta = 0;
+    unsigned long long test_wait_ns = 0;
 };
 
 namespace hd {

@@ -68,6 +68,11 @@ struct Ctl {
     // generation then, CTA 0's barrier count, phase, level and edit
     uint32_t diag[8];
     uint32_t bars0; // barriers CTA 0 has passed
+    // tests of the timeout path (hd_set_test_barrier_skip): CTA skip_cta - 1
+    // returns at once, never arriving (0: none); wait_ns bounds every
+    // barrier wait (0: kWaitNs)
+    uint32_t skip_cta;
+    unsigned long long wait_ns;
     Editor ed;
 };
 
@@ -123,13 +128,15 @@ HD_D bool grid_sync(Ctl* ctl, uint32_t* err, uint32_t& nbar)
             st_release(&ctl->gen, g + 1);
         } else {
             const unsigned long long t0 = now_ns();
+            const unsigned long long set_ns = __ldcg(&ctl->wait_ns);
+            const unsigned long long limit = set_ns ? set_ns : kWaitNs;
             uint32_t spins = 0;
             while (ld_acquire(&ctl->gen) == g) {
                 if (ld_acquire(&ctl->abort)) {
                     ok = 0;
                     break;
                 }
-                if ((++spins & 255u) == 0 && now_ns() - t0 > kWaitNs) {
+                if ((++spins & 255u) == 0 && now_ns() - t0 > limit) {
                     if (atomicExch(&ctl->abort, 1u) == 0) {
                         ctl->diag[0] = blockIdx.x;
                         ctl->diag[1] = nbar;
@@ -738,6 +745,11 @@ HD_D void local_advance(const Table& t, const PArgs& a, uint32_t ls, uint32_t L,
 template <int PW>
 __global__ void __launch_bounds__(kPT, 1) k_edit_persistent(Table t, PArgs a)
 {
+    {
+        const uint32_t skip = __ldcg(&a.ctl->skip_cta);
+        if (skip && blockIdx.x == skip - 1)
+            return; // a test of the timeout path: this CTA never arrives
+    }
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint32_t sm32[40];
     __shared__ Editor ed_s;
@@ -993,6 +1005,16 @@ void edit_batch_persistent(hd_ctx* c, const hd_edit* edits, uint32_t n, const st
         a.n_edits = m;
         HD_CUDA(cudaMemcpyAsync(d_edits, edits + done, sizeof(hd_edit) * m, cudaMemcpyHostToDevice, st));
         HD_CUDA(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st));
+        if (c->test_skip_cta) {
+            // one launch only: the hook switches itself off
+            const uint32_t skip = c->test_skip_cta;
+            const unsigned long long wait = c->test_wait_ns;
+            HD_CUDA(cudaMemcpyAsync(&ctl->skip_cta, &skip, 4, cudaMemcpyHostToDevice, st));
+            HD_CUDA(cudaMemcpyAsync(&ctl->wait_ns, &wait, 8, cudaMemcpyHostToDevice, st));
+            HD_CUDA(cudaStreamSynchronize(st));
+            c->test_skip_cta = 0;
+            c->test_wait_ns = 0;
+        }
         HD_CUDA(cudaEventRecord(c->ev0, st));
         void* args[] = {&c->t, &a};
         HD_CUDA(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(kPT), args, smem, st));

@@ -457,6 +457,16 @@ hd_status hd_gc_ex(hd_ctx* ctx, uint32_t* h_extra_roots, uint32_t n_extra, uint3
  * edit's). */
 hd_status hd_set_page_reserve(hd_ctx* ctx, uint32_t pages);
 
+/* A test of the persistent batch's failure path: in the next persistent
+ * hd_edit_batch launch (only), CTA cta_plus_one - 1 returns at once without
+ * ever reaching a grid barrier, and every barrier wait is bounded by wait_ms
+ * (0: the default 2 s).  The other CTAs' waits run out, the launch ends and
+ * the call returns HD_ERR_TIMEOUT; the edits finished before stay applied
+ * (hd_edit_batch_ex fills their per-edit results), the root is the last
+ * finished edit's, and the context stays usable.  cta_plus_one 0 clears
+ * it. */
+hd_status hd_set_test_barrier_skip(hd_ctx* ctx, uint32_t cta_plus_one, uint32_t wait_ms);
+
 /* ---- files (serializer.h:11-121) ---------------------------------------- */
 
 /* DAGInfo (dag_info.h:6-10): the scene's bounding box, carried by the files. */

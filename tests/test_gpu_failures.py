@@ -141,3 +141,48 @@ def test_bucket_full_edit_is_refused(gpu, batched):
     assert d.firstNodeIndex == ot2.root
     assert table_digest(d.export_table(), DEPTH, 9) == table_digest(ot2.export(), DEPTH, 9)
     d.free()
+
+
+def test_persistent_barrier_timeout_is_reported_and_context_stays_usable(gpu):
+    """The persistent batch's grid barriers are bounded waits.  A test hook
+    makes one CTA return without ever arriving (a barrier nothing completes):
+    the other CTAs' waits run out after 50 ms, the call returns
+    HD_ERR_TIMEOUT with where it stopped, the root is that of the last edit
+    the launch finished, and the context keeps working: the remaining edits
+    applied afterwards leave the same voxels as applying all of them one by
+    one."""
+    edits = workloads.mixed_edits(DEPTH, 12, (8.0, 96.0), seed=13)
+    eds = [hd.editor_from_tuple(e) for e in edits]
+    ref = hd.HashDAG(DEPTH)
+    ref.load_from_DAG(_words())
+    roots = [ref.firstNodeIndex]
+    for e in eds:
+        ref.edit_threads(e)
+        roots.append(ref.firstNodeIndex)
+    d = hd.HashDAG(DEPTH)
+    d.load_from_DAG(_words())
+    d.batch_tuning = hd.BatchTuning(4, 4, 304, 1)  # the persistent launch
+    d.set_test_barrier_skip(5, 50)
+    with pytest.raises(hd.HashDagError) as ei:
+        d.edit_batch(eds)
+    assert ei.value.status == _capi.HD_ERR_TIMEOUT and "ran out of time" in str(ei.value), str(ei.value)
+    # the edits the launch finished (CTA 0 finishes the first edit before the
+    # grid meets) are applied, in order
+    k = roots.index(d.firstNodeIndex)
+    assert k <= 1
+    # the hook is gone: the rest of the batch runs
+    d.edit_batch(eds[k:])
+    q = np.random.default_rng(5).integers(0, 1 << DEPTH, (60000, 3)).astype(np.uint32)
+    c = np.array([e[1] for e in edits], np.float64)
+    near = (c[np.arange(20000) % len(c)] + np.random.default_rng(6).uniform(-100, 100, (20000, 3)))
+    q = np.concatenate([q, np.clip(near, 0, (1 << DEPTH) - 1).astype(np.uint32)])
+    assert np.array_equal(d.get_values(q), ref.get_values(q))
+    fp = []
+    for x in (d, ref):
+        t = x.export_table()
+        ot = po.Table(po.default_config(DEPTH, pool_pages=int(t["pool"].size // 512) + 8))
+        ot.import_(t)
+        fp.append(ot.fingerprint())
+    assert fp[0] == fp[1]
+    d.free()
+    ref.free()
