@@ -426,13 +426,11 @@ HD_D uint32_t candidate_entry(const Table& t, uint32_t level, const Level& lv, c
         const uint32_t old = lv.old[i];
         uint32_t mask = 0, k = 1, total = 0;
         bool changed = false;
-        uint32_t omask = 0;
-        const NodeRead<CG> p(t, old != kInvalid ? old : 0u);
-        if (old != kInvalid)
-            omask = p[0] & 0xffu;
-        uint32_t ok = 1;
         for (uint32_t s = 0; s < 8; s++) {
-            const uint32_t oc = (omask & (1u << s)) ? p[ok++] : kInvalid;
+            // the old child in slot s: the spawned child's old node (all 8
+            // children were spawned; kInvalid where the old node had none),
+            // so the old node itself is not read again
+            const uint32_t oc = child.old[base + s];
             const uint8_t cs = child.state[base + s];
             const uint32_t nc = cs == kSkip ? oc : child.res[base + s];
             changed |= nc != oc;
