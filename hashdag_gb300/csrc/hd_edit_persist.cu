@@ -343,7 +343,9 @@ HD_D void candidates_range(const Table& t, const Level* lvs, uint32_t L, uint32_
 // the positions are split into one chunk per warp (ceil(n / nw), at least
 // one) and warp w of nw resolves every run that starts in its chunk, so that
 // short runs spread over all the warps.
-template <int PW>
+// SH: keys / vals in the CTA's shared memory (CTA 0's small levels), read
+// with plain loads; else global arrays another phase wrote, read from L2.
+template <int PW, bool SH = false>
 HD_D void foa_sorted(const Table& t, uint32_t L, const Level& lv, const uint32_t* keys, const uint32_t* vals,
                      uint32_t n, uint32_t w, uint32_t nw, uint32_t* page, uint32_t* q, FoaCache& cache,
                      EditCounters* ctr)
@@ -357,8 +359,8 @@ HD_D void foa_sorted(const Table& t, uint32_t L, const Level& lv, const uint32_t
     for (uint32_t c0 = cbeg; c0 < cend; c0 += 32) {
         const uint32_t j = c0 + lane;
         const bool in = j < cend;
-        const uint32_t key = in ? __ldcg(keys + j) : empty;
-        const uint32_t prev = (in && j > 0) ? __ldcg(keys + j - 1) : kNoBucket;
+        const uint32_t key = in ? (SH ? keys[j] : __ldcg(keys + j)) : empty;
+        const uint32_t prev = (in && j > 0) ? (SH ? keys[j - 1] : __ldcg(keys + j - 1)) : kNoBucket;
         uint32_t starts = __ballot_sync(0xffffffffu, in && key < empty && key != prev);
         while (starts) {
             const uint32_t s = __ffs(starts) - 1;
@@ -368,7 +370,7 @@ HD_D void foa_sorted(const Table& t, uint32_t L, const Level& lv, const uint32_t
             uint32_t j1 = j0 + 1;
             for (;;) {
                 const uint32_t jj = j1 + lane;
-                const uint32_t k = jj < n ? __ldcg(keys + jj) : kNoBucket;
+                const uint32_t k = jj < n ? (SH ? keys[jj] : __ldcg(keys + jj)) : kNoBucket;
                 const uint32_t diff = __ballot_sync(0xffffffffu, k != bucket);
                 if (diff) {
                     j1 += __ffs(diff) - 1;
@@ -392,7 +394,7 @@ HD_D void foa_sorted(const Table& t, uint32_t L, const Level& lv, const uint32_t
 // the CTA after its barriers, to the grid after the next grid barrier);
 // returns the number of bucket runs.
 HD_D uint32_t small_sort(const Table& t, uint32_t L, uint32_t n, uint32_t* keys, uint32_t* vals,
-                         unsigned long long* s64, uint32_t* sm32)
+                         unsigned long long* s64, uint32_t* sm32, uint32_t* sk, uint32_t* sv)
 {
     const uint32_t empty = t.g.buckets(L);
     if (n <= 32) {
@@ -412,6 +414,8 @@ HD_D uint32_t small_sort(const Table& t, uint32_t L, uint32_t n, uint32_t* keys,
             if (lane < n) {
                 keys[lane] = key;
                 vals[lane] = uint32_t(x);
+                sk[lane] = key;
+                sv[lane] = uint32_t(x);
             }
             const uint32_t runs = __popc(__ballot_sync(0xffffffffu, lane < n && key < empty && (lane == 0 || prev != key)));
             if (lane == 0)
@@ -443,6 +447,8 @@ HD_D uint32_t small_sort(const Table& t, uint32_t L, uint32_t n, uint32_t* keys,
         const uint32_t key = uint32_t(out[i] >> 32);
         keys[i] = key;
         vals[i] = uint32_t(out[i]);
+        sk[i] = key;
+        sv[i] = uint32_t(out[i]);
         runs = key < empty && (i == 0 || uint32_t(out[i - 1] >> 32) != key);
     }
     uint32_t total;
@@ -528,7 +534,21 @@ enum : uint32_t { kLsBegin = 0, kLsTopDown = 1, kLsBottomUp = 2, kLsFinish = 3 }
 // the grid step CTA 0 asks for
 enum : uint32_t { kPhNone = 0, kPhTopDown = 1, kPhBottomUp = 2, kPhGridFoa = 3 };
 
+// Bytes of the dynamic shared memory the find-or-add buffers and the small
+// sort share (a multiple of 16); the small level's sorted keys and entries
+// follow.
+HD_HD constexpr size_t persist_smem_core()
+{
+    return (size_t(kPWarps) * kPage * 4 + size_t(kPWarps) * 12 * 4 + size_t(kPWarps) * sizeof(FoaCache) >
+                    size_t(kPT) * 8 * 2
+                ? size_t(kPWarps) * kPage * 4 + size_t(kPWarps) * 12 * 4 + size_t(kPWarps) * sizeof(FoaCache)
+                : size_t(kPT) * 8 * 2) +
+           15 & ~size_t(15);
+}
+
 struct Smem {
+    uint32_t* sk; // a small level's sorted keys and entries (kPT each), past
+    uint32_t* sv; // the buffers below (which the find-or-add overwrites)
     uint32_t* page;
     uint32_t* q;
     FoaCache* cache;
@@ -717,7 +737,7 @@ HD_D void local_advance(const Table& t, const PArgs& a, uint32_t ls, uint32_t L,
                 }
                 candidates_range(t, a.lv, L, deepest, 0, n, a.keys, a.vals);
                 __syncthreads();
-                const uint32_t runs = small_sort(t, L, n, a.keys, a.vals, sm.s64, sm.sm32);
+                const uint32_t runs = small_sort(t, L, n, a.keys, a.vals, sm.s64, sm.sm32, sm.sk, sm.sv);
                 if (runs > 2 * kPWarps) {
                     // many buckets: the grid resolves them
                     if (threadIdx.x == 0) {
@@ -727,7 +747,7 @@ HD_D void local_advance(const Table& t, const PArgs& a, uint32_t ls, uint32_t L,
                     __syncthreads();
                     return;
                 }
-                foa_sorted<PW>(t, L, a.lv[L], a.keys, a.vals, n, warp, kPWarps, sm.page + warp * kPage,
+                foa_sorted<PW, true>(t, L, a.lv[L], sm.sk, sm.sv, n, warp, kPWarps, sm.page + warp * kPage,
                                sm.q + warp * 12, sm.cache[warp], ctr);
                 // the CTA barrier makes this level's results (lv.res, appended
                 // nodes) visible to CTA 0's next level; the grid barrier
@@ -761,6 +781,8 @@ __global__ void __launch_bounds__(kPT, 1) k_edit_persistent(Table t, PArgs a)
     sm.q = sm.page + kPWarps * kPage;
     sm.cache = reinterpret_cast<FoaCache*>(sm.q + kPWarps * 12);
     sm.s64 = reinterpret_cast<unsigned long long*>(smem_raw);
+    sm.sk = reinterpret_cast<uint32_t*>(smem_raw + persist_smem_core());
+    sm.sv = sm.sk + kPT;
     sm.list = sm.page;
     sm.sm32 = sm32;
     sm.ed = &ed_s;
@@ -934,12 +956,7 @@ struct PersistBuffers {
     uint32_t grid = 0;
 };
 
-static size_t persist_smem()
-{
-    const size_t foa = size_t(kPWarps) * kPage * 4 + size_t(kPWarps) * 12 * 4 + size_t(kPWarps) * sizeof(FoaCache);
-    const size_t sort = size_t(kPT) * 8 * 2; // the small sort's two arrays
-    return foa > sort ? foa : sort;
-}
+static size_t persist_smem() { return persist_smem_core() + size_t(kPT) * 4 * 2; }
 
 template <int PW>
 static const void* persist_kernel()
