@@ -5,9 +5,10 @@ Workload (Catmull-Rom traversal of the 2^15 scene): the seeded procedural
 scene at depth 15 generated and ingested on the device before timing; 64
 camera poses on a seeded Catmull-Rom path at 1920x1080 (90 degree FOV); one
 step = --views poses (default 16; 4 steps cover the path) traced by
-hd_trace_views: a primary ray per pixel of every view in one launch, then,
-for every hit, one shadow ray toward normalize(0.3, 1, 0.2) with bias 1 in
-one launch.  Metric: Mrays/s (primary + shadow).
+hd_trace_views: the views' camera tables, a primary ray per pixel of every
+view in one launch, then, for every hit, one shadow ray toward
+normalize(0.3, 1, 0.2) with bias 1 in one launch.  Metric: Mrays/s (primary
++ shadow).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
@@ -70,7 +71,8 @@ def parse():
     p.add_argument("--poses", type=int, default=64)
     p.add_argument("--e2e-chunk", type=int, default=0,
                    help="views per chunk of the end-to-end call (0: paths written straight to host memory)")
-    p.add_argument("--views", type=int, default=16, help="poses traced per step (one primary and one shadow launch)")
+    p.add_argument("--views", type=int, default=16,
+                   help="poses traced per step (camera tables, primary and shadow launches)")
     p.add_argument("--ref-views", type=int, default=2,
                    help="whole frames per step of the CPU reference arm (a sample of the step's views)")
     p.add_argument("--no-ref-gpu", action="store_true", help="skip timing the reference's GPU tracer")
@@ -946,7 +948,7 @@ def run_gpu(args, dist):
                     "d2h_bytes_per_step": V * (W * H * 16 + W * H), "api": "hd_trace_views_host",
                     "paths": ("written by the primary kernel into the pinned host buffer (NVLink-C2C)"
                               if not args.e2e_chunk else f"copied in chunks of {args.e2e_chunk} views")},
-            "gpu_launches": 2 * K, "roofline": roofline, "cpu_baseline": cpu, "ref_gpu": ref_gpu, "clocks": clk,
+            "gpu_launches": 3 * K, "roofline": roofline, "cpu_baseline": cpu, "ref_gpu": ref_gpu, "clocks": clk,
             "wall_s": wall, "trace_4k": trace_4k, "edits": edits, "colors": colors, "tools_files": tools,
             "serving": serving, "serving_d15": sweep}
     if dist.rank == 0:

@@ -939,8 +939,9 @@ void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const
                 d_root ? d_root : c->d_root, d_list);
 }
 
-// n_views frames in two launches: primary rays of every view with the
-// shadow-ray list, then the shadow rays of every hit pixel of every view.
+// n_views frames in three launches: the views' camera tables, primary rays
+// of every view with the shadow-ray list, then the shadow rays of every hit
+// pixel of every view.
 void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t w, uint32_t h, uint32_t* d_paths,
                  const float light[3], float bias, uint8_t* d_mask, cudaStream_t stream, uint32_t* d_list,
                  cudaEvent_t mid, const uint32_t* d_root, double* d_tables)
