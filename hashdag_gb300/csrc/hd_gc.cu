@@ -69,10 +69,14 @@ HD_D uint32_t lower_bound(const uint32_t* v, uint32_t n, uint32_t x)
 }
 
 // Gathers the live nodes of a level (children remapped) before the level is
-// emptied; hashes and links them into the bucket lists.
+// emptied; hashes and links them into the bucket lists.  A child's index in
+// the live list of the level below is its rank in that level's mark bitmap:
+// the live count of the bitmap words before it (child_pos) plus the bits
+// below it in its word.
 __global__ void k_gc_gather(Table t, uint32_t level, const uint32_t* __restrict__ live, uint32_t n,
-                            const uint32_t* __restrict__ child_live, uint32_t n_child,
-                            const uint32_t* __restrict__ child_new, uint32_t* __restrict__ content,
+                            const uint32_t* __restrict__ child_bitmap, const uint32_t* __restrict__ child_pos,
+                            uint32_t child_base, const uint32_t* __restrict__ child_new,
+                            uint32_t* __restrict__ content,
                             uint32_t* __restrict__ head, uint32_t* __restrict__ next, uint32_t* __restrict__ touched,
                             uint32_t* __restrict__ n_touched)
 {
@@ -89,8 +93,10 @@ __global__ void k_gc_gather(Table t, uint32_t level, const uint32_t* __restrict_
         } else {
             const uint32_t cnt = popc32(p[0] & 0xffu);
             c[0] = p[0];
-            for (uint32_t k = 0; k < cnt; k++)
-                c[1 + k] = child_new[lower_bound(child_live, n_child, p[1 + k])];
+            for (uint32_t k = 0; k < cnt; k++) {
+                const uint32_t off = p[1 + k] - child_base, w = off >> 5;
+                c[1 + k] = child_new[child_pos[w] + popc32(child_bitmap[w] & ((1u << (off & 31)) - 1u))];
+            }
             hash = hash_interior(cnt + 1, c);
         }
         const uint32_t bucket = hash & (t.g.buckets(level) - 1);
@@ -274,17 +280,25 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
     live[0] = s.get<uint32_t>("gc_live_0", r0.size());
     HD_CUDA(cudaMemcpyAsync(live[0], r0.data(), r0.size() * 4, cudaMemcpyHostToDevice, st));
     nlive[0] = uint32_t(r0.size());
-    // mark
+    // mark; every level's bitmap and word ranks stay for the gathers
+    std::vector<uint32_t*> bm(leafl + 1, nullptr), bpos(leafl + 1, nullptr);
+    std::vector<uint32_t> bbase(leafl + 1, 0);
     for (uint32_t L = 0; L < leafl; L++) {
         const uint32_t base = g.make_ptr(L + 1, 0, 0);
         const uint64_t range = uint64_t(g.buckets(L + 1)) * g.capacity(L + 1);
         const uint64_t nwords = (range + 31) / 32;
-        uint32_t* bitmap = s.get<uint32_t>("gc_bitmap", nwords);
+        char bn[32];
+        snprintf(bn, sizeof(bn), "gc_bitmap_%u", L + 1);
+        uint32_t* bitmap = s.get<uint32_t>(bn, nwords);
         HD_CUDA(cudaMemsetAsync(bitmap, 0, nwords * 4, st));
         k_gc_mark<<<grid_for(nlive[L], 256), 256, 0, st>>>(c->t, live[L], nlive[L], base, bitmap);
         HD_LAUNCH_CHECK();
         uint32_t* counts = s.get<uint32_t>("gc_counts", nwords);
-        uint32_t* pos = s.get<uint32_t>("gc_pos", nwords);
+        snprintf(bn, sizeof(bn), "gc_pos_%u", L + 1);
+        uint32_t* pos = s.get<uint32_t>(bn, nwords);
+        bm[L + 1] = bitmap;
+        bpos[L + 1] = pos;
+        bbase[L + 1] = base;
         k_popc_words<<<grid_for(nwords, 256), 256, 0, st>>>(bitmap, nwords, counts);
         HD_LAUNCH_CHECK();
         exclusive_scan<uint32_t, uint32_t>(s, counts, pos, nwords, d_n, st);
@@ -327,8 +341,9 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
             k_gc_dry_full<<<1, 1, 0, st>>>(c->t, uint32_t(L), dry_sizes, full_dry);
             HD_LAUNCH_CHECK();
             k_gc_gather<<<grid_for(n, 256), 256, 0, st>>>(c->t, uint32_t(L), live[L], n,
-                                                          L < int32_t(leafl) ? live[L + 1] : nullptr,
-                                                          L < int32_t(leafl) ? nlive[L + 1] : 0,
+                                                          L < int32_t(leafl) ? bm[L + 1] : nullptr,
+                                                          L < int32_t(leafl) ? bpos[L + 1] : nullptr,
+                                                          L < int32_t(leafl) ? bbase[L + 1] : 0u,
                                                           L < int32_t(leafl) ? child_addr : nullptr, content, head,
                                                           next, touched, d_n);
             HD_LAUNCH_CHECK();
@@ -370,8 +385,9 @@ void gc(hd_ctx* c, std::vector<uint32_t>& roots, bool release_pages)
         newaddr[L] = s.get<uint32_t>(nm, uint64_t(n) + 1);
         HD_CUDA(cudaMemsetAsync(d_n, 0, 4, st));
         k_gc_gather<<<grid_for(n, 256), 256, 0, st>>>(c->t, uint32_t(L), live[L], n,
-                                                      L < int32_t(leafl) ? live[L + 1] : nullptr,
-                                                      L < int32_t(leafl) ? nlive[L + 1] : 0,
+                                                      L < int32_t(leafl) ? bm[L + 1] : nullptr,
+                                                      L < int32_t(leafl) ? bpos[L + 1] : nullptr,
+                                                      L < int32_t(leafl) ? bbase[L + 1] : 0u,
                                                       L < int32_t(leafl) ? newaddr[L + 1] : nullptr, content, head,
                                                       next, touched, d_n);
         HD_LAUNCH_CHECK();
