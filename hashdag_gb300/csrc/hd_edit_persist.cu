@@ -253,6 +253,64 @@ HD_D void td_range(const Table& t, const Editor& ed, const Level* lvs, uint32_t 
     warp_add(&ctr->num_voxels, voxels);
 }
 
+// The grid's top-down step of a big level, in two phases so that the
+// children (8 per descended entry, and the work of classifying them) spread
+// evenly over the CTAs whatever chunks the descended entries fall in.
+// Phase 1: entries [i0, i1) get their positions (prefix: the descended
+// entries before i0) and are listed by position in dlist.
+HD_D void td_positions(const Level& lv, uint32_t i0, uint32_t i1, uint32_t prefix, uint32_t* dlist, uint32_t* sm32)
+{
+    uint32_t run = prefix;
+    for (uint32_t base = i0; base < i1; base += kPT) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t f = i < i1 ? lv.flag[i] : 0u;
+        uint32_t total;
+        const uint32_t off = cta_scan(f, &total, sm32);
+        if (f) {
+            lv.exp[i] = run + off;
+            dlist[run + off] = i;
+        }
+        run += total;
+    }
+}
+
+// Phase 2: children [k0, k1) of the level (child k of descended entry
+// dlist[k / 8], slot k % 8) spawned and classified; their descend flags
+// counted per top-down chunk of the next level into cnt_next.  k0 is a
+// multiple of 32, so each warp's 32 consecutive children fall in at most two
+// chunks.
+HD_D void td_children(const Table& t, const Editor& ed, const Level* lvs, uint32_t L, uint32_t k0, uint32_t k1,
+                      uint32_t n_next, uint32_t G, const uint32_t* dlist, uint32_t* cnt_next, EditCounters* ctr)
+{
+    const Level lv = lvs[L], nx = lvs[L + 1];
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned long long nodes = 0, voxels = 0;
+    for (uint32_t kb = k0 + (threadIdx.x & ~31u); kb < k1; kb += kPT) {
+        const uint32_t k = kb + lane;
+        const bool act = k < k1;
+        uint32_t fl = 0, ch = 0xFFFFFFFFu;
+        if (act) {
+            uint32_t x, y, z, old;
+            spawn_child(t, lv, nx, __ldcg(dlist + (k >> 3)), k & 7, k, x, y, z, old);
+            unsigned long long nn, vv;
+            classify_values<true>(t, ed, L + 1, nx, k, x, y, z, old, nn, vv);
+            nodes += nn;
+            voxels += vv;
+            fl = nx.flag[k];
+            ch = td_chunk(k, n_next, G);
+        }
+        const uint32_t ch0 = __shfl_sync(0xffffffffu, ch, 0);
+        const uint32_t b0 = __ballot_sync(0xffffffffu, act && fl && ch == ch0);
+        const uint32_t b1 = __ballot_sync(0xffffffffu, act && fl && ch != ch0);
+        if (lane == 0 && b0)
+            atomicAdd(cnt_next + ch0, uint32_t(__popc(b0)));
+        if (b1 && lane == uint32_t(__ffs(b1) - 1))
+            atomicAdd(cnt_next + ch, uint32_t(__popc(b1)));
+    }
+    warp_add(&ctr->num_nodes, nodes);
+    warp_add(&ctr->num_voxels, voxels);
+}
+
 // Top-down, one warp of CTA 0 alone: consecutive levels of at most 32
 // entries (the levels near the root), as td_range does them for a whole
 // level (positions, children spawned and classified, the next level's
@@ -855,10 +913,17 @@ __global__ void __launch_bounds__(kPT, 1) k_edit_persistent(Table t, PArgs a)
                 }
                 if (threadIdx.x == 0)
                     a.bsum[((L + 2) % 3) * G + cta] = 0;
+                // positions and the list of descended entries (keys2 is
+                // free until the edit's bottom-up levels), then the children
+                // spread evenly over the CTAs
                 const uint32_t chunk = chunk_len(n, G, kChunkAlign);
                 const uint32_t i0 = min(n, cta * chunk), i1 = min(n, i0 + chunk);
-                td_range(t, ed_s, a.lv, L, i0, i1, tb, uint32_t(n_next), G, a.bsum + ((L + 1) % 3) * G, ctr, sm32,
-                         sm.list);
+                td_positions(a.lv[L], i0, i1, tb, a.keys2, sm32);
+                if (!grid_sync(ctl, t.error, nbar))
+                    return;
+                const uint32_t cch = chunk_len(uint32_t(n_next), G, kChunkAlign);
+                const uint32_t k0 = min(uint32_t(n_next), cta * cch), k1 = min(uint32_t(n_next), k0 + cch);
+                td_children(t, ed_s, a.lv, L, k0, k1, uint32_t(n_next), G, a.keys2, a.bsum + ((L + 1) % 3) * G, ctr);
                 if (cta == 0 && threadIdx.x == 0)
                     ctl->count[L + 1] = uint32_t(n_next);
                 if (!grid_sync(ctl, t.error, nbar))
