@@ -135,33 +135,133 @@ HD_D double rsqrt_newton(double dot)
     return __fma_rn(y0 * e, 0.5, y0);
 }
 
-// float(normalize(v)) from v and its squared length (see camera_dir_float).
-HD_D bool dir_from_vec(const double v[3], double dot, F3& d)
+// ---- float(normalize(v)) on the FP32 pipe ------------------------------------
+// The reference normalises the camera ray in double: dot = |v|^2, 1 / sqrt(dot)
+// and the products, each rounded (relative error below 2^-50.8 against the
+// exact v / |v| of its own double v), then rounds each component to float.
+// The GB300 runs double operations at 2 per SM cycle against 128 for float,
+// and every primary ray pays for this normalisation, so it is done here in
+// float-float arithmetic (pairs hi + lo of floats) from the same double v:
+//  * v = hi + lo: hi keeps v's 24 leading significant bits, lo the other 29
+//    rounded to float (2^-47 |v|);
+//  * |v|^2 = S + Slo: the squares of the hi parts summed exactly (TwoSum),
+//    their fused-multiply-add remainders and the 2 hi lo terms added in float
+//    (2^-45 |v|^2);
+//  * y = 1 / |v| = r0 + corr: an rsqrtf seed refined by one float
+//    Newton-Raphson step (2^-22.9 even for a seed 64 ulps off), then one
+//    Newton-Raphson step in float-float, r0 + r0 (1 - |v|^2 r0^2) / 2, whose
+//    residual is formed with fused multiply-adds (1.5 e^2 plus roundings,
+//    below 2^-44.5);
+//  * each component y v = P + L, P = r0 hi and its exact remainder, plus the
+//    small cross terms (2^-45.5).
+// The sum P + L lies within 2^-44 (measured on 10^8 vectors: 2^-44.3) of the
+// exact component, and so within 2^-43.9 of the reference's double; when
+// P + L is more than 2^-40 |P + L| from every float rounding midpoint both
+// round to the same float.  False (about one ray in ten thousand, and for
+// components outside [2^-40, 2^40) or results below 2^-63) sends the ray to
+// the exact double path.
+
+// v = hi + lo within 2^-47 |v|; false for a nonzero |v| outside [2^-40, 2^40).
+HD_D bool split_f64(double v, float& hi, float& lo)
 {
-    if (!(dot >= 0x1p-100 && dot <= 0x1p100))
+    const uint64_t b = (uint64_t)__double_as_longlong(v);
+    const uint32_t sign = uint32_t(b >> 32) & 0x80000000u;
+    const uint64_t mag = b & 0x7FFFFFFFFFFFFFFFull;
+    if (mag == 0) {
+        hi = __uint_as_float(sign);
+        lo = 0.0f;
+        return true;
+    }
+    const int32_t e = int32_t(mag >> 52) - 1023;
+    if (e < -40 || e >= 40)
         return false;
-    const double y1 = rsqrt_newton(dot);
-    return round_to_float(y1 * v[0], 8192, d.x) && round_to_float(y1 * v[1], 8192, d.y) &&
-           round_to_float(y1 * v[2], 8192, d.z);
+    hi = __uint_as_float(sign | (uint32_t(e + 127) << 23) | (uint32_t(mag >> 29) & 0x7FFFFFu));
+    const float scale = __uint_as_float(sign | (uint32_t(e - 52 + 127) << 23)); // exact power of two
+    lo = __fmul_rn(__uint2float_rn(uint32_t(mag) & ((1u << 29) - 1u)), scale);
+    return true;
 }
 
-// float(normalize(...)) of camera_dir with a third of its double-precision
-// work (the GB300's FP64 pipe is narrow, and every primary ray pays for
-// this).  The reference rounds 1 / sqrt(dot) twice and the product once more
-// (relative error below 2^-51.4 against the exact v / |v|); here a float
-// rsqrtf seed (2 ulp; the seed's argument rounded from dot, 2^-24) takes
-// one Newton-Raphson step in double, y1 = y0 + y0 (1 - dot y0^2) / 2, whose
-// error is 1.5 e0^2 plus roundings, below 2^-43, and y1 * v is rounded once.
-// The two doubles differ by less than 2^-42.9 relative, about 1,100 ulps of
-// the double; where a component lies more than 8,192 ulps from a float
-// rounding midpoint both round to the same float.  False (for about one ray
-// in ten thousand) sends the ray to the exact path.
+// s + t = a + b exactly (Knuth's TwoSum)
+HD_D void two_sum(float a, float b, float& s, float& t)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    t = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// The float nearest to P + L (|L| well below |P|), when that sum lies more
+// than 2^-40 |P + L| from the rounding midpoints either side of it (and the
+// result's magnitude is in [2^-63, 2^64)).
+HD_D bool round_pair(float P, float L, float& out)
+{
+    const float R = __fadd_rn(P, L);
+    const float r = __fsub_rn(L, __fsub_rn(R, P)); // P + L - R exactly (Fast2Sum, |P| >= |L|)
+    const uint32_t rb = __float_as_uint(R);
+    const uint32_t ex = (rb >> 23) & 0xFFu;
+    if (ex < 64 || ex > 190)
+        return false;
+    const float half_up = __uint_as_float((ex - 24) << 23);                            // ulp(R) / 2
+    const float half_down = (rb & 0x7FFFFFu) ? half_up : __uint_as_float((ex - 25) << 23); // below a power of two
+    const float margin = __uint_as_float((ex - 39) << 23);                              // >= 2^-40 |R|
+    const float s = (rb >> 31) ? -r : r; // the remainder, positive away from zero
+    if (!(__fsub_rn(half_up, s) > margin && __fadd_rn(half_down, s) > margin))
+        return false;
+    out = R;
+    return true;
+}
+
+HD_D bool dir_from_vec(const double v[3], F3& d)
+{
+    float h[3], l[3];
+    if (!(split_f64(v[0], h[0], l[0]) && split_f64(v[1], h[1], l[1]) && split_f64(v[2], h[2], l[2])))
+        return false;
+    const float p0 = __fmul_rn(h[0], h[0]), p1 = __fmul_rn(h[1], h[1]), p2 = __fmul_rn(h[2], h[2]);
+    const float e = __fadd_rn(__fadd_rn(__fmaf_rn(h[0], h[0], -p0), __fmaf_rn(h[1], h[1], -p1)),
+                              __fmaf_rn(h[2], h[2], -p2));
+    const float c = __fadd_rn(__fadd_rn(__fmul_rn(__fadd_rn(h[0], h[0]), l[0]), __fmul_rn(__fadd_rn(h[1], h[1]), l[1])),
+                              __fmul_rn(__fadd_rn(h[2], h[2]), l[2]));
+    float s1, t1, S, t2;
+    two_sum(p0, p1, s1, t1);
+    two_sum(s1, p2, S, t2);
+    const float Slo = __fadd_rn(__fadd_rn(__fadd_rn(t1, t2), e), c);
+    if (!(S >= 0x1p-80f))
+        return false;
+    // the seed, refined once in float
+    const float x0 = __fadd_rn(S, Slo);
+    const float q0 = rsqrtf(x0);
+    const float xq = __fmul_rn(x0, q0);
+    const float r0 = __fmaf_rn(__fmul_rn(q0, __fmaf_rn(-xq, q0, 1.0f)), 0.5f, q0);
+    // float-float step: hh = 1 - (S + Slo) r0^2, with S r0 = A + Al exactly
+    const float A = __fmul_rn(S, r0);
+    const float Al = __fmaf_rn(S, r0, -A);
+    const float hh = __fsub_rn(__fmaf_rn(-A, r0, 1.0f), __fmaf_rn(Al, r0, __fmul_rn(__fmul_rn(Slo, r0), r0)));
+    const float corr = __fmul_rn(__fmul_rn(r0, hh), 0.5f);
+    float out[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        if (h[a] == 0.0f) { // a zero component keeps its sign, as inv * v does
+            out[a] = h[a];
+            continue;
+        }
+        const float P = __fmul_rn(r0, h[a]);
+        const float Pl = __fmaf_rn(r0, h[a], -P);
+        const float L =
+            __fadd_rn(Pl, __fadd_rn(__fmul_rn(r0, l[a]), __fadd_rn(__fmul_rn(corr, h[a]), __fmul_rn(corr, l[a]))));
+        if (!round_pair(P, L, out[a]))
+            return false;
+    }
+    d = F3{out[0], out[1], out[2]};
+    return true;
+}
+
+// float(normalize(...)) of camera_dir without double-precision arithmetic
+// past the ray's vector (dir_from_vec).
 template <int FMA>
 HD_D bool camera_dir_float(const hd_camera& cam, uint32_t x, uint32_t y, F3& d)
 {
     double v[3];
-    const double dot = camera_vec<FMA>(reload_camera(&cam), u32_to_double(x), u32_to_double(y), v);
-    return dir_from_vec(v, dot, d);
+    camera_vec<FMA>(reload_camera(&cam), u32_to_double(x), u32_to_double(y), v);
+    return dir_from_vec(v, d);
 }
 
 // ---- per-view camera tables -------------------------------------------------
@@ -509,8 +609,8 @@ HD_D uint4 primary_ray(const Table& t, uint32_t root, const hd_camera& cam, uint
     bool fast;
     if (TAB) {
         double v[3];
-        const double dot = camera_vec_tab<FMA>(&cam, tab, W, x, y, v);
-        fast = dir_from_vec(v, dot, d);
+        camera_vec_tab<FMA>(&cam, tab, W, x, y, v);
+        fast = dir_from_vec(v, d);
     } else {
         fast = camera_dir_float<FMA>(cam, x, y, d);
     }
