@@ -17,7 +17,9 @@ value  = device throughput (CUDA events around each step's call; L2
 e2e    = the same metric through the C ABI with host buffers
          (hd_trace_views_host): cameras from host memory, every view's paths
          and shadow mask in pinned host memory every step (the primary
-         kernel writes the paths there over NVLink-C2C; the mask is copied).
+         kernel writes five views' paths in eight there over NVLink-C2C, the
+         copy engine moves the other three during the shadow launch; the
+         mask is copied).
 --impl reference times the oracle's CPU restatement of the reference tracer
 (the reference has no CPU tracer) on all host cores, on the scene the
 oracle's own generator builds, whole frames (a sample of each step's views).
@@ -946,7 +948,8 @@ def run_gpu(args, dist):
                       "pages_used": int(lstats.pages_used), "nodes": int(sum(lstats.nodes[:depth - 1]))},
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": V * C.sizeof(_capi.Camera),
                     "d2h_bytes_per_step": V * (W * H * 16 + W * H), "api": "hd_trace_views_host",
-                    "paths": ("written by the primary kernel into the pinned host buffer (NVLink-C2C)"
+                    "paths": ("5 views in 8 written by the primary kernel into the pinned host buffer "
+                              "(NVLink-C2C), 3 copied during the shadow launch"
                               if not args.e2e_chunk else f"copied in chunks of {args.e2e_chunk} views")},
             "gpu_launches": 3 * K, "roofline": roofline, "cpu_baseline": cpu, "ref_gpu": ref_gpu, "clocks": clk,
             "wall_s": wall, "trace_4k": trace_4k, "edits": edits, "colors": colors, "tools_files": tools,

@@ -300,8 +300,12 @@ hd_status hd_trace_views_host(hd_ctx* c, const hd_camera* cams, uint32_t n_views
         const auto t0 = std::chrono::steady_clock::now();
         const uint64_t frame = uint64_t(width) * height;
         // Pinned host memory the device can address (Grace's NVLink-C2C):
-        // the primary rays write their paths straight into it, and only the
-        // shadow mask is copied.
+        // the primary rays write the paths of most views straight into it;
+        // the views view_copied names go to a device buffer that the copy
+        // engine moves to host memory during the shadow launch, so the host
+        // link carries paths through the whole step (the primary launch
+        // alone is shorter than the link needs for every view's paths).
+        // The shadow mask is copied at the end.
         cudaPointerAttributes attr{};
         void* direct = nullptr;
         if (cudaPointerGetAttributes(&attr, h_paths) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
@@ -313,9 +317,30 @@ hd_status hd_trace_views_host(hd_ctx* c, const hd_camera* cams, uint32_t n_views
                 throw StatusError{HD_ERR_INVALID, "views x width x height must stay below 2^32 pixels"};
             hd_camera* d_cams = c->scratch.get<hd_camera>("views_cams", n_views);
             uint8_t* d_mask = c->scratch.get<uint8_t>("vh_mask_direct", frame * n_views);
+            const uint32_t n_copied = copied_views(n_views);
+            uint32_t* d_copied = nullptr;
+            if (n_copied) {
+                d_copied = c->scratch.get<uint32_t>("vh_paths_copied", frame * n_copied * 4);
+                if (!c->copy_stream)
+                    HD_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+                if (!c->ev_traced[0])
+                    HD_CUDA(cudaEventCreateWithFlags(&c->ev_traced[0], cudaEventDisableTiming));
+            }
             HD_CUDA(cudaMemcpyAsync(d_cams, cams, sizeof(hd_camera) * n_views, cudaMemcpyHostToDevice, c->stream));
-            trace_views(c, d_cams, n_views, width, height, static_cast<uint32_t*>(direct), light, bias, d_mask);
+            trace_views(c, d_cams, n_views, width, height, static_cast<uint32_t*>(direct), light, bias, d_mask,
+                        c->stream, nullptr, n_copied ? c->ev_traced[0] : nullptr, nullptr, nullptr, d_copied);
+            if (n_copied) {
+                // after the primary launch, beside the shadow launch
+                HD_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_traced[0], 0));
+                uint64_t slot = 0;
+                for (uint32_t v = 0; v < n_views; v++)
+                    if (view_copied(v))
+                        HD_CUDA(cudaMemcpyAsync(h_paths + uint64_t(v) * frame * 4, d_copied + slot++ * frame * 4,
+                                                frame * 16, cudaMemcpyDeviceToHost, c->copy_stream));
+            }
             HD_CUDA(cudaMemcpyAsync(h_mask, d_mask, frame * n_views, cudaMemcpyDeviceToHost, c->stream));
+            if (n_copied)
+                HD_CUDA(cudaStreamSynchronize(c->copy_stream));
             HD_CUDA(cudaStreamSynchronize(c->stream));
             if (ms)
                 *ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();

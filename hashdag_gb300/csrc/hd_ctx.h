@@ -173,10 +173,21 @@ void get_values(hd_ctx* c, const uint32_t* d_xyz, uint64_t n, uint8_t* d_out);
 void set_claim_limit(hd_ctx* c, bool gc);
 // mid (optional): recorded between the primary and the shadow launches;
 // d_tables (optional): camera_table_words(w, h) * n_views doubles of
-// scratch for the per-view camera tables (default: the context's)
+// scratch for the per-view camera tables (default: the context's);
+// d_paths_copied (optional): the paths of the views view_copied names go
+// there, packed in view order, instead of into d_paths.
 void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t w, uint32_t h, uint32_t* d_paths,
                  const float light[3], float bias, uint8_t* d_mask, cudaStream_t stream = nullptr,
                  uint32_t* d_list = nullptr, cudaEvent_t mid = nullptr, const uint32_t* d_root = nullptr,
-                 double* d_tables = nullptr);
+                 double* d_tables = nullptr, uint32_t* d_paths_copied = nullptr);
+// Of every 8 views, trace_views sets aside (d_paths_copied) those from the
+// kCopiedFrom-th on (counting from 0).
+constexpr uint32_t kCopiedFrom = 5;
+inline bool view_copied(uint32_t v) { return (v & 7) >= kCopiedFrom; }
+// Views of n_views that trace_views sets aside with d_paths_copied.
+inline uint32_t copied_views(uint32_t n_views)
+{
+    return (n_views >> 3) * (8 - kCopiedFrom) + ((n_views & 7) > kCopiedFrom ? (n_views & 7) - kCopiedFrom : 0);
+}
 
 } // namespace hd

@@ -780,12 +780,26 @@ __device__ __noinline__ bool shadow_origin_fast(const hd_camera* cam, const doub
     return true;
 }
 
+// Where view v's paths go when a launch splits its output (out_copied set):
+// the views view_copied names (the last 8 - kCopiedFrom of every 8) to
+// out_copied, packed in view order, the others to out.  The host-buffer
+// entry point writes the first kind straight into host memory during the
+// primary launch and copies the second during the shadow launch, so that
+// both parts of the step move paths over the host link.
+HD_D uint4* view_paths(uint4* out, uint4* out_copied, uint32_t v, uint64_t frame)
+{
+    if (out_copied && (v & 7) >= kCopiedFrom)
+        return out_copied + (uint64_t(v >> 3) * (8 - kCopiedFrom) + (v & 7) - kCopiedFrom) * frame;
+    return out + uint64_t(v) * frame;
+}
+
 // Several views in one launch, as persistent warps: each warp takes 8x4
 // pixel tiles from a counter (view-major, then tile rows), so warps whose
 // rays end early take more tiles and every resident warp stays busy to the
 // end of the launch; the next tile is fetched before the current one is
 // traced.  View v writes its paths at out + v * W * H (the single-view
-// layout).  The shadow pass's set-up is fused in: a pixel whose primary ray
+// layout), or, with out_copied, the views view_paths sets aside there.  The
+// shadow pass's set-up is fused in: a pixel whose primary ray
 // hit appends its shadow ray (origin on the hit voxel, as shadow_origin) to
 // the list, warp by warp; a miss gets mask 2 at once.
 template <int FMA>
@@ -793,7 +807,7 @@ __global__ void __launch_bounds__(128, 16)
     k_trace_views(Table t, const uint32_t* __restrict__ d_root, const hd_camera* __restrict__ cams, uint32_t W,
                   uint32_t H, uint32_t n_views, uint4* __restrict__ out, F3 light, float bias,
                   uint8_t* __restrict__ mask, ShadowRay* __restrict__ list, uint32_t* __restrict__ head,
-                  const double* __restrict__ tables)
+                  const double* __restrict__ tables, uint4* __restrict__ out_copied)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t tx = (W + 7) / 8, ty = (H + 3) / 4;
@@ -810,8 +824,9 @@ __global__ void __launch_bounds__(128, 16)
         bool hit = false;
         uint4 p = make_uint4(0, 0, 0, 0);
         if (x < W && y < H) {
-            p = primary_ray<FMA, false, SharedStack, true>(t, root, cams[v], W, H, x, y, out + uint64_t(v) * W * H,
-                                                           nullptr, stack, tables + camera_table_words(W, H) * v);
+            p = primary_ray<FMA, false, SharedStack, true>(t, root, cams[v], W, H, x, y,
+                                                           view_paths(out, out_copied, v, uint64_t(W) * H), nullptr,
+                                                           stack, tables + camera_table_words(W, H) * v);
             hit = (p.x | p.y | p.z) != 0;
             if (!hit)
                 mask[i] = 2;
@@ -1044,7 +1059,7 @@ void trace_shadow(hd_ctx* c, const hd_camera& cam, uint32_t w, uint32_t h, const
 // pixel of every view.
 void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t w, uint32_t h, uint32_t* d_paths,
                  const float light[3], float bias, uint8_t* d_mask, cudaStream_t stream, uint32_t* d_list,
-                 cudaEvent_t mid, const uint32_t* d_root, double* d_tables)
+                 cudaEvent_t mid, const uint32_t* d_root, double* d_tables, uint32_t* d_paths_copied)
 {
     cudaStream_t st = stream ? stream : c->stream;
     const uint32_t* rt = d_root ? d_root : c->d_root;
@@ -1067,7 +1082,8 @@ void trace_views(hd_ctx* c, const hd_camera* d_cams, uint32_t n_views, uint32_t 
         const uint32_t smem = shared_stack_bytes(128, c->t.g.depth);
         const uint32_t blocks = uint32_t(std::min<uint64_t>(
             (tiles * n_views + 3) / 4, resident_blocks(reinterpret_cast<const void*>(kernel), 128, smem)));
-        kernel<<<blocks, 128, smem, st>>>(c->t, rt, d_cams, w, h, n_views, out, l, bias, d_mask, list, head, tables);
+        kernel<<<blocks, 128, smem, st>>>(c->t, rt, d_cams, w, h, n_views, out, l, bias, d_mask, list, head, tables,
+                                          reinterpret_cast<uint4*>(d_paths_copied));
     };
     if (c->fp_mode)
         launch(k_camera_tables<1>, k_trace_views<1>);

@@ -194,9 +194,10 @@ hd_status hd_trace_views(hd_ctx* ctx, const hd_camera* cams, uint32_t n_views, u
 /* hd_trace_views with host buffers: cameras read from host memory, every
  * view's paths (width * height * 4 uint32 each) and shadow mask written to
  * host memory.  With chunk_views = 0 and h_paths in pinned memory the
- * device can address, the primary rays write their paths straight into
- * host memory (over NVLink-C2C on a Grace host) and only the mask is
- * copied.  Otherwise the views are traced chunk_views at a time (0: half of
+ * device can address, the primary rays write the paths of five views in
+ * eight straight into host memory (over NVLink-C2C on a Grace host), the
+ * other three are copied there while the shadow rays run, and the mask is
+ * copied at the end.  Otherwise the views are traced chunk_views at a time (0: half of
  * them) and each chunk's copies run on a second stream while the next
  * chunk is traced.  ms: wall time of the call. */
 hd_status hd_trace_views_host(hd_ctx* ctx, const hd_camera* cams, uint32_t n_views, uint32_t width, uint32_t height,
