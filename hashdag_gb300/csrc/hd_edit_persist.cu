@@ -57,15 +57,15 @@ struct Cmd {
 // read: it writes the slot of the next barrier, which no CTA reads until
 // every CTA has left this one.
 struct Ctl {
-    uint32_t arrived, gen, abort, stop;
+    uint32_t arrived, abort, stop; // arrived: grid barrier arrivals of the launch
     uint32_t idx;       // edit being applied
     uint32_t phase;     // the grid step CTA 0 asks for (kPh*)
     uint32_t level;     // its level
     uint32_t deepest;   // deepest level of the current edit
     Cmd cmd[2];
     uint32_t count[HD_MAX_DEPTH];
-    // where a wait ran out: the CTA, its barrier count, the arrivals and the
-    // generation then, CTA 0's barrier count, phase, level and edit
+    // where a wait ran out: the CTA, its barrier count, the arrivals then and
+    // the count it waited for, CTA 0's barrier count, phase, level and edit
     uint32_t diag[8];
     uint32_t bars0; // barriers CTA 0 has passed
     // tests of the timeout path (hd_set_test_barrier_skip): CTA skip_cta - 1
@@ -104,13 +104,12 @@ HD_D uint32_t ld_acquire(const uint32_t* p)
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-HD_D void st_release(uint32_t* p, uint32_t v)
-{
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
 // Grid barrier of the cooperative launch with a bounded wait; false when a
-// wait ran out or another CTA gave up (the caller returns).
+// wait ran out or another CTA gave up (the caller returns).  The arrival
+// count only grows (the control block starts at zero every launch), so the
+// k-th barrier is passed once k x CTAs have arrived: no reset, and no
+// generation word for the last CTA to publish after its arrival.
 HD_D bool grid_sync(Ctl* ctl, uint32_t* err, uint32_t& nbar)
 {
     __shared__ uint32_t ok;
@@ -119,19 +118,15 @@ HD_D bool grid_sync(Ctl* ctl, uint32_t* err, uint32_t& nbar)
         ok = 1;
         nbar++;
         if (blockIdx.x == 0)
-            atomicExch(&ctl->bars0, nbar);
-        const uint32_t g = ld_acquire(&ctl->gen);
+            __stcg(&ctl->bars0, nbar);
+        const uint32_t target = nbar * gridDim.x;
         __threadfence();
-        if (atomicAdd(&ctl->arrived, 1u) == gridDim.x - 1) {
-            atomicExch(&ctl->arrived, 0u);
-            __threadfence();
-            st_release(&ctl->gen, g + 1);
-        } else {
+        if (atomicAdd(&ctl->arrived, 1u) + 1u != target) {
             const unsigned long long t0 = now_ns();
             const unsigned long long set_ns = __ldcg(&ctl->wait_ns);
             const unsigned long long limit = set_ns ? set_ns : kWaitNs;
             uint32_t spins = 0;
-            while (ld_acquire(&ctl->gen) == g) {
+            while (int32_t(ld_acquire(&ctl->arrived) - target) < 0) {
                 if (ld_acquire(&ctl->abort)) {
                     ok = 0;
                     break;
@@ -141,7 +136,7 @@ HD_D bool grid_sync(Ctl* ctl, uint32_t* err, uint32_t& nbar)
                         ctl->diag[0] = blockIdx.x;
                         ctl->diag[1] = nbar;
                         ctl->diag[2] = ld_acquire(&ctl->arrived);
-                        ctl->diag[3] = g;
+                        ctl->diag[3] = target;
                         ctl->diag[4] = ld_acquire(&ctl->bars0);
                         ctl->diag[5] = ld_acquire(&ctl->phase);
                         ctl->diag[6] = ld_acquire(&ctl->level);
@@ -1135,7 +1130,7 @@ void edit_batch_persistent(hd_ctx* c, const hd_edit* edits, uint32_t n, const st
                 where += (k ? " " : "") + std::to_string(fin.diag[k]);
             throw StatusError{HD_ERR_TIMEOUT, "edit " + std::to_string(done) +
                                                   ": a grid barrier of the persistent edit kernel ran out of time "
-                                                  "(cta, barriers, arrived, gen, cta0 barriers, phase, level, edit: " +
+                                                  "(cta, barriers, arrivals, arrivals awaited, cta0 barriers, phase, level, edit: " +
                                                   where + ")"};
         }
         if (fin.stop == kDone)
