@@ -707,10 +707,10 @@ __device__ __noinline__ F3 shadow_origin(const hd_camera& cam, uint32_t H, uint3
 }
 
 // shadow_origin of pixel (x, y) without its double square root and
-// divisions, for the many-view kernel (the GB300's FP64 pipe is narrow and
-// most pixels hit):
+// divisions, for the many-view kernel (the GB300's FP64 pipe is narrow):
 //  * the camera direction cd = y1 * v, y1 from rsqrt_newton: less than
-//    2^-42.9 relative from the reference's double (camera_dir_float);
+//    2^-42.9 relative from the reference's double (y1 within 2^-43, the
+//    product's rounding and the reference's own below 2^-50.8);
 //  * each 1 / cd from a float reciprocal seed (2^-22.4 from a truncated
 //    argument) and one Newton step in double, below 2^-44.5, so that each
 //    candidate t = numerator / cd (the numerators are the reference's
